@@ -1,0 +1,242 @@
+/*
+ * phdflux.h -- C ABI of the GB300 flux path for the AREPO-style moving-mesh code
+ * rickyfernandez/phd-code.
+ *
+ * All pointers in the structures and arguments below are DEVICE pointers unless
+ * marked host.  Arrays are structure-of-arrays, row-major [field][index]:
+ *   cells  : n_cells = n_real real cells followed by ghost cells
+ *   prim   : [dim+2][n_cells]  density, velocity-x.., pressure
+ *   cons   : [dim+2][n_cells]  mass, momentum-x.., energy (cell totals)
+ *   grad   : [(dim+2)*dim][n_cells]  row f*dim+k = d prim_f / d x_k
+ *   states, fluxes : [dim+2][n_faces] (same field order as prim / cons)
+ * Face f joins cells pair_i[f] (always real) and pair_j[f] (real with a larger
+ * index, or a ghost); nbr_ptr/nbr_idx list each cell's faces in ascending face id.
+ *
+ * Every entry point takes a cudaStream_t, never synchronises, and returns a host
+ * error code (PHD_OK or PHD_ERR_*) for argument / launch errors.  Physics status
+ * (negative mass, non-converged Riemann solve, bad index) is OR-ed as PHD_STATUS_*
+ * bits into phd_clock.status on the device; the host reads it when it chooses.
+ */
+#ifndef PHDFLUX_H
+#define PHDFLUX_H
+
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHDFLUX_ABI_VERSION 1
+
+/* host return codes */
+#define PHD_OK 0
+#define PHD_ERR_ARG 1
+#define PHD_ERR_LAUNCH 2
+#define PHD_ERR_UNSUPPORTED 3
+
+/* device status bits (phd_clock.status) -- same meaning as the reference's raises */
+#define PHD_STATUS_NEG_MASS 1              /* "Mass less than zero in flux update"   mesh.pyx:546-548 */
+#define PHD_STATUS_NEG_ENERGY 2            /* "Energy less than zero in flux update" mesh.pyx:549-551 */
+#define PHD_STATUS_RIEMANN_NONCONVERGED 4  /* "No convergence in Exact Riemann Solver" riemann.pyx:1088-1090 */
+#define PHD_STATUS_BAD_INDEX 8             /* "ERROR: incorrect neighbors!" reconstruction.pyx:651-652 */
+
+/* solver / reconstruction selectors */
+#define PHD_HLL 0                          /* riemann.pyx:225-504 */
+#define PHD_HLLC 1                         /* riemann.pyx:507-682 */
+#define PHD_EXACT 2                        /* riemann.pyx:684-1090 */
+#define PHD_CONSTANT 0                     /* PieceWiseConstant reconstruction.pyx:131-353 */
+#define PHD_LINEAR 1                       /* PieceWiseLinear   reconstruction.pyx:355-1079 */
+#define PHD_LIMITER_AREPO 0                /* reconstruction.pyx:683-703 */
+#define PHD_LIMITER_TESS 1                 /* reconstruction.pyx:705-731 */
+
+/* One tessellated state as the host mesh hands it over (mesh.pyx:255-323). */
+typedef struct phd_mesh {
+    int32_t dim, n_cells, n_real, n_faces;
+    const int8_t *tag;        /* [n_cells] 0 = Real, 1 = Ghost            (particle_tags.py) */
+    const int32_t *map;       /* [n_cells] image of each ghost             (domain_manager.pyx:519) */
+    const int8_t *flip;       /* [n_cells] bit k: reflective ghost outside the box in axis k */
+    const double *x;          /* [dim][n_cells] generator positions */
+    const double *dcom;       /* [dim][n_cells] centroid - generator (ghosts: the image's) */
+    const double *vol;        /* [n_cells] (ghosts: the image's) */
+    const int32_t *pair_i, *pair_j;   /* [n_faces] */
+    const double *area;       /* [n_faces] */
+    const double *com;        /* [dim][n_faces] face centroid */
+    const double *normal;     /* [dim][n_faces] (x_j - x_i)/|x_j - x_i| */
+    const int32_t *nbr_ptr;   /* [n_cells+1] */
+    const int32_t *nbr_idx;   /* [2*n_faces] */
+} phd_mesh;
+
+/* Per-step device clock: time step, time and the CFL reduction accumulator. */
+typedef struct phd_clock {
+    double dt;                /* time step of the current step */
+    double t;                 /* time at the start of the current step */
+    double t_end;             /* > 0: clip dt to land on t_end (simulation_finish.py:82-88) */
+    double dt_hydro;          /* last unclipped cfl * min(R/c) */
+    unsigned long long dtmin_bits;    /* accumulator; initialise to the bits of +inf */
+    unsigned int arrive;      /* accumulator; initialise to 0 */
+    int status;               /* PHD_STATUS_* bits, OR-ed by kernels */
+    long long step;           /* completed steps */
+} phd_clock;
+
+/* Physics parameters of a run. */
+typedef struct phd_params {
+    double gamma;             /* IdealGas.gamma (equation_state.pyx:40) */
+    double cfl;               /* RiemannBase.cfl */
+    double eta;               /* Mesh.eta, regularisation (mesh.pyx:87-89) */
+    int32_t reconstruction;   /* PHD_CONSTANT | PHD_LINEAR */
+    int32_t limiter;          /* PHD_LIMITER_AREPO | PHD_LIMITER_TESS */
+    int32_t gizmo;            /* PieceWiseLinear.gizmo_limiter */
+    int32_t solver;           /* PHD_HLL | PHD_HLLC | PHD_EXACT */
+    int32_t boost;            /* RiemannBase.boost (Exact: always 1) */
+    int32_t regularize;       /* Mesh.regularize */
+    int32_t exact_max_iter;   /* Exact.get_pstar MAX_ITER (1000) */
+    int32_t pad_;
+} phd_params;
+
+/* Library identity. */
+int phd_abi_version(void);
+const char *phd_status_string(int status_bit);
+
+/* ---- FP64 stage entry points: one per reference plugin method -------------------- */
+
+/* PieceWiseLinear.compute_gradients + DomainManager.update_ghost_gradients
+ * (reconstruction.pyx:563-739, domain_manager.pyx:776-835, boundary.pyx:265-307).
+ * grad must hold (dim+2)*dim rows of n_cells. */
+int phd_gradients_f64(const phd_mesh *mesh, const double *prim, int32_t limiter,
+                      double *grad, phd_clock *clk, cudaStream_t stream);
+
+/* PieceWiseLinear.add_spatial (stages & 1, reconstruction.pyx:741-921) and/or
+ * add_temporal (stages & 2, :923-1072; reads left/right when stage 1 is not run)
+ * with the half step dt_half -- stages = 3 is compute_states (:1074-1079) -- or
+ * PieceWiseConstant.compute_states (:254-353) when reconstruction == PHD_CONSTANT
+ * (grad may then be NULL). */
+#define PHD_STAGE_SPATIAL 1
+#define PHD_STAGE_TEMPORAL 2
+int phd_states_f64(const phd_mesh *mesh, const double *prim, const double *grad,
+                   const double *face_w, double gamma, double dt_half, int32_t boost,
+                   int32_t reconstruction, int32_t gizmo, int32_t stages, double *left,
+                   double *right, cudaStream_t stream);
+
+/* RiemannBase.compute_fluxes with HLL / HLLC / Exact and deboost
+ * (riemann.pyx:74-98, 190-222, 243-373, 521-682, 700-1090). */
+int phd_riemann_f64(const phd_mesh *mesh, int32_t solver, double gamma, int32_t boost,
+                    int32_t exact_max_iter, const double *left, const double *right,
+                    const double *face_w, double *flux, phd_clock *clk, cudaStream_t stream);
+
+/* Mesh.update_from_fluxes (mesh.pyx:479-551) as a per-cell segmented sum in
+ * ascending face order; real cells only; cons updated in place. */
+int phd_update_from_fluxes_f64(const phd_mesh *mesh, const double *flux, double dt,
+                               double *cons, phd_clock *clk, cudaStream_t stream);
+
+/* DomainManager.update_ghost_fields(conservative, True) (domain_manager.pyx:712-774,
+ * boundary.pyx:309-348): ghost cons = image cons, reflective momentum flip. */
+int phd_ghost_cons_f64(const phd_mesh *mesh, double *cons, cudaStream_t stream);
+
+/* IdealGas.primitive_from_conservative / conservative_from_primitive
+ * (equation_state.pyx:81-117 / 43-79), all cells. */
+int phd_prim_from_cons_f64(int32_t dim, int32_t n, double gamma, const double *vol,
+                           const double *cons, double *prim, cudaStream_t stream);
+int phd_cons_from_prim_f64(int32_t dim, int32_t n, double gamma, const double *vol,
+                           const double *prim, double *cons, cudaStream_t stream);
+
+/* RiemannBase.compute_time_step (riemann.pyx:120-188): clk->dt = cfl * min over real
+ * cells, a warp-shuffle min reduction.  advance != 0 also moves clk->t by the
+ * previous clk->dt and counts a step. */
+int phd_time_step_f64(const phd_mesh *mesh, const double *prim, double gamma, double cfl,
+                      int32_t boost, int32_t advance, phd_clock *clk, cudaStream_t stream);
+
+/* Mesh.assign_generator_velocities / assign_face_velocities (mesh.pyx:363-477). */
+int phd_generator_velocities_f64(const phd_mesh *mesh, const double *prim, double gamma,
+                                 double eta, int32_t regularize, double *w, cudaStream_t stream);
+int phd_face_velocities_f64(const phd_mesh *mesh, const double *w, double *face_w,
+                            cudaStream_t stream);
+
+/* ---- fused FP64 step (parity mode) -------------------------------------------------
+ * One step of the flux path on a fixed mesh in the order of
+ * MovingMeshMUSCLHancock.evolve_timestep (integrate.py:385-428) up to the host re-mesh
+ * (moving != 0: generator + face velocities first) or StaticMeshMUSCLHancock
+ * (integrate.py:349-378): gradients, states + Riemann + deboost fused per face,
+ * segmented conserved update with ghost refresh, primitive recovery and the next
+ * CFL time step.  Uses clk->dt; leaves the next step's dt in clk->dt.
+ * Work arrays: grad [(dim+2)*dim][n_cells], flux [dim+2][n_faces], w [dim][n_cells],
+ * face_w [dim][n_faces], cons_next [dim+2][n_cells].  cons and cons_next are swapped
+ * by the caller between steps (the step writes cons_next). */
+int phd_step_f64(const phd_mesh *mesh, const phd_params *par, int32_t moving,
+                 double *prim, const double *cons, double *cons_next, double *grad,
+                 double *w, double *face_w, double *flux, phd_clock *clk, cudaStream_t stream);
+
+/* phd_step_f64 with four stage-boundary events (see phd_step_f32_marked). */
+int phd_step_f64_marked(const phd_mesh *mesh, const phd_params *par, int32_t moving,
+                        double *prim, const double *cons, double *cons_next, double *grad,
+                        double *w, double *face_w, double *flux, phd_clock *clk,
+                        cudaStream_t stream, cudaEvent_t *marks);
+
+/* ---- fused FP32 step (FP32 reconstruction / Riemann, FP64 conserved totals) --------
+ * Mesh-relative FP32 geometry, formed in FP64 once per mesh by phd_prepare_f32:
+ *   face_geo [F][4] (n_x, n_y, c_x, c_y), c = face centroid - (x_i + x_j)/2
+ *   face_ar  [F][2] (area, |x_j - x_i|)
+ *   csr_face [2F]   per-cell face list (nbr_ptr order): face id where the cell is
+ *                   pair-i, ~face id where it is pair-j
+ *   csr_nbr  [2F]   the other cell of each listed face
+ *   cell_geo [n][4] (dcom_x, dcom_y, 1/vol, sqrt(vol/pi))
+ * twin (optional, [F]): for periodic faces the reference computes twice (once from each
+ * side, mesh.pyx:529-544), twin[f] = the kept copy's id for the dropped copy f, else -1;
+ * both cells then exchange the same FP32 flux and the totals are conserved exactly. */
+typedef struct phd_geom32 {
+    const float *face_geo;
+    const float *face_ar;
+    const int32_t *csr_face;
+    const int32_t *csr_nbr;
+    const float *cell_geo;
+} phd_geom32;
+
+typedef struct phd_geom32_out {
+    float *face_geo;
+    float *face_ar;
+    int32_t *csr_face;
+    int32_t *csr_nbr;
+    float *cell_geo;
+} phd_geom32_out;
+
+int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out,
+                    cudaStream_t stream);
+
+/* FP64 totals -> FP32 primitive cells prim4 [n][4] (rho, v_x, v_y, p) and clk->dt from
+ * the CFL minimum (clock not advanced). */
+int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4,
+                 phd_clock *clk, cudaStream_t stream);
+
+/* One fused step (same order as phd_step_f64): gradients (+ generator velocities when
+ * moving) -> per-face states, Riemann flux and deboost (face velocities formed on the
+ * fly) -> segmented update into cons_next, FP32 primitives, next dt.
+ * prim4 [n][4], grad8 [n][8], w2 [n][2], flux4 [F][4] (FP32); cons, cons_next [4][n] (FP64). */
+int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par,
+                 int32_t moving, float *prim4, const double *cons, double *cons_next, float *grad8,
+                 float *w2, float *flux4, phd_clock *clk, cudaStream_t stream);
+
+/* The same step with four caller-created events recorded on the stream around its
+ * three stages (before gradients, before the face kernel, before the update, after),
+ * so a caller can time each kernel inside a timed run; marks may be NULL. */
+int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par,
+                        int32_t moving, float *prim4, const double *cons, double *cons_next,
+                        float *grad8, float *w2, float *flux4, phd_clock *clk,
+                        cudaStream_t stream, cudaEvent_t *marks);
+
+/* ---- utilities ------------------------------------------------------------------ */
+
+/* Reflective flip bits from ghost positions (boundary.pyx:287-307): bit k set when
+ * type == Exterior and x_k lies outside [xmin_k, xmax_k].  xmin/xmax: host arrays. */
+int phd_flip_mask(int32_t dim, int32_t n, const int8_t *type, const double *x,
+                  const double *xmin, const double *xmax, int32_t reflective,
+                  int8_t *flip, cudaStream_t stream);
+
+/* hilbert_key_2d (hilbert.pyx:9-23) of positions quantised as in
+ * LoadBalance.compute_hilbert_keys (load_balance.pyx:195-217). */
+int phd_hilbert_keys_2d(int32_t n, const double *x, double corner_x, double corner_y,
+                        double fac, int32_t order, int64_t *keys, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PHDFLUX_H */

@@ -1,0 +1,80 @@
+"""Build the CUDA extension ``libphdflux.so`` in-tree for sm_103a (GB300).
+
+Each translation unit is compiled separately, in parallel, then linked into one
+shared library exporting the C ABI of ``include/phdflux.h``:
+
+* ``phd_f64.cu``  FP64 stage kernels and fused step, ``--fmad=false`` so products and
+  sums round like the reference's Cython arithmetic;
+* ``phd_f32.cu``  FP32 reconstruction / Riemann with FP64 accumulation (FMA allowed);
+* ``phd_util.cu`` mesh-preparation kernels.
+
+Usage: ``python phd-code_gb300/build.py`` (or ``__graft_entry__.build()``).
+"""
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libphdflux.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
+
+UNITS = {
+    "phd_f64.cu": ["--fmad=false"],
+    "phd_f32.cu": [],
+    "phd_util.cu": [],
+}
+
+
+def nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.isabs(c) and os.path.exists(c) or not os.path.isabs(c)):
+            return c
+    return "nvcc"
+
+
+def _sources_newer(obj, src):
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    deps = [src] + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
+    deps.append(os.path.join(INCLUDE, "phdflux.h"))
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(force=False, verbose=False, extra=()):
+    os.makedirs(BUILD, exist_ok=True)
+    units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u))]
+    objs = []
+
+    def compile_one(u):
+        src = os.path.join(CSRC, u)
+        obj = os.path.join(BUILD, u.replace(".cu", ".o"))
+        if force or _sources_newer(obj, src):
+            cmd = [nvcc()] + ARCH + COMMON + UNITS[u] + list(extra) + ["-c", src, "-o", obj + ".tmp"]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (u, " ".join(cmd), r.stderr))
+            if verbose and r.stderr:
+                sys.stderr.write(r.stderr)
+            os.replace(obj + ".tmp", obj)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(units)) as ex:
+        objs = list(ex.map(compile_one, units))
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
+        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

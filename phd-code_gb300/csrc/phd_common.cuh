@@ -1,0 +1,87 @@
+// phd_common.cuh -- shared constants, math overloads and small device helpers.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "../../include/phdflux.h"
+
+#define PHD_REAL_TAG 0
+#define PHD_EXTERIOR_TYPE 2
+
+namespace phd {
+
+// Type-generic math so one template body serves the FP64 and FP32 builds.
+__device__ __forceinline__ double t_sqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ float t_sqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ double t_pow(double a, double b) { return pow(a, b); }
+__device__ __forceinline__ float t_pow(float a, float b) { return powf(a, b); }
+__device__ __forceinline__ double t_fmax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float t_fmax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double t_fmin(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float t_fmin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double t_fabs(double a) { return fabs(a); }
+__device__ __forceinline__ float t_fabs(float a) { return fabsf(a); }
+// x**2 in the reference lowers to libm pow(x, 2.0); pow(x, 2) and x*x agree to 1 ulp.
+__device__ __forceinline__ double t_sq(double a) { return pow(a, 2.0); }
+__device__ __forceinline__ float t_sq(float a) { return a * a; }
+
+// Positive doubles order like their bit patterns: min-reduce them as integers.
+__device__ __forceinline__ unsigned long long dbits(double v) {
+    return static_cast<unsigned long long>(__double_as_longlong(v));
+}
+
+__device__ __forceinline__ double warp_min(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide min of positive doubles into *slot (bit-pattern atomicMin).  Every
+// thread of the block must call it.
+__device__ __forceinline__ void block_min_to(double v, unsigned long long *slot) {
+    __shared__ double s_min[32];
+    v = warp_min(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) s_min[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        double u = (lane < nw) ? s_min[lane] : INFINITY;
+        u = warp_min(u);
+        if (lane == 0 && u < INFINITY) atomicMin(slot, dbits(u));
+    }
+}
+
+// Finish a grid-wide CFL reduction: the last block to arrive turns the minimum
+// into the next time step (cfl * min, clipped to land on t_end) and re-arms the
+// accumulator.  With `advance` the clock first moves past the step just taken
+// (t += dt, step += 1).  No block waits on another: every block reads clk->dt before
+// its arrival is counted, and only the last arrival writes it.
+__device__ __forceinline__ void finish_cfl(phd_clock *clk, double cfl, bool advance) {
+    __shared__ bool s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned int prev = atomicAdd(&clk->arrive, 1u);
+        s_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        const unsigned long long bits = atomicAdd(&clk->dtmin_bits, 0ull);
+        const double mn = __longlong_as_double(static_cast<long long>(bits));
+        if (advance) {
+            clk->t = clk->t + clk->dt;
+            clk->step = clk->step + 1;
+        }
+        double dt = cfl * mn;
+        clk->dt_hydro = dt;
+        // Time.modify_timestep + Simulation.compute_time_step (simulation_finish.py:82-88,
+        // simulation.py:201-212): land exactly on t_end.
+        if (clk->t_end > 0.0 && clk->t + dt >= clk->t_end) dt = fmin(clk->t_end - clk->t, dt);
+        clk->dt = dt;
+        clk->dtmin_bits = dbits(INFINITY);
+        clk->arrive = 0u;
+        __threadfence();
+    }
+}
+
+}  // namespace phd

@@ -1,0 +1,457 @@
+// phd_f32.cu -- FP32 reconstruction / Riemann with FP64 conserved-state accumulation.
+//
+// Precision split: every geometric quantity that would cancel catastrophically in
+// FP32 (face centroid minus generator midpoint, generator separation) is formed in
+// FP64 once per mesh (k_prepare32) and stored relative; cell primitives and gradients
+// are FP32; each face flux is FP32; the per-face conserved increment is formed once in
+// FP32 and both cells of the face add exactly that value, so mass, momentum and energy
+// are exchanged exactly; the sum over a cell's faces is compensated (two-sum) and added
+// to the FP64 conserved totals.  The exact solver keeps its Newton pressure iteration in
+// FP64 (phd_physics.cuh).
+//
+// Layout (device):
+//   face_geo  float4 [F]  (n_x, n_y, c_x, c_y)  c = face centroid - (x_i + x_j)/2
+//   face_ar   float2 [F]  (area, r = |x_j - x_i|)
+//   csr_face  int32 [2F]  face id where the cell is pair-i, ~face id where it is pair-j
+//   csr_nbr   int32 [2F]  the other cell of that face
+//   cell_geo  float4 [n]  (dcom_x, dcom_y, 1/vol, R = sqrt(vol/pi))
+//   prim4     float4 [n]  (rho, v_x, v_y, p)
+//   grad8     float4 [2n] (d rho/dx, d rho/dy, d vx/dx, d vx/dy) (d vy/dx, d vy/dy, d p/dx, d p/dy)
+//   w2        float2 [n]  generator velocity
+//   flux4     float4 [F]  (mass, mom_x, mom_y, energy) flux through the face
+#include "phd_common.cuh"
+#include "phd_physics.cuh"
+
+namespace phd {
+
+constexpr int B32 = 256;
+
+__device__ __forceinline__ void set_status32(phd_clock *clk, int bits) {
+    if (bits) atomicOr(&clk->status, bits);
+}
+
+// ---- mesh preparation (once per uploaded mesh, FP64 arithmetic) -------------------
+__global__ void k_prepare_faces32(phd_mesh M, float4 *__restrict__ face_geo, float2 *__restrict__ face_ar) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M.n_faces) return;
+    const int n = M.n_cells, F = M.n_faces;
+    const int i = M.pair_i[m], j = M.pair_j[m];
+    double dx = 0, dy = 0, cx = 0, cy = 0;
+    if (i >= 0 && i < n && j >= 0 && j < n) {
+        const double xi = M.x[i], yi = M.x[(size_t)n + i], xj = M.x[j], yj = M.x[(size_t)n + j];
+        dx = xj - xi;
+        dy = yj - yi;
+        cx = M.com[m] - 0.5 * (xi + xj);
+        cy = M.com[(size_t)F + m] - 0.5 * (yi + yj);
+    }
+    const double r = sqrt(dx * dx + dy * dy);
+    face_geo[m] = make_float4((float)M.normal[m], (float)M.normal[(size_t)F + m], (float)cx, (float)cy);
+    face_ar[m] = make_float2((float)M.area[m], (float)r);
+}
+
+__global__ void k_prepare_cells32(phd_mesh M, float4 *__restrict__ cell_geo) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.n_cells) return;
+    const int n = M.n_cells;
+    const double v = M.vol[i];
+    cell_geo[i] = make_float4((float)M.dcom[i], (float)M.dcom[(size_t)n + i], (float)(1.0 / v),
+                              (float)sqrt(v / 3.141592653589793));
+}
+
+// CSR entries with the side folded into the face id, plus the neighbour cell.  Where a
+// twin table is given (periodic faces computed twice by the reference, once from
+// each side), the entry of the dropped twin points at the kept face from the other side.
+__global__ void k_prepare_csr32(phd_mesh M, const int32_t *__restrict__ twin, int32_t *__restrict__ csr_face,
+                                int32_t *__restrict__ csr_nbr) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M.n_cells) return;
+    const int n = M.n_cells, F = M.n_faces;
+    for (int e = M.nbr_ptr[c]; e < M.nbr_ptr[c + 1]; e++) {
+        int fid = M.nbr_idx[e];
+        if (fid < 0 || fid >= F) { csr_face[e] = 0; csr_nbr[e] = c; continue; }
+        const int a = M.pair_i[fid], b = M.pair_j[fid];
+        const bool as_i = (a == c);
+        int other = as_i ? b : a;
+        int code = as_i ? fid : ~fid;
+        if (twin && as_i) {
+            const int t = twin[fid];
+            if (t >= 0 && t < F) {       // this face is dropped: use the twin from the j side
+                code = ~t;
+                other = M.pair_i[t];
+            }
+        }
+        if (other < 0 || other >= n) other = c;
+        csr_face[e] = code;
+        csr_nbr[e] = other;
+    }
+}
+
+// ---- gradients + generator velocity ----------------------------------------------
+// Same estimator and limiter as cell_gradient_f64 (reconstruction.pyx:620-736) in
+// the relative geometry: with sigma = +1 for pair-i and -1 for pair-j,
+//   d phi/dx_k = 1/V sum_faces [ (A/r) (phi_j - phi_i) c_k + sigma A/2 (phi_j + phi_i) n_k ]
+//   limiter separation  f - (x + dcom) = c + sigma r/2 n - dcom.
+template <int LIMITER>
+__global__ void __launch_bounds__(B32) k_grad32(phd_mesh M, phd_params P, int moving,
+                                                const float4 *__restrict__ face_geo,
+                                                const float2 *__restrict__ face_ar,
+                                                const int32_t *__restrict__ csr_face,
+                                                const int32_t *__restrict__ csr_nbr,
+                                                const float4 *__restrict__ cell_geo,
+                                                const float4 *__restrict__ prim4, float4 *__restrict__ grad8,
+                                                float2 *__restrict__ w2, phd_clock *clk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.n_cells) return;
+    const bool real = M.tag[i] == PHD_REAL_TAG;
+    const int c = real ? i : M.map[i];
+    if (c < 0 || c >= M.n_cells) { set_status32(clk, PHD_STATUS_BAD_INDEX); return; }
+    const float4 pc = prim4[c];
+    const float4 gc = cell_geo[c];
+    const float P0[4] = {pc.x, pc.y, pc.z, pc.w};
+    float mx[4], mn[4], df[4][2];
+#pragma unroll
+    for (int f = 0; f < 4; f++) { mx[f] = mn[f] = P0[f]; df[f][0] = df[f][1] = 0.f; }
+    const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
+    for (int e = e0; e < e1; e++) {
+        const int code = csr_face[e];
+        const int fid = code < 0 ? ~code : code;
+        const float sg = code < 0 ? -1.f : 1.f;
+        const int j = csr_nbr[e];
+        const float4 g = face_geo[fid];
+        const float2 ar = face_ar[fid];
+        const float4 pj = prim4[j];
+        const float Pj[4] = {pj.x, pj.y, pj.z, pj.w};
+        const float a_r = ar.x / ar.y;
+        const float ha = 0.5f * sg * ar.x;
+#pragma unroll
+        for (int f = 0; f < 4; f++) {
+            mx[f] = fmaxf(mx[f], Pj[f]);
+            mn[f] = fminf(mn[f], Pj[f]);
+            const float dd = (Pj[f] - P0[f]) * a_r;
+            const float ds = (Pj[f] + P0[f]) * ha;
+            df[f][0] += dd * g.z + ds * g.x;
+            df[f][1] += dd * g.w + ds * g.y;
+        }
+    }
+    float alpha[4] = {1.f, 1.f, 1.f, 1.f};
+#pragma unroll
+    for (int f = 0; f < 4; f++) { df[f][0] *= gc.z; df[f][1] *= gc.z; }
+    for (int e = e0; e < e1; e++) {
+        const int code = csr_face[e];
+        const int fid = code < 0 ? ~code : code;
+        const float hs = code < 0 ? -0.5f : 0.5f;
+        const float4 g = face_geo[fid];
+        const float r = face_ar[fid].y;
+        const float sx = g.z + hs * r * g.x - gc.x;
+        const float sy = g.w + hs * r * g.y - gc.y;
+        if (LIMITER == PHD_LIMITER_AREPO) {
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                const float dphi = df[f][0] * sx + df[f][1] * sy;
+                float psi = 1.f;
+                if (dphi > 0.f) psi = (mx[f] - P0[f]) / dphi;
+                else if (dphi < 0.f) psi = (mn[f] - P0[f]) / dphi;
+                alpha[f] = fminf(alpha[f], fmaxf(psi, 0.f));
+            }
+        } else {
+            const float4 pj = prim4[csr_nbr[e]];
+            const float Pj[4] = {pj.x, pj.y, pj.z, pj.w};
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                const float dphi = df[f][0] * sx + df[f][1] * sy;
+                float psi = 1.f;
+                if (dphi != 0.f) psi = fmaxf((Pj[f] - P0[f]) / dphi, 0.f);
+                alpha[0] = fminf(alpha[0], fmaxf(psi, 0.f));     // only alpha[0] (:731)
+            }
+        }
+    }
+    float gv[8];
+#pragma unroll
+    for (int f = 0; f < 4; f++) { gv[2 * f] = alpha[f] * df[f][0]; gv[2 * f + 1] = alpha[f] * df[f][1]; }
+    const int fl = M.flip[i];
+    if (fl & 1) gv[2] = -gv[2];        // d vx / dx
+    if (fl & 2) gv[5] = -gv[5];        // d vy / dy
+    grad8[2 * (size_t)i] = make_float4(gv[0], gv[1], gv[2], gv[3]);
+    grad8[2 * (size_t)i + 1] = make_float4(gv[4], gv[5], gv[6], gv[7]);
+
+    if (moving) {   // Mesh.assign_generator_velocities mesh.pyx:397-426, own (ghost) cell data
+        const float4 p = prim4[i];
+        const float4 gi = (i == c) ? gc : cell_geo[i];
+        float wx = p.y, wy = p.z;
+        if (P.regularize) {
+            const float cs = sqrtf((float)P.gamma * p.w / p.x);
+            const float d = sqrtf(gi.x * gi.x + gi.y * gi.y);
+            const float eR = (float)P.eta * gi.w;
+            const float q = d / eR;
+            if (q >= 0.9f && q < 1.1f) {
+                const float s = cs * (d - 0.9f * eR) / (d * 0.2f * eR);
+                wx += s * gi.x;
+                wy += s * gi.y;
+            } else if (q >= 1.1f) {
+                wx += cs * gi.x / d;
+                wy += cs * gi.y / d;
+            }
+        }
+        w2[i] = make_float2(wx, wy);
+    }
+}
+
+// ---- fused face kernel ------------------------------------------------------------
+template <int SOLVER, bool LINEAR>
+__global__ void __launch_bounds__(B32) k_face32(phd_mesh M, phd_params P, int moving,
+                                                const float4 *__restrict__ face_geo,
+                                                const float2 *__restrict__ face_ar,
+                                                const float4 *__restrict__ cell_geo,
+                                                const float4 *__restrict__ prim4,
+                                                const float4 *__restrict__ grad8, const float2 *__restrict__ w2,
+                                                float4 *__restrict__ flux4, phd_clock *clk) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M.n_faces) return;
+    const int i = M.pair_i[m], j = M.pair_j[m];
+    if (i < 0 || i >= M.n_cells || j < 0 || j >= M.n_cells) { set_status32(clk, PHD_STATUS_BAD_INDEX); return; }
+    const bool boost = (SOLVER == PHD_EXACT) ? true : (P.boost != 0);
+    const float gamma = (float)P.gamma;
+    const float dt_half = (float)(0.5 * clk->dt);
+    const float4 g = face_geo[m];
+    const float2 ar = face_ar[m];
+    const float nrm[2] = {g.x, g.y};
+    const float4 a = prim4[i], b = prim4[j];
+    const float pi[4] = {a.x, a.y, a.z, a.w}, pj[4] = {b.x, b.y, b.z, b.w};
+    float w[2] = {0.f, 0.f};
+    if (moving) {   // Mesh.assign_face_velocities mesh.pyx:462-477: (w_i+w_j)/2 + ((w_i-w_j).c / r) n
+        const float2 wi = w2[i], wj = w2[j];
+        const float fac = ((wi.x - wj.x) * g.z + (wi.y - wj.y) * g.w) / ar.y;
+        w[0] = 0.5f * (wi.x + wj.x) + fac * g.x;
+        w[1] = 0.5f * (wi.y + wj.y) + fac * g.y;
+    }
+    float L[4], R[4];
+#pragma unroll
+    for (int f = 0; f < 4; f++) { L[f] = pi[f]; R[f] = pj[f]; }
+    if (boost) { L[1] -= w[0]; L[2] -= w[1]; R[1] -= w[0]; R[2] -= w[1]; }
+    if (LINEAR) {
+        const float4 gi0 = grad8[2 * (size_t)i], gi1 = grad8[2 * (size_t)i + 1];
+        const float4 gj0 = grad8[2 * (size_t)j], gj1 = grad8[2 * (size_t)j + 1];
+        const float gi[8] = {gi0.x, gi0.y, gi0.z, gi0.w, gi1.x, gi1.y, gi1.z, gi1.w};
+        const float gj[8] = {gj0.x, gj0.y, gj0.z, gj0.w, gj1.x, gj1.y, gj1.z, gj1.w};
+        const float4 ci = cell_geo[i], cj = cell_geo[j];
+        const float hr = 0.5f * ar.y;
+        const float six = g.z + hr * g.x - ci.x, siy = g.w + hr * g.y - ci.y;   // f - (x_i + dcom_i)
+        const float sjx = g.z - hr * g.x - cj.x, sjy = g.w - hr * g.y - cj.y;   // f - (x_j + dcom_j)
+        float sl[4], sr[4];
+#pragma unroll
+        for (int f = 0; f < 4; f++) {
+            sl[f] = L[f];
+            sr[f] = R[f];
+            L[f] += gi[2 * f] * six + gi[2 * f + 1] * siy;
+            R[f] += gj[2 * f] * sjx + gj[2 * f + 1] * sjy;
+        }
+        if (P.gizmo) {
+            const float smi = sqrtf(six * six + siy * siy), smj = sqrtf(sjx * sjx + sjy * sjy);
+#pragma unroll
+            for (int f = 0; f < 4; f++) gizmo_pair<float>(sl[f], sr[f], pi[f], pj[f], smi, smj, ar.y, L[f], R[f]);
+            if (L[0] < 0.f || L[3] < 0.f) {
+#pragma unroll
+                for (int f = 0; f < 4; f++) L[f] = sl[f];
+            }
+            if (R[0] < 0.f || R[3] < 0.f) {
+#pragma unroll
+                for (int f = 0; f < 4; f++) R[f] = sr[f];
+            }
+        }
+        temporal<float, 2>(L, R, pi, pj, gi, gj, w, gamma, dt_half, boost);
+    }
+    float f[4];
+    bool failed = false;
+    if (SOLVER == PHD_EXACT) exact_flux<float, 2>(L, R, nrm, w, gamma, P.exact_max_iter, f, &failed);
+    else hll_family<float, 2>(SOLVER == PHD_HLLC, L, R, nrm, w, gamma, boost, f);
+    if (failed) set_status32(clk, PHD_STATUS_RIEMANN_NONCONVERGED);
+    flux4[m] = make_float4(f[0], f[1], f[2], f[3]);
+}
+
+// ---- segmented update, primitive recovery and CFL -----------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+__global__ void __launch_bounds__(B32) k_update32(phd_mesh M, phd_params P, const float2 *__restrict__ face_ar,
+                                                  const int32_t *__restrict__ csr_face,
+                                                  const float4 *__restrict__ flux4, const double *__restrict__ cons,
+                                                  double *__restrict__ cons_next, float4 *__restrict__ prim4,
+                                                  phd_clock *clk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = M.n_cells;
+    const double dt = clk->dt;
+    const float dtf = (float)dt;
+    double cand = INFINITY;
+    if (i < n) {
+        const bool real = M.tag[i] == PHD_REAL_TAG;
+        const int c = real ? i : M.map[i];
+        if (c >= 0 && c < n) {
+            float hs[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+            for (int e = M.nbr_ptr[c]; e < M.nbr_ptr[c + 1]; e++) {
+                const int code = csr_face[e];
+                const int fid = code < 0 ? ~code : code;
+                // one increment per face, identical for both of its cells
+                const float s = dtf * face_ar[fid].x;
+                const float4 fl = flux4[fid];
+                const float inc[4] = {s * fl.x, s * fl.y, s * fl.z, s * fl.w};
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    float t, er;
+                    two_sum(hs[q], code < 0 ? inc[q] : -inc[q], t, er);
+                    hs[q] = t;
+                    lo[q] += er;
+                }
+            }
+            double U[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) U[q] = cons[(size_t)q * n + c] + ((double)hs[q] + (double)lo[q]);
+            if (U[0] <= 0.0) set_status32(clk, PHD_STATUS_NEG_MASS);
+            if (U[3] <= 0.0) set_status32(clk, PHD_STATUS_NEG_ENERGY);
+            if (!real) {
+                const int fl = M.flip[i];
+                if (fl & 1) U[1] = -U[1];
+                if (fl & 2) U[2] = -U[2];
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) cons_next[(size_t)q * n + i] = U[q];
+            // IdealGas.primitive_from_conservative equation_state.pyx:106-117
+            const double vol = M.vol[i];
+            const double rho = U[0] / vol;
+            const double rm = 1.0 / U[0];
+            const double vx = U[1] * rm, vy = U[2] * rm;
+            const double p = (U[3] / vol - 0.5 * rho * (vx * vx + vy * vy)) * (P.gamma - 1.0);
+            const float4 pr = make_float4((float)rho, (float)vx, (float)vy, (float)p);
+            prim4[i] = pr;
+            if (real) {   // riemann.pyx:170-187
+                const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
+                const float cs = sqrtf((float)P.gamma * pr.w / pr.x);
+                const float R = sqrtf((float)vol * (float)(1.0 / 3.141592653589793));
+                const float den = boost ? cs : cs + sqrtf(pr.y * pr.y + pr.z * pr.z);
+                cand = (double)(R / den);
+            }
+        } else {
+            set_status32(clk, PHD_STATUS_BAD_INDEX);
+        }
+    }
+    block_min_to(cand, &clk->dtmin_bits);
+    finish_cfl(clk, P.cfl, true);
+}
+
+// FP64 conserved totals -> FP32 primitive cells and the CFL step (no clock advance).
+__global__ void __launch_bounds__(B32) k_prim32(phd_mesh M, phd_params P, const double *__restrict__ cons,
+                                                float4 *__restrict__ prim4, phd_clock *clk) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = M.n_cells;
+    double cand = INFINITY;
+    if (i < n) {
+        const double U0 = cons[i], U1 = cons[(size_t)n + i], U2 = cons[2 * (size_t)n + i], U3 = cons[3 * (size_t)n + i];
+        const double vol = M.vol[i];
+        const double rho = U0 / vol;
+        const double vx = U1 / U0, vy = U2 / U0;
+        const double p = (U3 / vol - 0.5 * rho * (vx * vx + vy * vy)) * (P.gamma - 1.0);
+        const float4 pr = make_float4((float)rho, (float)vx, (float)vy, (float)p);
+        prim4[i] = pr;
+        if (M.tag[i] == PHD_REAL_TAG) {
+            const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
+            const float cs = sqrtf((float)P.gamma * pr.w / pr.x);
+            const float R = sqrtf((float)vol * (float)(1.0 / 3.141592653589793));
+            const float den = boost ? cs : cs + sqrtf(pr.y * pr.y + pr.z * pr.z);
+            cand = (double)(R / den);
+        }
+    }
+    block_min_to(cand, &clk->dtmin_bits);
+    finish_cfl(clk, P.cfl, false);
+}
+
+template <int SOLVER>
+void launch_face32(bool linear, int grid, cudaStream_t s, const phd_mesh &M, const phd_params &P, int moving,
+                   const phd_geom32 *G, const float4 *prim4, const float4 *grad8, const float2 *w2, float4 *flux4,
+                   phd_clock *clk) {
+    const float4 *fg = reinterpret_cast<const float4 *>(G->face_geo);
+    const float2 *fa = reinterpret_cast<const float2 *>(G->face_ar);
+    const float4 *cg = reinterpret_cast<const float4 *>(G->cell_geo);
+    if (linear)
+        k_face32<SOLVER, true><<<grid, B32, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clk);
+    else
+        k_face32<SOLVER, false><<<grid, B32, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clk);
+}
+
+inline int g32(int n) { return (n + B32 - 1) / B32; }
+
+}  // namespace phd
+
+using namespace phd;
+
+extern "C" {
+
+int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out, cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || !out || !out->face_geo || !out->face_ar || !out->csr_face || !out->csr_nbr ||
+        !out->cell_geo)
+        return PHD_ERR_ARG;
+    if (mesh->n_faces)
+        k_prepare_faces32<<<g32(mesh->n_faces), B32, 0, stream>>>(*mesh, reinterpret_cast<float4 *>(out->face_geo),
+                                                                 reinterpret_cast<float2 *>(out->face_ar));
+    k_prepare_cells32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, reinterpret_cast<float4 *>(out->cell_geo));
+    k_prepare_csr32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, twin, out->csr_face, out->csr_nbr);
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4, phd_clock *clk,
+                 cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || !par || !cons || !prim4 || !clk) return PHD_ERR_ARG;
+    k_prim32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, *par, cons, reinterpret_cast<float4 *>(prim4), clk);
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
+                        float *prim4, const double *cons, double *cons_next, float *grad8, float *w2,
+                        float *flux4, phd_clock *clk, cudaStream_t stream, cudaEvent_t *marks) {
+    if (!mesh || mesh->dim != 2 || !geo || !par || !prim4 || !cons || !cons_next || !flux4 || !clk)
+        return PHD_ERR_ARG;
+    const bool linear = par->reconstruction == PHD_LINEAR;
+    if ((linear || moving) && !grad8) return PHD_ERR_ARG;
+    if (moving && !w2) return PHD_ERR_ARG;
+    if (par->solver < PHD_HLL || par->solver > PHD_EXACT) return PHD_ERR_ARG;
+    const phd_mesh &M = *mesh;
+    const int gc = g32(M.n_cells), gf = g32(M.n_faces);
+    float4 *p4 = reinterpret_cast<float4 *>(prim4);
+    float4 *g8 = reinterpret_cast<float4 *>(grad8);
+    float2 *w = reinterpret_cast<float2 *>(w2);
+    float4 *fx = reinterpret_cast<float4 *>(flux4);
+    const float4 *fg = reinterpret_cast<const float4 *>(geo->face_geo);
+    const float2 *fa = reinterpret_cast<const float2 *>(geo->face_ar);
+    const float4 *cg = reinterpret_cast<const float4 *>(geo->cell_geo);
+    if (marks) cudaEventRecord(marks[0], stream);
+    if (linear || moving) {
+        if (par->limiter == PHD_LIMITER_TESS)
+            k_grad32<PHD_LIMITER_TESS><<<gc, B32, 0, stream>>>(M, *par, moving, fg, fa, geo->csr_face, geo->csr_nbr,
+                                                               cg, p4, g8, w, clk);
+        else
+            k_grad32<PHD_LIMITER_AREPO><<<gc, B32, 0, stream>>>(M, *par, moving, fg, fa, geo->csr_face,
+                                                                geo->csr_nbr, cg, p4, g8, w, clk);
+    }
+    if (marks) cudaEventRecord(marks[1], stream);
+    if (M.n_faces) {
+        switch (par->solver) {
+            case PHD_HLL: launch_face32<PHD_HLL>(linear, gf, stream, M, *par, moving, geo, p4, g8, w, fx, clk); break;
+            case PHD_HLLC: launch_face32<PHD_HLLC>(linear, gf, stream, M, *par, moving, geo, p4, g8, w, fx, clk); break;
+            default: launch_face32<PHD_EXACT>(linear, gf, stream, M, *par, moving, geo, p4, g8, w, fx, clk); break;
+        }
+    }
+    if (marks) cudaEventRecord(marks[2], stream);
+    k_update32<<<gc, B32, 0, stream>>>(M, *par, fa, geo->csr_face, fx, cons, cons_next, p4, clk);
+    if (marks) cudaEventRecord(marks[3], stream);
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
+                 float *prim4, const double *cons, double *cons_next, float *grad8, float *w2, float *flux4,
+                 phd_clock *clk, cudaStream_t stream) {
+    return phd_step_f32_marked(mesh, geo, par, moving, prim4, cons, cons_next, grad8, w2, flux4, clk, stream,
+                               nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,121 @@
+"""Device-resident mesh, clock and state for the GB300 flux path.
+
+``DeviceMesh`` uploads one tessellated state (the face list and cell geometry that
+the host mesh produces each step, ``mesh.pyx:255-323``) into HBM as
+structure-of-arrays tensors and exposes the ``phd_mesh`` C structure pointing at them.
+``DeviceClock`` is the device-side ``phd_clock`` (time step, time, CFL accumulator,
+status bits).  All arithmetic happens in ``libphdflux.so``.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+F64 = torch.float64
+
+
+def _dev(device):
+    d = torch.device(device)
+    if d.type != "cuda":
+        raise RuntimeError("phd_code_gb300 runs on CUDA devices only (got %s)" % d)
+    return d
+
+
+class DeviceMesh:
+    """One tessellation in HBM (cells real-then-ghost, faces, CSR neighbour lists)."""
+
+    def __init__(self, host, device="cuda", stream=None):
+        dev = _dev(device)
+        self.device = dev
+        self.host = host
+        self.dim = host.dim
+        self.n_cells = host.n_cells
+        self.n_real = host.n_real
+        self.n_faces = host.n_faces
+        self.boundary = host.boundary
+        self.xmin = tuple(host.xmin)
+        self.xmax = tuple(host.xmax)
+
+        def up(a, dt):
+            return torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(dev, non_blocking=False)
+
+        self.tag = up(host.tag, np.int8)
+        self.type = up(host.type, np.int8)
+        self.map = up(host.map, np.int32)
+        self.x = up(host.x, np.float64)
+        self.dcom = up(host.dcom, np.float64)
+        self.vol = up(host.vol, np.float64)
+        self.pair_i = up(host.pair_i, np.int32)
+        self.pair_j = up(host.pair_j, np.int32)
+        self.area = up(host.area, np.float64)
+        self.com = up(host.com, np.float64)
+        self.normal = up(host.normal, np.float64)
+        self.nbr_ptr = up(host.nbr_ptr, np.int32)
+        self.nbr_idx = up(host.nbr_idx, np.int32)
+        self.flip = torch.zeros(self.n_cells, dtype=torch.int8, device=dev)
+        xmin = (C.c_double * 3)(*(list(self.xmin) + [0.0] * (3 - self.dim)))
+        xmax = (C.c_double * 3)(*(list(self.xmax) + [0.0] * (3 - self.dim)))
+        L.check(L.lib().phd_flip_mask(self.dim, self.n_cells, L.ptr(self.type), L.ptr(self.x),
+                                      xmin, xmax, int(self.boundary == "reflective"),
+                                      L.ptr(self.flip), L.stream_handle(stream)), "phd_flip_mask")
+        s = L.PhdMesh()
+        s.dim, s.n_cells, s.n_real, s.n_faces = self.dim, self.n_cells, self.n_real, self.n_faces
+        for name in ("tag", "map", "flip", "x", "dcom", "vol", "pair_i", "pair_j", "area", "com",
+                     "normal", "nbr_ptr", "nbr_idx"):
+            setattr(s, name, getattr(self, name).data_ptr())
+        self.struct = s
+        self.ref = C.byref(s)
+
+    def h2d_bytes(self):
+        """Bytes of one mesh upload (the per-step host->device face list and geometry)."""
+        ts = (self.tag, self.type, self.map, self.x, self.dcom, self.vol, self.pair_i, self.pair_j,
+              self.area, self.com, self.normal, self.nbr_ptr, self.nbr_idx)
+        return sum(t.numel() * t.element_size() for t in ts)
+
+
+class DeviceClock:
+    """Device ``phd_clock``: dt, t, t_end, CFL accumulator and status bits."""
+
+    def __init__(self, device="cuda", dt=0.0, t=0.0, t_end=0.0):
+        self.device = _dev(device)
+        self.buf = torch.zeros(L.CLOCK_BYTES, dtype=torch.uint8, device=self.device)
+        self.set(dt=dt, t=t, t_end=t_end)
+
+    def set(self, dt=0.0, t=0.0, t_end=0.0, status=0, step=0):
+        c = L.PhdClock()
+        c.dt, c.t, c.t_end, c.dt_hydro = dt, t, t_end, 0.0
+        c.dtmin_bits = np.float64(np.inf).view(np.uint64).item()
+        c.arrive, c.status, c.step = 0, status, step
+        host = torch.frombuffer(bytearray(bytes(c)), dtype=torch.uint8)
+        self.buf.copy_(host)
+
+    def read(self):
+        """Copy the clock back to the host (synchronises the current stream)."""
+        raw = self.buf.cpu().numpy().tobytes()
+        return L.PhdClock.from_buffer_copy(raw)
+
+    @property
+    def ptr(self):
+        return C.c_void_p(self.buf.data_ptr())
+
+    def check_status(self):
+        st = self.read().status
+        L.raise_status(st)
+        return st
+
+
+def make_params(gamma=1.4, cfl=0.5, eta=0.25, reconstruction="linear", limiter="arepo",
+                gizmo=True, solver="hllc", boost=True, regularize=True, exact_max_iter=1000):
+    p = L.PhdParams()
+    p.gamma, p.cfl, p.eta = float(gamma), float(cfl), float(eta)
+    p.reconstruction = L.LINEAR if reconstruction in ("linear", L.LINEAR) else L.CONSTANT
+    p.limiter = {"arepo": L.LIMITER_AREPO, "tess": L.LIMITER_TESS}.get(limiter, limiter)
+    p.gizmo = int(bool(gizmo))
+    p.solver = {"hll": L.HLL, "hllc": L.HLLC, "exact": L.EXACT}.get(solver, solver)
+    p.boost = 1 if p.solver == L.EXACT else int(bool(boost))
+    p.regularize = int(bool(regularize))
+    p.exact_max_iter = int(exact_max_iter)
+    return p

@@ -1,0 +1,147 @@
+"""Fused device step of the flux path, with optional CUDA-graph replay.
+
+``FluxStepper`` keeps one mesh and one state resident in HBM and advances it by whole
+steps, each a short fixed sequence of kernel launches that needs no host round trip:
+the time step lives on the device (``phd_clock``), is produced by the CFL reduction at
+the end of each step and consumed by the next one.  The step follows
+``MovingMeshMUSCLHancock.evolve_timestep`` (``integrate.py:385-428``) up to the host
+re-mesh, or ``StaticMeshMUSCLHancock.evolve_timestep`` (``integrate.py:349-378``).
+
+Precision ``"fp64"`` is the parity mode (reference arithmetic); ``"fp32"`` runs
+reconstruction and Riemann fluxes in FP32 with FP64 conserved-state accumulation.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .device import DeviceClock, DeviceMesh, make_params
+from .twins import periodic_twins
+
+
+class FluxStepper:
+    def __init__(self, mesh, prim, gamma=1.4, cfl=0.5, solver="hllc", reconstruction="linear",
+                 limiter="arepo", gizmo=True, boost=True, moving=True, regularize=True, eta=0.25,
+                 precision="fp64", t_end=0.0, face_velocity=None, device="cuda", stream=None,
+                 dedup_periodic=True):
+        self.device = torch.device(device)
+        self.dmesh = mesh if isinstance(mesh, DeviceMesh) else DeviceMesh(mesh, device=self.device)
+        dm = self.dmesh
+        self.params = make_params(gamma=gamma, cfl=cfl, eta=eta, reconstruction=reconstruction,
+                                  limiter=limiter, gizmo=gizmo, solver=solver, boost=boost,
+                                  regularize=regularize)
+        self.moving = bool(moving)
+        if precision not in ("fp64", "fp32"):
+            raise ValueError("precision must be 'fp64' or 'fp32'")
+        self.precision = precision
+        self.stream = stream
+        n, F, d = dm.n_cells, dm.n_faces, dm.dim
+        nf = d + 2
+        dev = self.device
+        f64 = torch.float64
+        self.prim = torch.as_tensor(np.ascontiguousarray(prim, dtype=np.float64)).to(dev).contiguous()
+        if tuple(self.prim.shape) != (nf, n):
+            raise ValueError("prim must be [%d][%d]" % (nf, n))
+        self.cons = torch.empty((nf, n), dtype=f64, device=dev)
+        self.cons_next = torch.empty((nf, n), dtype=f64, device=dev)
+        self.clock = DeviceClock(dev, t_end=t_end)
+        self._graph = None
+        self._graph_steps = 0
+        s = L.stream_handle(stream)
+        lib = L.lib()
+        L.check(lib.phd_cons_from_prim_f64(d, n, self.params.gamma, L.ptr(dm.vol), L.ptr(self.prim),
+                                           L.ptr(self.cons), s), "phd_cons_from_prim_f64")
+        if precision == "fp64":
+            self.grad = torch.zeros((nf * d, n), dtype=f64, device=dev)
+            self.w = torch.zeros((d, n), dtype=f64, device=dev)
+            if face_velocity is None:
+                self.face_w = torch.zeros((d, F), dtype=f64, device=dev)
+            else:
+                self.face_w = torch.as_tensor(np.ascontiguousarray(face_velocity, dtype=np.float64)).to(dev)
+            self.flux = torch.zeros((nf, max(F, 1)), dtype=f64, device=dev)
+            self.initial_time_step()
+        else:
+            if face_velocity is not None:
+                raise ValueError("fp32 steps form face velocities on the device (moving=True)")
+            f32 = torch.float32
+            self.twin = torch.as_tensor(periodic_twins(dm.host) if dedup_periodic else
+                                        np.full(F, -1, np.int32)).to(dev)
+            self.face_geo = torch.zeros((max(F, 1), 4), dtype=f32, device=dev)
+            self.face_ar = torch.zeros((max(F, 1), 2), dtype=f32, device=dev)
+            self.csr_face = torch.zeros(max(2 * F, 1), dtype=torch.int32, device=dev)
+            self.csr_nbr = torch.zeros(max(2 * F, 1), dtype=torch.int32, device=dev)
+            self.cell_geo = torch.zeros((n, 4), dtype=f32, device=dev)
+            out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
+                                                            self.csr_nbr, self.cell_geo)))
+            L.check(lib.phd_prepare_f32(dm.ref, L.ptr(self.twin), ctypes.byref(out), s), "phd_prepare_f32")
+            self.geo = L.PhdGeom32(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
+                                                              self.csr_nbr, self.cell_geo)))
+            self.prim4 = torch.zeros((n, 4), dtype=f32, device=dev)
+            self.grad8 = torch.zeros((n, 8), dtype=f32, device=dev)
+            self.w2 = torch.zeros((n, 2), dtype=f32, device=dev)
+            self.flux4 = torch.zeros((max(F, 1), 4), dtype=f32, device=dev)
+            L.check(lib.phd_prim_f32(dm.ref, ctypes.byref(self.params), L.ptr(self.cons), L.ptr(self.prim4),
+                                     self.clock.ptr, s), "phd_prim_f32")
+
+    # ------------------------------------------------------------------------------
+    def initial_time_step(self):
+        """dt for the first step from the current primitives (riemann.pyx:120-188)."""
+        p = self.params
+        L.check(L.lib().phd_time_step_f64(self.dmesh.ref, L.ptr(self.prim), p.gamma, p.cfl, p.boost, 0,
+                                          self.clock.ptr, L.stream_handle(self.stream)), "phd_time_step_f64")
+
+    def _launch_step(self):
+        dm, p = self.dmesh, self.params
+        s = L.stream_handle(self.stream)
+        if self.precision == "fp64":
+            rc = L.lib().phd_step_f64(dm.ref, ctypes.byref(p), int(self.moving), L.ptr(self.prim),
+                                      L.ptr(self.cons), L.ptr(self.cons_next), L.ptr(self.grad), L.ptr(self.w),
+                                      L.ptr(self.face_w), L.ptr(self.flux), self.clock.ptr, s)
+        else:
+            rc = L.lib().phd_step_f32(dm.ref, ctypes.byref(self.geo), ctypes.byref(p), int(self.moving),
+                                      L.ptr(self.prim4), L.ptr(self.cons), L.ptr(self.cons_next),
+                                      L.ptr(self.grad8), L.ptr(self.w2), L.ptr(self.flux4), self.clock.ptr, s)
+        L.check(rc, "phd_step_" + self.precision)
+        self.cons, self.cons_next = self.cons_next, self.cons
+
+    def step(self, n=1):
+        """Launch n steps (asynchronous; read the clock or state to synchronise)."""
+        for _ in range(n):
+            self._launch_step()
+
+    def capture(self, n_steps=2):
+        """Record n_steps (even, so the double-buffered conserved state returns to the
+        same buffer) into a CUDA graph; replay() then launches them as one unit."""
+        if n_steps % 2:
+            raise ValueError("capture an even number of steps")
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        cap_stream = torch.cuda.Stream(self.device)
+        saved = self.stream
+        with torch.cuda.graph(g, stream=cap_stream):
+            self.stream = cap_stream
+            for _ in range(n_steps):
+                self._launch_step()
+        self.stream = saved
+        self._graph = g
+        self._graph_steps = n_steps
+        return g
+
+    def replay(self):
+        self._graph.replay()
+
+    # ------------------------------------------------------------------------------
+    def read_clock(self):
+        return self.clock.read()
+
+    def check_status(self):
+        return self.clock.check_status()
+
+    def prim_host(self):
+        if self.precision == "fp32":
+            return self.prim4.double().t().contiguous().cpu().numpy()
+        return self.prim.double().cpu().numpy()
+
+    def cons_host(self):
+        return self.cons.double().cpu().numpy()
