@@ -223,6 +223,28 @@ int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_p
                         float *grad8, float *w2, float *flux4, phd_clock *clk,
                         cudaStream_t stream, cudaEvent_t *marks);
 
+/* ---- adjoint of one FP64 step ----------------------------------------------------
+ * Reverse mode of U' = step(U) with the mesh, the face velocities and dt held fixed
+ * (HLL / HLLC, constant or linear reconstruction, both limiters).  Index tables:
+ *   partner [2F]          for each nbr_idx entry, the entry of the same face in the
+ *                         other cell's list
+ *   ghost_ptr [n_real+1], ghost_idx: the ghosts of each real cell (CSR by image).
+ * Inputs: cons [4][n_cells] (ghost columns refreshed), prim and grad of that state
+ * (as phd_prim_from_cons_f64 / phd_gradients_f64 produce them), face_w, dt, and
+ * lam_next = dLoss/dU' [4][n_cells] (real columns).  Output lam = dLoss/dU (ghost
+ * columns zero).  work: phd_adjoint_work_doubles(n_cells, n_faces) doubles. */
+typedef struct phd_adj_index {
+    const int32_t *partner;
+    const int32_t *ghost_ptr;
+    const int32_t *ghost_idx;
+} phd_adj_index;
+
+size_t phd_adjoint_work_doubles(int32_t n_cells, int32_t n_faces);
+int phd_adjoint_step_f64(const phd_mesh *mesh, const phd_adj_index *index, const phd_params *par,
+                         double dt, const double *cons, const double *prim, const double *grad,
+                         const double *face_w, const double *lam_next, double *lam, double *work,
+                         cudaStream_t stream);
+
 /* ---- utilities ------------------------------------------------------------------ */
 
 /* Reflective flip bits from ghost positions (boundary.pyx:287-307): bit k set when

@@ -54,6 +54,10 @@ class PhdGeom32(C.Structure):
                 ("csr_nbr", C.c_void_p), ("cell_geo", C.c_void_p)]
 
 
+class PhdAdjIndex(C.Structure):
+    _fields_ = [("partner", C.c_void_p), ("ghost_ptr", C.c_void_p), ("ghost_idx", C.c_void_p)]
+
+
 class PhdGeom32Out(C.Structure):
     _fields_ = PhdGeom32._fields_
 
@@ -87,6 +91,9 @@ SIGNATURES = {
     "phd_prepare_f32": ([_PM, _vp, C.POINTER(PhdGeom32Out), _vp], C.c_int),
     "phd_prim_f32": ([_PM, _PP, _vp, _vp, _vp, _vp], C.c_int),
     "phd_step_f32": ([_PM, _PG, _PP, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], C.c_int),
+    "phd_adjoint_work_doubles": ([_i32, _i32], C.c_size_t),
+    "phd_adjoint_step_f64": ([_PM, C.POINTER(PhdAdjIndex), _PP, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+                             C.c_int),
     "phd_flip_mask": ([_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp, _vp], C.c_int),
     "phd_hilbert_keys_2d": ([_i32, _vp, _f64, _f64, _f64, _i32, _vp, _vp], C.c_int),
 }

@@ -6,7 +6,9 @@ shared library exporting the C ABI of ``include/phdflux.h``:
 * ``phd_f64.cu``  FP64 stage kernels and fused step, ``--fmad=false`` so products and
   sums round like the reference's Cython arithmetic;
 * ``phd_f32.cu``  FP32 reconstruction / Riemann with FP64 accumulation (FMA allowed);
-* ``phd_util.cu`` mesh-preparation kernels.
+* ``phd_util.cu`` mesh-preparation kernels;
+* ``phd_adj.cu``  hand-written adjoint of the FP64 step, ``--fmad=false`` so its
+  recomputed forward branches are those of the forward kernels.
 
 Usage: ``python phd-code_gb300/build.py`` (or ``__graft_entry__.build()``).
 """
@@ -28,6 +30,7 @@ UNITS = {
     "phd_f64.cu": ["--fmad=false"],
     "phd_f32.cu": [],
     "phd_util.cu": [],
+    "phd_adj.cu": ["--fmad=false"],
 }
 
 

@@ -1,0 +1,479 @@
+// phd_adjoint.cuh -- hand-written reverse mode of the per-face and per-cell physics.
+//
+// Every function recomputes the forward quantities of its routine (same formulas and
+// branch decisions as phd_physics.cuh / phd_f64.cu) and then propagates adjoints
+// statement by statement in reverse.  Branch decisions (wave-speed estimate,
+// flux region, GIZMO clip, positivity reverts, limiter selections) are held fixed:
+// the derivative of the active branch.  Naming: aX = dLoss/dX.
+#pragma once
+#include "phd_physics.cuh"
+
+namespace phd {
+
+// ---- get_waves (riemann.pyx:375-504) --------------------------------------------
+template <typename T>
+PHD_HD void get_waves_adj(T dl, T ul, T pl, T dr, T ur, T pr, T gamma, T a_sl, T a_sc, T a_sr,
+                              T &a_dl, T &a_ul, T &a_pl, T &a_dr, T &a_ur, T &a_pr) {
+    const T c_floor = T(1.0E-10);
+    const T clr = t_sqrt((gamma * pl) / dl), crr = t_sqrt((gamma * pr) / dr);
+    const bool cl_fl = !(clr >= c_floor), cr_fl = !(crr >= c_floor);
+    const T cl = t_fmax(clr, c_floor), cr = t_fmax(crr, c_floor);
+    const T d_avg = T(.5) * (dl + dr);
+    const T c_avg = T(.5) * (cl + cr);
+    const T pv_raw = (T(.5) * (pl + pr)) + (((T(.5) * (ul - ur)) * d_avg) * c_avg);
+    const T pv = t_fmax(T(0.), pv_raw);
+    const T p_min = t_fmin(pl, pr), p_max = t_fmax(pl, pr);
+    int br;   // 0 PVRS, 1 TRRS, 2 TSRS
+    T p_star = pv;
+    // TRRS intermediates
+    T z = 0, plr = 0, num = 0, den = 0, u_star = 0, A1 = 0, A2 = 0, e = 0;
+    // TSRS intermediates
+    T Al = 0, Ar = 0, Bl = 0, Brr = 0, gl = 0, gr = 0, S = 0;
+    if (((p_max / p_min) < T(2.)) && ((p_min < pv) && (pv < p_max))) {
+        br = 0;
+    } else if (pv <= p_min) {
+        br = 1;
+        z = (gamma - T(1.)) / (T(2.) * gamma);
+        plr = t_pow(pl / pr, z);
+        num = (((plr * ul) / cl) + (ur / cr)) + ((T(2.) * (plr - T(1.))) / (gamma - T(1.)));
+        den = (plr / cl) + (T(1.) / cr);
+        u_star = num / den;
+        A1 = T(1.) + (((gamma - T(1.)) * (ul - u_star)) / (T(2.) * cl));
+        A2 = T(1.) + (((gamma - T(1.)) * (u_star - ur)) / (T(2.) * cr));
+        e = T(1.) / z;
+        p_star = (T(.5) * pl) * t_pow(A1, e);
+        p_star = p_star + ((T(.5) * pr) * t_pow(A2, e));
+    } else {
+        br = 2;
+        Al = T(2.) / ((gamma + T(1.)) * dl);
+        Ar = T(2.) / ((gamma + T(1.)) * dr);
+        Bl = pl * ((gamma - T(1.)) / (gamma + T(1.)));
+        Brr = pr * ((gamma - T(1.)) / (gamma + T(1.)));
+        gl = t_sqrt(Al / (pv + Bl));
+        gr = t_sqrt(Ar / (pv + Brr));
+        S = gl + gr;
+        p_star = (((gl * pl) + (gr * pr)) - (ur - ul)) / S;
+    }
+    const T k = (gamma + T(1.)) / (T(2.) * gamma);
+    const bool l_shock = !(p_star <= pl), r_shock = !(p_star <= pr);
+    T ql = 0, sqlv = 0, qr = 0, sqrv = 0;
+    T sl, sr;
+    if (!l_shock) sl = ul - cl;
+    else { ql = T(1.) + (k * ((p_star / pl) - T(1.))); sqlv = t_sqrt(ql); sl = ul - (cl * sqlv); }
+    if (!r_shock) sr = ur + cr;
+    else { qr = T(1.) + (k * ((p_star / pr) - T(1.))); sqrv = t_sqrt(qr); sr = ur + (cr * sqrv); }
+    const T N = (((pr - pl) + ((dl * ul) * (sl - ul))) - ((dr * ur) * (sr - ur)));
+    const T D = ((dl * (sl - ul)) - (dr * (sr - ur)));
+    const T sc = N / D;
+
+    // ---- reverse ----
+    T aN = a_sc / D, aD = -a_sc * sc / D;
+    T asl = a_sl, asr = a_sr, acl = 0, acr = 0, aps = 0;
+    a_pr += aN;
+    a_pl -= aN;
+    a_dl += aN * ul * (sl - ul) + aD * (sl - ul);
+    a_ul += aN * dl * (sl - T(2.) * ul) - aD * dl;
+    asl += aN * dl * ul + aD * dl;
+    a_dr += -aN * ur * (sr - ur) - aD * (sr - ur);
+    a_ur += -aN * dr * (sr - T(2.) * ur) + aD * dr;
+    asr += -aN * dr * ur - aD * dr;
+    // sl
+    a_ul += asl;
+    if (!l_shock) acl -= asl;
+    else {
+        acl -= sqlv * asl;
+        const T aq = (-cl * asl) / (T(2.) * sqlv);
+        aps += aq * k / pl;
+        a_pl -= aq * k * p_star / (pl * pl);
+    }
+    a_ur += asr;
+    if (!r_shock) acr += asr;
+    else {
+        acr += sqrv * asr;
+        const T aq = (cr * asr) / (T(2.) * sqrv);
+        aps += aq * k / pr;
+        a_pr -= aq * k * p_star / (pr * pr);
+    }
+    // p_star
+    T apv = 0;
+    if (br == 0) {
+        apv += aps;
+    } else if (br == 1) {
+        const T hA1e = T(.5) * t_pow(A1, e), hA2e = T(.5) * t_pow(A2, e);
+        a_pl += hA1e * aps;
+        a_pr += hA2e * aps;
+        const T aA1 = T(.5) * pl * e * t_pow(A1, e - T(1.)) * aps;
+        const T aA2 = T(.5) * pr * e * t_pow(A2, e - T(1.)) * aps;
+        const T g1 = gamma - T(1.);
+        T aus = 0;
+        a_ul += aA1 * g1 / (T(2.) * cl);
+        aus -= aA1 * g1 / (T(2.) * cl);
+        acl -= aA1 * g1 * (ul - u_star) / (T(2.) * cl * cl);
+        aus += aA2 * g1 / (T(2.) * cr);
+        a_ur -= aA2 * g1 / (T(2.) * cr);
+        acr -= aA2 * g1 * (u_star - ur) / (T(2.) * cr * cr);
+        const T anum = aus / den, aden = -aus * u_star / den;
+        T aplr = anum * (ul / cl + T(2.) / g1) + aden / cl;
+        a_ul += anum * plr / cl;
+        acl -= anum * plr * ul / (cl * cl) + aden * plr / (cl * cl);
+        a_ur += anum / cr;
+        acr -= anum * ur / (cr * cr) + aden / (cr * cr);
+        a_pl += aplr * z * plr / pl;
+        a_pr -= aplr * z * plr / pr;
+    } else {
+        const T aNn = aps / S, aS = -aps * p_star / S;
+        const T agl = aNn * pl + aS, agr = aNn * pr + aS;
+        a_pl += aNn * gl;
+        a_pr += aNn * gr;
+        a_ur -= aNn;
+        a_ul += aNn;
+        const T dnl = pv + Bl, dnr = pv + Brr;
+        const T ahl = agl / (T(2.) * gl), ahr = agr / (T(2.) * gr);
+        const T aAl = ahl / dnl, aAr = ahr / dnr;
+        apv -= ahl * Al / (dnl * dnl) + ahr * Ar / (dnr * dnr);
+        const T aBl = -ahl * Al / (dnl * dnl), aBr = -ahr * Ar / (dnr * dnr);
+        a_dl -= aAl * Al / dl;
+        a_dr -= aAr * Ar / dr;
+        a_pl += aBl * ((gamma - T(1.)) / (gamma + T(1.)));
+        a_pr += aBr * ((gamma - T(1.)) / (gamma + T(1.)));
+    }
+    if (pv_raw > T(0.)) {
+        a_pl += T(.5) * apv;
+        a_pr += T(.5) * apv;
+        a_ul += T(.5) * d_avg * c_avg * apv;
+        a_ur -= T(.5) * d_avg * c_avg * apv;
+        const T ada = T(.5) * (ul - ur) * c_avg * apv, aca = T(.5) * (ul - ur) * d_avg * apv;
+        a_dl += T(.5) * ada;
+        a_dr += T(.5) * ada;
+        acl += T(.5) * aca;
+        acr += T(.5) * aca;
+    }
+    if (!cl_fl) {
+        a_pl += acl * gamma / (T(2.) * cl * dl);
+        a_dl -= acl * cl / (T(2.) * dl);
+    }
+    if (!cr_fl) {
+        a_pr += acr * gamma / (T(2.) * cr * dr);
+        a_dr -= acr * cr / (T(2.) * dr);
+    }
+}
+
+// Adjoint of the left / right data flux  F = (d u, d v_k u + p n_k, E u + p Vn),
+// u = Vn - wn, E = d v^2 / 2 + p/(gamma-1).
+template <typename T>
+PHD_HD __forceinline__ void data_flux_adj(T d, const T *v, T p, T Vn, T v2, const T *n, T wn, T gamma,
+                                              const T *aF, T &ad, T *av, T &ap, T &aVn, T &av2) {
+    const T u = Vn - wn;
+    const T E = (T(0.5) * d) * v2 + p / (gamma - T(1.));
+    ad += aF[0] * u + (aF[1] * v[0] + aF[2] * v[1]) * u + aF[3] * T(0.5) * v2 * u;
+    const T au = aF[0] * d + (aF[1] * v[0] + aF[2] * v[1]) * d + aF[3] * E;
+    aVn += au + aF[3] * p;
+    av[0] += aF[1] * d * u;
+    av[1] += aF[2] * d * u;
+    ap += aF[1] * n[0] + aF[2] * n[1] + aF[3] * (u / (gamma - T(1.)) + Vn);
+    av2 += aF[3] * T(0.5) * d * u;
+}
+
+// Adjoint of the HLLC star-state flux of one side (riemann.pyx:636-670):
+// (d, v, p, Vn, v2, s = this side's wave speed) ; sc contact speed.
+template <typename T>
+PHD_HD __forceinline__ void star_flux_adj(T d, const T *v, T p, T Vn, T v2, T s, T sc, const T *n, T wn,
+                                              T gamma, const T *aF, T &ad, T *av, T &ap, T &aVn, T &av2, T &as,
+                                              T &asc) {
+    const T a = s - Vn, b = s - sc;
+    const T f1 = (d * a) / b;
+    const T f2 = ((f1 * (s - wn)) * (sc - Vn)) + p;
+    const T frho = (d * (Vn - s)) + (f1 * (s - wn));
+    const T el = ((T(0.5) * d) * v2) + (p / (gamma - T(1.0)));
+    const T t = p / (d * a);
+    const T Q = (el / d) + ((sc - Vn) * (sc + t));
+    (void)f2;
+    const T afrho = aF[0] + aF[1] * v[0] + aF[2] * v[1];
+    av[0] += aF[1] * frho;
+    av[1] += aF[2] * frho;
+    const T af2 = aF[1] * n[0] + aF[2] * n[1];
+    // fe = (el + p) Vn - s el + (s - wn) f1 Q
+    T ael = aF[3] * (Vn - s);
+    ap += aF[3] * Vn;
+    aVn += aF[3] * (el + p);
+    as += aF[3] * (-el + f1 * Q);
+    T af1 = aF[3] * (s - wn) * Q;
+    const T aQ = aF[3] * (s - wn) * f1;
+    // Q = el/d + (sc - Vn)(sc + t)
+    ael += aQ / d;
+    ad -= aQ * el / (d * d);
+    asc += aQ * (sc + t) + aQ * (sc - Vn);
+    aVn -= aQ * (sc + t);
+    const T at = aQ * (sc - Vn);
+    T aa = 0;
+    ap += at / (d * a);
+    ad -= at * t / d;
+    aa -= at * t / a;
+    // frho = d (Vn - s) + f1 (s - wn)
+    ad += afrho * (Vn - s);
+    aVn += afrho * d;
+    as += afrho * (-d + f1);
+    af1 += afrho * (s - wn);
+    // f2 = f1 (s - wn)(sc - Vn) + p
+    af1 += af2 * (s - wn) * (sc - Vn);
+    as += af2 * f1 * (sc - Vn);
+    asc += af2 * f1 * (s - wn);
+    aVn -= af2 * f1 * (s - wn);
+    ap += af2;
+    // f1 = d a / b
+    ad += af1 * a / b;
+    aa += af1 * d / b;
+    const T ab = -af1 * f1 / b;
+    as += aa + ab;
+    aVn -= aa;
+    asc -= ab;
+    // el
+    ad += ael * T(0.5) * v2;
+    av2 += ael * T(0.5) * d;
+    ap += ael / (gamma - T(1.0));
+}
+
+// Adjoint of hll_family (HLL / HLLC + deboost), 2D.  aF: adjoint of the (deboosted)
+// flux; accumulates into aL, aR.
+template <typename T>
+PHD_HD void hll_family_adj(bool hllc, const T *L, const T *R, const T *n, const T *w, T gamma, bool boost,
+                               const T *aFin, T *aL, T *aR) {
+    const T _dl = L[0], _pl = L[3], _dr = R[0], _pr = R[3];
+    const T vl[2] = {L[1], L[2]}, vr[2] = {R[1], R[2]};
+    T Vnl = T(0.0), Vnr = T(0.0), vl_sq = T(0.0), vr_sq = T(0.0), wn = T(0.0);
+    for (int k = 0; k < 2; k++) {
+        vl_sq = vl_sq + vl[k] * vl[k];
+        vr_sq = vr_sq + vr[k] * vr[k];
+        Vnl = Vnl + vl[k] * n[k];
+        Vnr = Vnr + vr[k] * n[k];
+        wn = wn + w[k] * n[k];
+    }
+    if (boost) wn = T(0.);
+    T sl, sc, sr;
+    get_waves<T>(_dl, Vnl, _pl, _dr, Vnr, _pr, gamma, sl, sc, sr);
+    // deboost reverse
+    T aF[4] = {aFin[0], aFin[1], aFin[2], aFin[3]};
+    if (boost) {
+        aF[0] = aFin[0] + w[0] * aFin[1] + w[1] * aFin[2] + T(0.5) * (w[0] * w[0] + w[1] * w[1]) * aFin[3];
+        aF[1] = aFin[1] + w[0] * aFin[3];
+        aF[2] = aFin[2] + w[1] * aFin[3];
+        aF[3] = aFin[3];
+    }
+    T adl = 0, apl = 0, aVnl = 0, avl2 = 0, adr = 0, apr = 0, aVnr = 0, avr2 = 0;
+    T avl[2] = {0, 0}, avr[2] = {0, 0};
+    T asl = 0, asc = 0, asr = 0;
+    if (wn <= sl) {
+        data_flux_adj<T>(_dl, vl, _pl, Vnl, vl_sq, n, wn, gamma, aF, adl, avl, apl, aVnl, avl2);
+    } else if ((sl < wn) && (wn <= sr)) {
+        if (!hllc) {
+            const T fac1 = sr - wn, fac2 = sl - wn, fac3 = sr - sl;
+            const T el = ((T(0.5) * _dl) * vl_sq) + (_pl / (gamma - T(1.0)));
+            const T er = ((T(0.5) * _dr) * vr_sq) + (_pr / (gamma - T(1.0)));
+            T f[4];
+            f[0] = (((((_dl * Vnl) * fac1) - ((_dr * Vnr) * fac2)) - ((sl * _dl) * fac1)) + ((sr * _dr) * fac2)) / fac3;
+            for (int k = 0; k < 2; k++)
+                f[1 + k] = ((((((((_dl * vl[k]) * Vnl) + (_pl * n[k])) * fac1) - ((((_dr * vr[k]) * Vnr) + (_pr * n[k])) * fac2)) -
+                             ((sl * (_dl * vl[k])) * fac1)) + ((sr * (_dr * vr[k])) * fac2))) / fac3;
+            f[3] = ((((((el + _pl) * Vnl) * fac1) - (((er + _pr) * Vnr) * fac2)) - ((sl * el) * fac1)) + ((sr * er) * fac2)) / fac3;
+            T af1 = 0, af2 = 0, af3 = 0;
+            for (int q = 0; q < 4; q++) af3 -= aF[q] * f[q] / fac3;
+            const T aNm = aF[0] / fac3;
+            adl += aNm * fac1 * (Vnl - sl);
+            aVnl += aNm * _dl * fac1;
+            af1 += aNm * _dl * (Vnl - sl);
+            adr += aNm * fac2 * (sr - Vnr);
+            aVnr -= aNm * _dr * fac2;
+            af2 += aNm * _dr * (sr - Vnr);
+            asl -= aNm * _dl * fac1;
+            asr += aNm * _dr * fac2;
+            for (int k = 0; k < 2; k++) {
+                const T aNk = aF[1 + k] / fac3;
+                adl += aNk * vl[k] * fac1 * (Vnl - sl);
+                avl[k] += aNk * _dl * fac1 * (Vnl - sl);
+                aVnl += aNk * _dl * vl[k] * fac1;
+                apl += aNk * n[k] * fac1;
+                af1 += aNk * (_dl * vl[k] * Vnl + _pl * n[k] - sl * _dl * vl[k]);
+                adr += aNk * vr[k] * fac2 * (sr - Vnr);
+                avr[k] += aNk * _dr * fac2 * (sr - Vnr);
+                aVnr -= aNk * _dr * vr[k] * fac2;
+                apr -= aNk * n[k] * fac2;
+                af2 += aNk * (-(_dr * vr[k] * Vnr + _pr * n[k]) + sr * _dr * vr[k]);
+                asl -= aNk * _dl * vl[k] * fac1;
+                asr += aNk * _dr * vr[k] * fac2;
+            }
+            const T aNe = aF[3] / fac3;
+            const T ael = aNe * fac1 * (Vnl - sl);
+            apl += aNe * Vnl * fac1;
+            aVnl += aNe * (el + _pl) * fac1;
+            af1 += aNe * ((el + _pl) * Vnl - sl * el);
+            const T aer = aNe * fac2 * (sr - Vnr);
+            apr -= aNe * Vnr * fac2;
+            aVnr -= aNe * (er + _pr) * fac2;
+            af2 += aNe * (-(er + _pr) * Vnr + sr * er);
+            asl -= aNe * el * fac1;
+            asr += aNe * er * fac2;
+            adl += ael * T(0.5) * vl_sq;
+            avl2 += ael * T(0.5) * _dl;
+            apl += ael / (gamma - T(1.0));
+            adr += aer * T(0.5) * vr_sq;
+            avr2 += aer * T(0.5) * _dr;
+            apr += aer / (gamma - T(1.0));
+            asr += af1 + af3;
+            asl += af2 - af3;
+        } else if (wn <= sc) {
+            star_flux_adj<T>(_dl, vl, _pl, Vnl, vl_sq, sl, sc, n, wn, gamma, aF, adl, avl, apl, aVnl, avl2, asl, asc);
+        } else {
+            star_flux_adj<T>(_dr, vr, _pr, Vnr, vr_sq, sr, sc, n, wn, gamma, aF, adr, avr, apr, aVnr, avr2, asr, asc);
+        }
+    } else {
+        data_flux_adj<T>(_dr, vr, _pr, Vnr, vr_sq, n, wn, gamma, aF, adr, avr, apr, aVnr, avr2);
+    }
+    if (asl != T(0) || asc != T(0) || asr != T(0))
+        get_waves_adj<T>(_dl, Vnl, _pl, _dr, Vnr, _pr, gamma, asl, asc, asr, adl, aVnl, apl, adr, aVnr, apr);
+    aL[0] += adl;
+    aL[3] += apl;
+    aR[0] += adr;
+    aR[3] += apr;
+    for (int k = 0; k < 2; k++) {
+        aL[1 + k] += avl[k] + aVnl * n[k] + T(2.) * vl[k] * avl2;
+        aR[1 + k] += avr[k] + aVnr * n[k] + T(2.) * vr[k] * avr2;
+    }
+}
+
+// Adjoint of the GIZMO pair limit of one field (gizmo_pair in phd_physics.cuh).
+// Returns adjoints of (sl, sr, xl, xr) given adjoints of the limited (xl, xr).
+template <typename T>
+PHD_HD __forceinline__ void gizmo_pair_adj(T sl, T sr, T ci, T cj, T smi, T smj, T dm, T xl, T xr, T axl_out,
+                                               T axr_out, T &asl, T &asr, T &axl, T &axr) {
+    const T diff = sl - sr;
+    const T sgn = diff > T(0) ? T(1) : (diff < T(0) ? T(-1) : T(0));
+    const T delta1 = T(0.5) * t_fabs(diff), delta2 = T(0.25) * t_fabs(diff);
+    const bool a_is_min = !(sr < sl);          // fmin(sl, sr) -> sl when sl <= sr
+    const T phi_min = t_fmin(sl, sr), phi_max = t_fmax(sl, sr);
+    const T si = smi / dm, sj = smj / dm;
+    const T phibar_l = sl + si * (sr - sl), phibar_r = sr + sj * (sl - sr);
+    const bool plus_lin = ((phi_max + delta1) * phi_max) >= T(0.);
+    const bool minus_lin = ((phi_min - delta1) * phi_min) >= T(0.);
+    const T phi_plus = plus_lin ? phi_max + delta1 : phi_max / (T(1) + (delta1 / t_fabs(phi_max)));
+    const T phi_minus = minus_lin ? phi_min - delta1 : phi_min / (T(1) + (delta1 / t_fabs(phi_min)));
+    T a_pp = 0, a_pm = 0, a_bl = 0, a_br = 0, a_d2 = 0;
+    if (ci < cj) {
+        // xl = max(phi_minus, min(bl + d2, x)); xr = min(phi_plus, max(br - d2, y))
+        const T inner = t_fmin(phibar_l + delta2, xl);
+        if (phi_minus >= inner) a_pm += axl_out;
+        else if (phibar_l + delta2 <= xl) { a_bl += axl_out; a_d2 += axl_out; }
+        else axl += axl_out;
+        const T inr = t_fmax(phibar_r - delta2, xr);
+        if (phi_plus <= inr) a_pp += axr_out;
+        else if (phibar_r - delta2 >= xr) { a_br += axr_out; a_d2 -= axr_out; }
+        else axr += axr_out;
+    } else if (ci > cj) {
+        // xl = min(phi_plus, max(bl - d2, x)); xr = max(phi_minus, min(br + d2, y))
+        const T inner = t_fmax(phibar_l - delta2, xl);
+        if (phi_plus <= inner) a_pp += axl_out;
+        else if (phibar_l - delta2 >= xl) { a_bl += axl_out; a_d2 -= axl_out; }
+        else axl += axl_out;
+        const T inr = t_fmin(phibar_r + delta2, xr);
+        if (phi_minus >= inr) a_pm += axr_out;
+        else if (phibar_r + delta2 <= xr) { a_br += axr_out; a_d2 += axr_out; }
+        else axr += axr_out;
+    } else {
+        asl += axl_out;
+        asr += axr_out;
+        return;
+    }
+    T a_d1 = 0, a_pmax = 0, a_pmin = 0;
+    if (plus_lin) { a_pmax += a_pp; a_d1 += a_pp; }
+    else {
+        const T q = T(1) + delta1 / t_fabs(phi_max);
+        a_pmax += a_pp * (T(1) / q + delta1 / (q * q * t_fabs(phi_max)));
+        const T sg = phi_max > T(0) ? T(1) : T(-1);
+        a_d1 -= a_pp * sg / (q * q);
+    }
+    if (minus_lin) { a_pmin += a_pm; a_d1 -= a_pm; }
+    else {
+        const T q = T(1) + delta1 / t_fabs(phi_min);
+        a_pmin += a_pm * (T(1) / q + delta1 / (q * q * t_fabs(phi_min)));
+        const T sg = phi_min > T(0) ? T(1) : T(-1);
+        a_d1 -= a_pm * sg / (q * q);
+    }
+    // phibar_l = sl + si (sr - sl); phibar_r = sr + sj (sl - sr)
+    asl += a_bl * (T(1) - si) + a_br * sj;
+    asr += a_bl * si + a_br * (T(1) - sj);
+    // delta1 = |sl - sr| / 2, delta2 = |sl - sr| / 4
+    const T ad = T(0.5) * a_d1 + T(0.25) * a_d2;
+    asl += ad * sgn;
+    asr -= ad * sgn;
+    if (a_is_min) { asl += a_pmin; asr += a_pmax; }
+    else { asr += a_pmin; asl += a_pmax; }
+}
+
+// Adjoint of the 2D temporal extrapolation (temporal<T,2>).  Lin/Rin are the states
+// entering it (spatial result); aL/aR the adjoints of its outputs; accumulates into
+// aLin/aRin and the cell-value / gradient adjoints.
+template <typename T>
+PHD_HD void temporal_adj(const T *Lin, const T *Rin, const T *pi, const T *pj, const T *gi, const T *gj,
+                             const T *w, T gamma, T dt, bool boost, const T *aL, const T *aR, T *aLin, T *aRin,
+                             T *api, T *apj, T *agi, T *agj) {
+    // forward (for the revert decisions)
+    T L[4], R[4];
+    for (int f = 0; f < 4; f++) { L[f] = Lin[f]; R[f] = Rin[f]; }
+    temporal<T, 2>(L, R, pi, pj, gi, gj, w, gamma, dt, boost);
+    // a side reverted to its input exactly when its output equals its input and the
+    // time-extrapolated density or pressure was negative; recompute that test
+    const T *sides_p[2] = {pi, pj};
+    const T *sides_g[2] = {gi, gj};
+    const T *ins[2] = {Lin, Rin};
+    const T *as[2] = {aL, aR};
+    T *ains[2] = {aLin, aRin};
+    T *aps[2] = {api, apj};
+    T *ags[2] = {agi, agj};
+    for (int s = 0; s < 2; s++) {
+        const T *p = sides_p[s];
+        const T *g = sides_g[s];
+        const T *in = ins[s];
+        const T *a = as[s];
+        T *ain = ains[s];
+        T *ap = aps[s];
+        T *ag = ags[s];
+        T v[2];
+        for (int k = 0; k < 2; k++) v[k] = boost ? p[1 + k] - w[k] : p[1 + k];
+        // time-extrapolated density / pressure (same order as temporal<>)
+        T Ld = in[0], Lp = in[3];
+        for (int k = 0; k < 2; k++) {
+            const T div = g[2 + 3 * k];
+            Ld = Ld - (dt * ((p[0] * div) + (v[k] * g[k])));
+            Lp = Lp - (dt * (((gamma * p[3]) * div) + (v[k] * g[6 + k])));
+        }
+        if (Ld < T(0.0) || Lp < T(0.0)) {
+            for (int f = 0; f < 4; f++) ain[f] += a[f];
+            continue;
+        }
+        for (int f = 0; f < 4; f++) ain[f] += a[f];
+        T av[2] = {0, 0};
+        for (int c = 0; c < 2; c++) {
+            const T aVc = a[1 + c];
+            ag[6 + c] -= dt / p[0] * aVc;
+            ap[0] += dt * g[6 + c] / (p[0] * p[0]) * aVc;
+            for (int k = 0; k < 2; k++) {
+                av[k] -= dt * g[2 + 2 * c + k] * aVc;
+                ag[2 + 2 * c + k] -= dt * v[k] * aVc;
+            }
+        }
+        for (int k = 0; k < 2; k++) {
+            const int dk = 2 + 3 * k;
+            ap[0] -= dt * g[dk] * a[0];
+            ag[dk] -= dt * p[0] * a[0];
+            av[k] -= dt * g[k] * a[0];
+            ag[k] -= dt * v[k] * a[0];
+            ap[3] -= dt * gamma * g[dk] * a[3];
+            ag[dk] -= dt * gamma * p[3] * a[3];
+            av[k] -= dt * g[6 + k] * a[3];
+            ag[6 + k] -= dt * v[k] * a[3];
+        }
+        ap[1] += av[0];
+        ap[2] += av[1];
+    }
+}
+
+}  // namespace phd

@@ -7,22 +7,26 @@
 #define PHD_REAL_TAG 0
 #define PHD_EXTERIOR_TYPE 2
 
+#ifndef PHD_HD
+#define PHD_HD __host__ __device__
+#endif
+
 namespace phd {
 
 // Type-generic math so one template body serves the FP64 and FP32 builds.
-__device__ __forceinline__ double t_sqrt(double a) { return sqrt(a); }
-__device__ __forceinline__ float t_sqrt(float a) { return sqrtf(a); }
-__device__ __forceinline__ double t_pow(double a, double b) { return pow(a, b); }
-__device__ __forceinline__ float t_pow(float a, float b) { return powf(a, b); }
-__device__ __forceinline__ double t_fmax(double a, double b) { return fmax(a, b); }
-__device__ __forceinline__ float t_fmax(float a, float b) { return fmaxf(a, b); }
-__device__ __forceinline__ double t_fmin(double a, double b) { return fmin(a, b); }
-__device__ __forceinline__ float t_fmin(float a, float b) { return fminf(a, b); }
-__device__ __forceinline__ double t_fabs(double a) { return fabs(a); }
-__device__ __forceinline__ float t_fabs(float a) { return fabsf(a); }
+PHD_HD __forceinline__ double t_sqrt(double a) { return sqrt(a); }
+PHD_HD __forceinline__ float t_sqrt(float a) { return sqrtf(a); }
+PHD_HD __forceinline__ double t_pow(double a, double b) { return pow(a, b); }
+PHD_HD __forceinline__ float t_pow(float a, float b) { return powf(a, b); }
+PHD_HD __forceinline__ double t_fmax(double a, double b) { return fmax(a, b); }
+PHD_HD __forceinline__ float t_fmax(float a, float b) { return fmaxf(a, b); }
+PHD_HD __forceinline__ double t_fmin(double a, double b) { return fmin(a, b); }
+PHD_HD __forceinline__ float t_fmin(float a, float b) { return fminf(a, b); }
+PHD_HD __forceinline__ double t_fabs(double a) { return fabs(a); }
+PHD_HD __forceinline__ float t_fabs(float a) { return fabsf(a); }
 // x**2 in the reference lowers to libm pow(x, 2.0); pow(x, 2) and x*x agree to 1 ulp.
-__device__ __forceinline__ double t_sq(double a) { return pow(a, 2.0); }
-__device__ __forceinline__ float t_sq(float a) { return a * a; }
+PHD_HD __forceinline__ double t_sq(double a) { return pow(a, 2.0); }
+PHD_HD __forceinline__ float t_sq(float a) { return a * a; }
 
 // Positive doubles order like their bit patterns: min-reduce them as integers.
 __device__ __forceinline__ unsigned long long dbits(double v) {

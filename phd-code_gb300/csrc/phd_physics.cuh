@@ -14,7 +14,7 @@ namespace phd {
 // HLL.get_waves riemann.pyx:375-504 (PVRS guess, TRRS/TSRS switch Q = 2, sound-speed
 // floor 1e-10, Toro eq. 10.68-10.70).
 template <typename T>
-__device__ __forceinline__ void get_waves(T dl, T ul, T pl, T dr, T ur, T pr, T gamma,
+PHD_HD __forceinline__ void get_waves(T dl, T ul, T pl, T dr, T ur, T pr, T gamma,
                                           T &sl, T &sc, T &sr) {
     const T Q = T(2.), c_floor = T(1.0E-10);
     T p_star;
@@ -53,7 +53,7 @@ __device__ __forceinline__ void get_waves(T dl, T ul, T pl, T dr, T ur, T pr, T 
 
 // RiemannBase.deboost riemann.pyx:190-222 (Pakmor & Springel 2011 eq. 17).
 template <typename T, int DIM>
-__device__ __forceinline__ void deboost(const T *w, T *f) {
+PHD_HD __forceinline__ void deboost(const T *w, T *f) {
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
         f[DIM + 1] = f[DIM + 1] + (w[k] * (((T(0.5) * w[k]) * f[0]) + f[1 + k]));
@@ -65,7 +65,7 @@ __device__ __forceinline__ void deboost(const T *w, T *f) {
 // riemann.pyx:521-682 (hllc = true); L/R are face states, n the unit normal, w the
 // face velocity.  Velocities stay in lab axes; only v.n enters the wave structure.
 template <typename T, int DIM>
-__device__ __forceinline__ void hll_family(bool hllc, const T *L, const T *R, const T *n,
+PHD_HD __forceinline__ void hll_family(bool hllc, const T *L, const T *R, const T *n,
                                            const T *w, T gamma, bool boost, T *f) {
     const int E = DIM + 1;
     const T _dl = L[0], _pl = L[E], _dr = R[0], _pr = R[E];
@@ -132,7 +132,7 @@ __device__ __forceinline__ void hll_family(bool hllc, const T *L, const T *R, co
 }
 
 // ---- Exact solver: Newton iteration on p* always in FP64 (riemann.pyx:974-1090) ----
-__device__ __forceinline__ double ex_p_guess(double dl, double ul, double pl, double cl, double dr,
+PHD_HD __forceinline__ double ex_p_guess(double dl, double ul, double pl, double cl, double dr,
                                              double ur, double pr, double cr, double gamma) {
     const double ppv = (.5 * (pl + pr)) - (((.125 * (ur - ul)) * (dl + dr)) * (cl + cr));
     const double p_max = (pr > pl) ? pr : pl;
@@ -152,14 +152,14 @@ __device__ __forceinline__ double ex_p_guess(double dl, double ul, double pl, do
     return (((gl * pl) + (gr * pr)) - (ur - ul)) / (gr + gl);
 }
 
-__device__ __forceinline__ double ex_p_func(double d, double p, double c, double gamma, double p_old) {
+PHD_HD __forceinline__ double ex_p_func(double d, double p, double c, double gamma, double p_old) {
     if (p_old <= p) return ((2. * c) / (gamma - 1.)) * (pow(p_old / p, (gamma - 1.) / (2. * gamma)) - 1.);
     const double Ak = 2. / (d * (gamma + 1.));
     const double Bk = (p * (gamma - 1.)) / (gamma + 1.);
     return (p_old - p) * sqrt(Ak / (p_old + Bk));
 }
 
-__device__ __forceinline__ double ex_p_func_deriv(double d, double p, double c, double gamma, double p_old) {
+PHD_HD __forceinline__ double ex_p_func_deriv(double d, double p, double c, double gamma, double p_old) {
     if (p_old <= p) return pow(p_old / p, ((-(gamma + 1.)) / (2. * gamma))) / (c * d);
     const double Ak = 2. / (d * (gamma + 1.));
     const double Bk = (p * (gamma - 1.)) / (gamma + 1.);
@@ -167,7 +167,7 @@ __device__ __forceinline__ double ex_p_func_deriv(double d, double p, double c, 
 }
 
 // Returns p*; sets *failed when max_iter Newton steps did not converge.
-__device__ __forceinline__ double ex_get_pstar(double dl, double ul, double pl, double cl, double dr,
+PHD_HD __forceinline__ double ex_get_pstar(double dl, double ul, double pl, double cl, double dr,
                                                double ur, double pr, double cr, double gamma,
                                                int max_iter, bool *failed) {
     const double TOL = 1.0e-6;
@@ -189,7 +189,7 @@ __device__ __forceinline__ double ex_get_pstar(double dl, double ul, double pl, 
 // Exact.riemann_solver riemann.pyx:700-972: exact solution sampled at xi = 0 in the
 // face frame, then deboosted (the Exact solver always boosts, riemann.pyx:695-698).
 template <typename T, int DIM>
-__device__ __forceinline__ void exact_flux(const T *L, const T *R, const T *n, const T *w, T gamma,
+PHD_HD __forceinline__ void exact_flux(const T *L, const T *R, const T *n, const T *w, T gamma,
                                            int max_iter, T *f, bool *failed) {
     const int E = DIM + 1;
     const T _dl = L[0], _pl = L[E], _dr = R[0], _pr = R[E];
@@ -297,7 +297,7 @@ __device__ __forceinline__ void exact_flux(const T *L, const T *R, const T *n, c
 }
 
 template <typename T, int DIM>
-__device__ __forceinline__ void riemann_flux(int solver, const T *L, const T *R, const T *n, const T *w,
+PHD_HD __forceinline__ void riemann_flux(int solver, const T *L, const T *R, const T *n, const T *w,
                                              T gamma, bool boost, int max_iter, T *f, bool *failed) {
     if (solver == PHD_EXACT) exact_flux<T, DIM>(L, R, n, w, gamma, max_iter, f, failed);
     else hll_family<T, DIM>(solver == PHD_HLLC, L, R, n, w, gamma, boost, f);
@@ -307,7 +307,7 @@ __device__ __forceinline__ void riemann_flux(int solver, const T *L, const T *R,
 // reconstruction.pyx:877-921.  X = extrapolated state (in/out), S = constant state of
 // the same side, ci/cj = unboosted cell values that decide the limiting direction.
 template <typename T>
-__device__ __forceinline__ void gizmo_pair(T sl, T sr, T ci, T cj, T sepi_mag, T sepj_mag, T diff_mag,
+PHD_HD __forceinline__ void gizmo_pair(T sl, T sr, T ci, T cj, T sepi_mag, T sepj_mag, T diff_mag,
                                            T &xl, T &xr) {
     const T psi1 = T(0.5), psi2 = T(0.25);
     const T delta1 = psi1 * t_fabs(sl - sr);
@@ -337,7 +337,7 @@ __device__ __forceinline__ void gizmo_pair(T sl, T sr, T ci, T cj, T sepi_mag, T
 // L/R enter as spatially extrapolated states and leave time-extrapolated (or reverted
 // to the spatial state where density or pressure would turn negative).
 template <typename T, int DIM>
-__device__ __forceinline__ void temporal(T *L, T *R, const T *pi, const T *pj, const T *gi, const T *gj,
+PHD_HD __forceinline__ void temporal(T *L, T *R, const T *pi, const T *pj, const T *gi, const T *gj,
                                          const T *w, T gamma, T dt, bool boost) {
     const int NF = DIM + 2, E = DIM + 1;
     T sl[NF], sr[NF], vi[DIM], vj[DIM];
