@@ -153,27 +153,44 @@ def algorithmic_bytes_f64(n, F, n_real):
 
 
 # --------------------------------------------------------------------------------------
-def cpu_baseline(n_side_sample, seconds, solver):
-    """The C restatement of the reference path (oracle/phd_oracle.c), one host thread,
-    on a bounded sample of the same workload (a smaller lattice of the same problem)."""
+def cpu_baseline(n_side_sample, seconds, solver, prefer_reference=True):
+    """CPU throughput of the same path, one host thread, on a bounded sample of the same
+    workload (a smaller lattice of the same problem): the reference's own Cython modules
+    when they are built on this machine (kind "reference"), else the C restatement
+    (oracle/phd_oracle.c, kind "port")."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-    O.build()
     mesh, prim = shear_layer(n_side_sample)
-    p = prim.copy()
-    c = O.cons_from_prim(mesh, p, 5.0 / 3.0)
-    stp = O.OracleStepper(mesh, gamma=5.0 / 3.0, solver=solver, moving=True)
+    gamma = 5.0 / 3.0
+    kind = "port"
+    if prefer_reference:
+        import ref_harness as rh
+        if rh.available():
+            kind = "reference"
+    if kind == "reference":
+        s = rh.RefStep(mesh, prim, gamma=gamma, riemann=solver)
+
+        def one():
+            s.moving_step_fixed_mesh(s.time_step())
+    else:
+        import oracle as O
+        O.build()
+        p = prim.copy()
+        c = O.cons_from_prim(mesh, p, gamma)
+        stp = O.OracleStepper(mesh, gamma=gamma, solver=solver, moving=True)
+
+        def one():
+            stp.step(O.time_step(mesh, p, gamma, 0.5, True), p, c)
     steps, t0 = 0, time.perf_counter()
     while True:
-        dt = O.time_step(mesh, p, 5.0 / 3.0, 0.5, True)
-        stp.step(dt, p, c)
+        one()
         steps += 1
         el = time.perf_counter() - t0
         if el >= seconds or steps >= 10000:
             break
-    return {"value": mesh.n_faces * steps / el, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "%d steps of the %dx%d shear layer (%d faces), moving-mesh HLLC FP64, 1 host thread"
-                      % (steps, n_side_sample, n_side_sample, mesh.n_faces)}
+    what = "the reference's Cython flux path" if kind == "reference" else "the C restatement"
+    return {"value": mesh.n_faces * steps / el, "unit": UNIT, "cores": 1, "kind": kind,
+            "sample": "%d moving-mesh %s steps (FP64) of %s on the %dx%d shear layer (%d faces), 1 host thread"
+                      % (steps, solver.upper(), what, n_side_sample, n_side_sample, mesh.n_faces)}
 
 
 def _cpu_worker(args):
@@ -195,13 +212,14 @@ def run_reference(args, rank, world):
         res = pool.map(_cpu_worker, [(n_side, max(5.0, args.cpu_seconds), args.solver)] * cores)
     value = float(sum(r["value"] for r in res))
     sample = "%s; %d concurrent replicas" % (res[0]["sample"].replace(", 1 host thread", ""), cores)
+    kind = res[0]["kind"]
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "impl": "reference",
            "config": {"workload": "shear layer %dx%d periodic (bounded CPU sample of the 1024x1024 run)"
                                   % (n_side, n_side), "solver": args.solver, "precision": "fp64"},
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 

@@ -27,6 +27,7 @@ Cython directives: ``language_level=2`` (the reference is Python 2 code),
 ``legacy_implicit_noexcept=True`` (``tree.pyx:606``).
 
 Usage:  python oracle/build_ref.py [--reference /root/reference] [--jobs 8]
+        python oracle/build_ref.py --compile-staged   (compile the staged C++ on this machine)
 """
 import argparse
 import os
@@ -210,11 +211,52 @@ def build(reference, jobs):
         fh.write("reference Cython hot path built from %s\n" % reference)
 
 
+def platform_suffix():
+    import sysconfig
+    return sysconfig.get_config_var("EXT_SUFFIX")
+
+
+def staged_built():
+    """True when the staged reference modules are compiled for this interpreter."""
+    return os.path.exists(os.path.join(BUILD, "phd", "riemann", "riemann" + platform_suffix()))
+
+
+def compile_staged(jobs=None):
+    """Compile the C++ that Cython generated from the staged reference sources (kept
+    under oracle/_ref/build) for this machine, with g++ and no Cython: the step that
+    turns the build into a working reference where the reference tree is absent."""
+    import sysconfig
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    if not os.path.exists(os.path.join(BUILD, "phd", "riemann", "riemann.cpp")):
+        return False
+    py_inc = sysconfig.get_paths()["include"]
+    suffix = platform_suffix()
+    incs = ["-I" + py_inc, "-I" + np.get_include(), "-I.", "-Iphd/mesh", "-Iphd/domain", "-Iphd/utils"]
+
+    def one(item):
+        name, extra = item
+        out = os.path.join(BUILD, name + suffix)
+        cmd = ["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-w"] + incs + \
+              [name + ".cpp"] + extra + ["-o", out + ".tmp"]
+        subprocess.check_call(cmd, cwd=BUILD)
+        os.replace(out + ".tmp", out)
+
+    with ThreadPoolExecutor(max_workers=jobs or os.cpu_count() or 4) as ex:
+        list(ex.map(one, MODULES))
+    return True
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--reference", default="/root/reference")
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
+    ap.add_argument("--compile-staged", action="store_true",
+                    help="compile the already staged sources for this machine (no reference tree needed)")
     a = ap.parse_args()
+    if a.compile_staged:
+        print("compiled" if compile_staged(a.jobs) else "nothing staged")
+        return 0
     if not os.path.isdir(os.path.join(a.reference, "phd")):
         print("reference tree not found at %s; nothing to build" % a.reference)
         return 0

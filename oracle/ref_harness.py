@@ -1,8 +1,10 @@
 """Drive the reference's own compiled Cython flux path on a given mesh and state.
 
-TEST INFRASTRUCTURE ONLY.  Needs the build made by ``oracle/build_ref.py`` (which
-needs the reference tree, so this runs in the development container only; the GPU
-tests use the committed golden fixtures and the C restatement instead).
+TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline, never the product
+path).  Needs the build made by ``oracle/build_ref.py``: from the reference tree where it
+is mounted, or ``--compile-staged`` from the staged Cython output elsewhere.  The GPU
+tests never depend on it; they use the committed golden fixtures and the C
+restatement.
 
 The reference objects are wired exactly as ``StaticMeshMUSCLHancock.initialize``
 does (``phd/integrate/integrate.py:302-338``); the face list and neighbour lists are
@@ -19,7 +21,10 @@ REF_BUILD = os.path.join(HERE, "_ref", "build")
 
 
 def available():
-    return os.path.exists(os.path.join(HERE, "_ref", "BUILT"))
+    """The reference modules are importable on this machine."""
+    import sysconfig
+    return os.path.exists(os.path.join(REF_BUILD, "phd", "riemann",
+                                       "riemann" + sysconfig.get_config_var("EXT_SUFFIX")))
 
 
 def _import():

@@ -5,7 +5,8 @@ shared library exporting the C ABI of ``include/phdflux.h``:
 
 * ``phd_f64.cu``  FP64 stage kernels and fused step, ``--fmad=false`` so products and
   sums round like the reference's Cython arithmetic;
-* ``phd_f32.cu``  FP32 reconstruction / Riemann with FP64 accumulation (FMA allowed);
+* ``phd_f32.cu``  FP32 reconstruction / Riemann with FP64 accumulation, fast FP32
+  division and square root (``--use_fast_math`` touches FP32 only);
 * ``phd_util.cu`` mesh-preparation kernels;
 * ``phd_adj.cu``  hand-written adjoint of the FP64 step, ``--fmad=false`` so its
   recomputed forward branches are those of the forward kernels.
@@ -28,7 +29,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUD
 
 UNITS = {
     "phd_f64.cu": ["--fmad=false"],
-    "phd_f32.cu": [],
+    "phd_f32.cu": ["--use_fast_math"],
     "phd_util.cu": [],
     "phd_adj.cu": ["--fmad=false"],
 }

@@ -54,6 +54,50 @@ __device__ __forceinline__ void block_min_to(double v, unsigned long long *slot)
     }
 }
 
+// FP32 <-> FP64 conversions done with integer operations, for kernels whose FP64
+// pipe is the bottleneck (GB300 issues FP64 at a small fraction of the FP32 rate).
+// Zero / denormal inputs map to signed zero; values are finite.
+__device__ __forceinline__ double widen_f32(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu;
+    const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    const unsigned lo = u << 29;
+    return __hiloint2double((int)(ex ? hi : (u & 0x80000000u)), (int)(ex ? lo : 0u));
+}
+
+// Round-to-nearest-even FP64 -> FP32 (finite, normal-range results; smaller
+// magnitudes flush to signed zero).
+__device__ __forceinline__ float narrow_f64(double d) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(d));
+    const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
+    const int ex = static_cast<int>((b >> 52) & 0x7ffull) - 896;
+    const unsigned m23 = static_cast<unsigned>((b >> 29) & 0x7fffffull);
+    const unsigned rem = static_cast<unsigned>(b & 0x1fffffffull);
+    const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (m23 & 1u));
+    const unsigned mag = ((static_cast<unsigned>(ex) << 23) | m23) + up;
+    return __uint_as_float(ex > 0 ? (sign | mag) : sign);
+}
+
+__device__ __forceinline__ float warp_min_f(float v) {
+    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide min of positive floats, merged into the double accumulator *slot.
+__device__ __forceinline__ void block_min_to_f(float v, unsigned long long *slot) {
+    __shared__ float s_minf[32];
+    v = warp_min_f(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) s_minf[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        float u = (lane < nw) ? s_minf[lane] : INFINITY;
+        u = warp_min_f(u);
+        if (lane == 0 && u < INFINITY) atomicMin(slot, dbits((double)u));
+    }
+}
+
 // Finish a grid-wide CFL reduction: the last block to arrive turns the minimum
 // into the next time step (cfl * min, clipped to land on t_end) and re-arms the
 // accumulator.  With `advance` the clock first moves past the step just taken

@@ -136,24 +136,41 @@ __global__ void __launch_bounds__(B32) k_grad32(phd_mesh M, phd_params P, int mo
     float alpha[4] = {1.f, 1.f, 1.f, 1.f};
 #pragma unroll
     for (int f = 0; f < 4; f++) { df[f][0] *= gc.z; df[f][1] *= gc.z; }
-    for (int e = e0; e < e1; e++) {
-        const int code = csr_face[e];
-        const int fid = code < 0 ? ~code : code;
-        const float hs = code < 0 ? -0.5f : 0.5f;
-        const float4 g = face_geo[fid];
-        const float r = face_ar[fid].y;
-        const float sx = g.z + hs * r * g.x - gc.x;
-        const float sy = g.w + hs * r * g.y - gc.y;
-        if (LIMITER == PHD_LIMITER_AREPO) {
+    if (LIMITER == PHD_LIMITER_AREPO) {
+        // alpha_f = min over faces of max(psi, 0), psi = (phi_max - phi)/dphi for dphi > 0
+        // and (phi_min - phi)/dphi for dphi < 0: the numerators do not depend on the
+        // face, so the minimum is reached at the largest |dphi| of each sign -- two
+        // divisions per field instead of one per face and field.
+        float dpos[4] = {0.f, 0.f, 0.f, 0.f}, dneg[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int e = e0; e < e1; e++) {
+            const int code = csr_face[e];
+            const int fid = code < 0 ? ~code : code;
+            const float hs = code < 0 ? -0.5f : 0.5f;
+            const float4 g = face_geo[fid];
+            const float r = face_ar[fid].y;
+            const float sx = g.z + hs * r * g.x - gc.x;
+            const float sy = g.w + hs * r * g.y - gc.y;
 #pragma unroll
             for (int f = 0; f < 4; f++) {
                 const float dphi = df[f][0] * sx + df[f][1] * sy;
-                float psi = 1.f;
-                if (dphi > 0.f) psi = (mx[f] - P0[f]) / dphi;
-                else if (dphi < 0.f) psi = (mn[f] - P0[f]) / dphi;
-                alpha[f] = fminf(alpha[f], fmaxf(psi, 0.f));
+                dpos[f] = fmaxf(dpos[f], dphi);
+                dneg[f] = fminf(dneg[f], dphi);
             }
-        } else {
+        }
+#pragma unroll
+        for (int f = 0; f < 4; f++) {
+            if (dpos[f] > 0.f) alpha[f] = fminf(alpha[f], fmaxf((mx[f] - P0[f]) / dpos[f], 0.f));
+            if (dneg[f] < 0.f) alpha[f] = fminf(alpha[f], fmaxf((mn[f] - P0[f]) / dneg[f], 0.f));
+        }
+    } else {
+        for (int e = e0; e < e1; e++) {
+            const int code = csr_face[e];
+            const int fid = code < 0 ? ~code : code;
+            const float hs = code < 0 ? -0.5f : 0.5f;
+            const float4 g = face_geo[fid];
+            const float r = face_ar[fid].y;
+            const float sx = g.z + hs * r * g.x - gc.x;
+            const float sy = g.w + hs * r * g.y - gc.y;
             const float4 pj = prim4[csr_nbr[e]];
             const float Pj[4] = {pj.x, pj.y, pj.z, pj.w};
 #pragma unroll
@@ -179,9 +196,9 @@ __global__ void __launch_bounds__(B32) k_grad32(phd_mesh M, phd_params P, int mo
         const float4 gi = (i == c) ? gc : cell_geo[i];
         float wx = p.y, wy = p.z;
         if (P.regularize) {
-            const float cs = sqrtf((float)P.gamma * p.w / p.x);
+            const float cs = sqrtf(narrow_f64(P.gamma) * p.w / p.x);
             const float d = sqrtf(gi.x * gi.x + gi.y * gi.y);
-            const float eR = (float)P.eta * gi.w;
+            const float eR = narrow_f64(P.eta) * gi.w;
             const float q = d / eR;
             if (q >= 0.9f && q < 1.1f) {
                 const float s = cs * (d - 0.9f * eR) / (d * 0.2f * eR);
@@ -210,8 +227,8 @@ __global__ void __launch_bounds__(B32) k_face32(phd_mesh M, phd_params P, int mo
     const int i = M.pair_i[m], j = M.pair_j[m];
     if (i < 0 || i >= M.n_cells || j < 0 || j >= M.n_cells) { set_status32(clk, PHD_STATUS_BAD_INDEX); return; }
     const bool boost = (SOLVER == PHD_EXACT) ? true : (P.boost != 0);
-    const float gamma = (float)P.gamma;
-    const float dt_half = (float)(0.5 * clk->dt);
+    const float gamma = narrow_f64(P.gamma);
+    const float dt_half = 0.5f * narrow_f64(clk->dt);
     const float4 g = face_geo[m];
     const float2 ar = face_ar[m];
     const float nrm[2] = {g.x, g.y};
@@ -277,14 +294,14 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 
 __global__ void __launch_bounds__(B32) k_update32(phd_mesh M, phd_params P, const float2 *__restrict__ face_ar,
                                                   const int32_t *__restrict__ csr_face,
-                                                  const float4 *__restrict__ flux4, const double *__restrict__ cons,
-                                                  double *__restrict__ cons_next, float4 *__restrict__ prim4,
-                                                  phd_clock *clk) {
+                                                  const float4 *__restrict__ flux4, const float4 *__restrict__ cell_geo,
+                                                  const double *__restrict__ cons, double *__restrict__ cons_next,
+                                                  float4 *__restrict__ prim4, phd_clock *clk) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int n = M.n_cells;
-    const double dt = clk->dt;
-    const float dtf = (float)dt;
-    double cand = INFINITY;
+    const float dtf = narrow_f64(clk->dt);
+    const float gam = narrow_f64(P.gamma);
+    float cand = INFINITY;
     if (i < n) {
         const bool real = M.tag[i] == PHD_REAL_TAG;
         const int c = real ? i : M.map[i];
@@ -305,38 +322,40 @@ __global__ void __launch_bounds__(B32) k_update32(phd_mesh M, phd_params P, cons
                     lo[q] += er;
                 }
             }
+            // FP64 totals: the only FP64 arithmetic of the step (two adds per field)
             double U[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) U[q] = cons[(size_t)q * n + c] + ((double)hs[q] + (double)lo[q]);
-            if (U[0] <= 0.0) set_status32(clk, PHD_STATUS_NEG_MASS);
-            if (U[3] <= 0.0) set_status32(clk, PHD_STATUS_NEG_ENERGY);
+            for (int q = 0; q < 4; q++) U[q] = (cons[(size_t)q * n + c] + widen_f32(hs[q])) + widen_f32(lo[q]);
+            float m = narrow_f64(U[0]), mx = narrow_f64(U[1]), my = narrow_f64(U[2]);
+            if (!(U[0] > 0.0)) set_status32(clk, PHD_STATUS_NEG_MASS);
+            if (!(U[3] > 0.0)) set_status32(clk, PHD_STATUS_NEG_ENERGY);
             if (!real) {
                 const int fl = M.flip[i];
-                if (fl & 1) U[1] = -U[1];
-                if (fl & 2) U[2] = -U[2];
+                if (fl & 1) { U[1] = -U[1]; mx = -mx; }
+                if (fl & 2) { U[2] = -U[2]; my = -my; }
             }
 #pragma unroll
             for (int q = 0; q < 4; q++) cons_next[(size_t)q * n + i] = U[q];
-            // IdealGas.primitive_from_conservative equation_state.pyx:106-117
-            const double vol = M.vol[i];
-            const double rho = U[0] / vol;
-            const double rm = 1.0 / U[0];
-            const double vx = U[1] * rm, vy = U[2] * rm;
-            const double p = (U[3] / vol - 0.5 * rho * (vx * vx + vy * vy)) * (P.gamma - 1.0);
-            const float4 pr = make_float4((float)rho, (float)vx, (float)vy, (float)p);
-            prim4[i] = pr;
-            if (real) {   // riemann.pyx:170-187
+            // IdealGas.primitive_from_conservative equation_state.pyx:106-117 with the
+            // internal energy E - m v^2/2 formed in FP64
+            const float4 cg = cell_geo[i];
+            const float rho = m * cg.z;
+            const float rm = 1.f / m;
+            const float vx = mx * rm, vy = my * rm;
+            const float ke = 0.5f * (mx * vx + my * vy);
+            const float eint = narrow_f64(U[3] - widen_f32(ke));
+            const float p = (gam - 1.f) * eint * cg.z;
+            prim4[i] = make_float4(rho, vx, vy, p);
+            if (real) {   // riemann.pyx:170-187, R = sqrt(vol/pi) precomputed
                 const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
-                const float cs = sqrtf((float)P.gamma * pr.w / pr.x);
-                const float R = sqrtf((float)vol * (float)(1.0 / 3.141592653589793));
-                const float den = boost ? cs : cs + sqrtf(pr.y * pr.y + pr.z * pr.z);
-                cand = (double)(R / den);
+                const float cs = sqrtf(gam * p / rho);
+                cand = cg.w / (boost ? cs : cs + sqrtf(vx * vx + vy * vy));
             }
         } else {
             set_status32(clk, PHD_STATUS_BAD_INDEX);
         }
     }
-    block_min_to(cand, &clk->dtmin_bits);
+    block_min_to_f(cand, &clk->dtmin_bits);
     finish_cfl(clk, P.cfl, true);
 }
 
@@ -442,7 +461,7 @@ int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_p
         }
     }
     if (marks) cudaEventRecord(marks[2], stream);
-    k_update32<<<gc, B32, 0, stream>>>(M, *par, fa, geo->csr_face, fx, cons, cons_next, p4, clk);
+    k_update32<<<gc, B32, 0, stream>>>(M, *par, fa, geo->csr_face, fx, cg, cons, cons_next, p4, clk);
     if (marks) cudaEventRecord(marks[3], stream);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
