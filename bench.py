@@ -43,6 +43,10 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--workload", default="shear", choices=["shear", "ensemble"])
+    ap.add_argument("--runs", type=int, default=256)
     return ap.parse_args()
 
 
@@ -313,6 +317,9 @@ def run_ours(args, rank, world):
     # end to end through the public API with host buffers: the host mesh hands over
     # its face list and cell geometry each step (pinned host -> device), the step runs,
     # and the generator velocities (what the host re-mesh needs) plus the clock come back
+    accuracy = None
+    if st.precision == "fp32" and not args.no_accuracy:
+        accuracy = fp32_accuracy(st, mesh, prim, max(3, args.warmup) + args.steps, dev, args.solver)
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(args, st, mesh, prim, dev)
@@ -320,6 +327,10 @@ def run_ours(args, rank, world):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(256, args.cpu_seconds, args.solver)
+
+    adjoint = None
+    if not args.no_adjoint and rank == 0:
+        adjoint = adjoint_cost(dev)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -335,9 +346,76 @@ def run_ours(args, rank, world):
                           "l2": "inputs larger than L2 (per-step working set %.0f MB > 129 MB)"
                                 % (sum(algo.values()) / 1e6),
                           "parallelism": "replicas" if world > 1 else "single GPU"},
-               "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+               "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
+               "adjoint": adjoint,
                "gpu_launches": 3 * args.steps, "clocks": clocks}
         print(json.dumps(out), flush=True)
+
+
+def fp32_accuracy(st, mesh, prim, n_steps, dev, solver):
+    """L1 density error of the FP32 run against an FP64 run of the same steps from the
+    same state (mean |rho32 - rho64| over real cells) and the FP32 run's relative
+    mass / energy drift |sum U(t) - sum U(0)| / sum U(0)."""
+    import torch
+    from phd_code_gb300.step import FluxStepper
+    ref = FluxStepper(st.dmesh, prim, gamma=5.0 / 3.0, cfl=0.5, solver=solver, moving=True, precision="fp64",
+                      device=dev)
+    ref.step(n_steps)
+    torch.cuda.synchronize()
+    nr = mesh.n_real
+    r32 = st.prim4[:nr, 0].double()
+    r64 = ref.prim[0, :nr]
+    l1 = float((r32 - r64).abs().mean())
+    u0 = torch.as_tensor(prim[:, :nr]).to(dev)
+    vol = st.dmesh.vol[:nr]
+    m0 = float((u0[0] * vol).sum())
+    e0 = float(((0.5 * u0[0] * (u0[1] ** 2 + u0[2] ** 2) + u0[3] / (5.0 / 3.0 - 1.0)) * vol).sum())
+    c = st.cons[:, :nr]
+    c64 = ref.cons[:, :nr]
+    return {"steps": n_steps, "l1_density_vs_fp64": l1, "mass_drift": abs(float(c[0].sum()) - m0) / m0,
+            "energy_drift": abs(float(c[3].sum()) - e0) / e0,
+            "fp64_mass_drift": abs(float(c64[0].sum()) - m0) / m0,
+            "fp64_energy_drift": abs(float(c64[3].sum()) - e0) / e0,
+            "t_fp32": st.read_clock().t, "t_fp64": ref.read_clock().t}
+
+
+def adjoint_cost(dev, n_side=128, n_steps=20, checkpoint=20):
+    """Adjoint / forward time of the FP64 step on the 128x128 Gaussian-bump problem
+    (static mesh, HLLC, CFL 0.4): forward run, then the full backward pass including
+    the recompute from checkpoints, both timed with CUDA events."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from phd_code_gb300.adjoint import FluxRun, FluxRunRecord, StepRecord
+    from phd_code_gb300.device import DeviceMesh
+    from phd_code_gb300.step import FluxStepper
+    mesh, prim, info = pkg.problems.gaussian_bump(n_side, background=False)
+    dm = DeviceMesh(mesh, device=dev)
+    st = FluxStepper(dm, prim, gamma=1.4, cfl=0.4, solver="hllc", moving=False, device=dev)
+    fw = torch.zeros((2, mesh.n_faces), dtype=torch.float64, device=dev)
+    recs = []
+    for _ in range(n_steps):
+        recs.append(StepRecord(dm, fw, st.read_clock().dt))
+        st.step(1)
+    run = FluxRunRecord(recs, gamma=1.4, solver="hllc", checkpoint=checkpoint)
+    p0 = torch.as_tensor(prim[:, :mesh.n_real]).to(dev).requires_grad_(True)
+    tgt = torch.ones(mesh.n_real, dtype=torch.float64, device=dev)
+    for _ in range(2):                                   # warm-up
+        loss = ((FluxRun.apply(p0, run) - tgt) ** 2).sum()
+        loss.backward()
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    e[0].record()
+    rho = FluxRun.apply(p0, run)
+    loss = ((rho - tgt) ** 2).sum()
+    e[1].record()
+    loss.backward()
+    e[2].record()
+    torch.cuda.synchronize()
+    fwd, bwd = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    return {"config": "gaussian bump %dx%d periodic, HLLC, FP64, %d steps, checkpoint every %d" %
+                      (n_side, n_side, n_steps, checkpoint),
+            "forward_ms": fwd, "backward_ms": bwd, "ratio": bwd / fwd}
 
 
 def run_e2e(args, st, mesh, prim, dev):
@@ -386,6 +464,63 @@ def run_e2e(args, st, mesh, prim, dev):
                     "prepare, flux step, generator velocities + clock D2H"}
 
 
+def run_ensemble(args, rank, world):
+    """Batched two-state Riemann ensemble: all runs advance through one launch per stage
+    (CUDA graph per step, autotuned launch shapes) vs the same runs launched one after
+    another; aggregate faces/s."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from phd_code_gb300.autotune import tune
+    from phd_code_gb300.ensemble import EnsembleStepper, SequentialEnsemble
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    runs, info = pkg.problems.riemann_ensemble(n_runs=args.runs, seed=rank)
+    ens = EnsembleStepper(runs, device=dev)
+    launch, table = tune(ens)
+    ens.launch = launch
+    ens.capture(2)
+    for _ in range(max(3, args.warmup)):
+        ens.replay()
+    steps = args.steps if args.steps % 2 == 0 else args.steps + 1
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    e0.record()
+    for _ in range(steps // 2):
+        ens.replay()
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    ens.check_status()
+    ms = e0.elapsed_time(e1)
+    batched = ens.faces * steps / (ms * 1e-3)
+    seq = SequentialEnsemble(runs, device=dev)
+    seq.step(2)
+    q = min(steps, 20)
+    torch.cuda.synchronize()
+    e0.record()
+    seq.step(q)
+    e1.record()
+    torch.cuda.synchronize()
+    seq_rate = seq.faces * q / (e0.elapsed_time(e1) * 1e-3)
+    if rank == 0:
+        out = {"metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": world, "steps": steps,
+               "warmup": max(3, args.warmup), "ms_per_step": ms / steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": "ensemble of %d two-state Riemann runs, N log-uniform in [1000, 65536], "
+                                      "reflective unit boxes, gamma 1.4, FP32+FP64-accumulate HLLC" % args.runs,
+                          "cells": int(ens.dmesh.n_real), "faces": int(ens.faces),
+                          "launch": {"block": [launch.block_grad, launch.block_face, launch.block_update],
+                                     "grid_cap": [launch.grid_cap_grad, launch.grid_cap_face,
+                                                  launch.grid_cap_update]}},
+               "sequential": {"value": seq_rate, "unit": UNIT, "steps": q,
+                              "what": "the same runs as separate single-run steppers launched in turn"},
+               "speedup_vs_sequential": batched / seq_rate, "gpu_launches": 3 * steps, "clocks": clocks}
+        print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -400,6 +535,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, rank, world)
+        elif args.workload == "ensemble":
+            run_ensemble(args, rank, world)
         else:
             run_ours(args, rank, world)
     finally:

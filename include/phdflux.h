@@ -207,6 +207,12 @@ int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *o
 int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4,
                  phd_clock *clk, cudaStream_t stream);
 
+/* phd_prim_f32 for a batch of runs (see phd_step_f32_batched): each run's clock gets
+ * its own CFL step. */
+int phd_prim_f32_batched(const phd_mesh *mesh, const phd_params *par, const double *cons,
+                         float *prim4, phd_clock *clocks, int32_t n_runs,
+                         const int32_t *cell_run, cudaStream_t stream);
+
 /* One fused step (same order as phd_step_f64): gradients (+ generator velocities when
  * moving) -> per-face states, Riemann flux and deboost (face velocities formed on the
  * fly) -> segmented update into cons_next, FP32 primitives, next dt.
@@ -214,6 +220,25 @@ int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons
 int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par,
                  int32_t moving, float *prim4, const double *cons, double *cons_next, float *grad8,
                  float *w2, float *flux4, phd_clock *clk, cudaStream_t stream);
+
+/* Launch shape of the three step kernels (chosen by an autotuner): threads per block
+ * (multiple of 32, <= 512) and a cap on blocks per grid (0: one thread per item; > 0:
+ * that many blocks, each looping over items -- a persistent launch). */
+typedef struct phd_launch {
+    int32_t block_grad, block_face, block_update;
+    int32_t grid_cap_grad, grid_cap_face, grid_cap_update;
+} phd_launch;
+
+/* Batched step: n_runs independent runs concatenated into one mesh (disjoint cell and
+ * face ranges; ghosts map inside their run) advance together, one launch per stage.
+ * clocks[n_runs] holds each run's dt / t / CFL accumulator; cell_run[n_cells] the run
+ * of each cell (may be NULL when n_runs == 1).  launch may be NULL (defaults).  Status
+ * bits of a run go to clocks[run] (index errors of the gradient stage to clocks[0]). */
+int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par,
+                         int32_t moving, const phd_launch *launch, float *prim4,
+                         const double *cons, double *cons_next, float *grad8, float *w2,
+                         float *flux4, phd_clock *clocks, int32_t n_runs,
+                         const int32_t *cell_run, cudaStream_t stream, cudaEvent_t *marks);
 
 /* The same step with four caller-created events recorded on the stream around its
  * three stages (before gradients, before the face kernel, before the update, after),

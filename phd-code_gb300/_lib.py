@@ -54,6 +54,11 @@ class PhdGeom32(C.Structure):
                 ("csr_nbr", C.c_void_p), ("cell_geo", C.c_void_p)]
 
 
+class PhdLaunch(C.Structure):
+    _fields_ = [("block_grad", C.c_int32), ("block_face", C.c_int32), ("block_update", C.c_int32),
+                ("grid_cap_grad", C.c_int32), ("grid_cap_face", C.c_int32), ("grid_cap_update", C.c_int32)]
+
+
 class PhdAdjIndex(C.Structure):
     _fields_ = [("partner", C.c_void_p), ("ghost_ptr", C.c_void_p), ("ghost_idx", C.c_void_p)]
 
@@ -88,8 +93,11 @@ SIGNATURES = {
     "phd_step_f64": ([_PM, _PP, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], C.c_int),
     "phd_step_f64_marked": ([_PM, _PP, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], C.c_int),
     "phd_step_f32_marked": ([_PM, _PG, _PP, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], C.c_int),
+    "phd_step_f32_batched": ([_PM, _PG, _PP, _i32, C.POINTER(PhdLaunch), _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32,
+                              _vp, _vp, _vp], C.c_int),
     "phd_prepare_f32": ([_PM, _vp, C.POINTER(PhdGeom32Out), _vp], C.c_int),
     "phd_prim_f32": ([_PM, _PP, _vp, _vp, _vp, _vp], C.c_int),
+    "phd_prim_f32_batched": ([_PM, _PP, _vp, _vp, _vp, _i32, _vp, _vp], C.c_int),
     "phd_step_f32": ([_PM, _PG, _PP, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], C.c_int),
     "phd_adjoint_work_doubles": ([_i32, _i32], C.c_size_t),
     "phd_adjoint_step_f64": ([_PM, C.POINTER(PhdAdjIndex), _PP, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],

@@ -98,38 +98,49 @@ __device__ __forceinline__ void block_min_to_f(float v, unsigned long long *slot
     }
 }
 
-// Finish a grid-wide CFL reduction: the last block to arrive turns the minimum
-// into the next time step (cfl * min, clipped to land on t_end) and re-arms the
-// accumulator.  With `advance` the clock first moves past the step just taken
-// (t += dt, step += 1).  No block waits on another: every block reads clk->dt before
-// its arrival is counted, and only the last arrival writes it.
-__device__ __forceinline__ void finish_cfl(phd_clock *clk, double cfl, bool advance) {
+// Turn one run's CFL minimum into its next time step (cfl * min, clipped to land on
+// t_end) and re-arm its accumulator; with `advance` the clock first moves past the
+// step just taken (t += dt, step += 1).
+__device__ __forceinline__ void finalize_clock(phd_clock *clk, double cfl, bool advance) {
+    const unsigned long long bits = atomicAdd(&clk->dtmin_bits, 0ull);
+    const double mn = __longlong_as_double(static_cast<long long>(bits));
+    if (advance) {
+        clk->t = clk->t + clk->dt;
+        clk->step = clk->step + 1;
+    }
+    double dt = cfl * mn;
+    clk->dt_hydro = dt;
+    // Time.modify_timestep + Simulation.compute_time_step (simulation_finish.py:82-88,
+    // simulation.py:201-212): land exactly on t_end.
+    if (clk->t_end > 0.0 && clk->t + dt >= clk->t_end) dt = fmin(clk->t_end - clk->t, dt);
+    clk->dt = dt;
+    clk->dtmin_bits = dbits(INFINITY);
+}
+
+// Finish a grid-wide CFL reduction over n_runs clocks: the last block to arrive
+// finalises every run.  No block waits on another: every block reads the clocks'
+// dt before its arrival is counted (clocks[0].arrive), and only the last arrival
+// writes them.
+__device__ __forceinline__ void finish_cfl_multi(phd_clock *clocks, int n_runs, double cfl, bool advance) {
     __shared__ bool s_last;
     __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned int prev = atomicAdd(&clk->arrive, 1u);
+        const unsigned int prev = atomicAdd(&clocks[0].arrive, 1u);
         s_last = (prev == gridDim.x - 1);
     }
     __syncthreads();
-    if (s_last && threadIdx.x == 0) {
+    if (s_last) {
         __threadfence();
-        const unsigned long long bits = atomicAdd(&clk->dtmin_bits, 0ull);
-        const double mn = __longlong_as_double(static_cast<long long>(bits));
-        if (advance) {
-            clk->t = clk->t + clk->dt;
-            clk->step = clk->step + 1;
-        }
-        double dt = cfl * mn;
-        clk->dt_hydro = dt;
-        // Time.modify_timestep + Simulation.compute_time_step (simulation_finish.py:82-88,
-        // simulation.py:201-212): land exactly on t_end.
-        if (clk->t_end > 0.0 && clk->t + dt >= clk->t_end) dt = fmin(clk->t_end - clk->t, dt);
-        clk->dt = dt;
-        clk->dtmin_bits = dbits(INFINITY);
-        clk->arrive = 0u;
+        for (int r = threadIdx.x; r < n_runs; r += blockDim.x) finalize_clock(clocks + r, cfl, advance);
+        __syncthreads();
+        if (threadIdx.x == 0) clocks[0].arrive = 0u;
         __threadfence();
     }
+}
+
+__device__ __forceinline__ void finish_cfl(phd_clock *clk, double cfl, bool advance) {
+    finish_cfl_multi(clk, 1, cfl, advance);
 }
 
 }  // namespace phd

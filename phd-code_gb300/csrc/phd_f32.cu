@@ -92,16 +92,14 @@ __global__ void k_prepare_csr32(phd_mesh M, const int32_t *__restrict__ twin, in
 //   d phi/dx_k = 1/V sum_faces [ (A/r) (phi_j - phi_i) c_k + sigma A/2 (phi_j + phi_i) n_k ]
 //   limiter separation  f - (x + dcom) = c + sigma r/2 n - dcom.
 template <int LIMITER>
-__global__ void __launch_bounds__(B32) k_grad32(phd_mesh M, phd_params P, int moving,
-                                                const float4 *__restrict__ face_geo,
-                                                const float2 *__restrict__ face_ar,
-                                                const int32_t *__restrict__ csr_face,
-                                                const int32_t *__restrict__ csr_nbr,
-                                                const float4 *__restrict__ cell_geo,
-                                                const float4 *__restrict__ prim4, float4 *__restrict__ grad8,
-                                                float2 *__restrict__ w2, phd_clock *clk) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M.n_cells) return;
+__device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_params &P, int moving,
+                                            const float4 *__restrict__ face_geo,
+                                            const float2 *__restrict__ face_ar,
+                                            const int32_t *__restrict__ csr_face,
+                                            const int32_t *__restrict__ csr_nbr,
+                                            const float4 *__restrict__ cell_geo,
+                                            const float4 *__restrict__ prim4, float4 *__restrict__ grad8,
+                                            float2 *__restrict__ w2, phd_clock *clk) {
     const bool real = M.tag[i] == PHD_REAL_TAG;
     const int c = real ? i : M.map[i];
     if (c < 0 || c >= M.n_cells) { set_status32(clk, PHD_STATUS_BAD_INDEX); return; }
@@ -213,19 +211,32 @@ __global__ void __launch_bounds__(B32) k_grad32(phd_mesh M, phd_params P, int mo
     }
 }
 
-// ---- fused face kernel ------------------------------------------------------------
-template <int SOLVER, bool LINEAR>
-__global__ void __launch_bounds__(B32) k_face32(phd_mesh M, phd_params P, int moving,
+template <int LIMITER>
+__global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int moving,
                                                 const float4 *__restrict__ face_geo,
                                                 const float2 *__restrict__ face_ar,
+                                                const int32_t *__restrict__ csr_face,
+                                                const int32_t *__restrict__ csr_nbr,
                                                 const float4 *__restrict__ cell_geo,
-                                                const float4 *__restrict__ prim4,
-                                                const float4 *__restrict__ grad8, const float2 *__restrict__ w2,
-                                                float4 *__restrict__ flux4, phd_clock *clk) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= M.n_faces) return;
+                                                const float4 *__restrict__ prim4, float4 *__restrict__ grad8,
+                                                float2 *__restrict__ w2, phd_clock *clk) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.n_cells; i += gridDim.x * blockDim.x)
+        grad32_cell<LIMITER>(i, M, P, moving, face_geo, face_ar, csr_face, csr_nbr, cell_geo, prim4, grad8, w2, clk);
+}
+
+// ---- fused face kernel ------------------------------------------------------------
+template <int SOLVER, bool LINEAR>
+__device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_params &P, int moving,
+                                            const float4 *__restrict__ face_geo,
+                                            const float2 *__restrict__ face_ar,
+                                            const float4 *__restrict__ cell_geo,
+                                            const float4 *__restrict__ prim4,
+                                            const float4 *__restrict__ grad8, const float2 *__restrict__ w2,
+                                            float4 *__restrict__ flux4, phd_clock *clocks,
+                                            const int32_t *__restrict__ cell_run) {
     const int i = M.pair_i[m], j = M.pair_j[m];
-    if (i < 0 || i >= M.n_cells || j < 0 || j >= M.n_cells) { set_status32(clk, PHD_STATUS_BAD_INDEX); return; }
+    if (i < 0 || i >= M.n_cells || j < 0 || j >= M.n_cells) { set_status32(clocks, PHD_STATUS_BAD_INDEX); return; }
+    phd_clock *clk = cell_run ? clocks + cell_run[i] : clocks;
     const bool boost = (SOLVER == PHD_EXACT) ? true : (P.boost != 0);
     const float gamma = narrow_f64(P.gamma);
     const float dt_half = 0.5f * narrow_f64(clk->dt);
@@ -285,6 +296,20 @@ __global__ void __launch_bounds__(B32) k_face32(phd_mesh M, phd_params P, int mo
     flux4[m] = make_float4(f[0], f[1], f[2], f[3]);
 }
 
+template <int SOLVER, bool LINEAR>
+__global__ void __launch_bounds__(512) k_face32(phd_mesh M, phd_params P, int moving,
+                                                const float4 *__restrict__ face_geo,
+                                                const float2 *__restrict__ face_ar,
+                                                const float4 *__restrict__ cell_geo,
+                                                const float4 *__restrict__ prim4,
+                                                const float4 *__restrict__ grad8, const float2 *__restrict__ w2,
+                                                float4 *__restrict__ flux4, phd_clock *clocks,
+                                                const int32_t *__restrict__ cell_run) {
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M.n_faces; m += gridDim.x * blockDim.x)
+        face32_face<SOLVER, LINEAR>(m, M, P, moving, face_geo, face_ar, cell_geo, prim4, grad8, w2, flux4, clocks,
+                                    cell_run);
+}
+
 // ---- segmented update, primitive recovery and CFL -----------------------------------
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = a + b;
@@ -292,113 +317,177 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     e = (a - (s - bb)) + (b - bb);
 }
 
-__global__ void __launch_bounds__(B32) k_update32(phd_mesh M, phd_params P, const float2 *__restrict__ face_ar,
+// One cell of the update: segmented sum, FP64 totals, primitives; returns the CFL
+// candidate (INFINITY for ghosts) and the cell's run.
+__device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const phd_params &P,
+                                               const float2 *__restrict__ face_ar,
+                                               const int32_t *__restrict__ csr_face,
+                                               const float4 *__restrict__ flux4,
+                                               const float4 *__restrict__ cell_geo,
+                                               const double *__restrict__ cons, double *__restrict__ cons_next,
+                                               float4 *__restrict__ prim4, phd_clock *clocks,
+                                               const int32_t *__restrict__ cell_run, float gam) {
+    const int n = M.n_cells;
+    phd_clock *clk = cell_run ? clocks + cell_run[i] : clocks;
+    const float dtf = narrow_f64(clk->dt);
+    const bool real = M.tag[i] == PHD_REAL_TAG;
+    const int c = real ? i : M.map[i];
+    if (c < 0 || c >= n) { set_status32(clk, PHD_STATUS_BAD_INDEX); return INFINITY; }
+    float hs[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+    for (int e = M.nbr_ptr[c]; e < M.nbr_ptr[c + 1]; e++) {
+        const int code = csr_face[e];
+        const int fid = code < 0 ? ~code : code;
+        // one increment per face, identical for both of its cells
+        const float s = dtf * face_ar[fid].x;
+        const float4 fl = flux4[fid];
+        const float inc[4] = {s * fl.x, s * fl.y, s * fl.z, s * fl.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float t, er;
+            two_sum(hs[q], code < 0 ? inc[q] : -inc[q], t, er);
+            hs[q] = t;
+            lo[q] += er;
+        }
+    }
+    // FP64 totals: the only FP64 arithmetic of the step (two adds per field)
+    double U[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) U[q] = (cons[(size_t)q * n + c] + widen_f32(hs[q])) + widen_f32(lo[q]);
+    float m = narrow_f64(U[0]), mx = narrow_f64(U[1]), my = narrow_f64(U[2]);
+    if (!(U[0] > 0.0)) set_status32(clk, PHD_STATUS_NEG_MASS);
+    if (!(U[3] > 0.0)) set_status32(clk, PHD_STATUS_NEG_ENERGY);
+    if (!real) {
+        const int fl = M.flip[i];
+        if (fl & 1) { U[1] = -U[1]; mx = -mx; }
+        if (fl & 2) { U[2] = -U[2]; my = -my; }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) cons_next[(size_t)q * n + i] = U[q];
+    // IdealGas.primitive_from_conservative equation_state.pyx:106-117 with the
+    // internal energy E - m v^2/2 formed in FP64
+    const float4 cg = cell_geo[i];
+    const float rho = m * cg.z;
+    const float rm = 1.f / m;
+    const float vx = mx * rm, vy = my * rm;
+    const float ke = 0.5f * (mx * vx + my * vy);
+    const float eint = narrow_f64(U[3] - widen_f32(ke));
+    const float p = (gam - 1.f) * eint * cg.z;
+    prim4[i] = make_float4(rho, vx, vy, p);
+    if (!real) return INFINITY;
+    // riemann.pyx:170-187, R = sqrt(vol/pi) precomputed
+    const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
+    const float cs = sqrtf(gam * p / rho);
+    return cg.w / (boost ? cs : cs + sqrtf(vx * vx + vy * vy));
+}
+
+__global__ void __launch_bounds__(512) k_update32(phd_mesh M, phd_params P, const float2 *__restrict__ face_ar,
                                                   const int32_t *__restrict__ csr_face,
                                                   const float4 *__restrict__ flux4, const float4 *__restrict__ cell_geo,
                                                   const double *__restrict__ cons, double *__restrict__ cons_next,
-                                                  float4 *__restrict__ prim4, phd_clock *clk) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+                                                  float4 *__restrict__ prim4, phd_clock *clocks,
+                                                  const int32_t *__restrict__ cell_run, int n_runs) {
     const int n = M.n_cells;
-    const float dtf = narrow_f64(clk->dt);
     const float gam = narrow_f64(P.gamma);
-    float cand = INFINITY;
-    if (i < n) {
-        const bool real = M.tag[i] == PHD_REAL_TAG;
-        const int c = real ? i : M.map[i];
-        if (c >= 0 && c < n) {
-            float hs[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
-            for (int e = M.nbr_ptr[c]; e < M.nbr_ptr[c + 1]; e++) {
-                const int code = csr_face[e];
-                const int fid = code < 0 ? ~code : code;
-                // one increment per face, identical for both of its cells
-                const float s = dtf * face_ar[fid].x;
-                const float4 fl = flux4[fid];
-                const float inc[4] = {s * fl.x, s * fl.y, s * fl.z, s * fl.w};
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    float t, er;
-                    two_sum(hs[q], code < 0 ? inc[q] : -inc[q], t, er);
-                    hs[q] = t;
-                    lo[q] += er;
-                }
-            }
-            // FP64 totals: the only FP64 arithmetic of the step (two adds per field)
-            double U[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) U[q] = (cons[(size_t)q * n + c] + widen_f32(hs[q])) + widen_f32(lo[q]);
-            float m = narrow_f64(U[0]), mx = narrow_f64(U[1]), my = narrow_f64(U[2]);
-            if (!(U[0] > 0.0)) set_status32(clk, PHD_STATUS_NEG_MASS);
-            if (!(U[3] > 0.0)) set_status32(clk, PHD_STATUS_NEG_ENERGY);
-            if (!real) {
-                const int fl = M.flip[i];
-                if (fl & 1) { U[1] = -U[1]; mx = -mx; }
-                if (fl & 2) { U[2] = -U[2]; my = -my; }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; q++) cons_next[(size_t)q * n + i] = U[q];
-            // IdealGas.primitive_from_conservative equation_state.pyx:106-117 with the
-            // internal energy E - m v^2/2 formed in FP64
-            const float4 cg = cell_geo[i];
-            const float rho = m * cg.z;
-            const float rm = 1.f / m;
-            const float vx = mx * rm, vy = my * rm;
-            const float ke = 0.5f * (mx * vx + my * vy);
-            const float eint = narrow_f64(U[3] - widen_f32(ke));
-            const float p = (gam - 1.f) * eint * cg.z;
-            prim4[i] = make_float4(rho, vx, vy, p);
-            if (real) {   // riemann.pyx:170-187, R = sqrt(vol/pi) precomputed
-                const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
-                const float cs = sqrtf(gam * p / rho);
-                cand = cg.w / (boost ? cs : cs + sqrtf(vx * vx + vy * vy));
-            }
+    const int stride = gridDim.x * blockDim.x;
+    const int n_iter = (n + stride - 1) / stride;     // uniform trip count: all lanes reach the shuffles
+    float cand_all = INFINITY;
+    for (int it = 0; it < n_iter; it++) {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x + it * stride;
+        float cand = INFINITY;
+        int run = 0;
+        if (i < n) {
+            cand = update32_cell(i, M, P, face_ar, csr_face, flux4, cell_geo, cons, cons_next, prim4, clocks,
+                                 cell_run, gam);
+            if (cell_run) run = cell_run[i];
+        }
+        if (!cell_run) {
+            cand_all = fminf(cand_all, cand);
         } else {
-            set_status32(clk, PHD_STATUS_BAD_INDEX);
+            // per-run minimum: one atomic per warp when the warp lies in one run
+            const int r0 = __shfl_sync(0xffffffffu, run, 0);
+            if (__all_sync(0xffffffffu, run == r0 || cand == INFINITY)) {
+                const float wm = warp_min_f(cand);
+                if ((threadIdx.x & 31) == 0 && wm < INFINITY) atomicMin(&clocks[r0].dtmin_bits, dbits((double)wm));
+            } else if (cand < INFINITY) {
+                atomicMin(&clocks[run].dtmin_bits, dbits((double)cand));
+            }
         }
     }
-    block_min_to_f(cand, &clk->dtmin_bits);
-    finish_cfl(clk, P.cfl, true);
+    if (!cell_run) block_min_to_f(cand_all, &clocks[0].dtmin_bits);
+    finish_cfl_multi(clocks, cell_run ? n_runs : 1, P.cfl, true);
 }
 
-// FP64 conserved totals -> FP32 primitive cells and the CFL step (no clock advance).
-__global__ void __launch_bounds__(B32) k_prim32(phd_mesh M, phd_params P, const double *__restrict__ cons,
-                                                float4 *__restrict__ prim4, phd_clock *clk) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// FP64 conserved totals -> FP32 primitive cells and each run's CFL step (clocks not
+// advanced).  Same per-run reduction as k_update32.
+__global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const double *__restrict__ cons,
+                                                float4 *__restrict__ prim4, phd_clock *clocks,
+                                                const int32_t *__restrict__ cell_run, int n_runs) {
     const int n = M.n_cells;
-    double cand = INFINITY;
-    if (i < n) {
-        const double U0 = cons[i], U1 = cons[(size_t)n + i], U2 = cons[2 * (size_t)n + i], U3 = cons[3 * (size_t)n + i];
-        const double vol = M.vol[i];
-        const double rho = U0 / vol;
-        const double vx = U1 / U0, vy = U2 / U0;
-        const double p = (U3 / vol - 0.5 * rho * (vx * vx + vy * vy)) * (P.gamma - 1.0);
-        const float4 pr = make_float4((float)rho, (float)vx, (float)vy, (float)p);
-        prim4[i] = pr;
-        if (M.tag[i] == PHD_REAL_TAG) {
-            const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
-            const float cs = sqrtf((float)P.gamma * pr.w / pr.x);
-            const float R = sqrtf((float)vol * (float)(1.0 / 3.141592653589793));
-            const float den = boost ? cs : cs + sqrtf(pr.y * pr.y + pr.z * pr.z);
-            cand = (double)(R / den);
+    const int stride = gridDim.x * blockDim.x;
+    const int n_iter = (n + stride - 1) / stride;
+    const float gam = narrow_f64(P.gamma);
+    float cand_all = INFINITY;
+    for (int it = 0; it < n_iter; it++) {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x + it * stride;
+        float cand = INFINITY;
+        int run = 0;
+        if (i < n) {
+            const double U0 = cons[i], U1 = cons[(size_t)n + i], U2 = cons[2 * (size_t)n + i];
+            const double U3 = cons[3 * (size_t)n + i];
+            const double vol = M.vol[i];
+            const double rho = U0 / vol;
+            const double vx = U1 / U0, vy = U2 / U0;
+            const double p = (U3 / vol - 0.5 * rho * (vx * vx + vy * vy)) * (P.gamma - 1.0);
+            const float4 pr = make_float4((float)rho, (float)vx, (float)vy, (float)p);
+            prim4[i] = pr;
+            if (M.tag[i] == PHD_REAL_TAG) {
+                const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
+                const float cs = sqrtf(gam * pr.w / pr.x);
+                const float R = sqrtf((float)vol * (float)(1.0 / 3.141592653589793));
+                cand = R / (boost ? cs : cs + sqrtf(pr.y * pr.y + pr.z * pr.z));
+            }
+            if (cell_run) run = cell_run[i];
+        }
+        if (!cell_run) {
+            cand_all = fminf(cand_all, cand);
+        } else {
+            const int r0 = __shfl_sync(0xffffffffu, run, 0);
+            if (__all_sync(0xffffffffu, run == r0 || cand == INFINITY)) {
+                const float wm = warp_min_f(cand);
+                if ((threadIdx.x & 31) == 0 && wm < INFINITY) atomicMin(&clocks[r0].dtmin_bits, dbits((double)wm));
+            } else if (cand < INFINITY) {
+                atomicMin(&clocks[run].dtmin_bits, dbits((double)cand));
+            }
         }
     }
-    block_min_to(cand, &clk->dtmin_bits);
-    finish_cfl(clk, P.cfl, false);
+    if (!cell_run) block_min_to_f(cand_all, &clocks[0].dtmin_bits);
+    finish_cfl_multi(clocks, cell_run ? n_runs : 1, P.cfl, false);
 }
 
 template <int SOLVER>
-void launch_face32(bool linear, int grid, cudaStream_t s, const phd_mesh &M, const phd_params &P, int moving,
-                   const phd_geom32 *G, const float4 *prim4, const float4 *grad8, const float2 *w2, float4 *flux4,
-                   phd_clock *clk) {
+void launch_face32(bool linear, int grid, int block, cudaStream_t s, const phd_mesh &M, const phd_params &P,
+                   int moving, const phd_geom32 *G, const float4 *prim4, const float4 *grad8, const float2 *w2,
+                   float4 *flux4, phd_clock *clocks, const int32_t *cell_run) {
     const float4 *fg = reinterpret_cast<const float4 *>(G->face_geo);
     const float2 *fa = reinterpret_cast<const float2 *>(G->face_ar);
     const float4 *cg = reinterpret_cast<const float4 *>(G->cell_geo);
     if (linear)
-        k_face32<SOLVER, true><<<grid, B32, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clk);
+        k_face32<SOLVER, true><<<grid, block, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clocks,
+                                                      cell_run);
     else
-        k_face32<SOLVER, false><<<grid, B32, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clk);
+        k_face32<SOLVER, false><<<grid, block, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clocks,
+                                                       cell_run);
 }
 
-inline int g32(int n) { return (n + B32 - 1) / B32; }
+// grid for n items: one thread per item, or at most `cap` blocks looping over the rest
+inline int grid_for(int n, int block, int cap) {
+    const int g = (n + block - 1) / block;
+    return (cap > 0 && g > cap) ? cap : (g > 0 ? g : 1);
+}
+
+inline bool block_ok(int b) { return b >= 32 && b <= 512 && (b % 32) == 0; }
+
+inline int g32(int n) { return n > 0 ? (n + B32 - 1) / B32 : 1; }
 
 }  // namespace phd
 
@@ -418,24 +507,41 @@ int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *o
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
-int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4, phd_clock *clk,
-                 cudaStream_t stream) {
-    if (!mesh || mesh->dim != 2 || !par || !cons || !prim4 || !clk) return PHD_ERR_ARG;
-    k_prim32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, *par, cons, reinterpret_cast<float4 *>(prim4), clk);
+int phd_prim_f32_batched(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4,
+                         phd_clock *clocks, int32_t n_runs, const int32_t *cell_run, cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || !par || !cons || !prim4 || !clocks) return PHD_ERR_ARG;
+    if (n_runs < 1 || (n_runs > 1 && !cell_run)) return PHD_ERR_ARG;
+    k_prim32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, *par, cons, reinterpret_cast<float4 *>(prim4), clocks,
+                                                     n_runs > 1 ? cell_run : nullptr, n_runs);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
-int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
-                        float *prim4, const double *cons, double *cons_next, float *grad8, float *w2,
-                        float *flux4, phd_clock *clk, cudaStream_t stream, cudaEvent_t *marks) {
-    if (!mesh || mesh->dim != 2 || !geo || !par || !prim4 || !cons || !cons_next || !flux4 || !clk)
+int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4, phd_clock *clk,
+                 cudaStream_t stream) {
+    return phd_prim_f32_batched(mesh, par, cons, prim4, clk, 1, nullptr, stream);
+}
+
+int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
+                         const phd_launch *launch, float *prim4, const double *cons, double *cons_next, float *grad8,
+                         float *w2, float *flux4, phd_clock *clocks, int32_t n_runs, const int32_t *cell_run,
+                         cudaStream_t stream, cudaEvent_t *marks) {
+    if (!mesh || mesh->dim != 2 || !geo || !par || !prim4 || !cons || !cons_next || !flux4 || !clocks)
         return PHD_ERR_ARG;
     const bool linear = par->reconstruction == PHD_LINEAR;
     if ((linear || moving) && !grad8) return PHD_ERR_ARG;
     if (moving && !w2) return PHD_ERR_ARG;
     if (par->solver < PHD_HLL || par->solver > PHD_EXACT) return PHD_ERR_ARG;
+    if (n_runs < 1 || (n_runs > 1 && !cell_run)) return PHD_ERR_ARG;
+    phd_launch L = {B32, B32, B32, 0, 0, 0};
+    if (launch) {
+        if (!block_ok(launch->block_grad) || !block_ok(launch->block_face) || !block_ok(launch->block_update))
+            return PHD_ERR_ARG;
+        L = *launch;
+    }
     const phd_mesh &M = *mesh;
-    const int gc = g32(M.n_cells), gf = g32(M.n_faces);
+    const int gc = grid_for(M.n_cells, L.block_grad, L.grid_cap_grad);
+    const int gf = grid_for(M.n_faces, L.block_face, L.grid_cap_face);
+    const int gu = grid_for(M.n_cells, L.block_update, L.grid_cap_update);
     float4 *p4 = reinterpret_cast<float4 *>(prim4);
     float4 *g8 = reinterpret_cast<float4 *>(grad8);
     float2 *w = reinterpret_cast<float2 *>(w2);
@@ -443,34 +549,52 @@ int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_p
     const float4 *fg = reinterpret_cast<const float4 *>(geo->face_geo);
     const float2 *fa = reinterpret_cast<const float2 *>(geo->face_ar);
     const float4 *cg = reinterpret_cast<const float4 *>(geo->cell_geo);
+    const int32_t *runs = n_runs > 1 ? cell_run : nullptr;
     if (marks) cudaEventRecord(marks[0], stream);
     if (linear || moving) {
         if (par->limiter == PHD_LIMITER_TESS)
-            k_grad32<PHD_LIMITER_TESS><<<gc, B32, 0, stream>>>(M, *par, moving, fg, fa, geo->csr_face, geo->csr_nbr,
-                                                               cg, p4, g8, w, clk);
+            k_grad32<PHD_LIMITER_TESS><<<gc, L.block_grad, 0, stream>>>(M, *par, moving, fg, fa, geo->csr_face,
+                                                                        geo->csr_nbr, cg, p4, g8, w, clocks);
         else
-            k_grad32<PHD_LIMITER_AREPO><<<gc, B32, 0, stream>>>(M, *par, moving, fg, fa, geo->csr_face,
-                                                                geo->csr_nbr, cg, p4, g8, w, clk);
+            k_grad32<PHD_LIMITER_AREPO><<<gc, L.block_grad, 0, stream>>>(M, *par, moving, fg, fa, geo->csr_face,
+                                                                         geo->csr_nbr, cg, p4, g8, w, clocks);
     }
     if (marks) cudaEventRecord(marks[1], stream);
     if (M.n_faces) {
         switch (par->solver) {
-            case PHD_HLL: launch_face32<PHD_HLL>(linear, gf, stream, M, *par, moving, geo, p4, g8, w, fx, clk); break;
-            case PHD_HLLC: launch_face32<PHD_HLLC>(linear, gf, stream, M, *par, moving, geo, p4, g8, w, fx, clk); break;
-            default: launch_face32<PHD_EXACT>(linear, gf, stream, M, *par, moving, geo, p4, g8, w, fx, clk); break;
+            case PHD_HLL:
+                launch_face32<PHD_HLL>(linear, gf, L.block_face, stream, M, *par, moving, geo, p4, g8, w, fx, clocks,
+                                       runs);
+                break;
+            case PHD_HLLC:
+                launch_face32<PHD_HLLC>(linear, gf, L.block_face, stream, M, *par, moving, geo, p4, g8, w, fx, clocks,
+                                        runs);
+                break;
+            default:
+                launch_face32<PHD_EXACT>(linear, gf, L.block_face, stream, M, *par, moving, geo, p4, g8, w, fx,
+                                         clocks, runs);
+                break;
         }
     }
     if (marks) cudaEventRecord(marks[2], stream);
-    k_update32<<<gc, B32, 0, stream>>>(M, *par, fa, geo->csr_face, fx, cg, cons, cons_next, p4, clk);
+    k_update32<<<gu, L.block_update, 0, stream>>>(M, *par, fa, geo->csr_face, fx, cg, cons, cons_next, p4, clocks,
+                                                  runs, n_runs);
     if (marks) cudaEventRecord(marks[3], stream);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
+                        float *prim4, const double *cons, double *cons_next, float *grad8, float *w2,
+                        float *flux4, phd_clock *clk, cudaStream_t stream, cudaEvent_t *marks) {
+    return phd_step_f32_batched(mesh, geo, par, moving, nullptr, prim4, cons, cons_next, grad8, w2, flux4, clk, 1,
+                                nullptr, stream, marks);
 }
 
 int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
                  float *prim4, const double *cons, double *cons_next, float *grad8, float *w2, float *flux4,
                  phd_clock *clk, cudaStream_t stream) {
-    return phd_step_f32_marked(mesh, geo, par, moving, prim4, cons, cons_next, grad8, w2, flux4, clk, stream,
-                               nullptr);
+    return phd_step_f32_batched(mesh, geo, par, moving, nullptr, prim4, cons, cons_next, grad8, w2, flux4, clk, 1,
+                                nullptr, stream, nullptr);
 }
 
 }  // extern "C"
