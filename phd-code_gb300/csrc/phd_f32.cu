@@ -110,25 +110,41 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
 #pragma unroll
     for (int f = 0; f < 4; f++) { mx[f] = mn[f] = P0[f]; df[f][0] = df[f][1] = 0.f; }
     const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
-    for (int e = e0; e < e1; e++) {
-        const int code = csr_face[e];
-        const int fid = code < 0 ? ~code : code;
-        const float sg = code < 0 ? -1.f : 1.f;
-        const int j = csr_nbr[e];
-        const float4 g = face_geo[fid];
-        const float2 ar = face_ar[fid];
-        const float4 pj = prim4[j];
-        const float Pj[4] = {pj.x, pj.y, pj.z, pj.w};
-        const float a_r = ar.x / ar.y;
-        const float ha = 0.5f * sg * ar.x;
+    // entries in chunks of CH: all of a chunk's dependent loads are issued before any
+    // arithmetic, so their latencies overlap (lanes past the end reload entry e0)
+    constexpr int CH = 4;
+    for (int eb = e0; eb < e1; eb += CH) {
+        int code[CH], nb[CH];
 #pragma unroll
-        for (int f = 0; f < 4; f++) {
-            mx[f] = fmaxf(mx[f], Pj[f]);
-            mn[f] = fminf(mn[f], Pj[f]);
-            const float dd = (Pj[f] - P0[f]) * a_r;
-            const float ds = (Pj[f] + P0[f]) * ha;
-            df[f][0] += dd * g.z + ds * g.x;
-            df[f][1] += dd * g.w + ds * g.y;
+        for (int k = 0; k < CH; k++) {
+            const int e = (eb + k < e1) ? eb + k : e0;
+            code[k] = csr_face[e];
+            nb[k] = csr_nbr[e];
+        }
+        float4 g[CH], pj[CH];
+        float2 ar[CH];
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            const int fid = code[k] < 0 ? ~code[k] : code[k];
+            g[k] = face_geo[fid];
+            ar[k] = face_ar[fid];
+            pj[k] = prim4[nb[k]];
+        }
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            if (eb + k >= e1) break;
+            const float Pj[4] = {pj[k].x, pj[k].y, pj[k].z, pj[k].w};
+            const float a_r = ar[k].x / ar[k].y;
+            const float ha = (code[k] < 0 ? -0.5f : 0.5f) * ar[k].x;
+#pragma unroll
+            for (int f = 0; f < 4; f++) {
+                mx[f] = fmaxf(mx[f], Pj[f]);
+                mn[f] = fminf(mn[f], Pj[f]);
+                const float dd = (Pj[f] - P0[f]) * a_r;
+                const float ds = (Pj[f] + P0[f]) * ha;
+                df[f][0] += dd * g[k].z + ds * g[k].x;
+                df[f][1] += dd * g[k].w + ds * g[k].y;
+            }
         }
     }
     float alpha[4] = {1.f, 1.f, 1.f, 1.f};
@@ -334,19 +350,33 @@ __device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const p
     const int c = real ? i : M.map[i];
     if (c < 0 || c >= n) { set_status32(clk, PHD_STATUS_BAD_INDEX); return INFINITY; }
     float hs[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
-    for (int e = M.nbr_ptr[c]; e < M.nbr_ptr[c + 1]; e++) {
-        const int code = csr_face[e];
-        const int fid = code < 0 ? ~code : code;
-        // one increment per face, identical for both of its cells
-        const float s = dtf * face_ar[fid].x;
-        const float4 fl = flux4[fid];
-        const float inc[4] = {s * fl.x, s * fl.y, s * fl.z, s * fl.w};
+    const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
+    constexpr int CH = 4;
+    for (int eb = e0; eb < e1; eb += CH) {
+        int code[CH];
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            float t, er;
-            two_sum(hs[q], code < 0 ? inc[q] : -inc[q], t, er);
-            hs[q] = t;
-            lo[q] += er;
+        for (int k = 0; k < CH; k++) code[k] = csr_face[(eb + k < e1) ? eb + k : e0];
+        float4 fl[CH];
+        float a[CH];
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            const int fid = code[k] < 0 ? ~code[k] : code[k];
+            a[k] = face_ar[fid].x;
+            fl[k] = flux4[fid];
+        }
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            if (eb + k >= e1) break;
+            // one increment per face, identical for both of its cells
+            const float s = dtf * a[k];
+            const float inc[4] = {s * fl[k].x, s * fl[k].y, s * fl[k].z, s * fl[k].w};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                float t, er;
+                two_sum(hs[q], code[k] < 0 ? inc[q] : -inc[q], t, er);
+                hs[q] = t;
+                lo[q] += er;
+            }
         }
     }
     // FP64 totals: the only FP64 arithmetic of the step (two adds per field)
