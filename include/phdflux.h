@@ -34,6 +34,7 @@ extern "C" {
 #define PHD_ERR_ARG 1
 #define PHD_ERR_LAUNCH 2
 #define PHD_ERR_UNSUPPORTED 3
+#define PHD_ERR_SCRATCH_TOO_SMALL 4        /* mesh larger than a fixed work array allows */
 
 /* device status bits (phd_clock.status) -- same meaning as the reference's raises */
 #define PHD_STATUS_NEG_MASS 1              /* "Mass less than zero in flux update"   mesh.pyx:546-548 */
@@ -269,6 +270,26 @@ int phd_adjoint_step_f64(const phd_mesh *mesh, const phd_adj_index *index, const
                          double dt, const double *cons, const double *prim, const double *grad,
                          const double *face_w, const double *lam_next, double *lam, double *work,
                          cudaStream_t stream);
+
+/* The same adjoint step for callers that cannot allocate device memory: a plugin
+ * whose host program gives it no device allocator (a ctypes binding, or a process
+ * whose device memory is owned by another framework's pool) can still run the
+ * adjoint.  No counterpart in the reference (which has no adjoint).  The work space
+ * is a fixed array compiled into the library (PHD_ADJ_NOALLOC_MAX_DOUBLES doubles =
+ * 32 MiB, present on every GPU that loads the library until the process exits), so
+ * the mesh must satisfy phd_adjoint_work_doubles(n_cells, n_faces) <=
+ * PHD_ADJ_NOALLOC_MAX_DOUBLES -- about 36,000 cells in 2D at three faces per cell --
+ * else PHD_ERR_SCRATCH_TOO_SMALL is returned and nothing runs.  The first call on a
+ * device looks up the array's device address (once per device, with that device
+ * current) and keeps it for later calls.  All calls share the one array:
+ * calls that overlap on the GPU (different streams, or two threads) race on it.
+ * Nothing is allocated; the entries that must start at zero are cleared on the
+ * stream by every call. */
+#define PHD_ADJ_NOALLOC_MAX_DOUBLES 4194304
+int phd_adjoint_step_f64_noalloc(const phd_mesh *mesh, const phd_adj_index *index,
+                                 const phd_params *par, double dt, const double *cons,
+                                 const double *prim, const double *grad, const double *face_w,
+                                 const double *lam_next, double *lam, cudaStream_t stream);
 
 /* ---- utilities ------------------------------------------------------------------ */
 

@@ -11,7 +11,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libphdflux.so")
 
 # host return codes / device status bits / selectors (phdflux.h)
-PHD_OK, PHD_ERR_ARG, PHD_ERR_LAUNCH, PHD_ERR_UNSUPPORTED = 0, 1, 2, 3
+PHD_OK, PHD_ERR_ARG, PHD_ERR_LAUNCH, PHD_ERR_UNSUPPORTED, PHD_ERR_SCRATCH_TOO_SMALL = 0, 1, 2, 3, 4
+ADJ_NOALLOC_MAX_DOUBLES = 4194304
 STATUS_NEG_MASS, STATUS_NEG_ENERGY, STATUS_RIEMANN_NONCONVERGED, STATUS_BAD_INDEX = 1, 2, 4, 8
 HLL, HLLC, EXACT = 0, 1, 2
 CONSTANT, LINEAR = 0, 1
@@ -102,6 +103,8 @@ SIGNATURES = {
     "phd_adjoint_work_doubles": ([_i32, _i32], C.c_size_t),
     "phd_adjoint_step_f64": ([_PM, C.POINTER(PhdAdjIndex), _PP, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
                              C.c_int),
+    "phd_adjoint_step_f64_noalloc": ([_PM, C.POINTER(PhdAdjIndex), _PP, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+                                     C.c_int),
     "phd_flip_mask": ([_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp, _vp], C.c_int),
     "phd_hilbert_keys_2d": ([_i32, _vp, _f64, _f64, _f64, _i32, _vp, _vp], C.c_int),
 }

@@ -12,6 +12,8 @@
 //   k_adj_gather2  per cell: own + partner-entry contributions -> lam_prim
 //   k_adj_final    per real cell: fold ghost rows, reverse the primitive recovery,
 //                  lam = lam' + J^T lam_prim
+#include <mutex>
+
 #include "phd_common.cuh"
 #include "phd_physics.cuh"
 #include "phd_adjoint.cuh"
@@ -402,6 +404,56 @@ int phd_adjoint_step_f64(const phd_mesh *mesh, const phd_adj_index *index, const
 
 size_t phd_adjoint_work_doubles(int32_t n_cells, int32_t n_faces) {
     return (size_t)24 * n_faces + 12 * (size_t)n_cells + 8 * (size_t)n_faces + 8 * (size_t)n_cells;
+}
+
+}  // extern "C"
+
+// ---- adjoint step that allocates nothing --------------------------------------------
+// Work space for phd_adjoint_step_f64_noalloc: a fixed array in the library's device
+// image, created on every GPU where the library is loaded and kept until the process
+// exits.  Its size is the limit of that entry point (PHD_ADJ_NOALLOC_MAX_DOUBLES).
+static __device__ __align__(256) double g_adj_scratch[PHD_ADJ_NOALLOC_MAX_DOUBLES];
+
+namespace {
+
+// Device address of g_adj_scratch on the current device.  In host code the symbol
+// name is only a host-side stand-in, so the address is asked from the runtime once per
+// device (with that device current) and cached.
+double *adj_scratch_on_current_device(int *rc) {
+    static std::mutex lock;
+    static double *addr[256] = {nullptr};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+        *rc = PHD_ERR_LAUNCH;
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> guard(lock);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_adj_scratch);
+        if (e != cudaSuccess || !p) {
+            *rc = PHD_ERR_LAUNCH;
+            return nullptr;
+        }
+        addr[dev] = static_cast<double *>(p);
+    }
+    return addr[dev];
+}
+
+}  // namespace
+
+extern "C" {
+
+int phd_adjoint_step_f64_noalloc(const phd_mesh *mesh, const phd_adj_index *index, const phd_params *par,
+                                 double dt, const double *cons, const double *prim, const double *grad,
+                                 const double *face_w, const double *lam_next, double *lam, cudaStream_t stream) {
+    if (!mesh || mesh->n_cells < 0 || mesh->n_faces < 0) return PHD_ERR_ARG;
+    if (phd_adjoint_work_doubles(mesh->n_cells, mesh->n_faces) > (size_t)PHD_ADJ_NOALLOC_MAX_DOUBLES)
+        return PHD_ERR_SCRATCH_TOO_SMALL;
+    int rc = PHD_OK;
+    double *work = adj_scratch_on_current_device(&rc);
+    if (!work) return rc;
+    return phd_adjoint_step_f64(mesh, index, par, dt, cons, prim, grad, face_w, lam_next, lam, work, stream);
 }
 
 }  // extern "C"
