@@ -413,9 +413,21 @@ def adjoint_cost(dev, n_side=128, n_steps=20, checkpoint=20):
     e[2].record()
     torch.cuda.synchronize()
     fwd, bwd = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    # the adjoint step alone (reverse kernels at recorded states) against the forward step
+    states = run._replay_segment(0, n_steps)
+    lam = torch.zeros((4, mesh.n_real), dtype=torch.float64, device=dev)
+    lam[0] = 1.0
+    torch.cuda.synchronize()
+    e[0].record()
+    for k in range(n_steps - 1, -1, -1):
+        lam = run._adjoint(recs[k], *states[k], lam)
+    e[1].record()
+    torch.cuda.synchronize()
+    adj_step = e[0].elapsed_time(e[1]) / n_steps
     return {"config": "gaussian bump %dx%d periodic, HLLC, FP64, %d steps, checkpoint every %d" %
                       (n_side, n_side, n_steps, checkpoint),
-            "forward_ms": fwd, "backward_ms": bwd, "ratio": bwd / fwd}
+            "forward_ms": fwd, "backward_ms": bwd, "ratio": bwd / fwd,
+            "forward_step_ms": fwd / n_steps, "adjoint_step_ms": adj_step, "step_ratio": adj_step * n_steps / fwd}
 
 
 def run_e2e(args, st, mesh, prim, dev):

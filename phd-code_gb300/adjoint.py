@@ -55,20 +55,50 @@ class StepRecord:
         self.dmesh = dmesh
         self.face_w = face_w
         self.dt = float(dt)
-        self._index = None
 
     def index(self):
-        if self._index is None:
-            dev = self.dmesh.device
-            p, gp, gi = adjoint_index(self.dmesh.host)
-            tens = [torch.as_tensor(a).to(dev) for a in (p, gp, gi)]
-            s = L.PhdAdjIndex(*(t.data_ptr() for t in tens))
-            self._index = (tens, s)
-        return self._index[1]
+        """Partner/ghost index of the step's mesh, built once per device mesh."""
+        dm = self.dmesh
+        cached = getattr(dm, "_adjoint_index", None)
+        if cached is None:
+            p, gp, gi = adjoint_index(dm.host)
+            tens = [torch.as_tensor(a).to(dm.device) for a in (p, gp, gi)]
+            cached = (tens, L.PhdAdjIndex(*(t.data_ptr() for t in tens)))
+            dm._adjoint_index = cached
+        return cached[1]
+
+
+class _MeshBuffers:
+    """Per-mesh device buffers reused by every step on that mesh."""
+
+    def __init__(self, dm, device):
+        n, F = dm.n_cells, max(dm.n_faces, 1)
+        self.cons = torch.zeros((4, n), dtype=F64, device=device)
+        self.nxt = torch.zeros_like(self.cons)
+        self.prim = torch.zeros_like(self.cons)
+        self.grad = torch.zeros((8, n), dtype=F64, device=device)
+        self.w = torch.zeros((2, n), dtype=F64, device=device)
+        self.flux = torch.zeros((4, F), dtype=F64, device=device)
+        self.lam_next = torch.zeros_like(self.cons)      # ghost rows stay zero
+        self.lam = torch.zeros_like(self.cons)
+        self.work = None
+
+    def adjoint_work(self, lib, dm, device):
+        if self.work is None:
+            self.work = torch.empty(int(lib.phd_adjoint_work_doubles(dm.n_cells, dm.n_faces)), dtype=F64,
+                                    device=device)
+        return self.work
 
 
 class FluxRunRecord:
-    """A recorded run: the per-step records and the options of the step."""
+    """A recorded run: the per-step records and the options of the step.
+
+    Consecutive steps on the same device mesh are chained on the device: the update
+    kernel already writes the next step's totals and primitives for every cell, ghosts
+    included, so only a change of mesh goes back through the real cells (ghost refresh
+    and primitive recovery on the new mesh).  Each step owns a row of a device clock
+    table (its dt), so no step waits on the host.
+    """
 
     def __init__(self, steps, gamma=1.4, solver="hllc", limiter="arepo", gizmo=True, boost=True,
                  reconstruction="linear", checkpoint=20, final_vol=None):
@@ -83,65 +113,132 @@ class FluxRunRecord:
         self.device = d0.device
         self.n_real = d0.n_real
         self.clock = DeviceClock(self.device)
+        rows = []
+        for rec in steps:
+            c = L.PhdClock()
+            c.dt = rec.dt
+            c.dtmin_bits = np.float64(np.inf).view(np.uint64).item()
+            rows.append(np.frombuffer(bytes(c), dtype=np.uint8))
+        self._clocks0 = torch.as_tensor(np.stack(rows)).to(self.device)
+        self.clocks = self._clocks0.clone()
+        self._bufs = {}
 
-    # --- one forward step on all-cell totals [4][n] of the step's mesh ---------------
+    def _buffers(self, dm):
+        b = self._bufs.get(id(dm))
+        if b is None:
+            b = self._bufs[id(dm)] = _MeshBuffers(dm, self.device)
+        return b
+
+    def _clock_ptr(self, k):
+        return ctypes.c_void_p(self.clocks[k].data_ptr())
+
+    def _load_real(self, dm, U_real, cons, prim):
+        """All-cell totals and primitives on mesh dm from the real cells' totals."""
+        s = L.stream_handle()
+        lib = L.lib()
+        cons[:, :dm.n_real].copy_(U_real)
+        L.check(lib.phd_ghost_cons_f64(dm.ref, L.ptr(cons), s), "ghost")
+        L.check(lib.phd_prim_from_cons_f64(2, dm.n_cells, self.params.gamma, L.ptr(dm.vol), L.ptr(cons),
+                                           L.ptr(prim), s), "prim")
+
+    def _step(self, k, prim, cons, nxt, grad):
+        """Step k: prim is overwritten with the next primitives, nxt receives the next
+        totals (all cells), grad the limited gradients of the incoming primitives."""
+        rec = self.steps[k]
+        b = self._buffers(rec.dmesh)
+        L.check(L.lib().phd_step_f64(rec.dmesh.ref, ctypes.byref(self.params), 0, L.ptr(prim), L.ptr(cons),
+                                     L.ptr(nxt), L.ptr(grad), L.ptr(b.w), L.ptr(rec.face_w), L.ptr(b.flux),
+                                     self._clock_ptr(k), L.stream_handle()), "step")
+
+    # --- one step in isolation, on real-cell totals (tests use these) ---------------
     def _forward_step(self, rec, U_real):
         dm = rec.dmesh
-        n = dm.n_cells
-        cons = torch.zeros((4, n), dtype=F64, device=self.device)
-        cons[:, :dm.n_real] = U_real
-        s = L.stream_handle()
-        lib = L.lib()
-        L.check(lib.phd_ghost_cons_f64(dm.ref, L.ptr(cons), s), "ghost")
-        prim = torch.empty_like(cons)
-        L.check(lib.phd_prim_from_cons_f64(2, n, self.params.gamma, L.ptr(dm.vol), L.ptr(cons), L.ptr(prim), s),
-                "prim")
-        nxt = torch.empty_like(cons)
-        grad = torch.zeros((8, n), dtype=F64, device=self.device)
-        w = torch.zeros((2, n), dtype=F64, device=self.device)
-        flux = torch.zeros((4, max(dm.n_faces, 1)), dtype=F64, device=self.device)
+        cons = torch.zeros((4, dm.n_cells), dtype=F64, device=self.device)
+        prim, nxt = torch.empty_like(cons), torch.empty_like(cons)
+        grad = torch.zeros((8, dm.n_cells), dtype=F64, device=self.device)
+        self._load_real(dm, U_real, cons, prim)
         self.clock.set(dt=rec.dt)
-        L.check(lib.phd_step_f64(dm.ref, ctypes.byref(self.params), 0, L.ptr(prim), L.ptr(cons), L.ptr(nxt),
-                                 L.ptr(grad), L.ptr(w), L.ptr(rec.face_w), L.ptr(flux), self.clock.ptr, s), "step")
+        b = self._buffers(dm)
+        L.check(L.lib().phd_step_f64(dm.ref, ctypes.byref(self.params), 0, L.ptr(prim), L.ptr(cons), L.ptr(nxt),
+                                     L.ptr(grad), L.ptr(b.w), L.ptr(rec.face_w), L.ptr(b.flux), self.clock.ptr,
+                                     L.stream_handle()), "step")
         return nxt[:, :dm.n_real].clone()
 
-    def forward(self, U0):
-        """Run all steps from U0 [4][n_real]; keep checkpoints; return U_T."""
-        self.ckpt = {0: U0.clone()}
-        U = U0
-        for k, rec in enumerate(self.steps):
-            U = self._forward_step(rec, U)
-            if (k + 1) % self.checkpoint == 0 and k + 1 < len(self.steps):
-                self.ckpt[k + 1] = U.clone()
-        st = self.clock.read().status
-        L.raise_status(st)
-        return U
-
-    # --- reverse ------------------------------------------------------------------
     def _adjoint_step(self, rec, U_real, lam_next_real):
         dm = rec.dmesh
-        n, nr = dm.n_cells, dm.n_real
-        lib = L.lib()
-        s = L.stream_handle()
-        cons = torch.zeros((4, n), dtype=F64, device=self.device)
-        cons[:, :nr] = U_real
-        L.check(lib.phd_ghost_cons_f64(dm.ref, L.ptr(cons), s), "ghost")
+        cons = torch.zeros((4, dm.n_cells), dtype=F64, device=self.device)
         prim = torch.empty_like(cons)
-        L.check(lib.phd_prim_from_cons_f64(2, n, self.params.gamma, L.ptr(dm.vol), L.ptr(cons), L.ptr(prim), s),
-                "prim")
-        grad = torch.zeros((8, n), dtype=F64, device=self.device)
+        grad = torch.zeros((8, dm.n_cells), dtype=F64, device=self.device)
+        self._load_real(dm, U_real, cons, prim)
         if self.params.reconstruction == L.LINEAR:
-            L.check(lib.phd_gradients_f64(dm.ref, L.ptr(prim), self.params.limiter, L.ptr(grad), self.clock.ptr, s),
-                    "gradients")
-        lam_next = torch.zeros((4, n), dtype=F64, device=self.device)
-        lam_next[:, :nr] = lam_next_real
-        lam = torch.empty_like(lam_next)
-        nwork = lib.phd_adjoint_work_doubles(n, dm.n_faces)
-        work = torch.empty(int(nwork), dtype=F64, device=self.device)
+            L.check(L.lib().phd_gradients_f64(dm.ref, L.ptr(prim), self.params.limiter, L.ptr(grad), self.clock.ptr,
+                                              L.stream_handle()), "gradients")
+        return self._adjoint(rec, cons, prim, grad, lam_next_real)
+
+    def _adjoint(self, rec, cons, prim, grad, lam_next_real):
+        """lam_n (real cells) from lam_{n+1} at the step's recorded all-cell state."""
+        dm = rec.dmesh
+        b = self._buffers(dm)
+        lib = L.lib()
+        b.lam_next[:, :dm.n_real].copy_(lam_next_real)
         L.check(lib.phd_adjoint_step_f64(dm.ref, ctypes.byref(rec.index()), ctypes.byref(self.params), rec.dt,
-                                         L.ptr(cons), L.ptr(prim), L.ptr(grad), L.ptr(rec.face_w), L.ptr(lam_next),
-                                         L.ptr(lam), L.ptr(work), s), "phd_adjoint_step_f64")
-        return lam[:, :nr].clone()
+                                         L.ptr(cons), L.ptr(prim), L.ptr(grad), L.ptr(rec.face_w),
+                                         L.ptr(b.lam_next), L.ptr(b.lam), L.ptr(b.adjoint_work(lib, dm, self.device)),
+                                         L.stream_handle()), "phd_adjoint_step_f64")
+        return b.lam[:, :dm.n_real].clone()
+
+    # --- whole run ------------------------------------------------------------------
+    def forward(self, U0):
+        """Run all steps from U0 [4][n_real]; keep checkpoints; return U_T."""
+        self.clocks.copy_(self._clocks0)
+        self.ckpt = {0: U0.clone()}
+        prev = None
+        for k, rec in enumerate(self.steps):
+            dm = rec.dmesh
+            b = self._buffers(dm)
+            if prev is None:
+                self._load_real(dm, U0, b.cons, b.prim)
+            elif prev is not b:
+                self._load_real(dm, prev.cons[:, :dm.n_real], b.cons, b.prim)
+            self._step(k, b.prim, b.cons, b.nxt, b.grad)
+            b.cons, b.nxt = b.nxt, b.cons
+            prev = b
+            if (k + 1) % self.checkpoint == 0 and k + 1 < len(self.steps):
+                self.ckpt[k + 1] = b.cons[:, :dm.n_real].clone()
+        UT = prev.cons[:, :self.steps[-1].dmesh.n_real].clone()
+        st = 0
+        for row in self.clocks.cpu().numpy():
+            st |= L.PhdClock.from_buffer_copy(row.tobytes()).status
+        L.raise_status(st)
+        return UT
+
+    def _replay_segment(self, a, b):
+        """Recompute the all-cell states (totals, primitives, gradients) entering steps
+        a..b-1 from the checkpoint at a."""
+        states = []
+        lib = L.lib()
+        cons = prim = None
+        self.clocks[a:b].copy_(self._clocks0[a:b])      # each step's CFL finish overwrote its dt
+        for k in range(a, b):
+            dm = self.steps[k].dmesh
+            n = dm.n_cells
+            if k == a or self.steps[k - 1].dmesh is not dm:
+                U_real = self.ckpt[a] if k == a else cons[:, :dm.n_real]
+                c = torch.empty((4, n), dtype=F64, device=self.device)
+                p = torch.empty_like(c)
+                self._load_real(dm, U_real, c, p)
+                cons, prim = c, p
+            grad = torch.zeros((8, n), dtype=F64, device=self.device)
+            states.append((cons, prim, grad))
+            if k + 1 < b:
+                nxt = torch.empty_like(cons)
+                p_next = prim.clone()                   # the step overwrites its primitives
+                self._step(k, p_next, cons, nxt, grad)
+                cons, prim = nxt, p_next
+            elif self.params.reconstruction == L.LINEAR:
+                L.check(lib.phd_gradients_f64(dm.ref, L.ptr(prim), self.params.limiter, L.ptr(grad),
+                                              self._clock_ptr(k), L.stream_handle()), "gradients")
+        return states
 
     def backward(self, lam_T):
         """dLoss/dU_0 from dLoss/dU_T, segment by segment (recompute from checkpoints)."""
@@ -151,11 +248,11 @@ class FluxRunRecord:
         for si in range(len(starts) - 1, -1, -1):
             a = starts[si]
             b = starts[si + 1] if si + 1 < len(starts) else N
-            states = [self.ckpt[a]]
-            for k in range(a, b - 1):
-                states.append(self._forward_step(self.steps[k], states[-1]))
+            states = self._replay_segment(a, b)
             for k in range(b - 1, a - 1, -1):
-                lam = self._adjoint_step(self.steps[k], states[k - a], lam)
+                cons, prim, grad = states[k - a]
+                lam = self._adjoint(self.steps[k], cons, prim, grad, lam)
+            del states
         return lam
 
 

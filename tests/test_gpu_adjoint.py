@@ -96,10 +96,13 @@ def multistep_case(m, prim, n_steps, limiter="arepo", checkpoint=5):
     return run, recs, p0, tgt, loss, p.grad.detach()
 
 
-@pytest.mark.parametrize("limiter", ["arepo", "tess"])
-def test_multistep_gradient_vs_finite_differences(limiter):
+def test_multistep_gradient_vs_finite_differences():
+    """AREPO limiter (the default and the adjoint workload's).  The TESS limiter takes
+    one minimum over every field's and face's ratio, so near-ties between candidates
+    put kinks within reach of a 1e-6 perturbation; it is checked against autograd
+    below, which follows the same branches."""
     m = lattice_mesh(16, "periodic", seed=4)
-    run, recs, p0, tgt, loss, g = multistep_case(m, generic_state(m), 12, limiter=limiter)
+    run, recs, p0, tgt, loss, g = multistep_case(m, generic_state(m), 12)
     rng = np.random.default_rng(7)
     h = 1e-6
     errs = []
@@ -113,8 +116,9 @@ def test_multistep_gradient_vs_finite_differences(limiter):
     assert max(errs) <= 1e-6, errs
 
 
-@pytest.mark.parametrize("state", ["generic", "noisy_background"])
-def test_multistep_gradient_vs_torch_autograd(state):
+@pytest.mark.parametrize("state,limiter", [("generic", "arepo"), ("noisy_background", "arepo"),
+                                           ("generic", "tess")])
+def test_multistep_gradient_vs_torch_autograd(state, limiter):
     """The recorded run's gradient (checkpoint-and-recompute through the hand-written
     kernels) against PyTorch autograd through the same steps (oracle/torch_step.py)."""
     m = lattice_mesh(16, "periodic", seed=4)
@@ -128,14 +132,14 @@ def test_multistep_gradient_vs_torch_autograd(state):
         prim = prim.copy()
         prim[:, :m.n_real] += 1e-3 * rng.uniform(-1.0, 1.0, (4, m.n_real))
         prim = pkg.meshgen.fill_ghosts(m, prim)
-    run, recs, p0, tgt, loss, g = multistep_case(m, prim, 10, checkpoint=4)
+    run, recs, p0, tgt, loss, g = multistep_case(m, prim, 10, limiter=limiter, checkpoint=4)
     tm = T.TorchMesh(m)
     w = torch.zeros((2, m.n_faces), dtype=torch.float64)
     vol = torch.tensor(m.vol[:m.n_real])
     pp = p0.cpu().clone().requires_grad_(True)
     U = T.cons_from_prim(pp, vol, 1.4)
     for rec in recs:
-        U = T.step(tm, U, w, rec.dt, 1.4)
+        U = T.step(tm, U, w, rec.dt, 1.4, limiter=limiter)
     ((U[0] / vol - tgt.cpu()) ** 2).sum().backward()
     gr = pp.grad.numpy()
     assert np.max(np.abs(g.cpu().numpy() - gr)) / np.max(np.abs(gr)) <= 1e-9
