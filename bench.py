@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--workload", default="shear", choices=["shear", "ensemble"])
     ap.add_argument("--runs", type=int, default=256)
+    ap.add_argument("--no-tune", action="store_true", help="FP32: default launch shapes instead of autotuned")
     return ap.parse_args()
 
 
@@ -250,23 +251,19 @@ def run_ours(args, rank, world):
     for e in marks:
         e.record()
     torch.cuda.synchronize()
+    launch_cfg = "default (256 threads, one per item)"
+    if st.precision == "fp32" and not args.no_tune:
+        from phd_code_gb300.autotune import tune
+        lch, _ = tune(st)
+        st.launch = lch
+        launch_cfg = {"blocks": [lch.block_grad, lch.block_face, lch.block_update],
+                      "grid_caps": [lch.grid_cap_grad, lch.grid_cap_face, lch.grid_cap_update]}
     st.step(max(3, args.warmup))
     torch.cuda.synchronize()
     st.check_status()
 
     def marked_step(k):
-        arr = (ctypes.c_void_p * 4)(*(marks[4 * k + q].cuda_event for q in range(4)))
-        s = L.stream_handle()
-        if st.precision == "fp32":
-            rc = lib.phd_step_f32_marked(st.dmesh.ref, ctypes.byref(st.geo), ctypes.byref(st.params),
-                                         int(st.moving), L.ptr(st.prim4), L.ptr(st.cons), L.ptr(st.cons_next),
-                                         L.ptr(st.grad8), L.ptr(st.w2), L.ptr(st.flux4), st.clock.ptr, s, arr)
-        else:
-            rc = lib.phd_step_f64_marked(st.dmesh.ref, ctypes.byref(st.params), int(st.moving), L.ptr(st.prim),
-                                         L.ptr(st.cons), L.ptr(st.cons_next), L.ptr(st.grad), L.ptr(st.w),
-                                         L.ptr(st.face_w), L.ptr(st.flux), st.clock.ptr, s, arr)
-        L.check(rc, "step")
-        st.cons, st.cons_next = st.cons_next, st.cons
+        st._launch_step(marks=(ctypes.c_void_p * 4)(*(marks[4 * k + q].cuda_event for q in range(4))))
 
     if world > 1:
         torch.distributed.barrier()
@@ -345,7 +342,7 @@ def run_ours(args, rank, world):
                           "mesh": "fixed across steps (host re-mesh outside the path)",
                           "l2": "inputs larger than L2 (per-step working set %.0f MB > 129 MB)"
                                 % (sum(algo.values()) / 1e6),
-                          "parallelism": "replicas" if world > 1 else "single GPU"},
+                          "parallelism": "replicas" if world > 1 else "single GPU", "launch": launch_cfg},
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
                "adjoint": adjoint,
                "gpu_launches": 3 * args.steps, "clocks": clocks}
@@ -431,27 +428,23 @@ def adjoint_cost(dev, n_side=128, n_steps=20, checkpoint=20):
 
 
 def run_e2e(args, st, mesh, prim, dev):
+    """The same step through the public API with host buffers: every step the host
+    hands over its tessellation (face list: pair-i/j, area, centroid; cell geometry:
+    x, dcom, vol, tag, type, map) from pinned memory with FluxStepper.load_mesh, which
+    forms the neighbour lists, flip bits, periodic twins and FP32 geometry on the
+    device, re-creates the ghosts and recovers the primitives; the step runs; the
+    generator velocities (what the host re-mesh needs) and the clock come back."""
     import torch
     from phd_code_gb300 import _lib as L
-    import ctypes
     dm = st.dmesh
-    names = ("tag", "type", "map", "x", "dcom", "vol", "pair_i", "pair_j", "area", "com", "normal",
-             "nbr_ptr", "nbr_idx")
-    host = {nm: getattr(dm, nm).cpu().pin_memory() for nm in names}
+    pinned = dm.pinned_host(mesh)
     w_host = torch.empty_like(st.w2 if st.precision == "fp32" else st.w, device="cpu").pin_memory()
     clk_host = torch.empty(L.CLOCK_BYTES, dtype=torch.uint8).pin_memory()
-    lib = L.lib()
-    h2d = sum(t.numel() * t.element_size() for t in host.values())
     d2h = w_host.numel() * w_host.element_size() + clk_host.numel()
+    h2d = [0]
 
     def one():
-        s = L.stream_handle()
-        for nm in names:
-            getattr(dm, nm).copy_(host[nm], non_blocking=True)
-        if st.precision == "fp32":
-            out = L.PhdGeom32Out(*(t.data_ptr() for t in (st.face_geo, st.face_ar, st.csr_face, st.csr_nbr,
-                                                           st.cell_geo)))
-            L.check(lib.phd_prepare_f32(dm.ref, L.ptr(st.twin), ctypes.byref(out), s), "prepare")
+        h2d[0] = st.load_mesh(pinned)
         st.step(1)
         w_host.copy_(st.w2 if st.precision == "fp32" else st.w, non_blocking=True)
         clk_host.copy_(st.clock.buf, non_blocking=True)
@@ -459,6 +452,8 @@ def run_e2e(args, st, mesh, prim, dev):
     for _ in range(2):
         one()
     torch.cuda.synchronize()
+    if dm.upload_errors():
+        raise RuntimeError("mesh upload reported faces with out-of-range cells")
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     t0 = time.perf_counter()
@@ -468,12 +463,14 @@ def run_e2e(args, st, mesh, prim, dev):
     e1.record()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    st.check_status()
     ms = e0.elapsed_time(e1) / args.e2e_steps
     return {"value": mesh.n_faces / (max(ms * 1e-3, wall / args.e2e_steps)), "unit": UNIT,
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "h2d_bytes_per_step": int(h2d[0]), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": max(ms, 1e3 * wall / args.e2e_steps), "steps": args.e2e_steps,
-            "what": "per step: host mesh (face list + cell geometry) H2D from pinned memory, FP32 geometry "
-                    "prepare, flux step, generator velocities + clock D2H"}
+            "what": "per step: host tessellation (face list + cell geometry) H2D from pinned memory; neighbour "
+                    "lists, flip bits, periodic twins, FP32 geometry, ghost refresh and primitives formed on the "
+                    "device; flux step; generator velocities + clock D2H"}
 
 
 def run_ensemble(args, rank, world):

@@ -63,7 +63,9 @@ typedef struct phd_mesh {
     const int32_t *pair_i, *pair_j;   /* [n_faces] */
     const double *area;       /* [n_faces] */
     const double *com;        /* [dim][n_faces] face centroid */
-    const double *normal;     /* [dim][n_faces] (x_j - x_i)/|x_j - x_i| */
+    const double *normal;     /* [dim][n_faces] (x_j - x_i)/|x_j - x_i|; may be NULL for
+                                 phd_prepare_f32 (which then forms FP32 normals), entries
+                                 that read FP64 normals return PHD_ERR_ARG without them */
     const int32_t *nbr_ptr;   /* [n_cells+1] */
     const int32_t *nbr_idx;   /* [2*n_faces] */
 } phd_mesh;
@@ -174,8 +176,11 @@ int phd_step_f64_marked(const phd_mesh *mesh, const phd_params *par, int32_t mov
                         cudaStream_t stream, cudaEvent_t *marks);
 
 /* ---- fused FP32 step (FP32 reconstruction / Riemann, FP64 conserved totals) --------
- * Mesh-relative FP32 geometry, formed in FP64 once per mesh by phd_prepare_f32:
- *   face_geo [F][4] (n_x, n_y, c_x, c_y), c = face centroid - (x_i + x_j)/2
+ * Mesh-relative FP32 geometry, formed once per mesh by phd_prepare_f32 (the
+ * cancelling differences in FP64, each rounded once to FP32):
+ *   face_geo [F][4] (n_x, n_y, c_x, c_y), c = face centroid - (x_i + x_j)/2; the
+ *                   normal is mesh->normal rounded, or (x_j - x_i)/|x_j - x_i| in FP32
+ *                   when mesh->normal is NULL
  *   face_ar  [F][2] (area, |x_j - x_i|)
  *   csr_face [2F]   per-cell face list (nbr_ptr order): face id where the cell is
  *                   pair-i, ~face id where it is pair-j
@@ -303,6 +308,37 @@ int phd_flip_mask(int32_t dim, int32_t n, const int8_t *type, const double *x,
  * LoadBalance.compute_hilbert_keys (load_balance.pyx:195-217). */
 int phd_hilbert_keys_2d(int32_t n, const double *x, double corner_x, double corner_y,
                         double fac, int32_t order, int64_t *keys, cudaStream_t stream);
+
+/* ---- quantities of an uploaded mesh derived on the device ------------------------
+ * A host re-mesh hands over the face list (pair-i/j, area, centroid) and the cell
+ * geometry every step; the normals and the neighbour lists follow from those, so the
+ * device forms them instead of receiving them (Tess2d::extract_geometry tess.cpp:
+ * 285-398 is where the reference forms them on the host). */
+
+/* Face normals (x_j - x_i)/|x_j - x_i| (tess.cpp:320-327, 367-369) in IEEE
+ * round-to-nearest FP64, bit-identical to the same formula evaluated on a host without
+ * fused multiply-add.  normal: [2][n_faces].  Faces with out-of-range cells get a zero
+ * normal and are counted into *bad (device int32, may be NULL). */
+int phd_face_normals_f64(const phd_mesh *mesh, double *normal, int32_t *bad, cudaStream_t stream);
+
+/* Neighbour lists (Mesh.neighbors mesh.pxd:34, filled at tess.cpp:378-379): for every
+ * cell, the ids of the faces it belongs to in ascending order, as CSR nbr_ptr[n_cells+1],
+ * nbr_idx[2*n_faces], from mesh->pair_i/pair_j only.  work: phd_csr_work_ints(n_cells)
+ * device int32 of scratch.  Faces whose cells are out of range or equal are left out and
+ * counted into *bad (device int32, may be NULL).  Deterministic: the same lists whatever
+ * order the device visits the faces in. */
+size_t phd_csr_work_ints(int32_t n_cells);
+int phd_build_csr(const phd_mesh *mesh, int32_t *nbr_ptr, int32_t *nbr_idx, int32_t *work, int32_t *bad,
+                  cudaStream_t stream);
+
+/* Periodic twin table for phd_prepare_f32 (see phd_geom32): a boundary face emitted
+ * from both sides (tess.cpp:363, mesh.pyx:529-544) as (i, ghost of k) and (k, ghost
+ * of i) with opposite periodic shifts; twin[f] = the lower id for the higher-id copy f,
+ * -1 elsewhere.  box_x/box_y: the periodic box lengths.  Needs mesh->map, x and the
+ * neighbour lists.  periodic = 0 (reflective ghosts, whose mirror-image faces are
+ * distinct faces) fills every entry with -1. */
+int phd_periodic_twins(const phd_mesh *mesh, int32_t periodic, double box_x, double box_y,
+                       int32_t *twin, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -107,6 +107,10 @@ SIGNATURES = {
                                      C.c_int),
     "phd_flip_mask": ([_i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp, _vp], C.c_int),
     "phd_hilbert_keys_2d": ([_i32, _vp, _f64, _f64, _f64, _i32, _vp, _vp], C.c_int),
+    "phd_face_normals_f64": ([_PM, _vp, _vp, _vp], C.c_int),
+    "phd_csr_work_ints": ([_i32], C.c_size_t),
+    "phd_build_csr": ([_PM, _vp, _vp, _vp, _vp, _vp], C.c_int),
+    "phd_periodic_twins": ([_PM, _i32, _f64, _f64, _vp, _vp], C.c_int),
 }
 
 

@@ -30,7 +30,11 @@ __device__ __forceinline__ void set_status32(phd_clock *clk, int bits) {
     if (bits) atomicOr(&clk->status, bits);
 }
 
-// ---- mesh preparation (once per uploaded mesh, FP64 arithmetic) -------------------
+// ---- mesh preparation (once per uploaded mesh) ----------------------------------
+// The differences that cancel (x_j - x_i, face centroid minus generator midpoint) are
+// taken in FP64 and rounded once to FP32; everything formed from them afterwards
+// (separation length, normal when the mesh carries none, 1/V, R) is FP32.  The
+// FP64 -> FP32 roundings use integer arithmetic (narrow_f64), off the FP64 pipe.
 __global__ void k_prepare_faces32(phd_mesh M, float4 *__restrict__ face_geo, float2 *__restrict__ face_ar) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M.n_faces) return;
@@ -44,18 +48,28 @@ __global__ void k_prepare_faces32(phd_mesh M, float4 *__restrict__ face_geo, flo
         cx = M.com[m] - 0.5 * (xi + xj);
         cy = M.com[(size_t)F + m] - 0.5 * (yi + yj);
     }
-    const double r = sqrt(dx * dx + dy * dy);
-    face_geo[m] = make_float4((float)M.normal[m], (float)M.normal[(size_t)F + m], (float)cx, (float)cy);
-    face_ar[m] = make_float2((float)M.area[m], (float)r);
+    const float fx = narrow_f64(dx), fy = narrow_f64(dy);
+    const float r = sqrtf(fx * fx + fy * fy);
+    float nx, ny;
+    if (M.normal) {
+        nx = narrow_f64(M.normal[m]);
+        ny = narrow_f64(M.normal[(size_t)F + m]);
+    } else {                       // n = (x_j - x_i)/|x_j - x_i| (tess.cpp:367-369)
+        const float inv = r > 0.f ? 1.f / r : 0.f;
+        nx = fx * inv;
+        ny = fy * inv;
+    }
+    face_geo[m] = make_float4(nx, ny, narrow_f64(cx), narrow_f64(cy));
+    face_ar[m] = make_float2(narrow_f64(M.area[m]), r);
 }
 
 __global__ void k_prepare_cells32(phd_mesh M, float4 *__restrict__ cell_geo) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M.n_cells) return;
     const int n = M.n_cells;
-    const double v = M.vol[i];
-    cell_geo[i] = make_float4((float)M.dcom[i], (float)M.dcom[(size_t)n + i], (float)(1.0 / v),
-                              (float)sqrt(v / 3.141592653589793));
+    const float v = narrow_f64(M.vol[i]);
+    cell_geo[i] = make_float4(narrow_f64(M.dcom[i]), narrow_f64(M.dcom[(size_t)n + i]), 1.f / v,
+                              sqrtf(v * 0.3183098861837907f));
 }
 
 // CSR entries with the side folded into the face id, plus the neighbour cell.  Where a

@@ -557,6 +557,7 @@ int phd_riemann_f64(const phd_mesh *mesh, int32_t solver, double gamma, int32_t 
                     const double *left, const double *right, const double *face_w, double *flux,
                     phd_clock *clk, cudaStream_t stream) {
     if (!mesh_ok(mesh) || !left || !right || !flux) return PHD_ERR_ARG;
+    if (mesh->n_faces && !mesh->normal) return PHD_ERR_ARG;
     if (solver < PHD_HLL || solver > PHD_EXACT) return PHD_ERR_ARG;
     if (mesh->n_faces == 0) return PHD_OK;
     k_riemann<2><<<grid_of(mesh->n_faces), BLOCK, 0, stream>>>(*mesh, solver, gamma, boost, exact_max_iter,
@@ -616,6 +617,7 @@ int phd_step_f64_marked(const phd_mesh *mesh, const phd_params *par, int32_t mov
                         const double *cons, double *cons_next, double *grad, double *w, double *face_w,
                         double *flux, phd_clock *clk, cudaStream_t stream, cudaEvent_t *marks) {
     if (!mesh_ok(mesh) || !par || !prim || !cons || !cons_next || !flux || !clk) return PHD_ERR_ARG;
+    if (mesh->n_faces && !mesh->normal) return PHD_ERR_ARG;
     const bool linear = par->reconstruction == PHD_LINEAR;
     if (linear && !grad) return PHD_ERR_ARG;
     if (moving && (!w || !face_w)) return PHD_ERR_ARG;

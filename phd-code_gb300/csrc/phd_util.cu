@@ -1,4 +1,6 @@
-// phd_util.cu -- mesh-preparation kernels: reflective flip bits and Hilbert keys.
+// phd_util.cu -- mesh-preparation kernels: reflective flip bits, Hilbert keys, and the
+// quantities of an uploaded face list that the device derives instead of receiving them
+// (face normals, neighbour lists).
 #include "phd_common.cuh"
 
 namespace phd {
@@ -47,6 +49,189 @@ __global__ void k_hilbert_2d(int n, const double *__restrict__ x, double cx, dou
     keys[p] = key;
 }
 
+
+// Face normal n = (x_j - x_i) / |x_j - x_i| as the tessellation forms it
+// (tess.cpp:320-327, 367-369): h = sqrt(xr*xr + yr*yr), n = (xr/h, yr/h).  Explicit
+// round-to-nearest operations keep the products and the sum unfused, so the result is
+// the same double a host computes with IEEE arithmetic.
+__global__ void k_face_normals(int n, int F, const int32_t *__restrict__ pair_i, const int32_t *__restrict__ pair_j,
+                               const double *__restrict__ x, double *__restrict__ normal,
+                               int32_t *__restrict__ bad) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= F) return;
+    const int i = pair_i[m], j = pair_j[m];
+    double nx = 0.0, ny = 0.0;
+    if (i >= 0 && i < n && j >= 0 && j < n) {
+        const double xr = __dsub_rn(x[j], x[i]);
+        const double yr = __dsub_rn(x[(size_t)n + j], x[(size_t)n + i]);
+        const double h = __dsqrt_rn(__dadd_rn(__dmul_rn(xr, xr), __dmul_rn(yr, yr)));
+        nx = __ddiv_rn(xr, h);
+        ny = __ddiv_rn(yr, h);
+    } else if (bad) {
+        atomicAdd(bad, 1);
+    }
+    normal[m] = nx;
+    normal[(size_t)F + m] = ny;
+}
+
+// ---- neighbour lists from the face pairs -----------------------------------------
+// The tessellation appends every face id to the lists of both its cells in creation
+// order (tess.cpp:378-379), so each cell's list is its face ids in ascending order.
+// Built here as: count per cell, exclusive scan to offsets, scatter with a per-cell
+// cursor, then sort each cell's short list -- the scatter order does not matter, the
+// result is deterministic.
+constexpr int SCAN_THREADS = 1024, SCAN_ITEMS = 4, SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+__global__ void k_csr_count(int n, int F, const int32_t *__restrict__ pair_i, const int32_t *__restrict__ pair_j,
+                            int32_t *__restrict__ cnt, int32_t *__restrict__ bad) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= F) return;
+    const int i = pair_i[m], j = pair_j[m];
+    if (i >= 0 && i < n && j >= 0 && j < n && i != j) {
+        atomicAdd(&cnt[i], 1);
+        atomicAdd(&cnt[j], 1);
+    } else if (bad) {
+        atomicAdd(bad, 1);
+    }
+}
+
+// Exclusive prefix sum of one block's SCAN_TILE items (returns this thread's four
+// exclusive prefixes and the tile total).
+__device__ __forceinline__ void tile_scan(const int32_t v[SCAN_ITEMS], int32_t ex[SCAN_ITEMS], int32_t &total) {
+    __shared__ int32_t s_warp[SCAN_THREADS / 32];
+    int32_t run = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) { ex[k] = run; run += v[k]; }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int32_t inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) s_warp[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        int32_t w = s_warp[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        s_warp[lane] = w;                       // inclusive over warps
+    }
+    __syncthreads();
+    const int32_t before = (wid ? s_warp[wid - 1] : 0) + inc - run;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) ex[k] += before;
+    total = s_warp[SCAN_THREADS / 32 - 1];
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(int n, const int32_t *__restrict__ cnt,
+                                                             int32_t *__restrict__ tile_sum) {
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    int32_t v[SCAN_ITEMS], ex[SCAN_ITEMS], total;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = (base + k < n) ? cnt[base + k] : 0;
+    tile_scan(v, ex, total);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// one block: exclusive scan of the tile sums in place
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_sums(int n_tiles, int32_t *__restrict__ tile_sum) {
+    int32_t carry = 0;
+    for (int b0 = 0; b0 < n_tiles; b0 += SCAN_TILE) {
+        const int base = b0 + threadIdx.x * SCAN_ITEMS;
+        int32_t v[SCAN_ITEMS], ex[SCAN_ITEMS], total;
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++) v[k] = (base + k < n_tiles) ? tile_sum[base + k] : 0;
+        tile_scan(v, ex, total);
+#pragma unroll
+        for (int k = 0; k < SCAN_ITEMS; k++)
+            if (base + k < n_tiles) tile_sum[base + k] = carry + ex[k];
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_offsets(int n, const int32_t *__restrict__ cnt,
+                                                               const int32_t *__restrict__ tile_sum,
+                                                               int32_t *__restrict__ ptr) {
+    const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    int32_t v[SCAN_ITEMS], ex[SCAN_ITEMS], total;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = (base + k < n) ? cnt[base + k] : 0;
+    tile_scan(v, ex, total);
+    const int32_t off = tile_sum[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        if (base + k < n) ptr[base + k] = off + ex[k];
+        if (base + k == n - 1) ptr[n] = off + ex[k] + v[k];
+    }
+}
+
+__global__ void k_csr_scatter(int n, int F, const int32_t *__restrict__ pair_i, const int32_t *__restrict__ pair_j,
+                              const int32_t *__restrict__ ptr, int32_t *__restrict__ cursor,
+                              int32_t *__restrict__ idx) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= F) return;
+    const int i = pair_i[m], j = pair_j[m];
+    if (i >= 0 && i < n && j >= 0 && j < n && i != j) {
+        idx[ptr[i] + atomicAdd(&cursor[i], 1)] = m;
+        idx[ptr[j] + atomicAdd(&cursor[j], 1)] = m;
+    }
+}
+
+__global__ void k_csr_sort(int n, const int32_t *__restrict__ ptr, int32_t *__restrict__ idx) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const int e0 = ptr[c], e1 = ptr[c + 1];
+    for (int e = e0 + 1; e < e1; e++) {          // insertion sort: lists hold a few entries
+        const int32_t v = idx[e];
+        int k = e - 1;
+        while (k >= e0 && idx[k] > v) {
+            idx[k + 1] = idx[k];
+            k--;
+        }
+        idx[k + 1] = v;
+    }
+}
+
+// ---- periodic twin faces -----------------------------------------------------------
+// With periodic ghosts a boundary face is emitted twice: as (i, ghost of k) while
+// tessellating i and as (k, ghost of i) while tessellating k (tess.cpp:363, each copy
+// updating only its real cell, mesh.pyx:529-544).  For each copy a = (i, g), k = map[g],
+// with periodic shift s = rint((x_g - x_k)/L), the twin is the face b = (k, g') in k's
+// list with map[g'] = i and shift -s.  twin[a] = b when b < a (the lower id is kept),
+// else -1.  Same pairing as the host's periodic_twins (phd_code_gb300.twins).
+__global__ void k_periodic_twins(phd_mesh M, int periodic, double Lx, double Ly, int32_t *__restrict__ twin) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= M.n_faces) return;
+    const int n = M.n_cells, nr = M.n_real;
+    int32_t out = -1;
+    const int i = M.pair_i[a], g = M.pair_j[a];
+    if (periodic && i >= 0 && i < nr && g >= nr && g < n) {
+        const int k = M.map[g];
+        if (k >= 0 && k < nr && k != i) {
+            const double sx = rint(__ddiv_rn(__dsub_rn(M.x[g], M.x[k]), Lx));
+            const double sy = rint(__ddiv_rn(__dsub_rn(M.x[(size_t)n + g], M.x[(size_t)n + k]), Ly));
+            for (int e = M.nbr_ptr[k]; e < M.nbr_ptr[k + 1]; e++) {
+                const int b = M.nbr_idx[e];
+                if (b < 0 || b >= M.n_faces || b == a || M.pair_i[b] != k) continue;
+                const int g2 = M.pair_j[b];
+                if (g2 < nr || g2 >= n || M.map[g2] != i) continue;
+                const double tx = rint(__ddiv_rn(__dsub_rn(M.x[g2], M.x[i]), Lx));
+                const double ty = rint(__ddiv_rn(__dsub_rn(M.x[(size_t)n + g2], M.x[(size_t)n + i]), Ly));
+                if (tx == -sx && ty == -sy) {
+                    if (b < a) out = b;
+                    break;
+                }
+            }
+        }
+    }
+    twin[a] = out;
+}
+
 }  // namespace phd
 
 extern "C" {
@@ -66,6 +251,54 @@ int phd_hilbert_keys_2d(int32_t n, const double *x, double corner_x, double corn
     if (n <= 0 || !x || !keys || order < 1 || order > 31) return PHD_ERR_ARG;
     phd::k_hilbert_2d<<<(n + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(n, x, corner_x, corner_y,
                                                                                      fac, order, keys);
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+
+int phd_face_normals_f64(const phd_mesh *mesh, double *normal, int32_t *bad, cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || mesh->n_cells < 0 || mesh->n_faces < 0 || !normal) return PHD_ERR_ARG;
+    if (mesh->n_faces && (!mesh->pair_i || !mesh->pair_j || !mesh->x)) return PHD_ERR_ARG;
+    if (!mesh->n_faces) return PHD_OK;
+    phd::k_face_normals<<<(mesh->n_faces + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(
+        mesh->n_cells, mesh->n_faces, mesh->pair_i, mesh->pair_j, mesh->x, normal, bad);
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+size_t phd_csr_work_ints(int32_t n_cells) {
+    const size_t n = n_cells > 0 ? (size_t)n_cells : 0;
+    return 2 * n + (n + phd::SCAN_TILE - 1) / phd::SCAN_TILE;
+}
+
+int phd_build_csr(const phd_mesh *mesh, int32_t *nbr_ptr, int32_t *nbr_idx, int32_t *work, int32_t *bad,
+                  cudaStream_t stream) {
+    if (!mesh || mesh->n_cells <= 0 || mesh->n_faces < 0 || !nbr_ptr || !work) return PHD_ERR_ARG;
+    if (mesh->n_faces && (!mesh->pair_i || !mesh->pair_j || !nbr_idx)) return PHD_ERR_ARG;
+    const int n = mesh->n_cells, F = mesh->n_faces;
+    const int n_tiles = (n + phd::SCAN_TILE - 1) / phd::SCAN_TILE;
+    int32_t *cnt = work, *cursor = work + n, *tile_sum = work + 2 * (size_t)n;
+    cudaMemsetAsync(work, 0, sizeof(int32_t) * phd_csr_work_ints(n), stream);
+    const int gf = F ? (F + phd::UBLOCK - 1) / phd::UBLOCK : 1;
+    if (F) phd::k_csr_count<<<gf, phd::UBLOCK, 0, stream>>>(n, F, mesh->pair_i, mesh->pair_j, cnt, bad);
+    phd::k_scan_tiles<<<n_tiles, phd::SCAN_THREADS, 0, stream>>>(n, cnt, tile_sum);
+    phd::k_scan_tile_sums<<<1, phd::SCAN_THREADS, 0, stream>>>(n_tiles, tile_sum);
+    phd::k_scan_offsets<<<n_tiles, phd::SCAN_THREADS, 0, stream>>>(n, cnt, tile_sum, nbr_ptr);
+    if (F) {
+        phd::k_csr_scatter<<<gf, phd::UBLOCK, 0, stream>>>(n, F, mesh->pair_i, mesh->pair_j, nbr_ptr, cursor,
+                                                            nbr_idx);
+        phd::k_csr_sort<<<(n + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(n, nbr_ptr, nbr_idx);
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+int phd_periodic_twins(const phd_mesh *mesh, int32_t periodic, double box_x, double box_y, int32_t *twin,
+                       cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || mesh->n_cells <= 0 || mesh->n_faces < 0 || !twin) return PHD_ERR_ARG;
+    if (periodic && (!(box_x > 0.0) || !(box_y > 0.0))) return PHD_ERR_ARG;
+    if (!mesh->n_faces) return PHD_OK;
+    if (!mesh->pair_i || !mesh->pair_j || !mesh->map || !mesh->x || !mesh->nbr_ptr || !mesh->nbr_idx)
+        return PHD_ERR_ARG;
+    phd::k_periodic_twins<<<(mesh->n_faces + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(
+        *mesh, periodic != 0, box_x, box_y, twin);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 

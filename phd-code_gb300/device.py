@@ -17,6 +17,14 @@ from . import _lib as L
 F64 = torch.float64
 
 
+class _nullctx:
+    def __enter__(self):
+        return None
+
+    def __exit__(self, *a):
+        return False
+
+
 def _dev(device):
     d = torch.device(device)
     if d.type != "cuda":
@@ -68,6 +76,68 @@ class DeviceMesh:
             setattr(s, name, getattr(self, name).data_ptr())
         self.struct = s
         self.ref = C.byref(s)
+
+    # --- per-step hand-over of a new tessellation of the same size -----------------
+    UPLOAD = (("tag", np.int8), ("type", np.int8), ("map", np.int32), ("x", np.float64),
+              ("dcom", np.float64), ("vol", np.float64), ("pair_i", np.int32), ("pair_j", np.int32),
+              ("area", np.float64), ("com", np.float64))
+
+    def pinned_host(self, host=None):
+        """Pinned host copies of a host mesh's per-step arrays (the face list and the
+        cell geometry a host re-mesh writes, ``mesh.pyx:255-323``)."""
+        host = self.host if host is None else host
+        return {nm: torch.from_numpy(np.ascontiguousarray(getattr(host, nm), dtype=dt)).pin_memory()
+                for nm, dt in self.UPLOAD}
+
+    def upload(self, pinned, normals="device", stream=None):
+        """Hand over a new tessellation with this mesh's cell and face counts.
+
+        Copies the face list (pair-i/j, area, centroid) and the cell geometry (x, dcom,
+        vol, tag, type, map) from pinned host buffers, then forms on the device what
+        follows from them: the neighbour lists (phd_build_csr), the reflective flip bits
+        and, with ``normals="device"``, the FP64 face normals (phd_face_normals_f64).
+        ``normals="none"`` leaves the mesh without FP64 normals (FP32 consumers form
+        their own; FP64 entries then refuse the mesh).  Returns the bytes copied."""
+        if normals not in ("device", "none"):
+            raise ValueError("normals must be 'device' or 'none'")
+        shapes = {"tag": (self.n_cells,), "type": (self.n_cells,), "map": (self.n_cells,),
+                  "x": (self.dim, self.n_cells), "dcom": (self.dim, self.n_cells), "vol": (self.n_cells,),
+                  "pair_i": (self.n_faces,), "pair_j": (self.n_faces,), "area": (self.n_faces,),
+                  "com": (self.dim, self.n_faces)}
+        for nm, _ in self.UPLOAD:
+            if tuple(pinned[nm].shape) != shapes[nm]:
+                raise ValueError("upload: %s has shape %s, this mesh holds %s" % (nm, tuple(pinned[nm].shape),
+                                                                                 shapes[nm]))
+        lib = L.lib()
+        s = L.stream_handle(stream)
+        ctx = torch.cuda.stream(stream) if stream is not None else _nullctx()
+        nbytes = 0
+        with ctx:
+            for nm, _ in self.UPLOAD:
+                getattr(self, nm).copy_(pinned[nm], non_blocking=True)
+                nbytes += pinned[nm].numel() * pinned[nm].element_size()
+            if not hasattr(self, "_bad"):
+                self._bad = torch.zeros(1, dtype=torch.int32, device=self.device)
+                self._csr_work = torch.empty(int(lib.phd_csr_work_ints(self.n_cells)), dtype=torch.int32,
+                                             device=self.device)
+            self._bad.zero_()
+        L.check(lib.phd_build_csr(self.ref, L.ptr(self.nbr_ptr), L.ptr(self.nbr_idx), L.ptr(self._csr_work),
+                                  L.ptr(self._bad), s), "phd_build_csr")
+        xmin = (C.c_double * 3)(*(list(self.xmin) + [0.0] * (3 - self.dim)))
+        xmax = (C.c_double * 3)(*(list(self.xmax) + [0.0] * (3 - self.dim)))
+        L.check(lib.phd_flip_mask(self.dim, self.n_cells, L.ptr(self.type), L.ptr(self.x), xmin, xmax,
+                                  int(self.boundary == "reflective"), L.ptr(self.flip), s), "phd_flip_mask")
+        if normals == "device":
+            self.struct.normal = self.normal.data_ptr()
+            L.check(lib.phd_face_normals_f64(self.ref, L.ptr(self.normal), L.ptr(self._bad), s),
+                    "phd_face_normals_f64")
+        else:
+            self.struct.normal = None
+        return nbytes
+
+    def upload_errors(self):
+        """Faces of the last upload whose cells were out of range (synchronises)."""
+        return int(self._bad.item()) if hasattr(self, "_bad") else 0
 
     def h2d_bytes(self):
         """Bytes of one mesh upload (the per-step host->device face list and geometry)."""

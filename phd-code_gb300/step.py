@@ -36,6 +36,8 @@ class FluxStepper:
             raise ValueError("precision must be 'fp64' or 'fp32'")
         self.precision = precision
         self.stream = stream
+        self.dedup_periodic = bool(dedup_periodic)
+        self.launch = None          # FP32 launch shapes (PhdLaunch, e.g. from autotune.tune)
         n, F, d = dm.n_cells, dm.n_faces, dm.dim
         nf = d + 2
         dev = self.device
@@ -91,17 +93,53 @@ class FluxStepper:
         L.check(L.lib().phd_time_step_f64(self.dmesh.ref, L.ptr(self.prim), p.gamma, p.cfl, p.boost, 0,
                                           self.clock.ptr, L.stream_handle(self.stream)), "phd_time_step_f64")
 
-    def _launch_step(self):
+    def load_mesh(self, pinned):
+        """Continue on a new tessellation handed over from pinned host buffers
+        (``DeviceMesh.pinned_host`` layout; same cell and face counts, real cells in
+        the same order, as after the host re-mesh of ``integrate.py:410-417``).
+
+        The device forms the neighbour lists, flip bits and, for FP32, the periodic twin
+        table and FP32 geometry (normals included); FP64 forms its FP64 normals.  The
+        ghosts are re-created from their images (``domain_manager.pyx:712-774``), the
+        primitives recovered with the new volumes and the next dt taken from them
+        (Appendix steps 6-8 of the moving-mesh step).  Returns the bytes copied."""
+        dm, p = self.dmesh, self.params
+        lib = L.lib()
+        s = L.stream_handle(self.stream)
+        nbytes = dm.upload(pinned, normals="none" if self.precision == "fp32" else "device", stream=self.stream)
+        L.check(lib.phd_ghost_cons_f64(dm.ref, L.ptr(self.cons), s), "phd_ghost_cons_f64")
+        if self.precision == "fp32":
+            box = [b - a for a, b in zip(dm.xmin, dm.xmax)]
+            L.check(lib.phd_periodic_twins(dm.ref, int(self.dedup_periodic and dm.boundary == "periodic"),
+                                           float(box[0]), float(box[1]), L.ptr(self.twin), s),
+                    "phd_periodic_twins")
+            out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
+                                                            self.csr_nbr, self.cell_geo)))
+            L.check(lib.phd_prepare_f32(dm.ref, L.ptr(self.twin), ctypes.byref(out), s), "phd_prepare_f32")
+            L.check(lib.phd_prim_f32(dm.ref, ctypes.byref(p), L.ptr(self.cons), L.ptr(self.prim4),
+                                     self.clock.ptr, s), "phd_prim_f32")
+        else:
+            L.check(lib.phd_prim_from_cons_f64(dm.dim, dm.n_cells, p.gamma, L.ptr(dm.vol), L.ptr(self.cons),
+                                               L.ptr(self.prim), s), "phd_prim_from_cons_f64")
+            self.initial_time_step()
+        return nbytes
+
+    def _launch_step(self, marks=None):
+        """One step; marks: optional array of four CUDA events recorded at the stage
+        boundaries (before gradients, before faces, before the update, after it)."""
         dm, p = self.dmesh, self.params
         s = L.stream_handle(self.stream)
         if self.precision == "fp64":
-            rc = L.lib().phd_step_f64(dm.ref, ctypes.byref(p), int(self.moving), L.ptr(self.prim),
-                                      L.ptr(self.cons), L.ptr(self.cons_next), L.ptr(self.grad), L.ptr(self.w),
-                                      L.ptr(self.face_w), L.ptr(self.flux), self.clock.ptr, s)
+            rc = L.lib().phd_step_f64_marked(dm.ref, ctypes.byref(p), int(self.moving), L.ptr(self.prim),
+                                             L.ptr(self.cons), L.ptr(self.cons_next), L.ptr(self.grad),
+                                             L.ptr(self.w), L.ptr(self.face_w), L.ptr(self.flux), self.clock.ptr, s,
+                                             marks)
         else:
-            rc = L.lib().phd_step_f32(dm.ref, ctypes.byref(self.geo), ctypes.byref(p), int(self.moving),
-                                      L.ptr(self.prim4), L.ptr(self.cons), L.ptr(self.cons_next),
-                                      L.ptr(self.grad8), L.ptr(self.w2), L.ptr(self.flux4), self.clock.ptr, s)
+            lch = ctypes.byref(self.launch) if self.launch is not None else None
+            rc = L.lib().phd_step_f32_batched(dm.ref, ctypes.byref(self.geo), ctypes.byref(p), int(self.moving), lch,
+                                              L.ptr(self.prim4), L.ptr(self.cons), L.ptr(self.cons_next),
+                                              L.ptr(self.grad8), L.ptr(self.w2), L.ptr(self.flux4), self.clock.ptr,
+                                              1, None, s, marks)
         L.check(rc, "phd_step_" + self.precision)
         self.cons, self.cons_next = self.cons_next, self.cons
 
