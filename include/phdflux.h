@@ -222,7 +222,9 @@ int phd_prim_f32_batched(const phd_mesh *mesh, const phd_params *par, const doub
 /* One fused step (same order as phd_step_f64): gradients (+ generator velocities when
  * moving) -> per-face states, Riemann flux and deboost (face velocities formed on the
  * fly) -> segmented update into cons_next, FP32 primitives, next dt.
- * prim4 [n][4], grad8 [n][8], w2 [n][2], flux4 [F][4] (FP32); cons, cons_next [4][n] (FP64). */
+ * prim4 [n][4], grad8 [n][8], w2 [n][2], flux4 [F][4] (FP32; each face's conserved
+ * increment dt*A*F, applied with opposite signs to its two cells); cons, cons_next [4][n]
+ * (FP64). */
 int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par,
                  int32_t moving, float *prim4, const double *cons, double *cons_next, float *grad8,
                  float *w2, float *flux4, phd_clock *clk, cudaStream_t stream);

@@ -24,52 +24,71 @@ namespace phd {
 constexpr int BA = 256;
 constexpr int FACE_ADJ = 24;   // api[4] apj[4] agi[8] agj[8]
 
-// add_spatial (reference geometry) forward + reverse for one face.
-__device__ void spatial_adj_f64(const phd_mesh &M, int m, int i, int j, const double *pi, const double *pj,
-                                const double *gi, const double *gj, const double *w, bool boost, bool gizmo,
-                                const double *aL, const double *aR, double *api, double *apj, double *agi,
-                                double *agj) {
+// add_spatial (reference geometry) for one face, split into a forward pass that keeps
+// what the reverse needs (the "tape") and the reverse itself, so the adjoint kernel
+// evaluates the forward once.  The forward is face_spatial_f64's arithmetic in the
+// same order (so the same branches): boosted cell states, extrapolation along the
+// centroid separations, GIZMO pair limiter, revert where density or pressure < 0.
+struct SpatialTape {
+    double sl[4], sr[4], L0[4], R0[4], sepi[2], sepj[2], sepi_mag, sepj_mag, diff_mag;
+    bool revL, revR;
+};
+
+__device__ __forceinline__ void spatial_fwd_f64(const phd_mesh &M, int m, int i, int j, const double *pi,
+                                                const double *pj, const double *gi, const double *gj,
+                                                const double *w, bool boost, bool gizmo, SpatialTape &t,
+                                                double *Ls, double *Rs) {
     const int n = M.n_cells, F = M.n_faces;
-    double sl[4], sr[4], L0[4], R0[4], sepi[2], sepj[2];
-    for (int f = 0; f < 4; f++) { sl[f] = pi[f]; sr[f] = pj[f]; }
-    if (boost) for (int k = 0; k < 2; k++) { sl[1 + k] = pi[1 + k] - w[k]; sr[1 + k] = pj[1 + k] - w[k]; }
-    for (int f = 0; f < 4; f++) { L0[f] = sl[f]; R0[f] = sr[f]; }
+    for (int f = 0; f < 4; f++) { t.sl[f] = pi[f]; t.sr[f] = pj[f]; }
+    if (boost)
+        for (int k = 0; k < 2; k++) { t.sl[1 + k] = pi[1 + k] - w[k]; t.sr[1 + k] = pj[1 + k] - w[k]; }
+    for (int f = 0; f < 4; f++) { t.L0[f] = t.sl[f]; t.R0[f] = t.sr[f]; }
     double diff_mag = 0.0, sepi_mag = 0.0, sepj_mag = 0.0;
     for (int k = 0; k < 2; k++) {
         const double fc = M.com[(size_t)k * F + m];
         const double xik = M.x[(size_t)k * n + i], xjk = M.x[(size_t)k * n + j];
-        sepi[k] = fc - (xik + M.dcom[(size_t)k * n + i]);
-        sepj[k] = fc - (xjk + M.dcom[(size_t)k * n + j]);
-        sepi_mag = sepi_mag + sepi[k] * sepi[k];
-        sepj_mag = sepj_mag + sepj[k] * sepj[k];
+        t.sepi[k] = fc - (xik + M.dcom[(size_t)k * n + i]);
+        t.sepj[k] = fc - (xjk + M.dcom[(size_t)k * n + j]);
+        sepi_mag = sepi_mag + t.sepi[k] * t.sepi[k];
+        sepj_mag = sepj_mag + t.sepj[k] * t.sepj[k];
         diff_mag = diff_mag + t_sq(xjk - xik);
         for (int f = 0; f < 4; f++) {
-            L0[f] = L0[f] + gi[f * 2 + k] * sepi[k];
-            R0[f] = R0[f] + gj[f * 2 + k] * sepj[k];
+            t.L0[f] = t.L0[f] + gi[f * 2 + k] * t.sepi[k];
+            t.R0[f] = t.R0[f] + gj[f * 2 + k] * t.sepj[k];
         }
     }
-    sepi_mag = sqrt(sepi_mag);
-    sepj_mag = sqrt(sepj_mag);
-    diff_mag = sqrt(diff_mag);
+    t.sepi_mag = sqrt(sepi_mag);
+    t.sepj_mag = sqrt(sepj_mag);
+    t.diff_mag = sqrt(diff_mag);
+    t.revL = t.revR = false;
+    for (int f = 0; f < 4; f++) { Ls[f] = t.L0[f]; Rs[f] = t.R0[f]; }
+    if (gizmo) {
+        for (int f = 0; f < 4; f++)
+            gizmo_pair<double>(t.sl[f], t.sr[f], pi[f], pj[f], t.sepi_mag, t.sepj_mag, t.diff_mag, Ls[f], Rs[f]);
+        t.revL = (Ls[0] < 0.0 || Ls[3] < 0.0);
+        t.revR = (Rs[0] < 0.0 || Rs[3] < 0.0);
+        for (int f = 0; f < 4; f++) {
+            if (t.revL) Ls[f] = t.sl[f];
+            if (t.revR) Rs[f] = t.sr[f];
+        }
+    }
+}
+
+__device__ __forceinline__ void spatial_rev_f64(const SpatialTape &t, const double *pi, const double *pj,
+                                                bool gizmo, const double *aL, const double *aR, double *api,
+                                                double *apj, double *agi, double *agj) {
     double asl[4] = {0, 0, 0, 0}, asr[4] = {0, 0, 0, 0}, aL0[4] = {0, 0, 0, 0}, aR0[4] = {0, 0, 0, 0};
     if (gizmo) {
-        double L1[4], R1[4];
-        for (int f = 0; f < 4; f++) {
-            L1[f] = L0[f];
-            R1[f] = R0[f];
-            gizmo_pair<double>(sl[f], sr[f], pi[f], pj[f], sepi_mag, sepj_mag, diff_mag, L1[f], R1[f]);
-        }
-        const bool revL = (L1[0] < 0.0 || L1[3] < 0.0), revR = (R1[0] < 0.0 || R1[3] < 0.0);
         double aL1[4], aR1[4];
         for (int f = 0; f < 4; f++) {
-            aL1[f] = revL ? 0.0 : aL[f];
-            aR1[f] = revR ? 0.0 : aR[f];
-            if (revL) asl[f] += aL[f];
-            if (revR) asr[f] += aR[f];
+            aL1[f] = t.revL ? 0.0 : aL[f];
+            aR1[f] = t.revR ? 0.0 : aR[f];
+            if (t.revL) asl[f] += aL[f];
+            if (t.revR) asr[f] += aR[f];
         }
         for (int f = 0; f < 4; f++)
-            gizmo_pair_adj<double>(sl[f], sr[f], pi[f], pj[f], sepi_mag, sepj_mag, diff_mag, L0[f], R0[f], aL1[f],
-                                   aR1[f], asl[f], asr[f], aL0[f], aR0[f]);
+            gizmo_pair_adj<double>(t.sl[f], t.sr[f], pi[f], pj[f], t.sepi_mag, t.sepj_mag, t.diff_mag, t.L0[f],
+                                   t.R0[f], aL1[f], aR1[f], asl[f], asr[f], aL0[f], aR0[f]);
     } else {
         for (int f = 0; f < 4; f++) { aL0[f] = aL[f]; aR0[f] = aR[f]; }
     }
@@ -77,8 +96,8 @@ __device__ void spatial_adj_f64(const phd_mesh &M, int m, int i, int j, const do
         asl[f] += aL0[f];
         asr[f] += aR0[f];
         for (int k = 0; k < 2; k++) {
-            agi[f * 2 + k] += aL0[f] * sepi[k];
-            agj[f * 2 + k] += aR0[f] * sepj[k];
+            agi[f * 2 + k] += aL0[f] * t.sepi[k];
+            agj[f * 2 + k] += aR0[f] * t.sepj[k];
         }
         api[f] += asl[f];
         apj[f] += asr[f];
@@ -113,10 +132,11 @@ __global__ void __launch_bounds__(BA) k_adj_face(phd_mesh M, phd_params P, doubl
         double aF[4];
         for (int q = 0; q < 4; q++)
             aF[q] = da * ((jr ? lam_next[(size_t)q * n + j] : 0.0) - lam_next[(size_t)q * n + i]);
-        // forward states
+        // forward states (the spatial stage once, its tape kept for the reverse)
         double Ls[4], Rs[4], L[4], R[4];
+        SpatialTape tape;
         if (linear) {
-            face_spatial_f64<2>(M, m, i, j, pi, pj, gi, gj, w, boost, P.gizmo != 0, Ls, Rs);
+            spatial_fwd_f64(M, m, i, j, pi, pj, gi, gj, w, boost, P.gizmo != 0, tape, Ls, Rs);
             for (int f = 0; f < 4; f++) { L[f] = Ls[f]; R[f] = Rs[f]; }
             temporal<double, 2>(L, R, pi, pj, gi, gj, w, P.gamma, 0.5 * dt, boost);
         } else {
@@ -130,7 +150,7 @@ __global__ void __launch_bounds__(BA) k_adj_face(phd_mesh M, phd_params P, doubl
             double aLs[4] = {0, 0, 0, 0}, aRs[4] = {0, 0, 0, 0};
             temporal_adj<double>(Ls, Rs, pi, pj, gi, gj, w, P.gamma, 0.5 * dt, boost, aL, aR, aLs, aRs, api, apj,
                                  agi, agj);
-            spatial_adj_f64(M, m, i, j, pi, pj, gi, gj, w, boost, P.gizmo != 0, aLs, aRs, api, apj, agi, agj);
+            spatial_rev_f64(tape, pi, pj, P.gizmo != 0, aLs, aRs, api, apj, agi, agj);
         } else {
             for (int f = 0; f < 4; f++) { api[f] += aL[f]; apj[f] += aR[f]; }
         }
@@ -382,6 +402,7 @@ int phd_adjoint_step_f64(const phd_mesh *mesh, const phd_adj_index *index, const
                          const double *lam_next, double *lam, double *work, cudaStream_t stream) {
     if (!mesh || mesh->dim != 2 || !index || !par || !cons || !prim || !lam_next || !lam || !work)
         return PHD_ERR_ARG;
+    if (mesh->n_faces && !mesh->normal) return PHD_ERR_ARG;
     if (par->solver != PHD_HLL && par->solver != PHD_HLLC) return PHD_ERR_UNSUPPORTED;
     if (par->reconstruction == PHD_LINEAR && !grad) return PHD_ERR_ARG;
     const phd_mesh &M = *mesh;

@@ -18,7 +18,7 @@
 //   prim4     float4 [n]  (rho, v_x, v_y, p)
 //   grad8     float4 [2n] (d rho/dx, d rho/dy, d vx/dx, d vx/dy) (d vy/dx, d vy/dy, d p/dx, d p/dy)
 //   w2        float2 [n]  generator velocity
-//   flux4     float4 [F]  (mass, mom_x, mom_y, energy) flux through the face
+//   flux4     float4 [F]  dt*A*F: the face's conserved increment (mass, mom_x, mom_y, energy)
 #include "phd_common.cuh"
 #include "phd_physics.cuh"
 
@@ -80,23 +80,35 @@ __global__ void k_prepare_csr32(phd_mesh M, const int32_t *__restrict__ twin, in
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M.n_cells) return;
     const int n = M.n_cells, F = M.n_faces;
-    for (int e = M.nbr_ptr[c]; e < M.nbr_ptr[c + 1]; e++) {
-        int fid = M.nbr_idx[e];
-        if (fid < 0 || fid >= F) { csr_face[e] = 0; csr_nbr[e] = c; continue; }
-        const int a = M.pair_i[fid], b = M.pair_j[fid];
-        const bool as_i = (a == c);
-        int other = as_i ? b : a;
-        int code = as_i ? fid : ~fid;
-        if (twin && as_i) {
-            const int t = twin[fid];
-            if (t >= 0 && t < F) {       // this face is dropped: use the twin from the j side
-                code = ~t;
-                other = M.pair_i[t];
-            }
+    const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
+    constexpr int CH = 4;          // a chunk's independent gathers are issued together
+    for (int eb = e0; eb < e1; eb += CH) {
+        int fid[CH], a[CH], b[CH], t[CH];
+#pragma unroll
+        for (int k = 0; k < CH; k++) fid[k] = M.nbr_idx[(eb + k < e1) ? eb + k : e0];
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            const bool ok = fid[k] >= 0 && fid[k] < F;
+            a[k] = ok ? M.pair_i[fid[k]] : -1;
+            b[k] = ok ? M.pair_j[fid[k]] : -1;
+            t[k] = (ok && twin) ? twin[fid[k]] : -1;
         }
-        if (other < 0 || other >= n) other = c;
-        csr_face[e] = code;
-        csr_nbr[e] = other;
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            const int e = eb + k;
+            if (e >= e1) break;
+            if (fid[k] < 0 || fid[k] >= F) { csr_face[e] = 0; csr_nbr[e] = c; continue; }
+            const bool as_i = (a[k] == c);
+            int other = as_i ? b[k] : a[k];
+            int code = as_i ? fid[k] : ~fid[k];
+            if (as_i && t[k] >= 0 && t[k] < F) {   // this face is dropped: use the twin from the j side
+                code = ~t[k];
+                other = M.pair_i[t[k]];
+            }
+            if (other < 0 || other >= n) other = c;
+            csr_face[e] = code;
+            csr_nbr[e] = other;
+        }
     }
 }
 
@@ -269,7 +281,8 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
     phd_clock *clk = cell_run ? clocks + cell_run[i] : clocks;
     const bool boost = (SOLVER == PHD_EXACT) ? true : (P.boost != 0);
     const float gamma = narrow_f64(P.gamma);
-    const float dt_half = 0.5f * narrow_f64(clk->dt);
+    const float dtf = narrow_f64(clk->dt);
+    const float dt_half = 0.5f * dtf;
     const float4 g = face_geo[m];
     const float2 ar = face_ar[m];
     const float nrm[2] = {g.x, g.y};
@@ -323,7 +336,10 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
     if (SOLVER == PHD_EXACT) exact_flux<float, 2>(L, R, nrm, w, gamma, P.exact_max_iter, f, &failed);
     else hll_family<float, 2>(SOLVER == PHD_HLLC, L, R, nrm, w, gamma, boost, f);
     if (failed) set_status32(clk, PHD_STATUS_RIEMANN_NONCONVERGED);
-    flux4[m] = make_float4(f[0], f[1], f[2], f[3]);
+    // the face's conserved increment dt*A*F (mesh.pyx:519-544), formed once here so both
+    // cells of the face apply exactly the same value
+    const float s = dtf * ar.x;
+    flux4[m] = make_float4(s * f[0], s * f[1], s * f[2], s * f[3]);
 }
 
 template <int SOLVER, bool LINEAR>
@@ -350,7 +366,6 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 // One cell of the update: segmented sum, FP64 totals, primitives; returns the CFL
 // candidate (INFINITY for ghosts) and the cell's run.
 __device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const phd_params &P,
-                                               const float2 *__restrict__ face_ar,
                                                const int32_t *__restrict__ csr_face,
                                                const float4 *__restrict__ flux4,
                                                const float4 *__restrict__ cell_geo,
@@ -359,31 +374,24 @@ __device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const p
                                                const int32_t *__restrict__ cell_run, float gam) {
     const int n = M.n_cells;
     phd_clock *clk = cell_run ? clocks + cell_run[i] : clocks;
-    const float dtf = narrow_f64(clk->dt);
     const bool real = M.tag[i] == PHD_REAL_TAG;
     const int c = real ? i : M.map[i];
     if (c < 0 || c >= n) { set_status32(clk, PHD_STATUS_BAD_INDEX); return INFINITY; }
     float hs[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
     const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
-    constexpr int CH = 4;
+    constexpr int CH = 8;          // measured best for this kernel (CH = 1, 2, 4, 8 tried)
     for (int eb = e0; eb < e1; eb += CH) {
         int code[CH];
 #pragma unroll
         for (int k = 0; k < CH; k++) code[k] = csr_face[(eb + k < e1) ? eb + k : e0];
         float4 fl[CH];
-        float a[CH];
 #pragma unroll
-        for (int k = 0; k < CH; k++) {
-            const int fid = code[k] < 0 ? ~code[k] : code[k];
-            a[k] = face_ar[fid].x;
-            fl[k] = flux4[fid];
-        }
+        for (int k = 0; k < CH; k++) fl[k] = flux4[code[k] < 0 ? ~code[k] : code[k]];
 #pragma unroll
         for (int k = 0; k < CH; k++) {
             if (eb + k >= e1) break;
-            // one increment per face, identical for both of its cells
-            const float s = dtf * a[k];
-            const float inc[4] = {s * fl[k].x, s * fl[k].y, s * fl[k].z, s * fl[k].w};
+            // the face's increment dt*A*F, identical for both of its cells
+            const float inc[4] = {fl[k].x, fl[k].y, fl[k].z, fl[k].w};
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 float t, er;
@@ -424,8 +432,7 @@ __device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const p
     return cg.w / (boost ? cs : cs + sqrtf(vx * vx + vy * vy));
 }
 
-__global__ void __launch_bounds__(512) k_update32(phd_mesh M, phd_params P, const float2 *__restrict__ face_ar,
-                                                  const int32_t *__restrict__ csr_face,
+__global__ void __launch_bounds__(512) k_update32(phd_mesh M, phd_params P, const int32_t *__restrict__ csr_face,
                                                   const float4 *__restrict__ flux4, const float4 *__restrict__ cell_geo,
                                                   const double *__restrict__ cons, double *__restrict__ cons_next,
                                                   float4 *__restrict__ prim4, phd_clock *clocks,
@@ -440,8 +447,8 @@ __global__ void __launch_bounds__(512) k_update32(phd_mesh M, phd_params P, cons
         float cand = INFINITY;
         int run = 0;
         if (i < n) {
-            cand = update32_cell(i, M, P, face_ar, csr_face, flux4, cell_geo, cons, cons_next, prim4, clocks,
-                                 cell_run, gam);
+            cand = update32_cell(i, M, P, csr_face, flux4, cell_geo, cons, cons_next, prim4, clocks, cell_run,
+                                 gam);
             if (cell_run) run = cell_run[i];
         }
         if (!cell_run) {
@@ -476,18 +483,22 @@ __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const 
         float cand = INFINITY;
         int run = 0;
         if (i < n) {
-            const double U0 = cons[i], U1 = cons[(size_t)n + i], U2 = cons[2 * (size_t)n + i];
+            // the primitive recovery of k_update32 (FP32, internal energy formed in FP64)
             const double U3 = cons[3 * (size_t)n + i];
-            const double vol = M.vol[i];
-            const double rho = U0 / vol;
-            const double vx = U1 / U0, vy = U2 / U0;
-            const double p = (U3 / vol - 0.5 * rho * (vx * vx + vy * vy)) * (P.gamma - 1.0);
-            const float4 pr = make_float4((float)rho, (float)vx, (float)vy, (float)p);
+            const float m = narrow_f64(cons[i]), mx = narrow_f64(cons[(size_t)n + i]);
+            const float my = narrow_f64(cons[2 * (size_t)n + i]);
+            const float v = narrow_f64(M.vol[i]);
+            const float inv_v = 1.f / v;
+            const float rm = 1.f / m;
+            const float vx = mx * rm, vy = my * rm;
+            const float ke = 0.5f * (mx * vx + my * vy);
+            const float p = (gam - 1.f) * narrow_f64(U3 - widen_f32(ke)) * inv_v;
+            const float4 pr = make_float4(m * inv_v, vx, vy, p);
             prim4[i] = pr;
             if (M.tag[i] == PHD_REAL_TAG) {
                 const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
                 const float cs = sqrtf(gam * pr.w / pr.x);
-                const float R = sqrtf((float)vol * (float)(1.0 / 3.141592653589793));
+                const float R = sqrtf(v * 0.3183098861837907f);
                 cand = R / (boost ? cs : cs + sqrtf(pr.y * pr.y + pr.z * pr.z));
             }
             if (cell_run) run = cell_run[i];
@@ -621,7 +632,7 @@ int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_
         }
     }
     if (marks) cudaEventRecord(marks[2], stream);
-    k_update32<<<gu, L.block_update, 0, stream>>>(M, *par, fa, geo->csr_face, fx, cg, cons, cons_next, p4, clocks,
+    k_update32<<<gu, L.block_update, 0, stream>>>(M, *par, geo->csr_face, fx, cg, cons, cons_next, p4, clocks,
                                                   runs, n_runs);
     if (marks) cudaEventRecord(marks[3], stream);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;

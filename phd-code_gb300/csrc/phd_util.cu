@@ -182,11 +182,36 @@ __global__ void k_csr_scatter(int n, int F, const int32_t *__restrict__ pair_i, 
     }
 }
 
+// Sort each cell's list.  Lists of up to 16 entries (every cell of a 2D Voronoi mesh
+// but rare outliers) are sorted in registers with an odd-even transposition network of
+// 8 or 16 lanes; longer lists fall back to an insertion sort in place.
+template <int N>
+__device__ __forceinline__ void sort_list_regs(int32_t *__restrict__ idx, int e0, int d) {
+    int32_t v[N];
+#pragma unroll
+    for (int k = 0; k < N; k++) v[k] = (k < d) ? idx[e0 + k] : INT32_MAX;
+#pragma unroll
+    for (int r = 0; r < N; r++) {
+#pragma unroll
+        for (int k = (r & 1); k + 1 < N; k += 2) {
+            const int32_t a = v[k], b = v[k + 1];
+            v[k] = min(a, b);
+            v[k + 1] = max(a, b);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < N; k++)
+        if (k < d) idx[e0 + k] = v[k];
+}
+
 __global__ void k_csr_sort(int n, const int32_t *__restrict__ ptr, int32_t *__restrict__ idx) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
-    const int e0 = ptr[c], e1 = ptr[c + 1];
-    for (int e = e0 + 1; e < e1; e++) {          // insertion sort: lists hold a few entries
+    const int e0 = ptr[c], e1 = ptr[c + 1], d = e1 - e0;
+    if (d <= 1) return;
+    if (d <= 8) { sort_list_regs<8>(idx, e0, d); return; }
+    if (d <= 16) { sort_list_regs<16>(idx, e0, d); return; }
+    for (int e = e0 + 1; e < e1; e++) {
         const int32_t v = idx[e];
         int k = e - 1;
         while (k >= e0 && idx[k] > v) {
@@ -197,13 +222,12 @@ __global__ void k_csr_sort(int n, const int32_t *__restrict__ ptr, int32_t *__re
     }
 }
 
-// ---- periodic twin faces -----------------------------------------------------------
-// With periodic ghosts a boundary face is emitted twice: as (i, ghost of k) while
-// tessellating i and as (k, ghost of i) while tessellating k (tess.cpp:363, each copy
-// updating only its real cell, mesh.pyx:529-544).  For each copy a = (i, g), k = map[g],
-// with periodic shift s = rint((x_g - x_k)/L), the twin is the face b = (k, g') in k's
-// list with map[g'] = i and shift -s.  twin[a] = b when b < a (the lower id is kept),
-// else -1.  Same pairing as the host's periodic_twins (phd_code_gb300.twins).
+// rint(d / L) for the offsets of periodic images (|d| < 1.5 L), by comparison
+__device__ __forceinline__ int shift_of(double d, double L) {
+    const double h = 0.5 * L;
+    return d > h ? 1 : (d < -h ? -1 : 0);
+}
+
 __global__ void k_periodic_twins(phd_mesh M, int periodic, double Lx, double Ly, int32_t *__restrict__ twin) {
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= M.n_faces) return;
@@ -213,15 +237,15 @@ __global__ void k_periodic_twins(phd_mesh M, int periodic, double Lx, double Ly,
     if (periodic && i >= 0 && i < nr && g >= nr && g < n) {
         const int k = M.map[g];
         if (k >= 0 && k < nr && k != i) {
-            const double sx = rint(__ddiv_rn(__dsub_rn(M.x[g], M.x[k]), Lx));
-            const double sy = rint(__ddiv_rn(__dsub_rn(M.x[(size_t)n + g], M.x[(size_t)n + k]), Ly));
+            const int sx = shift_of(M.x[g] - M.x[k], Lx);
+            const int sy = shift_of(M.x[(size_t)n + g] - M.x[(size_t)n + k], Ly);
             for (int e = M.nbr_ptr[k]; e < M.nbr_ptr[k + 1]; e++) {
                 const int b = M.nbr_idx[e];
                 if (b < 0 || b >= M.n_faces || b == a || M.pair_i[b] != k) continue;
                 const int g2 = M.pair_j[b];
                 if (g2 < nr || g2 >= n || M.map[g2] != i) continue;
-                const double tx = rint(__ddiv_rn(__dsub_rn(M.x[g2], M.x[i]), Lx));
-                const double ty = rint(__ddiv_rn(__dsub_rn(M.x[(size_t)n + g2], M.x[(size_t)n + i]), Ly));
+                const int tx = shift_of(M.x[g2] - M.x[i], Lx);
+                const int ty = shift_of(M.x[(size_t)n + g2] - M.x[(size_t)n + i], Ly);
                 if (tx == -sx && ty == -sy) {
                     if (b < a) out = b;
                     break;

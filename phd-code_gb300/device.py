@@ -89,17 +89,8 @@ class DeviceMesh:
         return {nm: torch.from_numpy(np.ascontiguousarray(getattr(host, nm), dtype=dt)).pin_memory()
                 for nm, dt in self.UPLOAD}
 
-    def upload(self, pinned, normals="device", stream=None):
-        """Hand over a new tessellation with this mesh's cell and face counts.
-
-        Copies the face list (pair-i/j, area, centroid) and the cell geometry (x, dcom,
-        vol, tag, type, map) from pinned host buffers, then forms on the device what
-        follows from them: the neighbour lists (phd_build_csr), the reflective flip bits
-        and, with ``normals="device"``, the FP64 face normals (phd_face_normals_f64).
-        ``normals="none"`` leaves the mesh without FP64 normals (FP32 consumers form
-        their own; FP64 entries then refuse the mesh).  Returns the bytes copied."""
-        if normals not in ("device", "none"):
-            raise ValueError("normals must be 'device' or 'none'")
+    def check_upload(self, pinned):
+        """Raise unless the pinned arrays have this mesh's cell and face counts."""
         shapes = {"tag": (self.n_cells,), "type": (self.n_cells,), "map": (self.n_cells,),
                   "x": (self.dim, self.n_cells), "dcom": (self.dim, self.n_cells), "vol": (self.n_cells,),
                   "pair_i": (self.n_faces,), "pair_j": (self.n_faces,), "area": (self.n_faces,),
@@ -108,31 +99,66 @@ class DeviceMesh:
             if tuple(pinned[nm].shape) != shapes[nm]:
                 raise ValueError("upload: %s has shape %s, this mesh holds %s" % (nm, tuple(pinned[nm].shape),
                                                                                  shapes[nm]))
-        lib = L.lib()
-        s = L.stream_handle(stream)
-        ctx = torch.cuda.stream(stream) if stream is not None else _nullctx()
+
+    def copy_fields(self, pinned, names, stream=None):
+        """Asynchronous host->device copies of the named arrays; returns their bytes."""
         nbytes = 0
-        with ctx:
-            for nm, _ in self.UPLOAD:
+        with (torch.cuda.stream(stream) if stream is not None else _nullctx()):
+            for nm in names:
                 getattr(self, nm).copy_(pinned[nm], non_blocking=True)
                 nbytes += pinned[nm].numel() * pinned[nm].element_size()
+        return nbytes
+
+    def reset_errors(self, stream=None):
+        lib = L.lib()
+        with (torch.cuda.stream(stream) if stream is not None else _nullctx()):
             if not hasattr(self, "_bad"):
                 self._bad = torch.zeros(1, dtype=torch.int32, device=self.device)
                 self._csr_work = torch.empty(int(lib.phd_csr_work_ints(self.n_cells)), dtype=torch.int32,
                                              device=self.device)
             self._bad.zero_()
-        L.check(lib.phd_build_csr(self.ref, L.ptr(self.nbr_ptr), L.ptr(self.nbr_idx), L.ptr(self._csr_work),
-                                  L.ptr(self._bad), s), "phd_build_csr")
+
+    def build_lists(self, stream=None):
+        """Neighbour lists from the face pairs on the device (phd_build_csr)."""
+        L.check(L.lib().phd_build_csr(self.ref, L.ptr(self.nbr_ptr), L.ptr(self.nbr_idx), L.ptr(self._csr_work),
+                                      L.ptr(self._bad), L.stream_handle(stream)), "phd_build_csr")
+
+    def set_flip(self, stream=None):
         xmin = (C.c_double * 3)(*(list(self.xmin) + [0.0] * (3 - self.dim)))
         xmax = (C.c_double * 3)(*(list(self.xmax) + [0.0] * (3 - self.dim)))
-        L.check(lib.phd_flip_mask(self.dim, self.n_cells, L.ptr(self.type), L.ptr(self.x), xmin, xmax,
-                                  int(self.boundary == "reflective"), L.ptr(self.flip), s), "phd_flip_mask")
+        L.check(L.lib().phd_flip_mask(self.dim, self.n_cells, L.ptr(self.type), L.ptr(self.x), xmin, xmax,
+                                      int(self.boundary == "reflective"), L.ptr(self.flip),
+                                      L.stream_handle(stream)), "phd_flip_mask")
+
+    def set_normals(self, normals, stream=None):
+        """"device": FP64 normals formed on the device; "none": the mesh carries no FP64
+        normals (FP32 consumers form their own; FP64 entries then refuse the mesh)."""
         if normals == "device":
             self.struct.normal = self.normal.data_ptr()
-            L.check(lib.phd_face_normals_f64(self.ref, L.ptr(self.normal), L.ptr(self._bad), s),
-                    "phd_face_normals_f64")
-        else:
+            L.check(L.lib().phd_face_normals_f64(self.ref, L.ptr(self.normal), L.ptr(self._bad),
+                                                 L.stream_handle(stream)), "phd_face_normals_f64")
+        elif normals == "none":
             self.struct.normal = None
+        else:
+            raise ValueError("normals must be 'device' or 'none'")
+
+    def upload(self, pinned, normals="device", stream=None):
+        """Hand over a new tessellation with this mesh's cell and face counts.
+
+        Copies the face list (pair-i/j, area, centroid) and the cell geometry (x, dcom,
+        vol, tag, type, map) from pinned host buffers, then forms on the device what
+        follows from them: the neighbour lists (phd_build_csr), the reflective flip bits
+        and, with ``normals="device"``, the FP64 face normals (phd_face_normals_f64).
+        ``normals="none"`` leaves the mesh without FP64 normals.  Returns the bytes
+        copied."""
+        if normals not in ("device", "none"):
+            raise ValueError("normals must be 'device' or 'none'")
+        self.check_upload(pinned)
+        self.reset_errors(stream)
+        nbytes = self.copy_fields(pinned, [nm for nm, _ in self.UPLOAD], stream)
+        self.build_lists(stream)
+        self.set_flip(stream)
+        self.set_normals(normals, stream)
         return nbytes
 
     def upload_errors(self):

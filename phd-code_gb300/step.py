@@ -102,17 +102,38 @@ class FluxStepper:
         table and FP32 geometry (normals included); FP64 forms its FP64 normals.  The
         ghosts are re-created from their images (``domain_manager.pyx:712-774``), the
         primitives recovered with the new volumes and the next dt taken from them
-        (Appendix steps 6-8 of the moving-mesh step).  Returns the bytes copied."""
+        (steps 6-8 of the moving-mesh step).  The neighbour lists and the twin table are
+        built on a second stream while the rest of the mesh is still being copied.
+        Returns the bytes copied."""
         dm, p = self.dmesh, self.params
+        dm.check_upload(pinned)
         lib = L.lib()
-        s = L.stream_handle(self.stream)
-        nbytes = dm.upload(pinned, normals="none" if self.precision == "fp32" else "device", stream=self.stream)
-        L.check(lib.phd_ghost_cons_f64(dm.ref, L.ptr(self.cons), s), "phd_ghost_cons_f64")
+        main = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        if getattr(self, "_side", None) is None:
+            self._side = torch.cuda.Stream(self.device)
+            self._ev = [torch.cuda.Event() for _ in range(3)]
+        side, ev = self._side, self._ev
+        s, ss = L.stream_handle(main), L.stream_handle(side)
+        dm.reset_errors(main)
+        nbytes = dm.copy_fields(pinned, ("pair_i", "pair_j"), main)
+        ev[0].record(main)
+        side.wait_event(ev[0])
+        dm.build_lists(side)
+        nbytes += dm.copy_fields(pinned, ("x", "map"), main)
+        ev[1].record(main)
         if self.precision == "fp32":
+            side.wait_event(ev[1])
             box = [b - a for a, b in zip(dm.xmin, dm.xmax)]
             L.check(lib.phd_periodic_twins(dm.ref, int(self.dedup_periodic and dm.boundary == "periodic"),
-                                           float(box[0]), float(box[1]), L.ptr(self.twin), s),
+                                           float(box[0]), float(box[1]), L.ptr(self.twin), ss),
                     "phd_periodic_twins")
+        ev[2].record(side)
+        nbytes += dm.copy_fields(pinned, ("com", "area", "dcom", "vol", "tag", "type"), main)
+        main.wait_event(ev[2])
+        dm.set_flip(main)
+        dm.set_normals("none" if self.precision == "fp32" else "device", main)
+        L.check(lib.phd_ghost_cons_f64(dm.ref, L.ptr(self.cons), s), "phd_ghost_cons_f64")
+        if self.precision == "fp32":
             out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
                                                             self.csr_nbr, self.cell_geo)))
             L.check(lib.phd_prepare_f32(dm.ref, L.ptr(self.twin), ctypes.byref(out), s), "phd_prepare_f32")
