@@ -145,7 +145,7 @@ def algorithmic_bytes(n, F, n_real):
     e = 2 * F
     grad = n * (16 + 16 + 4 + 1 + 32 + 8) + e * 8 + F * (16 + 8)
     face = F * (8 + 16 + 8 + 16) + n * (16 + 32 + 16 + 8)
-    update = n * (4 + 1 + 32 + 32 + 8 + 16) + e * 4 + F * (8 + 16)
+    update = n * (4 + 1 + 32 + 32 + 8 + 16) + e * 4 + F * 16
     return {"k_grad32": grad, "k_face32": face, "k_update32": update}
 
 
@@ -376,43 +376,65 @@ def fp32_accuracy(st, mesh, prim, n_steps, dev, solver):
             "t_fp32": st.read_clock().t, "t_fp64": ref.read_clock().t}
 
 
-def adjoint_cost(dev, n_side=128, n_steps=20, checkpoint=20):
-    """Adjoint / forward time of the FP64 step on the 128x128 Gaussian-bump problem
-    (static mesh, HLLC, CFL 0.4): forward run, then the full backward pass including
-    the recompute from checkpoints, both timed with CUDA events."""
+def adjoint_cost(dev, n_side=128, n_steps=200, checkpoint=20, n_dirs=16, h=1e-6, h_small=1e-10, noise=1e-3):
+    """The differentiation workload: 128x128 periodic box, gamma 1.4, HLLC, CFL 0.4,
+    static mesh.  The target density is a Gaussian bump (amplitude 0.1, width 0.05) on
+    rho = p = 1 evolved for n_steps in FP64; the differentiated run starts from the
+    background with seeded noise of amplitude `noise` on rho, v and p (an exactly uniform
+    state sits on the limiters' non-differentiable point, where no derivative is
+    unique); loss = sum (rho_T - rho_target)^2.  Timed with CUDA events: forward, backward
+    (recompute from checkpoints every `checkpoint` steps), and the adjoint step alone
+    against the forward step.  The gradient is checked against central differences
+    along n_dirs seeded random directions at step h and at h_small: the limited scheme is
+    piecewise smooth, and over 200 steps a perturbation of 1e-6 crosses limiter branch
+    switches in most directions (seen in the one-sided slopes), so only the smaller step
+    measures the local derivative."""
     import torch
     import __graft_entry__ as ge
     pkg = ge.load_package()
     from phd_code_gb300.adjoint import FluxRun, FluxRunRecord, StepRecord
     from phd_code_gb300.device import DeviceMesh
     from phd_code_gb300.step import FluxStepper
-    mesh, prim, info = pkg.problems.gaussian_bump(n_side, background=False)
+    mesh, prim_bump, info = pkg.problems.gaussian_bump(n_side, background=False)
+    _, prim_bg, _ = pkg.problems.gaussian_bump(n_side, background=True)
+    nr = mesh.n_real
     dm = DeviceMesh(mesh, device=dev)
-    st = FluxStepper(dm, prim, gamma=1.4, cfl=0.4, solver="hllc", moving=False, device=dev)
+    st_t = FluxStepper(dm, prim_bump, gamma=1.4, cfl=0.4, solver="hllc", moving=False, device=dev)
+    st_t.step(n_steps)
+    st_t.check_status()
+    target = st_t.prim[0, :nr].clone()
+    rng = np.random.default_rng(3)
+    p_init = prim_bg.copy()
+    p_init[:, :nr] += noise * rng.uniform(-1.0, 1.0, (4, nr))
+    p_init = pkg.meshgen.fill_ghosts(mesh, p_init)
+    st = FluxStepper(dm, p_init, gamma=1.4, cfl=0.4, solver="hllc", moving=False, device=dev)
     fw = torch.zeros((2, mesh.n_faces), dtype=torch.float64, device=dev)
     recs = []
     for _ in range(n_steps):
         recs.append(StepRecord(dm, fw, st.read_clock().dt))
         st.step(1)
     run = FluxRunRecord(recs, gamma=1.4, solver="hllc", checkpoint=checkpoint)
-    p0 = torch.as_tensor(prim[:, :mesh.n_real]).to(dev).requires_grad_(True)
-    tgt = torch.ones(mesh.n_real, dtype=torch.float64, device=dev)
+    p0 = torch.as_tensor(p_init[:, :nr]).to(dev).requires_grad_(True)
+
+    def loss_of(p):
+        return ((FluxRun.apply(p, run) - target) ** 2).sum()
+
     for _ in range(2):                                   # warm-up
-        loss = ((FluxRun.apply(p0, run) - tgt) ** 2).sum()
-        loss.backward()
+        loss_of(p0).backward()
+    p0.grad = None
     e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     torch.cuda.synchronize()
     e[0].record()
-    rho = FluxRun.apply(p0, run)
-    loss = ((rho - tgt) ** 2).sum()
+    loss = loss_of(p0)
     e[1].record()
     loss.backward()
     e[2].record()
     torch.cuda.synchronize()
     fwd, bwd = e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+    g = p0.grad.detach().clone()
     # the adjoint step alone (reverse kernels at recorded states) against the forward step
     states = run._replay_segment(0, n_steps)
-    lam = torch.zeros((4, mesh.n_real), dtype=torch.float64, device=dev)
+    lam = torch.zeros((4, nr), dtype=torch.float64, device=dev)
     lam[0] = 1.0
     torch.cuda.synchronize()
     e[0].record()
@@ -421,10 +443,34 @@ def adjoint_cost(dev, n_side=128, n_steps=20, checkpoint=20):
     e[1].record()
     torch.cuda.synchronize()
     adj_step = e[0].elapsed_time(e[1]) / n_steps
-    return {"config": "gaussian bump %dx%d periodic, HLLC, FP64, %d steps, checkpoint every %d" %
-                      (n_side, n_side, n_steps, checkpoint),
+    del states
+    # central differences along seeded directions, at the configured step and at a step
+    # small enough to stay between the limiters' branch switches; the one-sided slopes'
+    # spread shows whether [-h, h] crossed a switch (a kink of the piecewise-smooth map)
+    drng = np.random.default_rng(11)
+    fd_rows = []
+    with torch.no_grad():
+        L0 = float(loss_of(p0.detach()))
+        for _ in range(n_dirs):
+            d = torch.as_tensor(drng.standard_normal((4, nr))).to(dev)
+            gd = float((g * d).sum())
+            row = {"gd": gd}
+            for tag, hh in (("h", h), ("h_small", h_small)):
+                Lp, Lm = float(loss_of(p0.detach() + hh * d)), float(loss_of(p0.detach() - hh * d))
+                fd = (Lp - Lm) / (2 * hh)
+                row[tag] = {"rel_err": abs(fd - gd) / max(abs(gd), 1e-300),
+                            "one_sided_spread": abs((Lp - L0) - (L0 - Lm)) / hh / max(abs(gd), 1e-300)}
+            fd_rows.append(row)
+    return {"config": "gaussian bump %dx%d periodic, HLLC, FP64, CFL 0.4, %d steps, checkpoint every %d; start = "
+                      "background + %g noise" % (n_side, n_side, n_steps, checkpoint, noise),
             "forward_ms": fwd, "backward_ms": bwd, "ratio": bwd / fwd,
-            "forward_step_ms": fwd / n_steps, "adjoint_step_ms": adj_step, "step_ratio": adj_step * n_steps / fwd}
+            "forward_step_ms": fwd / n_steps, "adjoint_step_ms": adj_step, "step_ratio": adj_step * n_steps / fwd,
+            "fd_check": {"directions": n_dirs, "h": h, "h_small": h_small,
+                         "max_rel_err_h": max(r["h"]["rel_err"] for r in fd_rows),
+                         "max_rel_err_h_small": max(r["h_small"]["rel_err"] for r in fd_rows),
+                         "median_rel_err_h_small": float(np.median([r["h_small"]["rel_err"] for r in fd_rows])),
+                         "directions_crossing_a_switch_at_h": sum(r["h"]["one_sided_spread"] > 1e-3 for r in fd_rows),
+                         "max_one_sided_spread_h_small": max(r["h_small"]["one_sided_spread"] for r in fd_rows)}}
 
 
 def run_e2e(args, st, mesh, prim, dev):

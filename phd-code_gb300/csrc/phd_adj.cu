@@ -389,7 +389,8 @@ __global__ void __launch_bounds__(BA) k_adj_final(phd_mesh M, phd_adj_index A, d
     lam[3 * (size_t)n + c] = lam_next[3 * (size_t)n + c] + aE;
 }
 
-inline int ga(int n) { return (n + BA - 1) / BA; }
+inline int ba(int n) { return block_for(n, BA); }
+inline int ga(int n) { return grid_for_block(n, ba(n)); }
 
 }  // namespace phd
 
@@ -414,12 +415,12 @@ int phd_adjoint_step_f64(const phd_mesh *mesh, const phd_adj_index *index, const
     double *prim_adj = self_adj + 4 * n;           // [4][n]
     cudaMemsetAsync(entry_adj, 0, sizeof(double) * 8 * F, stream);
     cudaMemsetAsync(self_adj, 0, sizeof(double) * 4 * n, stream);
-    if (F) k_adj_face<<<ga((int)F), BA, 0, stream>>>(M, *par, dt, prim, grad, face_w, lam_next, face_adj);
-    k_adj_gather<<<ga((int)n), BA, 0, stream>>>(M, face_adj, cell_adj);
+    if (F) k_adj_face<<<ga((int)F), ba((int)F), 0, stream>>>(M, *par, dt, prim, grad, face_w, lam_next, face_adj);
+    k_adj_gather<<<ga((int)n), ba((int)n), 0, stream>>>(M, face_adj, cell_adj);
     if (par->reconstruction == PHD_LINEAR)
-        k_adj_grad<<<ga((int)n), BA, 0, stream>>>(M, *index, par->limiter, prim, cell_adj, entry_adj, self_adj);
-    k_adj_gather2<<<ga((int)n), BA, 0, stream>>>(M, *index, cell_adj, entry_adj, self_adj, prim_adj);
-    k_adj_final<<<ga((int)n), BA, 0, stream>>>(M, *index, par->gamma, cons, prim_adj, lam_next, lam);
+        k_adj_grad<<<ga((int)n), ba((int)n), 0, stream>>>(M, *index, par->limiter, prim, cell_adj, entry_adj, self_adj);
+    k_adj_gather2<<<ga((int)n), ba((int)n), 0, stream>>>(M, *index, cell_adj, entry_adj, self_adj, prim_adj);
+    k_adj_final<<<ga((int)n), ba((int)n), 0, stream>>>(M, *index, par->gamma, cons, prim_adj, lam_next, lam);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 

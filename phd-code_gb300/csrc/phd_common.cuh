@@ -1,5 +1,6 @@
 // phd_common.cuh -- shared constants, math overloads and small device helpers.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "../../include/phdflux.h"
@@ -13,6 +14,30 @@
 
 namespace phd {
 
+// Threads per block for a launch over n items with at most max_block threads: halved
+// (down to one warp) while the grid would not cover every SM twice, so small meshes
+// (16k cells) still spread FP64-bound work over the whole GPU.
+inline int sm_count_current() {
+    static std::atomic<int> cached[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    int v = cached[dev].load(std::memory_order_relaxed);
+    if (v <= 0) {
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) v = 152;
+        cached[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
+
+inline int block_for(int n, int max_block) {
+    int b = max_block;
+    const long long want = 2LL * sm_count_current();
+    while (b > 32 && ((long long)n + b - 1) / b < want) b >>= 1;
+    return b;
+}
+
+inline int grid_for_block(int n, int b) { return n > 0 ? (n + b - 1) / b : 1; }
+
 // Type-generic math so one template body serves the FP64 and FP32 builds.
 PHD_HD __forceinline__ double t_sqrt(double a) { return sqrt(a); }
 PHD_HD __forceinline__ float t_sqrt(float a) { return sqrtf(a); }
@@ -24,8 +49,10 @@ PHD_HD __forceinline__ double t_fmin(double a, double b) { return fmin(a, b); }
 PHD_HD __forceinline__ float t_fmin(float a, float b) { return fminf(a, b); }
 PHD_HD __forceinline__ double t_fabs(double a) { return fabs(a); }
 PHD_HD __forceinline__ float t_fabs(float a) { return fabsf(a); }
-// x**2 in the reference lowers to libm pow(x, 2.0); pow(x, 2) and x*x agree to 1 ulp.
-PHD_HD __forceinline__ double t_sq(double a) { return pow(a, 2.0); }
+// x**2 in the reference lowers to libm pow(x, 2.0).  Neither CUDA's pow nor the
+// product reproduces every glibc result bit for bit (each is within an ulp of it); the
+// product is the exactly rounded square and costs one FP64 multiply instead of a pow.
+PHD_HD __forceinline__ double t_sq(double a) { return a * a; }
 PHD_HD __forceinline__ float t_sq(float a) { return a * a; }
 
 // Positive doubles order like their bit patterns: min-reduce them as integers.

@@ -505,7 +505,8 @@ __global__ void __launch_bounds__(BLOCK) k_face_vel(phd_mesh M, const double *__
     }
 }
 
-inline int grid_of(int n) { return (n + BLOCK - 1) / BLOCK; }
+inline int blk_of(int n) { return block_for(n, BLOCK); }
+inline int grid_of(int n) { return grid_for_block(n, blk_of(n)); }
 
 inline int launch_status() {
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
@@ -536,7 +537,7 @@ const char *phd_status_string(int bit) {
 int phd_gradients_f64(const phd_mesh *mesh, const double *prim, int32_t limiter, double *grad,
                       phd_clock *clk, cudaStream_t stream) {
     if (!mesh_ok(mesh) || !prim || !grad) return PHD_ERR_ARG;
-    k_gradients<2><<<grid_of(mesh->n_cells), BLOCK, 0, stream>>>(*mesh, prim, limiter, grad, clk);
+    k_gradients<2><<<grid_of(mesh->n_cells), blk_of(mesh->n_cells), 0, stream>>>(*mesh, prim, limiter, grad, clk);
     return launch_status();
 }
 
@@ -547,7 +548,7 @@ int phd_states_f64(const phd_mesh *mesh, const double *prim, const double *grad,
     if (reconstruction == PHD_LINEAR && !grad) return PHD_ERR_ARG;
     if (stages < 1 || stages > 3) return PHD_ERR_ARG;
     if (mesh->n_faces == 0) return PHD_OK;
-    k_states<2><<<grid_of(mesh->n_faces), BLOCK, 0, stream>>>(*mesh, prim, grad, face_w, gamma, dt_half, boost,
+    k_states<2><<<grid_of(mesh->n_faces), blk_of(mesh->n_faces), 0, stream>>>(*mesh, prim, grad, face_w, gamma, dt_half, boost,
                                                              reconstruction == PHD_LINEAR, gizmo, stages,
                                                              left, right);
     return launch_status();
@@ -560,7 +561,7 @@ int phd_riemann_f64(const phd_mesh *mesh, int32_t solver, double gamma, int32_t 
     if (mesh->n_faces && !mesh->normal) return PHD_ERR_ARG;
     if (solver < PHD_HLL || solver > PHD_EXACT) return PHD_ERR_ARG;
     if (mesh->n_faces == 0) return PHD_OK;
-    k_riemann<2><<<grid_of(mesh->n_faces), BLOCK, 0, stream>>>(*mesh, solver, gamma, boost, exact_max_iter,
+    k_riemann<2><<<grid_of(mesh->n_faces), blk_of(mesh->n_faces), 0, stream>>>(*mesh, solver, gamma, boost, exact_max_iter,
                                                               left, right, face_w, flux, clk);
     return launch_status();
 }
@@ -568,48 +569,48 @@ int phd_riemann_f64(const phd_mesh *mesh, int32_t solver, double gamma, int32_t 
 int phd_update_from_fluxes_f64(const phd_mesh *mesh, const double *flux, double dt, double *cons,
                                phd_clock *clk, cudaStream_t stream) {
     if (!mesh_ok(mesh) || !flux || !cons) return PHD_ERR_ARG;
-    k_update<2><<<grid_of(mesh->n_cells), BLOCK, 0, stream>>>(*mesh, flux, dt, cons, clk);
+    k_update<2><<<grid_of(mesh->n_cells), blk_of(mesh->n_cells), 0, stream>>>(*mesh, flux, dt, cons, clk);
     return launch_status();
 }
 
 int phd_ghost_cons_f64(const phd_mesh *mesh, double *cons, cudaStream_t stream) {
     if (!mesh_ok(mesh) || !cons) return PHD_ERR_ARG;
-    k_ghost_cons<2><<<grid_of(mesh->n_cells), BLOCK, 0, stream>>>(*mesh, cons);
+    k_ghost_cons<2><<<grid_of(mesh->n_cells), blk_of(mesh->n_cells), 0, stream>>>(*mesh, cons);
     return launch_status();
 }
 
 int phd_prim_from_cons_f64(int32_t dim, int32_t n, double gamma, const double *vol, const double *cons,
                            double *prim, cudaStream_t stream) {
     if (dim != 2 || n <= 0 || !vol || !cons || !prim) return PHD_ERR_ARG;
-    k_prim_from_cons<2><<<grid_of(n), BLOCK, 0, stream>>>(n, gamma, vol, cons, prim);
+    k_prim_from_cons<2><<<grid_of(n), blk_of(n), 0, stream>>>(n, gamma, vol, cons, prim);
     return launch_status();
 }
 
 int phd_cons_from_prim_f64(int32_t dim, int32_t n, double gamma, const double *vol, const double *prim,
                            double *cons, cudaStream_t stream) {
     if (dim != 2 || n <= 0 || !vol || !cons || !prim) return PHD_ERR_ARG;
-    k_cons_from_prim<2><<<grid_of(n), BLOCK, 0, stream>>>(n, gamma, vol, prim, cons);
+    k_cons_from_prim<2><<<grid_of(n), blk_of(n), 0, stream>>>(n, gamma, vol, prim, cons);
     return launch_status();
 }
 
 int phd_time_step_f64(const phd_mesh *mesh, const double *prim, double gamma, double cfl, int32_t boost,
                       int32_t advance, phd_clock *clk, cudaStream_t stream) {
     if (!mesh_ok(mesh) || !prim || !clk) return PHD_ERR_ARG;
-    k_time_step<2><<<grid_of(mesh->n_cells), BLOCK, 0, stream>>>(*mesh, prim, gamma, cfl, boost, advance, clk);
+    k_time_step<2><<<grid_of(mesh->n_cells), blk_of(mesh->n_cells), 0, stream>>>(*mesh, prim, gamma, cfl, boost, advance, clk);
     return launch_status();
 }
 
 int phd_generator_velocities_f64(const phd_mesh *mesh, const double *prim, double gamma, double eta,
                                  int32_t regularize, double *w, cudaStream_t stream) {
     if (!mesh_ok(mesh) || !prim || !w) return PHD_ERR_ARG;
-    k_gen_vel<2><<<grid_of(mesh->n_cells), BLOCK, 0, stream>>>(*mesh, prim, gamma, eta, regularize, w);
+    k_gen_vel<2><<<grid_of(mesh->n_cells), blk_of(mesh->n_cells), 0, stream>>>(*mesh, prim, gamma, eta, regularize, w);
     return launch_status();
 }
 
 int phd_face_velocities_f64(const phd_mesh *mesh, const double *w, double *face_w, cudaStream_t stream) {
     if (!mesh_ok(mesh) || !w || !face_w) return PHD_ERR_ARG;
     if (mesh->n_faces == 0) return PHD_OK;
-    k_face_vel<2><<<grid_of(mesh->n_faces), BLOCK, 0, stream>>>(*mesh, w, face_w);
+    k_face_vel<2><<<grid_of(mesh->n_faces), blk_of(mesh->n_faces), 0, stream>>>(*mesh, w, face_w);
     return launch_status();
 }
 
@@ -622,17 +623,18 @@ int phd_step_f64_marked(const phd_mesh *mesh, const phd_params *par, int32_t mov
     if (linear && !grad) return PHD_ERR_ARG;
     if (moving && (!w || !face_w)) return PHD_ERR_ARG;
     const int gc = grid_of(mesh->n_cells), gf = grid_of(mesh->n_faces);
+    const int bc = blk_of(mesh->n_cells), bf = blk_of(mesh->n_faces);
     if (marks) cudaEventRecord(marks[0], stream);
     if (moving) {
-        k_gen_vel<2><<<gc, BLOCK, 0, stream>>>(*mesh, prim, par->gamma, par->eta, par->regularize, w);
-        if (mesh->n_faces) k_face_vel<2><<<gf, BLOCK, 0, stream>>>(*mesh, w, face_w);
+        k_gen_vel<2><<<gc, bc, 0, stream>>>(*mesh, prim, par->gamma, par->eta, par->regularize, w);
+        if (mesh->n_faces) k_face_vel<2><<<gf, bf, 0, stream>>>(*mesh, w, face_w);
     }
-    if (linear) k_gradients<2><<<gc, BLOCK, 0, stream>>>(*mesh, prim, par->limiter, grad, clk);
+    if (linear) k_gradients<2><<<gc, bc, 0, stream>>>(*mesh, prim, par->limiter, grad, clk);
     if (marks) cudaEventRecord(marks[1], stream);
     if (mesh->n_faces)
-        k_face_flux<2><<<gf, BLOCK, 0, stream>>>(*mesh, *par, prim, grad, face_w, flux, clk);
+        k_face_flux<2><<<gf, bf, 0, stream>>>(*mesh, *par, prim, grad, face_w, flux, clk);
     if (marks) cudaEventRecord(marks[2], stream);
-    k_update_step<2><<<gc, BLOCK, 0, stream>>>(*mesh, *par, flux, cons, cons_next, prim, clk);
+    k_update_step<2><<<gc, bc, 0, stream>>>(*mesh, *par, flux, cons, cons_next, prim, clk);
     if (marks) cudaEventRecord(marks[3], stream);
     return launch_status();
 }
