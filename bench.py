@@ -45,7 +45,9 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--workload", default="shear", choices=["shear", "ensemble"])
+    ap.add_argument("--workload", default="shear", choices=["shear", "ensemble", "adjoint"])
+    ap.add_argument("--adj-steps", type=int, default=200, help="adjoint workload: recorded steps")
+    ap.add_argument("--adj-dirs", type=int, default=16, help="adjoint workload: finite-difference directions")
     ap.add_argument("--runs", type=int, default=256)
     ap.add_argument("--no-tune", action="store_true", help="FP32: default launch shapes instead of autotuned")
     return ap.parse_args()
@@ -466,11 +468,13 @@ def adjoint_cost(dev, n_side=128, n_steps=200, checkpoint=20, n_dirs=16, h=1e-6,
             "forward_ms": fwd, "backward_ms": bwd, "ratio": bwd / fwd,
             "forward_step_ms": fwd / n_steps, "adjoint_step_ms": adj_step, "step_ratio": adj_step * n_steps / fwd,
             "fd_check": {"directions": n_dirs, "h": h, "h_small": h_small,
-                         "max_rel_err_h": max(r["h"]["rel_err"] for r in fd_rows),
-                         "max_rel_err_h_small": max(r["h_small"]["rel_err"] for r in fd_rows),
-                         "median_rel_err_h_small": float(np.median([r["h_small"]["rel_err"] for r in fd_rows])),
+                         "max_rel_err_h": max((r["h"]["rel_err"] for r in fd_rows), default=None),
+                         "max_rel_err_h_small": max((r["h_small"]["rel_err"] for r in fd_rows), default=None),
+                         "median_rel_err_h_small": float(np.median([r["h_small"]["rel_err"] for r in fd_rows]))
+                         if fd_rows else None,
                          "directions_crossing_a_switch_at_h": sum(r["h"]["one_sided_spread"] > 1e-3 for r in fd_rows),
-                         "max_one_sided_spread_h_small": max(r["h_small"]["one_sided_spread"] for r in fd_rows)}}
+                         "max_one_sided_spread_h_small": max((r["h_small"]["one_sided_spread"] for r in fd_rows),
+                                                             default=None)}}
 
 
 def run_e2e(args, st, mesh, prim, dev):
@@ -576,6 +580,23 @@ def run_ensemble(args, rank, world):
         print(json.dumps(out), flush=True)
 
 
+def run_adjoint(args, rank, world):
+    """The differentiation workload alone (one replica per rank): adjoint_cost's line
+    with the backward/forward time ratio as the value."""
+    import torch
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    adj = adjoint_cost(dev, n_steps=args.adj_steps, n_dirs=args.adj_dirs)
+    clocks = sampler.stop()
+    if rank == 0:
+        print(json.dumps({"metric": "adjoint / forward time ratio (backward with recompute)", "value": adj["ratio"],
+                          "unit": "x", "n_gpus": world, "steps": args.adj_steps, "higher_is_better": False,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": adj["config"]}, "adjoint": adj, "clocks": clocks}), flush=True)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -592,6 +613,8 @@ def main():
             run_reference(args, rank, world)
         elif args.workload == "ensemble":
             run_ensemble(args, rank, world)
+        elif args.workload == "adjoint":
+            run_adjoint(args, rank, world)
         else:
             run_ours(args, rank, world)
     finally:

@@ -266,6 +266,111 @@ __global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int mo
         grad32_cell<LIMITER>(i, M, P, moving, face_geo, face_ar, csr_face, csr_nbr, cell_geo, prim4, grad8, w2, clk);
 }
 
+// ---- FP32 Riemann solver with the gas constants formed once on the host -------------
+// HLL.get_waves riemann.pyx:375-504 and HLL/HLLC.riemann_solver riemann.pyx:243-373,
+// 521-682 in FP32: the same formulas as hll_family<float> with every quantity that
+// depends only on gamma ((g-1)/(2g), 1/(g-1), (g+1)/(2g), ...) precomputed, and the
+// HLLC left / right star branches merged into one (selects instead of divergence).
+struct GasC {
+    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1;
+};
+
+inline GasC gas_consts(double gamma) {
+    const float g = (float)gamma;
+    GasC c;
+    c.g = g;
+    c.gm1 = g - 1.f;
+    c.inv_gm1 = 1.f / (g - 1.f);
+    c.gp1_2g = (g + 1.f) / (2.f * g);
+    c.z = (g - 1.f) / (2.f * g);
+    c.inv_z = 1.f / c.z;
+    c.two_gp1 = 2.f / (g + 1.f);
+    c.gm1_gp1 = (g - 1.f) / (g + 1.f);
+    return c;
+}
+
+__device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float dr, float ur, float pr,
+                                            const GasC &C, float &sl, float &sc, float &sr) {
+    float p_star;
+    const float cl = fmaxf(sqrtf((C.g * pl) / dl), 1.0e-10f);
+    const float cr = fmaxf(sqrtf((C.g * pr) / dr), 1.0e-10f);
+    const float d_avg = 0.5f * (dl + dr);
+    const float c_avg = 0.5f * (cl + cr);
+    p_star = fmaxf(0.f, ((0.5f * (pl + pr)) + (((0.5f * (ul - ur)) * d_avg) * c_avg)));
+    const float p_min = fminf(pl, pr);
+    const float p_max = fmaxf(pl, pr);
+    if (((p_max / p_min) < 2.f) && ((p_min < p_star) && (p_star < p_max))) {
+        // PVRS estimate stands
+    } else if (p_star <= p_min) {          // two-rarefaction (TRRS)
+        const float plr = __powf(pl / pr, C.z);
+        const float u_star = ((((plr * ul) / cl) + (ur / cr)) + ((2.f * (plr - 1.f)) * C.inv_gm1)) /
+                             ((plr / cl) + (1.f / cr));
+        p_star = (0.5f * pl) * __powf((1.f + ((C.gm1 * (ul - u_star)) / (2.f * cl))), C.inv_z);
+        p_star = p_star + ((0.5f * pr) * __powf((1.f + ((C.gm1 * (u_star - ur)) / (2.f * cr))), C.inv_z));
+    } else {                               // two-shock (TSRS)
+        const float Al = C.two_gp1 / dl;
+        const float Ar = C.two_gp1 / dr;
+        const float gl = sqrtf(Al / (p_star + pl * C.gm1_gp1));
+        const float gr = sqrtf(Ar / (p_star + pr * C.gm1_gp1));
+        p_star = (((gl * pl) + (gr * pr)) - (ur - ul)) / (gl + gr);
+    }
+    if (p_star <= pl) sl = ul - cl;
+    else sl = ul - (cl * sqrtf((1.f + (C.gp1_2g * ((p_star / pl) - 1.f)))));
+    if (p_star <= pr) sr = ur + cr;
+    else sr = ur + (cr * sqrtf((1.f + (C.gp1_2g * ((p_star / pr) - 1.f)))));
+    sc = (((pr - pl) + ((dl * ul) * (sl - ul))) - ((dr * ur) * (sr - ur))) /
+         ((dl * (sl - ul)) - (dr * (sr - ur)));
+}
+
+__device__ __forceinline__ void hll_family32(bool hllc, const float *L, const float *R, const float *n,
+                                             const float *w, const GasC &C, bool boost, float *f) {
+    const float _dl = L[0], _pl = L[3], _dr = R[0], _pr = R[3];
+    const float vl_sq = L[1] * L[1] + L[2] * L[2], vr_sq = R[1] * R[1] + R[2] * R[2];
+    const float Vnl = L[1] * n[0] + L[2] * n[1], Vnr = R[1] * n[0] + R[2] * n[1];
+    const float wn = boost ? 0.f : (w[0] * n[0] + w[1] * n[1]);
+    float sl, sc, sr;
+    get_waves32(_dl, Vnl, _pl, _dr, Vnr, _pr, C, sl, sc, sr);
+    if (wn <= sl) {
+        f[0] = _dl * (Vnl - wn);
+        f[3] = ((((0.5f * _dl) * vl_sq) + (_pl * C.inv_gm1)) * (Vnl - wn)) + (_pl * Vnl);
+        for (int k = 0; k < 2; k++) f[1 + k] = ((_dl * L[1 + k]) * (Vnl - wn)) + (_pl * n[k]);
+    } else if ((sl < wn) && (wn <= sr)) {
+        if (!hllc) {
+            const float fac1 = sr - wn, fac2 = sl - wn, inv3 = 1.f / (sr - sl);
+            f[0] = (((((_dl * Vnl) * fac1) - ((_dr * Vnr) * fac2)) - ((sl * _dl) * fac1)) + ((sr * _dr) * fac2)) *
+                   inv3;
+            for (int k = 0; k < 2; k++) {
+                const float vl = L[1 + k], vr = R[1 + k];
+                f[1 + k] = ((((((((_dl * vl) * Vnl) + (_pl * n[k])) * fac1) -
+                               ((((_dr * vr) * Vnr) + (_pr * n[k])) * fac2)) -
+                              ((sl * (_dl * vl)) * fac1)) + ((sr * (_dr * vr)) * fac2))) * inv3;
+            }
+            const float el = ((0.5f * _dl) * vl_sq) + (_pl * C.inv_gm1);
+            const float er = ((0.5f * _dr) * vr_sq) + (_pr * C.inv_gm1);
+            f[3] = ((((((el + _pl) * Vnl) * fac1) - (((er + _pr) * Vnr) * fac2)) - ((sl * el) * fac1)) +
+                    ((sr * er) * fac2)) * inv3;
+        } else {                           // star region on the side of the contact
+            const bool left = wn <= sc;
+            const float d = left ? _dl : _dr, p = left ? _pl : _pr, Vn = left ? Vnl : Vnr, s = left ? sl : sr;
+            const float vsq = left ? vl_sq : vr_sq;
+            const float *S = left ? L : R;
+            const float factor_1 = (d * (s - Vn)) / (s - sc);
+            const float factor_2 = ((factor_1 * (s - wn)) * (sc - Vn)) + p;
+            const float frho = (d * (Vn - s)) + (factor_1 * (s - wn));
+            const float e = ((0.5f * d) * vsq) + (p * C.inv_gm1);
+            f[0] = frho;
+            f[3] = (((e + p) * Vn) - (s * e)) +
+                   (((s - wn) * factor_1) * ((e / d) + ((sc - Vn) * (sc + (p / (d * (s - Vn)))))));
+            for (int k = 0; k < 2; k++) f[1 + k] = (frho * S[1 + k]) + (factor_2 * n[k]);
+        }
+    } else {
+        f[0] = _dr * (Vnr - wn);
+        f[3] = ((((0.5f * _dr) * vr_sq) + (_pr * C.inv_gm1)) * (Vnr - wn)) + (_pr * Vnr);
+        for (int k = 0; k < 2; k++) f[1 + k] = ((_dr * R[1 + k]) * (Vnr - wn)) + (_pr * n[k]);
+    }
+    if (boost) deboost<float, 2>(w, f);
+}
+
 // ---- fused face kernel ------------------------------------------------------------
 template <int SOLVER, bool LINEAR>
 __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_params &P, int moving,
@@ -275,12 +380,12 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
                                             const float4 *__restrict__ prim4,
                                             const float4 *__restrict__ grad8, const float2 *__restrict__ w2,
                                             float4 *__restrict__ flux4, phd_clock *clocks,
-                                            const int32_t *__restrict__ cell_run) {
+                                            const int32_t *__restrict__ cell_run, const GasC &GC) {
     const int i = M.pair_i[m], j = M.pair_j[m];
     if (i < 0 || i >= M.n_cells || j < 0 || j >= M.n_cells) { set_status32(clocks, PHD_STATUS_BAD_INDEX); return; }
     phd_clock *clk = cell_run ? clocks + cell_run[i] : clocks;
     const bool boost = (SOLVER == PHD_EXACT) ? true : (P.boost != 0);
-    const float gamma = narrow_f64(P.gamma);
+    const float gamma = GC.g;
     const float dtf = narrow_f64(clk->dt);
     const float dt_half = 0.5f * dtf;
     const float4 g = face_geo[m];
@@ -334,7 +439,7 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
     float f[4];
     bool failed = false;
     if (SOLVER == PHD_EXACT) exact_flux<float, 2>(L, R, nrm, w, gamma, P.exact_max_iter, f, &failed);
-    else hll_family<float, 2>(SOLVER == PHD_HLLC, L, R, nrm, w, gamma, boost, f);
+    else hll_family32(SOLVER == PHD_HLLC, L, R, nrm, w, GC, boost, f);
     if (failed) set_status32(clk, PHD_STATUS_RIEMANN_NONCONVERGED);
     // the face's conserved increment dt*A*F (mesh.pyx:519-544), formed once here so both
     // cells of the face apply exactly the same value
@@ -350,10 +455,10 @@ __global__ void __launch_bounds__(512) k_face32(phd_mesh M, phd_params P, int mo
                                                 const float4 *__restrict__ prim4,
                                                 const float4 *__restrict__ grad8, const float2 *__restrict__ w2,
                                                 float4 *__restrict__ flux4, phd_clock *clocks,
-                                                const int32_t *__restrict__ cell_run) {
+                                                const int32_t *__restrict__ cell_run, const GasC GC) {
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M.n_faces; m += gridDim.x * blockDim.x)
         face32_face<SOLVER, LINEAR>(m, M, P, moving, face_geo, face_ar, cell_geo, prim4, grad8, w2, flux4, clocks,
-                                    cell_run);
+                                    cell_run, GC);
 }
 
 // ---- segmented update, primitive recovery and CFL -----------------------------------
@@ -528,10 +633,10 @@ void launch_face32(bool linear, int grid, int block, cudaStream_t s, const phd_m
     const float4 *cg = reinterpret_cast<const float4 *>(G->cell_geo);
     if (linear)
         k_face32<SOLVER, true><<<grid, block, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clocks,
-                                                      cell_run);
+                                                      cell_run, gas_consts(P.gamma));
     else
         k_face32<SOLVER, false><<<grid, block, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clocks,
-                                                       cell_run);
+                                                       cell_run, gas_consts(P.gamma));
 }
 
 // grid for n items: one thread per item, or at most `cap` blocks looping over the rest
@@ -550,16 +655,25 @@ using namespace phd;
 
 extern "C" {
 
-int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out, cudaStream_t stream) {
-    if (!mesh || mesh->dim != 2 || !out || !out->face_geo || !out->face_ar || !out->csr_face || !out->csr_nbr ||
-        !out->cell_geo)
-        return PHD_ERR_ARG;
-    if (mesh->n_faces)
+int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out, int32_t parts,
+                          cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || !out || parts < 0 || parts > PHD_PREP_ALL) return PHD_ERR_ARG;
+    if ((parts & PHD_PREP_FACES) && (!out->face_geo || !out->face_ar)) return PHD_ERR_ARG;
+    if ((parts & PHD_PREP_CELLS) && !out->cell_geo) return PHD_ERR_ARG;
+    if ((parts & PHD_PREP_LISTS) && (!out->csr_face || !out->csr_nbr)) return PHD_ERR_ARG;
+    if ((parts & PHD_PREP_FACES) && mesh->n_faces)
         k_prepare_faces32<<<g32(mesh->n_faces), B32, 0, stream>>>(*mesh, reinterpret_cast<float4 *>(out->face_geo),
                                                                  reinterpret_cast<float2 *>(out->face_ar));
-    k_prepare_cells32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, reinterpret_cast<float4 *>(out->cell_geo));
-    k_prepare_csr32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, twin, out->csr_face, out->csr_nbr);
+    if (parts & PHD_PREP_CELLS)
+        k_prepare_cells32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh,
+                                                                 reinterpret_cast<float4 *>(out->cell_geo));
+    if (parts & PHD_PREP_LISTS)
+        k_prepare_csr32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, twin, out->csr_face, out->csr_nbr);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out, cudaStream_t stream) {
+    return phd_prepare_f32_parts(mesh, twin, out, PHD_PREP_ALL, stream);
 }
 
 int phd_prim_f32_batched(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4,
