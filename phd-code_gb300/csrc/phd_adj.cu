@@ -86,9 +86,10 @@ __device__ __forceinline__ void spatial_rev_f64(const SpatialTape &t, const doub
             if (t.revL) asl[f] += aL[f];
             if (t.revR) asr[f] += aR[f];
         }
+        const double si = t.sepi_mag / t.diff_mag, sj = t.sepj_mag / t.diff_mag;
         for (int f = 0; f < 4; f++)
-            gizmo_pair_adj<double>(t.sl[f], t.sr[f], pi[f], pj[f], t.sepi_mag, t.sepj_mag, t.diff_mag, t.L0[f],
-                                   t.R0[f], aL1[f], aR1[f], asl[f], asr[f], aL0[f], aR0[f]);
+            gizmo_pair_adj_q<double>(t.sl[f], t.sr[f], pi[f], pj[f], si, sj, t.L0[f], t.R0[f], aL1[f], aR1[f],
+                                     asl[f], asr[f], aL0[f], aR0[f]);
     } else {
         for (int f = 0; f < 4; f++) { aL0[f] = aL[f]; aR0[f] = aR[f]; }
     }

@@ -11,63 +11,85 @@
 namespace phd {
 
 // ---- get_waves (riemann.pyx:375-504) --------------------------------------------
+// Forward pass with the same formulas and operation order as get_waves in
+// phd_physics.cuh (so the same branch decisions), keeping what the reverse needs.
 template <typename T>
-PHD_HD void get_waves_adj(T dl, T ul, T pl, T dr, T ur, T pr, T gamma, T a_sl, T a_sc, T a_sr,
-                              T &a_dl, T &a_ul, T &a_pl, T &a_dr, T &a_ur, T &a_pr) {
+struct WaveTape {
+    T cl, cr, d_avg, c_avg, pv_raw, p_star;
+    T z, plr, den, u_star, A1, A2, e, PA1, PA2;       // two-rarefaction branch
+    T Al, Ar, Bl, Brr, gl, gr, S;                      // two-shock branch
+    T k, sqlv, sqrv, sl, sr, D, sc;
+    int br;                                            // 0 PVRS, 1 TRRS, 2 TSRS
+    bool cl_fl, cr_fl, l_shock, r_shock;
+};
+
+template <typename T>
+PHD_HD __forceinline__ void get_waves_fwd(T dl, T ul, T pl, T dr, T ur, T pr, T gamma, WaveTape<T> &t) {
     const T c_floor = T(1.0E-10);
     const T clr = t_sqrt((gamma * pl) / dl), crr = t_sqrt((gamma * pr) / dr);
-    const bool cl_fl = !(clr >= c_floor), cr_fl = !(crr >= c_floor);
-    const T cl = t_fmax(clr, c_floor), cr = t_fmax(crr, c_floor);
-    const T d_avg = T(.5) * (dl + dr);
-    const T c_avg = T(.5) * (cl + cr);
-    const T pv_raw = (T(.5) * (pl + pr)) + (((T(.5) * (ul - ur)) * d_avg) * c_avg);
-    const T pv = t_fmax(T(0.), pv_raw);
+    t.cl_fl = !(clr >= c_floor);
+    t.cr_fl = !(crr >= c_floor);
+    t.cl = t_fmax(clr, c_floor);
+    t.cr = t_fmax(crr, c_floor);
+    const T cl = t.cl, cr = t.cr;
+    t.d_avg = T(.5) * (dl + dr);
+    t.c_avg = T(.5) * (cl + cr);
+    t.pv_raw = (T(.5) * (pl + pr)) + (((T(.5) * (ul - ur)) * t.d_avg) * t.c_avg);
+    const T pv = t_fmax(T(0.), t.pv_raw);
     const T p_min = t_fmin(pl, pr), p_max = t_fmax(pl, pr);
-    int br;   // 0 PVRS, 1 TRRS, 2 TSRS
     T p_star = pv;
-    // TRRS intermediates
-    T z = 0, plr = 0, num = 0, den = 0, u_star = 0, A1 = 0, A2 = 0, e = 0;
-    // TSRS intermediates
-    T Al = 0, Ar = 0, Bl = 0, Brr = 0, gl = 0, gr = 0, S = 0;
+    t.z = t.plr = t.den = t.u_star = t.A1 = t.A2 = t.e = t.PA1 = t.PA2 = T(0);
+    t.Al = t.Ar = t.Bl = t.Brr = t.gl = t.gr = t.S = T(0);
     if (((p_max / p_min) < T(2.)) && ((p_min < pv) && (pv < p_max))) {
-        br = 0;
+        t.br = 0;
     } else if (pv <= p_min) {
-        br = 1;
-        z = (gamma - T(1.)) / (T(2.) * gamma);
-        plr = t_pow(pl / pr, z);
-        num = (((plr * ul) / cl) + (ur / cr)) + ((T(2.) * (plr - T(1.))) / (gamma - T(1.)));
-        den = (plr / cl) + (T(1.) / cr);
-        u_star = num / den;
-        A1 = T(1.) + (((gamma - T(1.)) * (ul - u_star)) / (T(2.) * cl));
-        A2 = T(1.) + (((gamma - T(1.)) * (u_star - ur)) / (T(2.) * cr));
-        e = T(1.) / z;
-        p_star = (T(.5) * pl) * t_pow(A1, e);
-        p_star = p_star + ((T(.5) * pr) * t_pow(A2, e));
+        t.br = 1;
+        t.z = (gamma - T(1.)) / (T(2.) * gamma);
+        t.plr = t_pow(pl / pr, t.z);
+        const T num = (((t.plr * ul) / cl) + (ur / cr)) + ((T(2.) * (t.plr - T(1.))) / (gamma - T(1.)));
+        t.den = (t.plr / cl) + (T(1.) / cr);
+        t.u_star = num / t.den;
+        t.A1 = T(1.) + (((gamma - T(1.)) * (ul - t.u_star)) / (T(2.) * cl));
+        t.A2 = T(1.) + (((gamma - T(1.)) * (t.u_star - ur)) / (T(2.) * cr));
+        t.e = T(1.) / t.z;
+        t.PA1 = t_pow(t.A1, t.e);
+        t.PA2 = t_pow(t.A2, t.e);
+        p_star = (T(.5) * pl) * t.PA1;
+        p_star = p_star + ((T(.5) * pr) * t.PA2);
     } else {
-        br = 2;
-        Al = T(2.) / ((gamma + T(1.)) * dl);
-        Ar = T(2.) / ((gamma + T(1.)) * dr);
-        Bl = pl * ((gamma - T(1.)) / (gamma + T(1.)));
-        Brr = pr * ((gamma - T(1.)) / (gamma + T(1.)));
-        gl = t_sqrt(Al / (pv + Bl));
-        gr = t_sqrt(Ar / (pv + Brr));
-        S = gl + gr;
-        p_star = (((gl * pl) + (gr * pr)) - (ur - ul)) / S;
+        t.br = 2;
+        t.Al = T(2.) / ((gamma + T(1.)) * dl);
+        t.Ar = T(2.) / ((gamma + T(1.)) * dr);
+        t.Bl = pl * ((gamma - T(1.)) / (gamma + T(1.)));
+        t.Brr = pr * ((gamma - T(1.)) / (gamma + T(1.)));
+        t.gl = t_sqrt(t.Al / (pv + t.Bl));
+        t.gr = t_sqrt(t.Ar / (pv + t.Brr));
+        t.S = t.gl + t.gr;
+        p_star = (((t.gl * pl) + (t.gr * pr)) - (ur - ul)) / t.S;
     }
-    const T k = (gamma + T(1.)) / (T(2.) * gamma);
-    const bool l_shock = !(p_star <= pl), r_shock = !(p_star <= pr);
-    T ql = 0, sqlv = 0, qr = 0, sqrv = 0;
-    T sl, sr;
-    if (!l_shock) sl = ul - cl;
-    else { ql = T(1.) + (k * ((p_star / pl) - T(1.))); sqlv = t_sqrt(ql); sl = ul - (cl * sqlv); }
-    if (!r_shock) sr = ur + cr;
-    else { qr = T(1.) + (k * ((p_star / pr) - T(1.))); sqrv = t_sqrt(qr); sr = ur + (cr * sqrv); }
-    const T N = (((pr - pl) + ((dl * ul) * (sl - ul))) - ((dr * ur) * (sr - ur)));
-    const T D = ((dl * (sl - ul)) - (dr * (sr - ur)));
-    const T sc = N / D;
+    t.p_star = p_star;
+    t.k = (gamma + T(1.)) / (T(2.) * gamma);
+    t.l_shock = !(p_star <= pl);
+    t.r_shock = !(p_star <= pr);
+    t.sqlv = t.sqrv = T(0);
+    if (!t.l_shock) t.sl = ul - cl;
+    else { t.sqlv = t_sqrt(T(1.) + (t.k * ((p_star / pl) - T(1.)))); t.sl = ul - (cl * t.sqlv); }
+    if (!t.r_shock) t.sr = ur + cr;
+    else { t.sqrv = t_sqrt(T(1.) + (t.k * ((p_star / pr) - T(1.)))); t.sr = ur + (cr * t.sqrv); }
+    const T N = (((pr - pl) + ((dl * ul) * (t.sl - ul))) - ((dr * ur) * (t.sr - ur)));
+    t.D = ((dl * (t.sl - ul)) - (dr * (t.sr - ur)));
+    t.sc = N / t.D;
+}
 
-    // ---- reverse ----
-    T aN = a_sc / D, aD = -a_sc * sc / D;
+// Reverse of get_waves_fwd: adjoints of (sl, sc, sr) -> adjoints of the inputs.
+// Derivative-only arithmetic (no branch depends on it) uses reciprocals.
+template <typename T>
+PHD_HD __forceinline__ void get_waves_rev(const WaveTape<T> &t, T dl, T ul, T pl, T dr, T ur, T pr, T gamma,
+                                          T a_sl, T a_sc, T a_sr, T &a_dl, T &a_ul, T &a_pl, T &a_dr, T &a_ur,
+                                          T &a_pr) {
+    const T cl = t.cl, cr = t.cr, sl = t.sl, sr = t.sr, sc = t.sc, p_star = t.p_star, k = t.k;
+    const T iD = T(1.) / t.D, ipl = T(1.) / pl, ipr = T(1.) / pr;
+    T aN = a_sc * iD, aD = -a_sc * sc * iD;
     T asl = a_sl, asr = a_sr, acl = 0, acr = 0, aps = 0;
     a_pr += aN;
     a_pl -= aN;
@@ -77,85 +99,98 @@ PHD_HD void get_waves_adj(T dl, T ul, T pl, T dr, T ur, T pr, T gamma, T a_sl, T
     a_dr += -aN * ur * (sr - ur) - aD * (sr - ur);
     a_ur += -aN * dr * (sr - T(2.) * ur) + aD * dr;
     asr += -aN * dr * ur - aD * dr;
-    // sl
+    // sl, sr
     a_ul += asl;
-    if (!l_shock) acl -= asl;
+    if (!t.l_shock) acl -= asl;
     else {
-        acl -= sqlv * asl;
-        const T aq = (-cl * asl) / (T(2.) * sqlv);
-        aps += aq * k / pl;
-        a_pl -= aq * k * p_star / (pl * pl);
+        acl -= t.sqlv * asl;
+        const T aq = (-cl * asl) / (T(2.) * t.sqlv);
+        aps += aq * k * ipl;
+        a_pl -= aq * k * p_star * ipl * ipl;
     }
     a_ur += asr;
-    if (!r_shock) acr += asr;
+    if (!t.r_shock) acr += asr;
     else {
-        acr += sqrv * asr;
-        const T aq = (cr * asr) / (T(2.) * sqrv);
-        aps += aq * k / pr;
-        a_pr -= aq * k * p_star / (pr * pr);
+        acr += t.sqrv * asr;
+        const T aq = (cr * asr) / (T(2.) * t.sqrv);
+        aps += aq * k * ipr;
+        a_pr -= aq * k * p_star * ipr * ipr;
     }
     // p_star
     T apv = 0;
-    if (br == 0) {
+    if (t.br == 0) {
         apv += aps;
-    } else if (br == 1) {
-        const T hA1e = T(.5) * t_pow(A1, e), hA2e = T(.5) * t_pow(A2, e);
-        a_pl += hA1e * aps;
-        a_pr += hA2e * aps;
-        const T aA1 = T(.5) * pl * e * t_pow(A1, e - T(1.)) * aps;
-        const T aA2 = T(.5) * pr * e * t_pow(A2, e - T(1.)) * aps;
-        const T g1 = gamma - T(1.);
+    } else if (t.br == 1) {
+        const T icl = T(1.) / cl, icr = T(1.) / cr, g1 = gamma - T(1.);
+        a_pl += T(.5) * t.PA1 * aps;
+        a_pr += T(.5) * t.PA2 * aps;
+        // d(A^e)/dA = e A^e / A
+        const T aA1 = T(.5) * pl * t.e * (t.PA1 / t.A1) * aps;
+        const T aA2 = T(.5) * pr * t.e * (t.PA2 / t.A2) * aps;
         T aus = 0;
-        a_ul += aA1 * g1 / (T(2.) * cl);
-        aus -= aA1 * g1 / (T(2.) * cl);
-        acl -= aA1 * g1 * (ul - u_star) / (T(2.) * cl * cl);
-        aus += aA2 * g1 / (T(2.) * cr);
-        a_ur -= aA2 * g1 / (T(2.) * cr);
-        acr -= aA2 * g1 * (u_star - ur) / (T(2.) * cr * cr);
-        const T anum = aus / den, aden = -aus * u_star / den;
-        T aplr = anum * (ul / cl + T(2.) / g1) + aden / cl;
-        a_ul += anum * plr / cl;
-        acl -= anum * plr * ul / (cl * cl) + aden * plr / (cl * cl);
-        a_ur += anum / cr;
-        acr -= anum * ur / (cr * cr) + aden / (cr * cr);
-        a_pl += aplr * z * plr / pl;
-        a_pr -= aplr * z * plr / pr;
+        a_ul += aA1 * g1 * T(.5) * icl;
+        aus -= aA1 * g1 * T(.5) * icl;
+        acl -= aA1 * g1 * (ul - t.u_star) * T(.5) * icl * icl;
+        aus += aA2 * g1 * T(.5) * icr;
+        a_ur -= aA2 * g1 * T(.5) * icr;
+        acr -= aA2 * g1 * (t.u_star - ur) * T(.5) * icr * icr;
+        const T iden = T(1.) / t.den;
+        const T anum = aus * iden, aden = -aus * t.u_star * iden;
+        T aplr = anum * (ul * icl + T(2.) / g1) + aden * icl;
+        a_ul += anum * t.plr * icl;
+        acl -= (anum * t.plr * ul + aden * t.plr) * icl * icl;
+        a_ur += anum * icr;
+        acr -= (anum * ur + aden) * icr * icr;
+        a_pl += aplr * t.z * t.plr * ipl;
+        a_pr -= aplr * t.z * t.plr * ipr;
     } else {
-        const T aNn = aps / S, aS = -aps * p_star / S;
+        const T iS = T(1.) / t.S;
+        const T aNn = aps * iS, aS = -aps * p_star * iS;
         const T agl = aNn * pl + aS, agr = aNn * pr + aS;
-        a_pl += aNn * gl;
-        a_pr += aNn * gr;
+        a_pl += aNn * t.gl;
+        a_pr += aNn * t.gr;
         a_ur -= aNn;
         a_ul += aNn;
-        const T dnl = pv + Bl, dnr = pv + Brr;
-        const T ahl = agl / (T(2.) * gl), ahr = agr / (T(2.) * gr);
-        const T aAl = ahl / dnl, aAr = ahr / dnr;
-        apv -= ahl * Al / (dnl * dnl) + ahr * Ar / (dnr * dnr);
-        const T aBl = -ahl * Al / (dnl * dnl), aBr = -ahr * Ar / (dnr * dnr);
-        a_dl -= aAl * Al / dl;
-        a_dr -= aAr * Ar / dr;
+        const T pv = t_fmax(T(0.), t.pv_raw);
+        const T idnl = T(1.) / (pv + t.Bl), idnr = T(1.) / (pv + t.Brr);
+        const T ahl = agl / (T(2.) * t.gl), ahr = agr / (T(2.) * t.gr);
+        const T aAl = ahl * idnl, aAr = ahr * idnr;
+        apv -= ahl * t.Al * idnl * idnl + ahr * t.Ar * idnr * idnr;
+        const T aBl = -ahl * t.Al * idnl * idnl, aBr = -ahr * t.Ar * idnr * idnr;
+        a_dl -= aAl * t.Al / dl;
+        a_dr -= aAr * t.Ar / dr;
         a_pl += aBl * ((gamma - T(1.)) / (gamma + T(1.)));
         a_pr += aBr * ((gamma - T(1.)) / (gamma + T(1.)));
     }
-    if (pv_raw > T(0.)) {
+    if (t.pv_raw > T(0.)) {
         a_pl += T(.5) * apv;
         a_pr += T(.5) * apv;
-        a_ul += T(.5) * d_avg * c_avg * apv;
-        a_ur -= T(.5) * d_avg * c_avg * apv;
-        const T ada = T(.5) * (ul - ur) * c_avg * apv, aca = T(.5) * (ul - ur) * d_avg * apv;
+        a_ul += T(.5) * t.d_avg * t.c_avg * apv;
+        a_ur -= T(.5) * t.d_avg * t.c_avg * apv;
+        const T ada = T(.5) * (ul - ur) * t.c_avg * apv, aca = T(.5) * (ul - ur) * t.d_avg * apv;
         a_dl += T(.5) * ada;
         a_dr += T(.5) * ada;
         acl += T(.5) * aca;
         acr += T(.5) * aca;
     }
-    if (!cl_fl) {
-        a_pl += acl * gamma / (T(2.) * cl * dl);
-        a_dl -= acl * cl / (T(2.) * dl);
+    if (!t.cl_fl) {
+        const T idl = T(1.) / dl;
+        a_pl += acl * gamma * T(.5) * idl / cl;
+        a_dl -= acl * cl * T(.5) * idl;
     }
-    if (!cr_fl) {
-        a_pr += acr * gamma / (T(2.) * cr * dr);
-        a_dr -= acr * cr / (T(2.) * dr);
+    if (!t.cr_fl) {
+        const T idr = T(1.) / dr;
+        a_pr += acr * gamma * T(.5) * idr / cr;
+        a_dr -= acr * cr * T(.5) * idr;
     }
+}
+
+template <typename T>
+PHD_HD void get_waves_adj(T dl, T ul, T pl, T dr, T ur, T pr, T gamma, T a_sl, T a_sc, T a_sr,
+                              T &a_dl, T &a_ul, T &a_pl, T &a_dr, T &a_ur, T &a_pr) {
+    WaveTape<T> t;
+    get_waves_fwd<T>(dl, ul, pl, dr, ur, pr, gamma, t);
+    get_waves_rev<T>(t, dl, ul, pl, dr, ur, pr, gamma, a_sl, a_sc, a_sr, a_dl, a_ul, a_pl, a_dr, a_ur, a_pr);
 }
 
 // Adjoint of the left / right data flux  F = (d u, d v_k u + p n_k, E u + p Vn),
@@ -181,13 +216,12 @@ PHD_HD __forceinline__ void star_flux_adj(T d, const T *v, T p, T Vn, T v2, T s,
                                               T gamma, const T *aF, T &ad, T *av, T &ap, T &aVn, T &av2, T &as,
                                               T &asc) {
     const T a = s - Vn, b = s - sc;
-    const T f1 = (d * a) / b;
-    const T f2 = ((f1 * (s - wn)) * (sc - Vn)) + p;
+    const T id = T(1.) / d, ia = T(1.) / a, ib = T(1.) / b, igm1 = T(1.) / (gamma - T(1.0));
+    const T f1 = d * a * ib;
     const T frho = (d * (Vn - s)) + (f1 * (s - wn));
-    const T el = ((T(0.5) * d) * v2) + (p / (gamma - T(1.0)));
-    const T t = p / (d * a);
-    const T Q = (el / d) + ((sc - Vn) * (sc + t));
-    (void)f2;
+    const T el = ((T(0.5) * d) * v2) + (p * igm1);
+    const T t = p * id * ia;
+    const T Q = (el * id) + ((sc - Vn) * (sc + t));
     const T afrho = aF[0] + aF[1] * v[0] + aF[2] * v[1];
     av[0] += aF[1] * frho;
     av[1] += aF[2] * frho;
@@ -200,15 +234,15 @@ PHD_HD __forceinline__ void star_flux_adj(T d, const T *v, T p, T Vn, T v2, T s,
     T af1 = aF[3] * (s - wn) * Q;
     const T aQ = aF[3] * (s - wn) * f1;
     // Q = el/d + (sc - Vn)(sc + t)
-    ael += aQ / d;
-    ad -= aQ * el / (d * d);
+    ael += aQ * id;
+    ad -= aQ * el * id * id;
     asc += aQ * (sc + t) + aQ * (sc - Vn);
     aVn -= aQ * (sc + t);
     const T at = aQ * (sc - Vn);
     T aa = 0;
-    ap += at / (d * a);
-    ad -= at * t / d;
-    aa -= at * t / a;
+    ap += at * id * ia;
+    ad -= at * t * id;
+    aa -= at * t * ia;
     // frho = d (Vn - s) + f1 (s - wn)
     ad += afrho * (Vn - s);
     aVn += afrho * d;
@@ -221,16 +255,16 @@ PHD_HD __forceinline__ void star_flux_adj(T d, const T *v, T p, T Vn, T v2, T s,
     aVn -= af2 * f1 * (s - wn);
     ap += af2;
     // f1 = d a / b
-    ad += af1 * a / b;
-    aa += af1 * d / b;
-    const T ab = -af1 * f1 / b;
+    ad += af1 * a * ib;
+    aa += af1 * d * ib;
+    const T ab = -af1 * f1 * ib;
     as += aa + ab;
     aVn -= aa;
     asc -= ab;
     // el
     ad += ael * T(0.5) * v2;
     av2 += ael * T(0.5) * d;
-    ap += ael / (gamma - T(1.0));
+    ap += ael * igm1;
 }
 
 // Adjoint of hll_family (HLL / HLLC + deboost), 2D.  aF: adjoint of the (deboosted)
@@ -249,8 +283,9 @@ PHD_HD void hll_family_adj(bool hllc, const T *L, const T *R, const T *n, const 
         wn = wn + w[k] * n[k];
     }
     if (boost) wn = T(0.);
-    T sl, sc, sr;
-    get_waves<T>(_dl, Vnl, _pl, _dr, Vnr, _pr, gamma, sl, sc, sr);
+    WaveTape<T> wt;
+    get_waves_fwd<T>(_dl, Vnl, _pl, _dr, Vnr, _pr, gamma, wt);
+    const T sl = wt.sl, sc = wt.sc, sr = wt.sr;
     // deboost reverse
     T aF[4] = {aFin[0], aFin[1], aFin[2], aFin[3]};
     if (boost) {
@@ -320,16 +355,27 @@ PHD_HD void hll_family_adj(bool hllc, const T *L, const T *R, const T *n, const 
             apr += aer / (gamma - T(1.0));
             asr += af1 + af3;
             asl += af2 - af3;
-        } else if (wn <= sc) {
-            star_flux_adj<T>(_dl, vl, _pl, Vnl, vl_sq, sl, sc, n, wn, gamma, aF, adl, avl, apl, aVnl, avl2, asl, asc);
         } else {
-            star_flux_adj<T>(_dr, vr, _pr, Vnr, vr_sq, sr, sc, n, wn, gamma, aF, adr, avr, apr, aVnr, avr2, asr, asc);
+            // one star-state adjoint for either side of the contact (no divergence)
+            const bool left = wn <= sc;
+            const T vs[2] = {left ? vl[0] : vr[0], left ? vl[1] : vr[1]};
+            T ad = 0, av[2] = {0, 0}, ap = 0, aVn = 0, av2 = 0, as = 0;
+            star_flux_adj<T>(left ? _dl : _dr, vs, left ? _pl : _pr, left ? Vnl : Vnr, left ? vl_sq : vr_sq,
+                             left ? sl : sr, sc, n, wn, gamma, aF, ad, av, ap, aVn, av2, as, asc);
+            const T kl = left ? T(1) : T(0), kr = T(1) - kl;
+            adl += kl * ad; adr += kr * ad;
+            avl[0] += kl * av[0]; avr[0] += kr * av[0];
+            avl[1] += kl * av[1]; avr[1] += kr * av[1];
+            apl += kl * ap; apr += kr * ap;
+            aVnl += kl * aVn; aVnr += kr * aVn;
+            avl2 += kl * av2; avr2 += kr * av2;
+            asl += kl * as; asr += kr * as;
         }
     } else {
         data_flux_adj<T>(_dr, vr, _pr, Vnr, vr_sq, n, wn, gamma, aF, adr, avr, apr, aVnr, avr2);
     }
     if (asl != T(0) || asc != T(0) || asr != T(0))
-        get_waves_adj<T>(_dl, Vnl, _pl, _dr, Vnr, _pr, gamma, asl, asc, asr, adl, aVnl, apl, adr, aVnr, apr);
+        get_waves_rev<T>(wt, _dl, Vnl, _pl, _dr, Vnr, _pr, gamma, asl, asc, asr, adl, aVnl, apl, adr, aVnr, apr);
     aL[0] += adl;
     aL[3] += apl;
     aR[0] += adr;
@@ -342,15 +388,16 @@ PHD_HD void hll_family_adj(bool hllc, const T *L, const T *R, const T *n, const 
 
 // Adjoint of the GIZMO pair limit of one field (gizmo_pair in phd_physics.cuh).
 // Returns adjoints of (sl, sr, xl, xr) given adjoints of the limited (xl, xr).
+// si = |sep_i| / |x_j - x_i|, sj = |sep_j| / |x_j - x_i| (the same quotients the forward
+// limiter forms, computed once per face by the caller).
 template <typename T>
-PHD_HD __forceinline__ void gizmo_pair_adj(T sl, T sr, T ci, T cj, T smi, T smj, T dm, T xl, T xr, T axl_out,
-                                               T axr_out, T &asl, T &asr, T &axl, T &axr) {
+PHD_HD __forceinline__ void gizmo_pair_adj_q(T sl, T sr, T ci, T cj, T si, T sj, T xl, T xr, T axl_out,
+                                                 T axr_out, T &asl, T &asr, T &axl, T &axr) {
     const T diff = sl - sr;
     const T sgn = diff > T(0) ? T(1) : (diff < T(0) ? T(-1) : T(0));
     const T delta1 = T(0.5) * t_fabs(diff), delta2 = T(0.25) * t_fabs(diff);
     const bool a_is_min = !(sr < sl);          // fmin(sl, sr) -> sl when sl <= sr
     const T phi_min = t_fmin(sl, sr), phi_max = t_fmax(sl, sr);
-    const T si = smi / dm, sj = smj / dm;
     const T phibar_l = sl + si * (sr - sl), phibar_r = sr + sj * (sl - sr);
     const bool plus_lin = ((phi_max + delta1) * phi_max) >= T(0.);
     const bool minus_lin = ((phi_min - delta1) * phi_min) >= T(0.);
@@ -406,6 +453,12 @@ PHD_HD __forceinline__ void gizmo_pair_adj(T sl, T sr, T ci, T cj, T smi, T smj,
     asr -= ad * sgn;
     if (a_is_min) { asl += a_pmin; asr += a_pmax; }
     else { asr += a_pmin; asl += a_pmax; }
+}
+
+template <typename T>
+PHD_HD __forceinline__ void gizmo_pair_adj(T sl, T sr, T ci, T cj, T smi, T smj, T dm, T xl, T xr, T axl_out,
+                                               T axr_out, T &asl, T &asr, T &axl, T &axr) {
+    gizmo_pair_adj_q<T>(sl, sr, ci, cj, smi / dm, smj / dm, xl, xr, axl_out, axr_out, asl, asr, axl, axr);
 }
 
 // Adjoint of the 2D temporal extrapolation (temporal<T,2>).  Lin/Rin are the states
