@@ -441,7 +441,7 @@ def adjoint_cost(dev, n_side=128, n_steps=200, checkpoint=20, n_dirs=16, h=1e-6,
     torch.cuda.synchronize()
     e[0].record()
     for k in range(n_steps - 1, -1, -1):
-        lam = run._adjoint(recs[k], *states[k], lam)
+        lam = run._adjoint(recs[k], states[k], lam)
     e[1].record()
     torch.cuda.synchronize()
     adj_step = e[0].elapsed_time(e[1]) / n_steps

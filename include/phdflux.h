@@ -175,6 +175,22 @@ int phd_step_f64_marked(const phd_mesh *mesh, const phd_params *par, int32_t mov
                         double *w, double *face_w, double *flux, phd_clock *clk,
                         cudaStream_t stream, cudaEvent_t *marks);
 
+/* Limiter record ("tape") of the FP64 gradients, for the adjoint (no reference
+ * counterpart: the reference has no adjoint).  tape_f64 [PHD_GRAD_TAPE_F64_ROWS][n]:
+ * the unlimited gradient estimate (8 rows) and the limiter values (4 rows); tape_i32
+ * [PHD_GRAD_TAPE_I32_ROWS][n]: per field the CSR entry of the active limit (-1 none,
+ * -2 a clamp at zero or a flat field), the entries of the neighbour maximum and
+ * minimum (-1: the cell itself), and the TESS limiter's active field.  Written for real
+ * cells; the gradients themselves are those of phd_gradients_f64 / phd_step_f64. */
+#define PHD_GRAD_TAPE_F64_ROWS 12
+#define PHD_GRAD_TAPE_I32_ROWS 13
+int phd_gradients_f64_taped(const phd_mesh *mesh, const double *prim, int32_t limiter, double *grad,
+                            double *tape_f64, int32_t *tape_i32, phd_clock *clk, cudaStream_t stream);
+int phd_step_f64_taped(const phd_mesh *mesh, const phd_params *par, int32_t moving, double *prim,
+                       const double *cons, double *cons_next, double *grad, double *w, double *face_w,
+                       double *flux, double *tape_f64, int32_t *tape_i32, phd_clock *clk,
+                       cudaStream_t stream);
+
 /* ---- fused FP32 step (FP32 reconstruction / Riemann, FP64 conserved totals) --------
  * Mesh-relative FP32 geometry, formed once per mesh by phd_prepare_f32 (the
  * cancelling differences in FP64, each rounded once to FP32):
@@ -207,6 +223,17 @@ typedef struct phd_geom32_out {
 
 int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out,
                     cudaStream_t stream);
+
+/* phd_prepare_f32 in parts, so each part can run as soon as its inputs are on the
+ * device: PHD_PREP_FACES (face_geo, face_ar: needs pair ids, x, com, area), PHD_PREP_CELLS
+ * (cell_geo: dcom, vol), PHD_PREP_LISTS (csr_face, csr_nbr: neighbour lists, pair ids,
+ * twin table). */
+#define PHD_PREP_FACES 1
+#define PHD_PREP_CELLS 2
+#define PHD_PREP_LISTS 4
+#define PHD_PREP_ALL 7
+int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out,
+                          int32_t parts, cudaStream_t stream);
 
 /* FP64 totals -> FP32 primitive cells prim4 [n][4] (rho, v_x, v_y, p) and clk->dt from
  * the CFL minimum (clock not advanced). */
@@ -277,6 +304,15 @@ int phd_adjoint_step_f64(const phd_mesh *mesh, const phd_adj_index *index, const
                          double dt, const double *cons, const double *prim, const double *grad,
                          const double *face_w, const double *lam_next, double *lam, double *work,
                          cudaStream_t stream);
+
+/* phd_adjoint_step_f64 reading the limiter record that the taped forward step (or
+ * phd_gradients_f64_taped) wrote for the same state, instead of recomputing the
+ * limiter's selections. */
+int phd_adjoint_step_f64_taped(const phd_mesh *mesh, const phd_adj_index *index,
+                               const phd_params *par, double dt, const double *cons,
+                               const double *prim, const double *grad, const double *face_w,
+                               const double *lam_next, double *lam, double *work,
+                               const double *tape_f64, const int32_t *tape_i32, cudaStream_t stream);
 
 /* The same adjoint step for callers that cannot allocate device memory: a plugin
  * whose host program gives it no device allocator (a ctypes binding, or a process

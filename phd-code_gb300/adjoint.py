@@ -141,14 +141,22 @@ class FluxRunRecord:
         L.check(lib.phd_prim_from_cons_f64(2, dm.n_cells, self.params.gamma, L.ptr(dm.vol), L.ptr(cons),
                                            L.ptr(prim), s), "prim")
 
-    def _step(self, k, prim, cons, nxt, grad):
+    def _step(self, k, prim, cons, nxt, grad, tape=None):
         """Step k: prim is overwritten with the next primitives, nxt receives the next
-        totals (all cells), grad the limited gradients of the incoming primitives."""
+        totals (all cells), grad the limited gradients of the incoming primitives and,
+        with a tape (f64, i32), the limiter's record for the adjoint."""
         rec = self.steps[k]
         b = self._buffers(rec.dmesh)
-        L.check(L.lib().phd_step_f64(rec.dmesh.ref, ctypes.byref(self.params), 0, L.ptr(prim), L.ptr(cons),
+        lib = L.lib()
+        if tape is None:
+            L.check(lib.phd_step_f64(rec.dmesh.ref, ctypes.byref(self.params), 0, L.ptr(prim), L.ptr(cons),
                                      L.ptr(nxt), L.ptr(grad), L.ptr(b.w), L.ptr(rec.face_w), L.ptr(b.flux),
                                      self._clock_ptr(k), L.stream_handle()), "step")
+        else:
+            L.check(lib.phd_step_f64_taped(rec.dmesh.ref, ctypes.byref(self.params), 0, L.ptr(prim), L.ptr(cons),
+                                           L.ptr(nxt), L.ptr(grad), L.ptr(b.w), L.ptr(rec.face_w), L.ptr(b.flux),
+                                           L.ptr(tape[0]), L.ptr(tape[1]), self._clock_ptr(k),
+                                           L.stream_handle()), "step")
 
     # --- one step in isolation, on real-cell totals (tests use these) ---------------
     def _forward_step(self, rec, U_real):
@@ -173,18 +181,25 @@ class FluxRunRecord:
         if self.params.reconstruction == L.LINEAR:
             L.check(L.lib().phd_gradients_f64(dm.ref, L.ptr(prim), self.params.limiter, L.ptr(grad), self.clock.ptr,
                                               L.stream_handle()), "gradients")
-        return self._adjoint(rec, cons, prim, grad, lam_next_real)
+        return self._adjoint(rec, (cons, prim, grad, None), lam_next_real)
 
-    def _adjoint(self, rec, cons, prim, grad, lam_next_real):
-        """lam_n (real cells) from lam_{n+1} at the step's recorded all-cell state."""
+    def _adjoint(self, rec, state, lam_next_real):
+        """lam_n (real cells) from lam_{n+1} at the step's recorded all-cell state
+        (cons, prim, grad, tape); with a limiter tape the reverse reads the forward's
+        selections instead of recomputing them."""
+        cons, prim, grad, tape = state
         dm = rec.dmesh
         b = self._buffers(dm)
         lib = L.lib()
         b.lam_next[:, :dm.n_real].copy_(lam_next_real)
-        L.check(lib.phd_adjoint_step_f64(dm.ref, ctypes.byref(rec.index()), ctypes.byref(self.params), rec.dt,
-                                         L.ptr(cons), L.ptr(prim), L.ptr(grad), L.ptr(rec.face_w),
-                                         L.ptr(b.lam_next), L.ptr(b.lam), L.ptr(b.adjoint_work(lib, dm, self.device)),
-                                         L.stream_handle()), "phd_adjoint_step_f64")
+        common = (dm.ref, ctypes.byref(rec.index()), ctypes.byref(self.params), rec.dt, L.ptr(cons), L.ptr(prim),
+                  L.ptr(grad), L.ptr(rec.face_w), L.ptr(b.lam_next), L.ptr(b.lam),
+                  L.ptr(b.adjoint_work(lib, dm, self.device)))
+        if tape is None:
+            L.check(lib.phd_adjoint_step_f64(*common, L.stream_handle()), "phd_adjoint_step_f64")
+        else:
+            L.check(lib.phd_adjoint_step_f64_taped(*common, L.ptr(tape[0]), L.ptr(tape[1]), L.stream_handle()),
+                    "phd_adjoint_step_f64_taped")
         return b.lam[:, :dm.n_real].clone()
 
     # --- whole run ------------------------------------------------------------------
@@ -213,8 +228,8 @@ class FluxRunRecord:
         return UT
 
     def _replay_segment(self, a, b):
-        """Recompute the all-cell states (totals, primitives, gradients) entering steps
-        a..b-1 from the checkpoint at a."""
+        """Recompute the all-cell states (totals, primitives, gradients and the
+        gradients' limiter tape) entering steps a..b-1 from the checkpoint at a."""
         states = []
         lib = L.lib()
         cons = prim = None
@@ -229,15 +244,20 @@ class FluxRunRecord:
                 self._load_real(dm, U_real, c, p)
                 cons, prim = c, p
             grad = torch.zeros((8, n), dtype=F64, device=self.device)
-            states.append((cons, prim, grad))
+            tape = None
+            if self.params.reconstruction == L.LINEAR:
+                tape = (torch.empty((L.GRAD_TAPE_F64_ROWS, n), dtype=F64, device=self.device),
+                        torch.empty((L.GRAD_TAPE_I32_ROWS, n), dtype=torch.int32, device=self.device))
+            states.append((cons, prim, grad, tape))
             if k + 1 < b:
                 nxt = torch.empty_like(cons)
                 p_next = prim.clone()                   # the step overwrites its primitives
-                self._step(k, p_next, cons, nxt, grad)
+                self._step(k, p_next, cons, nxt, grad, tape)
                 cons, prim = nxt, p_next
-            elif self.params.reconstruction == L.LINEAR:
-                L.check(lib.phd_gradients_f64(dm.ref, L.ptr(prim), self.params.limiter, L.ptr(grad),
-                                              self._clock_ptr(k), L.stream_handle()), "gradients")
+            elif tape is not None:
+                L.check(lib.phd_gradients_f64_taped(dm.ref, L.ptr(prim), self.params.limiter, L.ptr(grad),
+                                                    L.ptr(tape[0]), L.ptr(tape[1]), self._clock_ptr(k),
+                                                    L.stream_handle()), "gradients")
         return states
 
     def backward(self, lam_T):
@@ -250,8 +270,7 @@ class FluxRunRecord:
             b = starts[si + 1] if si + 1 < len(starts) else N
             states = self._replay_segment(a, b)
             for k in range(b - 1, a - 1, -1):
-                cons, prim, grad = states[k - a]
-                lam = self._adjoint(self.steps[k], cons, prim, grad, lam)
+                lam = self._adjoint(self.steps[k], states[k - a], lam)
             del states
         return lam
 

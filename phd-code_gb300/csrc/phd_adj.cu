@@ -179,10 +179,16 @@ __global__ void __launch_bounds__(BA) k_adj_gather(phd_mesh M, const double *__r
 }
 
 // per real cell: reverse of the limited gradient (cell_gradient_f64).
+// TAPED: the forward selections (unlimited estimate, limiter values, active entries,
+// neighbour extrema) come from the limiter record of a taped forward step instead of
+// being recomputed.
+template <bool TAPED>
 __global__ void __launch_bounds__(BA) k_adj_grad(phd_mesh M, phd_adj_index A, int limiter,
                                                  const double *__restrict__ prim, const double *__restrict__ cell_adj,
                                                  double *__restrict__ entry_adj /* [4][2F] */,
-                                                 double *__restrict__ self_adj /* [4][n] */) {
+                                                 double *__restrict__ self_adj /* [4][n] */,
+                                                 const double *__restrict__ tape_f64,
+                                                 const int32_t *__restrict__ tape_i32) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M.n_cells || M.tag[c] != PHD_REAL_TAG) return;
     const int n = M.n_cells, F = M.n_faces;
@@ -214,7 +220,20 @@ __global__ void __launch_bounds__(BA) k_adj_grad(phd_mesh M, phd_adj_index A, in
         df[2 * f] = df[2 * f + 1] = 0.0;
     }
     const int m0 = M.nbr_ptr[c], m1 = M.nbr_ptr[c + 1];
-    for (int e = m0; e < m1; e++) {
+    double alpha[4] = {1.0, 1.0, 1.0, 1.0};
+    int act[4] = {-1, -1, -1, -1};     // entry whose psi is the active limit
+    int act_f0 = -1;                   // TESS: field of the active psi
+    if (TAPED) {
+        for (int r = 0; r < 8; r++) df[r] = tape_f64[(size_t)r * n + c];
+        for (int f = 0; f < 4; f++) {
+            alpha[f] = tape_f64[(size_t)(8 + f) * n + c];
+            act[f] = tape_i32[(size_t)f * n + c];
+            arg_max[f] = tape_i32[(size_t)(4 + f) * n + c];
+            arg_min[f] = tape_i32[(size_t)(8 + f) * n + c];
+        }
+        act_f0 = tape_i32[(size_t)12 * n + c];
+    }
+    for (int e = m0; e < (TAPED ? m0 : m1); e++) {
         const int fid = M.nbr_idx[e];
         const int j = (M.pair_i[fid] == c) ? M.pair_j[fid] : M.pair_i[fid];
         const double area = M.area[fid];
@@ -235,10 +254,7 @@ __global__ void __launch_bounds__(BA) k_adj_grad(phd_mesh M, phd_adj_index A, in
                 df[2 * f + k] = df[2 * f + k] + (area * ((d_dif * cfx[k]) - ((0.5 * d_sum) * dr[k]))) / (r * vol);
         }
     }
-    double alpha[4] = {1.0, 1.0, 1.0, 1.0};
-    int act[4] = {-1, -1, -1, -1};     // entry whose psi is the active limit
-    int act_f0 = -1;                   // TESS: field of the active psi
-    for (int e = m0; e < m1; e++) {
+    for (int e = m0; e < (TAPED ? m0 : m1); e++) {
         const int fid = M.nbr_idx[e];
         const int j = (M.pair_i[fid] == c) ? M.pair_j[fid] : M.pair_i[fid];
         double sep[2];
@@ -399,9 +415,31 @@ using namespace phd;
 
 extern "C" {
 
+static int adjoint_step(const phd_mesh *mesh, const phd_adj_index *index, const phd_params *par, double dt,
+                        const double *cons, const double *prim, const double *grad, const double *face_w,
+                        const double *lam_next, double *lam, double *work, const double *tape_f64,
+                        const int32_t *tape_i32, cudaStream_t stream);
+
 int phd_adjoint_step_f64(const phd_mesh *mesh, const phd_adj_index *index, const phd_params *par, double dt,
                          const double *cons, const double *prim, const double *grad, const double *face_w,
                          const double *lam_next, double *lam, double *work, cudaStream_t stream) {
+    return adjoint_step(mesh, index, par, dt, cons, prim, grad, face_w, lam_next, lam, work, nullptr, nullptr,
+                        stream);
+}
+
+int phd_adjoint_step_f64_taped(const phd_mesh *mesh, const phd_adj_index *index, const phd_params *par,
+                               double dt, const double *cons, const double *prim, const double *grad,
+                               const double *face_w, const double *lam_next, double *lam, double *work,
+                               const double *tape_f64, const int32_t *tape_i32, cudaStream_t stream) {
+    if (!tape_f64 || !tape_i32) return PHD_ERR_ARG;
+    return adjoint_step(mesh, index, par, dt, cons, prim, grad, face_w, lam_next, lam, work, tape_f64, tape_i32,
+                        stream);
+}
+
+static int adjoint_step(const phd_mesh *mesh, const phd_adj_index *index, const phd_params *par, double dt,
+                        const double *cons, const double *prim, const double *grad, const double *face_w,
+                        const double *lam_next, double *lam, double *work, const double *tape_f64,
+                        const int32_t *tape_i32, cudaStream_t stream) {
     if (!mesh || mesh->dim != 2 || !index || !par || !cons || !prim || !lam_next || !lam || !work)
         return PHD_ERR_ARG;
     if (mesh->n_faces && !mesh->normal) return PHD_ERR_ARG;
@@ -419,7 +457,14 @@ int phd_adjoint_step_f64(const phd_mesh *mesh, const phd_adj_index *index, const
     if (F) k_adj_face<<<ga((int)F), ba((int)F), 0, stream>>>(M, *par, dt, prim, grad, face_w, lam_next, face_adj);
     k_adj_gather<<<ga((int)n), ba((int)n), 0, stream>>>(M, face_adj, cell_adj);
     if (par->reconstruction == PHD_LINEAR)
-        k_adj_grad<<<ga((int)n), ba((int)n), 0, stream>>>(M, *index, par->limiter, prim, cell_adj, entry_adj, self_adj);
+    {
+        if (tape_f64)
+            k_adj_grad<true><<<ga((int)n), ba((int)n), 0, stream>>>(M, *index, par->limiter, prim, cell_adj,
+                                                                  entry_adj, self_adj, tape_f64, tape_i32);
+        else
+            k_adj_grad<false><<<ga((int)n), ba((int)n), 0, stream>>>(M, *index, par->limiter, prim, cell_adj,
+                                                                   entry_adj, self_adj, nullptr, nullptr);
+    }
     k_adj_gather2<<<ga((int)n), ba((int)n), 0, stream>>>(M, *index, cell_adj, entry_adj, self_adj, prim_adj);
     k_adj_final<<<ga((int)n), ba((int)n), 0, stream>>>(M, *index, par->gamma, cons, prim_adj, lam_next, lam);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;

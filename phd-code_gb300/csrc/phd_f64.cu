@@ -16,14 +16,27 @@ __device__ __forceinline__ void set_status(phd_clock *clk, int bits) {
 }
 
 // ---- gradients ------------------------------------------------------------------
+// Limiter record of one cell's gradient, kept by a taped forward step for the adjoint:
+// f64 [12][n]: the unlimited estimate (8 rows) and the limiter values (4 rows);
+// i32 [13][n]: per field the CSR entry of the active limit (-1: none, -2: a clamp at
+// zero or a flat field), the entries of the neighbour maximum and minimum (-1: the
+// cell itself), and (TESS) the field of the active limit.
+struct GradTape {
+    double *f64;
+    int32_t *i32;
+};
+
 // PieceWiseLinear.compute_gradients reconstruction.pyx:620-736 for cell c, result in
-// df (limited).  Returns status bits.
-template <int DIM>
+// df (limited).  Returns status bits.  TAPE: also records the limiter's selections
+// (same arithmetic; only bookkeeping is added) when `record`.
+template <int DIM, bool TAPE = false>
 __device__ int cell_gradient_f64(const phd_mesh &M, const double *__restrict__ prim, int limiter,
-                                 int c, double *df) {
+                                 int c, double *df, GradTape tape = GradTape{nullptr, nullptr},
+                                 bool record = false) {
     constexpr int NF = DIM + 2;
     const int n = M.n_cells, F = M.n_faces;
     double phi_max[NF], phi_min[NF], alpha[NF], xi[DIM], cx[DIM], pc[NF];
+    int arg_max[NF], arg_min[NF], act[NF], act_f0 = -1;
     int status = 0;
 #pragma unroll
     for (int k = 0; k < DIM; k++) {
@@ -36,6 +49,7 @@ __device__ int cell_gradient_f64(const phd_mesh &M, const double *__restrict__ p
         pc[f] = prim[(size_t)f * n + c];
         phi_max[f] = phi_min[f] = pc[f];
         alpha[f] = 1.0;
+        arg_max[f] = arg_min[f] = act[f] = -1;
 #pragma unroll
         for (int k = 0; k < DIM; k++) df[DIM * f + k] = 0;
     }
@@ -62,6 +76,10 @@ __device__ int cell_gradient_f64(const phd_mesh &M, const double *__restrict__ p
 #pragma unroll
         for (int f = 0; f < NF; f++) {
             const double pj = prim[(size_t)f * n + j];
+            if (TAPE) {
+                if (pj > phi_max[f]) arg_max[f] = m;
+                if (pj < phi_min[f]) arg_min[f] = m;
+            }
             phi_max[f] = fmax(phi_max[f], pj);
             phi_min[f] = fmin(phi_min[f], pj);
             const double d_dif = pj - pc[f];
@@ -86,6 +104,7 @@ __device__ int cell_gradient_f64(const phd_mesh &M, const double *__restrict__ p
                 if (dphi > 0) psi = (phi_max[f] - pc[f]) / dphi;
                 else if (dphi < 0) psi = (phi_min[f] - pc[f]) / dphi;
                 else psi = 1.0;
+                if (TAPE && fmax(psi, 0.) < alpha[f]) act[f] = (psi > 0.0 && dphi != 0.0) ? m : -2;
                 alpha[f] = fmin(alpha[f], fmax(psi, 0.));
             }
         }
@@ -108,9 +127,25 @@ __device__ int cell_gradient_f64(const phd_mesh &M, const double *__restrict__ p
                     const double t = (prim[(size_t)f * n + j] - pc[f]) / dphi;
                     psi = (0. > t) ? 0. : t;
                 } else psi = 1.0;
+                if (TAPE && fmax(psi, 0.) < alpha[0]) {
+                    act[0] = (psi > 0.0 && dphi != 0.0) ? m : -2;
+                    act_f0 = f;
+                }
                 alpha[0] = fmin(alpha[0], fmax(psi, 0.));     // only alpha[0]: :731
             }
         }
+    }
+    if (TAPE && record) {
+#pragma unroll
+        for (int r = 0; r < NF * DIM; r++) tape.f64[(size_t)r * n + c] = df[r];
+#pragma unroll
+        for (int f = 0; f < NF; f++) {
+            tape.f64[(size_t)(NF * DIM + f) * n + c] = alpha[f];
+            tape.i32[(size_t)f * n + c] = act[f];
+            tape.i32[(size_t)(NF + f) * n + c] = arg_max[f];
+            tape.i32[(size_t)(2 * NF + f) * n + c] = arg_min[f];
+        }
+        tape.i32[(size_t)(3 * NF) * n + c] = act_f0;
     }
 #pragma unroll
     for (int f = 0; f < NF; f++)
@@ -122,10 +157,10 @@ __device__ int cell_gradient_f64(const phd_mesh &M, const double *__restrict__ p
 // Real rows: own gradient.  Ghost rows: the image's gradient (computed again from the
 // image's faces, bit-identical), with the reflective diagonal flip of grad v
 // (domain_manager.pyx:819-835, boundary.pyx:287-307).
-template <int DIM>
+template <int DIM, bool TAPE = false>
 __global__ void __launch_bounds__(BLOCK) k_gradients(phd_mesh M, const double *__restrict__ prim,
                                                       int limiter, double *__restrict__ grad,
-                                                      phd_clock *clk) {
+                                                      phd_clock *clk, GradTape tape = GradTape{nullptr, nullptr}) {
     constexpr int NF = DIM + 2;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= M.n_cells) return;
@@ -135,7 +170,7 @@ __global__ void __launch_bounds__(BLOCK) k_gradients(phd_mesh M, const double *_
         if (c < 0 || c >= M.n_cells) { set_status(clk, PHD_STATUS_BAD_INDEX); return; }
     }
     double df[NF * DIM];
-    const int st = cell_gradient_f64<DIM>(M, prim, limiter, c, df);
+    const int st = cell_gradient_f64<DIM, TAPE>(M, prim, limiter, c, df, tape, i == c);
     set_status(clk, st);
     const int fl = M.flip ? M.flip[i] : 0;
 #pragma unroll
@@ -541,6 +576,14 @@ int phd_gradients_f64(const phd_mesh *mesh, const double *prim, int32_t limiter,
     return launch_status();
 }
 
+int phd_gradients_f64_taped(const phd_mesh *mesh, const double *prim, int32_t limiter, double *grad,
+                            double *tape_f64, int32_t *tape_i32, phd_clock *clk, cudaStream_t stream) {
+    if (!mesh_ok(mesh) || !prim || !grad || !tape_f64 || !tape_i32) return PHD_ERR_ARG;
+    k_gradients<2, true><<<grid_of(mesh->n_cells), blk_of(mesh->n_cells), 0, stream>>>(
+        *mesh, prim, limiter, grad, clk, GradTape{tape_f64, tape_i32});
+    return launch_status();
+}
+
 int phd_states_f64(const phd_mesh *mesh, const double *prim, const double *grad, const double *face_w,
                    double gamma, double dt_half, int32_t boost, int32_t reconstruction, int32_t gizmo,
                    int32_t stages, double *left, double *right, cudaStream_t stream) {
@@ -614,9 +657,28 @@ int phd_face_velocities_f64(const phd_mesh *mesh, const double *w, double *face_
     return launch_status();
 }
 
+static int step_f64(const phd_mesh *mesh, const phd_params *par, int32_t moving, double *prim, const double *cons,
+                    double *cons_next, double *grad, double *w, double *face_w, double *flux, phd_clock *clk,
+                    cudaStream_t stream, cudaEvent_t *marks, GradTape tape);
+
 int phd_step_f64_marked(const phd_mesh *mesh, const phd_params *par, int32_t moving, double *prim,
                         const double *cons, double *cons_next, double *grad, double *w, double *face_w,
                         double *flux, phd_clock *clk, cudaStream_t stream, cudaEvent_t *marks) {
+    return step_f64(mesh, par, moving, prim, cons, cons_next, grad, w, face_w, flux, clk, stream, marks,
+                    GradTape{nullptr, nullptr});
+}
+
+int phd_step_f64_taped(const phd_mesh *mesh, const phd_params *par, int32_t moving, double *prim,
+                       const double *cons, double *cons_next, double *grad, double *w, double *face_w,
+                       double *flux, double *tape_f64, int32_t *tape_i32, phd_clock *clk, cudaStream_t stream) {
+    if (!tape_f64 || !tape_i32) return PHD_ERR_ARG;
+    return step_f64(mesh, par, moving, prim, cons, cons_next, grad, w, face_w, flux, clk, stream, nullptr,
+                    GradTape{tape_f64, tape_i32});
+}
+
+static int step_f64(const phd_mesh *mesh, const phd_params *par, int32_t moving, double *prim, const double *cons,
+                    double *cons_next, double *grad, double *w, double *face_w, double *flux, phd_clock *clk,
+                    cudaStream_t stream, cudaEvent_t *marks, GradTape tape) {
     if (!mesh_ok(mesh) || !par || !prim || !cons || !cons_next || !flux || !clk) return PHD_ERR_ARG;
     if (mesh->n_faces && !mesh->normal) return PHD_ERR_ARG;
     const bool linear = par->reconstruction == PHD_LINEAR;
@@ -629,7 +691,10 @@ int phd_step_f64_marked(const phd_mesh *mesh, const phd_params *par, int32_t mov
         k_gen_vel<2><<<gc, bc, 0, stream>>>(*mesh, prim, par->gamma, par->eta, par->regularize, w);
         if (mesh->n_faces) k_face_vel<2><<<gf, bf, 0, stream>>>(*mesh, w, face_w);
     }
-    if (linear) k_gradients<2><<<gc, bc, 0, stream>>>(*mesh, prim, par->limiter, grad, clk);
+    if (linear) {
+        if (tape.f64) k_gradients<2, true><<<gc, bc, 0, stream>>>(*mesh, prim, par->limiter, grad, clk, tape);
+        else k_gradients<2><<<gc, bc, 0, stream>>>(*mesh, prim, par->limiter, grad, clk);
+    }
     if (marks) cudaEventRecord(marks[1], stream);
     if (mesh->n_faces)
         k_face_flux<2><<<gf, bf, 0, stream>>>(*mesh, *par, prim, grad, face_w, flux, clk);

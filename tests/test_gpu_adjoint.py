@@ -8,7 +8,7 @@ import torch
 
 import torch_step as T
 import phd_code_gb300 as pkg
-from phd_code_gb300.adjoint import FluxRun, FluxRunRecord, StepRecord
+from phd_code_gb300.adjoint import FluxRun, FluxRunRecord, StepRecord, cons_from_prim_t
 from phd_code_gb300.device import DeviceMesh
 from _util import lattice_mesh, smooth_state
 
@@ -143,3 +143,23 @@ def test_multistep_gradient_vs_torch_autograd(state, limiter):
     ((U[0] / vol - tgt.cpu()) ** 2).sum().backward()
     gr = pp.grad.numpy()
     assert np.max(np.abs(g.cpu().numpy() - gr)) / np.max(np.abs(gr)) <= 1e-9
+
+
+@pytest.mark.parametrize("limiter", ["arepo", "tess"])
+def test_taped_adjoint_equals_recomputing_adjoint(limiter):
+    """The reverse step reading the limiter record of a taped forward step gives the same
+    result as the one recomputing the limiter's selections (same arithmetic)."""
+    m = lattice_mesh(16, "periodic", seed=8)
+    prim = generic_state(m)
+    run, recs, p0, tgt, loss, g = multistep_case(m, prim, 3, limiter=limiter, checkpoint=3)
+    U0 = cons_from_prim_t(p0.detach(), recs[0].dmesh.vol[:m.n_real], 1.4).contiguous()
+    run.forward(U0)
+    states = run._replay_segment(0, 3)
+    lam = torch.tensor(np.random.default_rng(2).standard_normal((4, m.n_real)), device="cuda")
+    for k in range(2, -1, -1):
+        cons, prim_k, grad, tape = states[k]
+        assert tape is not None
+        a = run._adjoint(recs[k], (cons, prim_k, grad, tape), lam)
+        b = run._adjoint(recs[k], (cons, prim_k, grad, None), lam)
+        assert torch.equal(a, b)
+        lam = a
