@@ -160,11 +160,13 @@ def algorithmic_bytes_f64(n, F, n_real):
 
 
 # --------------------------------------------------------------------------------------
-def cpu_baseline(n_side_sample, seconds, solver, prefer_reference=True):
+def cpu_baseline(n_side_sample, seconds, solver, prefer_reference=True, steps=None, warmup=0):
     """CPU throughput of the same path, one host thread, on a bounded sample of the same
     workload (a smaller lattice of the same problem): the reference's own Cython modules
     when they are built on this machine (kind "reference"), else the C restatement
-    (oracle/phd_oracle.c, kind "port")."""
+    (oracle/phd_oracle.c, kind "port").  With `steps`, `warmup` untimed steps are run and
+    then `steps` timed ones (stopping early once `seconds` have passed); otherwise steps
+    are timed until `seconds` have passed."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     mesh, prim = shear_layer(n_side_sample)
     gamma = 5.0 / 3.0
@@ -187,22 +189,26 @@ def cpu_baseline(n_side_sample, seconds, solver, prefer_reference=True):
 
         def one():
             stp.step(O.time_step(mesh, p, gamma, 0.5, True), p, c)
-    steps, t0 = 0, time.perf_counter()
+    for _ in range(warmup):
+        one()
+    limit = steps if steps is not None else 10000
+    done, t0 = 0, time.perf_counter()
     while True:
         one()
-        steps += 1
+        done += 1
         el = time.perf_counter() - t0
-        if el >= seconds or steps >= 10000:
+        if done >= limit or el >= seconds:
             break
     what = "the reference's Cython flux path" if kind == "reference" else "the C restatement"
-    return {"value": mesh.n_faces * steps / el, "unit": UNIT, "cores": 1, "kind": kind,
+    return {"value": mesh.n_faces * done / el, "unit": UNIT, "cores": 1, "kind": kind, "steps": done,
+            "ms_per_step": 1e3 * el / done, "faces": mesh.n_faces,
             "sample": "%d moving-mesh %s steps (FP64) of %s on the %dx%d shear layer (%d faces), 1 host thread"
-                      % (steps, solver.upper(), what, n_side_sample, n_side_sample, mesh.n_faces)}
+                      % (done, solver.upper(), what, n_side_sample, n_side_sample, mesh.n_faces)}
 
 
 def _cpu_worker(args):
-    n_side, seconds, solver = args
-    return cpu_baseline(n_side, seconds, solver)
+    n_side, seconds, solver, steps, warmup = args
+    return cpu_baseline(n_side, seconds, solver, steps=steps, warmup=warmup)
 
 
 def run_reference(args, rank, world):
@@ -215,17 +221,22 @@ def run_reference(args, rank, world):
     n_side = 256
     cores = max(1, os.cpu_count() or 1)
     ctx = mp.get_context("spawn")
+    # each replica: `warmup` untimed steps, then `steps` timed steps of its 256x256
+    # sample (about 0.17 s per step per core), capped at 150 s
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(n_side, max(5.0, args.cpu_seconds), args.solver)] * cores)
+        res = pool.map(_cpu_worker, [(n_side, 150.0, args.solver, args.steps, args.warmup)] * cores)
     value = float(sum(r["value"] for r in res))
-    sample = "%s; %d concurrent replicas" % (res[0]["sample"].replace(", 1 host thread", ""), cores)
+    sample = ("each host core steps its own %dx%d sample of the same problem (%d faces): %s; %d concurrent "
+              "replicas" % (n_side, n_side, res[0]["faces"], res[0]["sample"].replace(", 1 host thread", ""), cores))
     kind = res[0]["kind"]
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": min(r["steps"] for r in res),
+           "warmup": args.warmup, "ms_per_step": float(np.median([r["ms_per_step"] for r in res])),
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "impl": "reference",
-           "config": {"workload": "shear layer %dx%d periodic (bounded CPU sample of the 1024x1024 run)"
-                                  % (n_side, n_side), "solver": args.solver, "precision": "fp64"},
+           "config": {"workload": "shear layer 1024x1024 jittered lattice, periodic, gamma 5/3",
+                      "solver": args.solver, "precision": "fp64 (the reference computes in FP64)",
+                      "sample": "bounded: a %dx%d lattice of the same problem per host core" % (n_side, n_side),
+                      "parallelism": "%d host cores, one replica each" % cores},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind, "sample": sample},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
