@@ -232,6 +232,11 @@ int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *o
 #define PHD_PREP_CELLS 2
 #define PHD_PREP_LISTS 4
 #define PHD_PREP_ALL 7
+/* cell_geo formed from the prepared faces instead of mesh->vol / dcom (the volume and
+ * centre of mass sums of tess.cpp:330-393, in FP32); needs PHD_PREP_FACES and
+ * PHD_PREP_LISTS done before it (same call or earlier on the stream); excludes
+ * PHD_PREP_CELLS.  The FP32 path then needs no volumes or centroids from the host. */
+#define PHD_PREP_CELLS_FROM_FACES 8
 int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out,
                           int32_t parts, cudaStream_t stream);
 
@@ -239,6 +244,11 @@ int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_
  * the CFL minimum (clock not advanced). */
 int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4,
                  phd_clock *clk, cudaStream_t stream);
+
+/* phd_prim_f32 with the volumes of a prepared cell_geo [n][4] (e.g. formed with
+ * PHD_PREP_CELLS_FROM_FACES) instead of mesh->vol. */
+int phd_prim_f32_cells(const phd_mesh *mesh, const float *cell_geo, const phd_params *par,
+                       const double *cons, float *prim4, phd_clock *clk, cudaStream_t stream);
 
 /* phd_prim_f32 for a batch of runs (see phd_step_f32_batched): each run's clock gets
  * its own CFL step. */
@@ -257,8 +267,9 @@ int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *
                  float *w2, float *flux4, phd_clock *clk, cudaStream_t stream);
 
 /* Launch shape of the three step kernels (chosen by an autotuner): threads per block
- * (multiple of 32, <= 512) and a cap on blocks per grid (0: one thread per item; > 0:
- * that many blocks, each looping over items -- a persistent launch). */
+ * (multiple of 32, <= 512; the face kernel <= 384) and a cap on blocks per grid (0: one
+ * thread per item; > 0: that many blocks, each looping over items -- a persistent
+ * launch). */
 typedef struct phd_launch {
     int32_t block_grad, block_face, block_update;
     int32_t grid_cap_grad, grid_cap_face, grid_cap_update;

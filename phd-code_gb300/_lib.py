@@ -16,7 +16,7 @@ ADJ_NOALLOC_MAX_DOUBLES = 4194304
 GRAD_TAPE_F64_ROWS, GRAD_TAPE_I32_ROWS = 12, 13
 STATUS_NEG_MASS, STATUS_NEG_ENERGY, STATUS_RIEMANN_NONCONVERGED, STATUS_BAD_INDEX = 1, 2, 4, 8
 HLL, HLLC, EXACT = 0, 1, 2
-PREP_FACES, PREP_CELLS, PREP_LISTS, PREP_ALL = 1, 2, 4, 7
+PREP_FACES, PREP_CELLS, PREP_LISTS, PREP_ALL, PREP_CELLS_FROM_FACES = 1, 2, 4, 7, 8
 CONSTANT, LINEAR = 0, 1
 LIMITER_AREPO, LIMITER_TESS = 0, 1
 STAGE_SPATIAL, STAGE_TEMPORAL = 1, 2
@@ -103,6 +103,7 @@ SIGNATURES = {
     "phd_prepare_f32": ([_PM, _vp, C.POINTER(PhdGeom32Out), _vp], C.c_int),
     "phd_prepare_f32_parts": ([_PM, _vp, C.POINTER(PhdGeom32Out), _i32, _vp], C.c_int),
     "phd_prim_f32": ([_PM, _PP, _vp, _vp, _vp, _vp], C.c_int),
+    "phd_prim_f32_cells": ([_PM, _vp, _PP, _vp, _vp, _vp, _vp], C.c_int),
     "phd_prim_f32_batched": ([_PM, _PP, _vp, _vp, _vp, _i32, _vp, _vp], C.c_int),
     "phd_step_f32": ([_PM, _PG, _PP, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], C.c_int),
     "phd_adjoint_work_doubles": ([_i32, _i32], C.c_size_t),

@@ -15,6 +15,7 @@ import torch
 from . import _lib as L
 
 BLOCKS = (128, 256, 384, 512)
+FACE_MAX_BLOCK = 384           # k_face32's launch bound (56 registers per thread)
 CAP_WAVES = (0, 2, 4, 8)       # 0: one thread per item; k: k blocks per SM
 
 
@@ -42,7 +43,7 @@ def tune(stepper, blocks=BLOCKS, cap_waves=CAP_WAVES, reps=3):
     for b in blocks:
         for w in cap_waves:
             cap = w * sms
-            lch = L.PhdLaunch(b, b, b, cap, cap, cap)
+            lch = L.PhdLaunch(b, min(b, FACE_MAX_BLOCK), b, cap, cap, cap)
             for k in range(reps + 1):
                 arr = None
                 if k > 0:
@@ -67,5 +68,6 @@ def tune(stepper, blocks=BLOCKS, cap_waves=CAP_WAVES, reps=3):
     def cap_of(key):
         return key[1] * sms
 
-    launch = L.PhdLaunch(best[0][0], best[1][0], best[2][0], cap_of(best[0]), cap_of(best[1]), cap_of(best[2]))
+    launch = L.PhdLaunch(best[0][0], min(best[1][0], FACE_MAX_BLOCK), best[2][0], cap_of(best[0]), cap_of(best[1]),
+                         cap_of(best[2]))
     return launch, table

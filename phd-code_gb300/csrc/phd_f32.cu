@@ -72,6 +72,38 @@ __global__ void k_prepare_cells32(phd_mesh M, float4 *__restrict__ cell_geo) {
                               sqrtf(v * 0.3183098861837907f));
 }
 
+// Cell geometry from the prepared faces, as the tessellation forms it
+// (Tess2d::extract_geometry tess.cpp:330-393): each face contributes the triangle
+// (generator, face) of area w = A h / 4 (h = |x_j - x_i|) to the volume and w times
+// its centroid (2 f + x) / 3 to the centre of mass, so
+//   vol = sum w,   dcom = (2/3) sum w (f - x) / vol,
+// with f - x = c + r n / 2 from pair-i and c - r n / 2 from pair-j.  Ghost rows take
+// their image's values (dcom unflipped, as the ghost copies do).  FP32 throughout: the
+// relative vectors have no cancellation left.
+__global__ void k_cells_from_faces32(phd_mesh M, const float4 *__restrict__ face_geo,
+                                     const float2 *__restrict__ face_ar, const int32_t *__restrict__ csr_face,
+                                     float4 *__restrict__ cell_geo) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.n_cells) return;
+    const int c = (M.tag[i] == PHD_REAL_TAG) ? i : M.map[i];
+    float vol = 0.f, sx = 0.f, sy = 0.f;
+    if (c >= 0 && c < M.n_cells) {
+        for (int e = M.nbr_ptr[c]; e < M.nbr_ptr[c + 1]; e++) {
+            const int code = csr_face[e];
+            const int fid = code < 0 ? ~code : code;
+            const float4 g = face_geo[fid];
+            const float2 ar = face_ar[fid];
+            const float hr = (code < 0 ? -0.5f : 0.5f) * ar.y;
+            const float w = 0.25f * ar.x * ar.y;
+            vol += w;
+            sx += w * (g.z + hr * g.x);
+            sy += w * (g.w + hr * g.y);
+        }
+    }
+    const float inv = vol > 0.f ? 1.f / vol : 0.f;
+    cell_geo[i] = make_float4((2.f / 3.f) * sx * inv, (2.f / 3.f) * sy * inv, inv, sqrtf(vol * 0.3183098861837907f));
+}
+
 // CSR entries with the side folded into the face id, plus the neighbour cell.  Where a
 // twin table is given (periodic faces computed twice by the reference, once from
 // each side), the entry of the dropped twin points at the kept face from the other side.
@@ -447,8 +479,13 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
     flux4[m] = make_float4(s * f[0], s * f[1], s * f[2], s * f[3]);
 }
 
+// At most 384 threads per block and at least 3 blocks per SM: 56 registers per thread,
+// which lets more warps hide the face kernel's gather latency (measured faster than the
+// 61-register build at 512 threads).
+constexpr int FACE_MAX_BLOCK = 384;
+
 template <int SOLVER, bool LINEAR>
-__global__ void __launch_bounds__(512) k_face32(phd_mesh M, phd_params P, int moving,
+__global__ void __launch_bounds__(FACE_MAX_BLOCK, 3) k_face32(phd_mesh M, phd_params P, int moving,
                                                 const float4 *__restrict__ face_geo,
                                                 const float2 *__restrict__ face_ar,
                                                 const float4 *__restrict__ cell_geo,
@@ -577,7 +614,8 @@ __global__ void __launch_bounds__(512) k_update32(phd_mesh M, phd_params P, cons
 // advanced).  Same per-run reduction as k_update32.
 __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const double *__restrict__ cons,
                                                 float4 *__restrict__ prim4, phd_clock *clocks,
-                                                const int32_t *__restrict__ cell_run, int n_runs) {
+                                                const int32_t *__restrict__ cell_run, int n_runs,
+                                                const float4 *__restrict__ cell_geo) {
     const int n = M.n_cells;
     const int stride = gridDim.x * blockDim.x;
     const int n_iter = (n + stride - 1) / stride;
@@ -592,8 +630,16 @@ __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const 
             const double U3 = cons[3 * (size_t)n + i];
             const float m = narrow_f64(cons[i]), mx = narrow_f64(cons[(size_t)n + i]);
             const float my = narrow_f64(cons[2 * (size_t)n + i]);
-            const float v = narrow_f64(M.vol[i]);
-            const float inv_v = 1.f / v;
+            float v, inv_v, R;
+            if (cell_geo) {                    // volumes formed on the device from the faces
+                const float4 cg = cell_geo[i];
+                inv_v = cg.z;
+                R = cg.w;
+            } else {
+                v = narrow_f64(M.vol[i]);
+                inv_v = 1.f / v;
+                R = sqrtf(v * 0.3183098861837907f);
+            }
             const float rm = 1.f / m;
             const float vx = mx * rm, vy = my * rm;
             const float ke = 0.5f * (mx * vx + my * vy);
@@ -603,7 +649,6 @@ __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const 
             if (M.tag[i] == PHD_REAL_TAG) {
                 const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
                 const float cs = sqrtf(gam * pr.w / pr.x);
-                const float R = sqrtf(v * 0.3183098861837907f);
                 cand = R / (boost ? cs : cs + sqrtf(pr.y * pr.y + pr.z * pr.z));
             }
             if (cell_run) run = cell_run[i];
@@ -657,7 +702,12 @@ extern "C" {
 
 int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out, int32_t parts,
                           cudaStream_t stream) {
-    if (!mesh || mesh->dim != 2 || !out || parts < 0 || parts > PHD_PREP_ALL) return PHD_ERR_ARG;
+    if (!mesh || mesh->dim != 2 || !out || parts < 0 || parts > (PHD_PREP_ALL | PHD_PREP_CELLS_FROM_FACES))
+        return PHD_ERR_ARG;
+    if ((parts & PHD_PREP_CELLS) && (parts & PHD_PREP_CELLS_FROM_FACES)) return PHD_ERR_ARG;
+    if ((parts & PHD_PREP_CELLS_FROM_FACES) &&
+        (!out->cell_geo || !out->face_geo || !out->face_ar || !out->csr_face))
+        return PHD_ERR_ARG;
     if ((parts & PHD_PREP_FACES) && (!out->face_geo || !out->face_ar)) return PHD_ERR_ARG;
     if ((parts & PHD_PREP_CELLS) && !out->cell_geo) return PHD_ERR_ARG;
     if ((parts & PHD_PREP_LISTS) && (!out->csr_face || !out->csr_nbr)) return PHD_ERR_ARG;
@@ -669,6 +719,10 @@ int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_
                                                                  reinterpret_cast<float4 *>(out->cell_geo));
     if (parts & PHD_PREP_LISTS)
         k_prepare_csr32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, twin, out->csr_face, out->csr_nbr);
+    if (parts & PHD_PREP_CELLS_FROM_FACES)     // after the faces and lists (stream order)
+        k_cells_from_faces32<<<g32(mesh->n_cells), B32, 0, stream>>>(
+            *mesh, reinterpret_cast<const float4 *>(out->face_geo), reinterpret_cast<const float2 *>(out->face_ar),
+            out->csr_face, reinterpret_cast<float4 *>(out->cell_geo));
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
@@ -681,13 +735,21 @@ int phd_prim_f32_batched(const phd_mesh *mesh, const phd_params *par, const doub
     if (!mesh || mesh->dim != 2 || !par || !cons || !prim4 || !clocks) return PHD_ERR_ARG;
     if (n_runs < 1 || (n_runs > 1 && !cell_run)) return PHD_ERR_ARG;
     k_prim32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, *par, cons, reinterpret_cast<float4 *>(prim4), clocks,
-                                                     n_runs > 1 ? cell_run : nullptr, n_runs);
+                                                     n_runs > 1 ? cell_run : nullptr, n_runs, nullptr);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
 int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4, phd_clock *clk,
                  cudaStream_t stream) {
     return phd_prim_f32_batched(mesh, par, cons, prim4, clk, 1, nullptr, stream);
+}
+
+int phd_prim_f32_cells(const phd_mesh *mesh, const float *cell_geo, const phd_params *par, const double *cons,
+                       float *prim4, phd_clock *clk, cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || !cell_geo || !par || !cons || !prim4 || !clk) return PHD_ERR_ARG;
+    k_prim32<<<g32(mesh->n_cells), B32, 0, stream>>>(*mesh, *par, cons, reinterpret_cast<float4 *>(prim4), clk,
+                                                     nullptr, 1, reinterpret_cast<const float4 *>(cell_geo));
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
 int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
@@ -703,7 +765,8 @@ int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_
     if (n_runs < 1 || (n_runs > 1 && !cell_run)) return PHD_ERR_ARG;
     phd_launch L = {B32, B32, B32, 0, 0, 0};
     if (launch) {
-        if (!block_ok(launch->block_grad) || !block_ok(launch->block_face) || !block_ok(launch->block_update))
+        if (!block_ok(launch->block_grad) || !block_ok(launch->block_face) || !block_ok(launch->block_update) ||
+            launch->block_face > FACE_MAX_BLOCK)
             return PHD_ERR_ARG;
         L = *launch;
     }

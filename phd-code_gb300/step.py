@@ -99,21 +99,29 @@ class FluxStepper:
         the same order, as after the host re-mesh of ``integrate.py:410-417``).
 
         The device forms the neighbour lists, flip bits and, for FP32, the periodic twin
-        table and FP32 geometry (normals included); FP64 forms its FP64 normals.  The
+        table and FP32 geometry (normals, cell volumes and centroids included, so FP32
+        copies neither); FP64 forms its FP64 normals.  The
         ghosts are re-created from their images (``domain_manager.pyx:712-774``), the
         primitives recovered with the new volumes and the next dt taken from them
-        (steps 6-8 of the moving-mesh step).  The neighbour lists and the twin table are
-        built on a second stream while the rest of the mesh is still being copied.
-        Returns the bytes copied."""
+        (steps 6-8 of the moving-mesh step).  The neighbour lists, twin table, FP32 list
+        codes and face geometry are formed on a second stream while the rest of the mesh
+        is still being copied.  Returns the bytes copied."""
         dm, p = self.dmesh, self.params
         dm.check_upload(pinned)
         lib = L.lib()
+        fp32 = self.precision == "fp32"
         main = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
         if getattr(self, "_side", None) is None:
             self._side = torch.cuda.Stream(self.device)
-            self._ev = [torch.cuda.Event() for _ in range(3)]
+            self._ev = [torch.cuda.Event() for _ in range(4)]
         side, ev = self._side, self._ev
         s, ss = L.stream_handle(main), L.stream_handle(side)
+        out = None
+        if fp32:
+            out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
+                                                            self.csr_nbr, self.cell_geo)))
+        # copies on the main stream in the order the side stream needs them; the side
+        # stream builds the neighbour lists, twins, list codes and face geometry meanwhile
         dm.reset_errors(main)
         nbytes = dm.copy_fields(pinned, ("pair_i", "pair_j"), main)
         ev[0].record(main)
@@ -121,25 +129,33 @@ class FluxStepper:
         dm.build_lists(side)
         nbytes += dm.copy_fields(pinned, ("x", "map"), main)
         ev[1].record(main)
-        if self.precision == "fp32":
+        if fp32:
             side.wait_event(ev[1])
             box = [b - a for a, b in zip(dm.xmin, dm.xmax)]
             L.check(lib.phd_periodic_twins(dm.ref, int(self.dedup_periodic and dm.boundary == "periodic"),
                                            float(box[0]), float(box[1]), L.ptr(self.twin), ss),
                     "phd_periodic_twins")
-        ev[2].record(side)
-        nbytes += dm.copy_fields(pinned, ("com", "area", "dcom", "vol", "tag", "type"), main)
-        main.wait_event(ev[2])
+            L.check(lib.phd_prepare_f32_parts(dm.ref, L.ptr(self.twin), ctypes.byref(out), L.PREP_LISTS, ss),
+                    "phd_prepare_f32_parts")
+        nbytes += dm.copy_fields(pinned, ("com", "area"), main)
+        if fp32:
+            # face geometry, then the cells' volumes and centroids from it (the FP32 path
+            # needs neither host volumes nor host centroids)
+            ev[2].record(main)
+            side.wait_event(ev[2])
+            dm.set_normals("none", side)
+            L.check(lib.phd_prepare_f32_parts(dm.ref, None, ctypes.byref(out),
+                                              L.PREP_FACES | L.PREP_CELLS_FROM_FACES, ss), "phd_prepare_f32_parts")
+        ev[3].record(side)
+        nbytes += dm.copy_fields(pinned, ("tag", "type") if fp32 else ("dcom", "vol", "tag", "type"), main)
         dm.set_flip(main)
-        dm.set_normals("none" if self.precision == "fp32" else "device", main)
+        main.wait_event(ev[3])
         L.check(lib.phd_ghost_cons_f64(dm.ref, L.ptr(self.cons), s), "phd_ghost_cons_f64")
-        if self.precision == "fp32":
-            out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
-                                                            self.csr_nbr, self.cell_geo)))
-            L.check(lib.phd_prepare_f32(dm.ref, L.ptr(self.twin), ctypes.byref(out), s), "phd_prepare_f32")
-            L.check(lib.phd_prim_f32(dm.ref, ctypes.byref(p), L.ptr(self.cons), L.ptr(self.prim4),
-                                     self.clock.ptr, s), "phd_prim_f32")
+        if fp32:
+            L.check(lib.phd_prim_f32_cells(dm.ref, L.ptr(self.cell_geo), ctypes.byref(p), L.ptr(self.cons),
+                                           L.ptr(self.prim4), self.clock.ptr, s), "phd_prim_f32_cells")
         else:
+            dm.set_normals("device", main)
             L.check(lib.phd_prim_from_cons_f64(dm.dim, dm.n_cells, p.gamma, L.ptr(dm.vol), L.ptr(self.cons),
                                                L.ptr(self.prim), s), "phd_prim_from_cons_f64")
             self.initial_time_step()

@@ -144,3 +144,37 @@ def test_load_mesh_fp32_conserves_and_tracks_fp64():
     rho32 = cons[0] / m.vol[:m.n_real]
     rho64 = c[0, :m.n_real] / m.vol[:m.n_real]
     assert np.mean(np.abs(rho32 - rho64)) <= 1e-5
+
+
+def _geom32_buffers(n, F):
+    f32 = torch.float32
+    return [torch.zeros((F, 4), dtype=f32, device="cuda"), torch.zeros((F, 2), dtype=f32, device="cuda"),
+            torch.zeros(2 * F, dtype=torch.int32, device="cuda"), torch.zeros(2 * F, dtype=torch.int32, device="cuda"),
+            torch.zeros((n, 4), dtype=f32, device="cuda")]
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+def test_cell_geometry_from_faces_matches_host_volumes(boundary):
+    """PHD_PREP_CELLS_FROM_FACES (volume and centre-of-mass sums of tess.cpp:330-393 in
+    FP32 from the prepared faces) against the FP32 rounding of the host's FP64 volumes
+    and centroids."""
+    m = lattice_mesh(24, boundary, seed=4)
+    dm = DeviceMesh(m)
+    n, F = dm.n_cells, dm.n_faces
+    lib = L.lib()
+    twin = torch.as_tensor(periodic_twins(m)).cuda()
+    a, b = _geom32_buffers(n, F), _geom32_buffers(n, F)
+    oa = L.PhdGeom32Out(*(t.data_ptr() for t in a))
+    ob = L.PhdGeom32Out(*(t.data_ptr() for t in b))
+    s = L.stream_handle()
+    L.check(lib.phd_prepare_f32(dm.ref, L.ptr(twin), ctypes.byref(oa), s), "prepare")
+    L.check(lib.phd_prepare_f32_parts(dm.ref, L.ptr(twin), ctypes.byref(ob),
+                                      L.PREP_FACES | L.PREP_LISTS | L.PREP_CELLS_FROM_FACES, s), "prepare parts")
+    torch.cuda.synchronize()
+    ga, gb = a[4].double().cpu().numpy(), b[4].double().cpu().numpy()
+    dx = 1.0 / 24
+    assert np.max(np.abs(gb[:, 2] / ga[:, 2] - 1.0)) <= 2e-6          # 1/V
+    assert np.max(np.abs(gb[:, 3] / ga[:, 3] - 1.0)) <= 2e-6          # sqrt(V/pi)
+    assert np.max(np.abs(gb[:, :2] - ga[:, :2])) <= 1e-6 * dx          # dcom
+    for k in range(4):                                                 # faces and lists unchanged
+        assert torch.equal(a[k], b[k])
