@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--workload", default="shear", choices=["shear", "ensemble", "adjoint"])
+    ap.add_argument("--workload", default="shear", choices=["shear", "ensemble", "adjoint", "explosion"])
     ap.add_argument("--adj-steps", type=int, default=200, help="adjoint workload: recorded steps")
     ap.add_argument("--adj-dirs", type=int, default=16, help="adjoint workload: finite-difference directions")
     ap.add_argument("--runs", type=int, default=256)
@@ -358,7 +358,9 @@ def run_ours(args, rank, world):
                           "parallelism": "replicas" if world > 1 else "single GPU", "launch": launch_cfg},
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
                "adjoint": adjoint,
-               "gpu_launches": 3 * args.steps, "clocks": clocks}
+               # per step: FP32 k_grad32 (with the generator velocities), k_face32, k_update32;
+               # FP64 k_gen_vel, k_face_vel, k_gradients, k_face_flux, k_update_step
+               "gpu_launches": (3 if st.precision == "fp32" else 5) * args.steps, "clocks": clocks}
         print(json.dumps(out), flush=True)
 
 
@@ -591,6 +593,65 @@ def run_ensemble(args, rank, world):
         print(json.dumps(out), flush=True)
 
 
+def run_explosion(args, rank, world):
+    """The point-explosion workload: 256x256 jittered periodic box, rho = 1, p = 1e-5,
+    E = 1 deposited within two lattice spacings of the centre, gamma 1.4, run to
+    t = 0.05 (the clock clips the last step onto t_end) with HLLC and with the exact
+    solver, each in FP64 and in FP32 + FP64 accumulation (moving-mesh stage order, mesh
+    held fixed).  Reports each run's faces/s, the FP32 run's L1 density error against
+    the FP64 run (the FP64 path matches the reference to 1e-12, tests/) and both runs'
+    total-energy drift."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from phd_code_gb300.step import FluxStepper
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    mesh, prim, info = pkg.problems.point_explosion(256, seed=rank)
+    nr, F = mesh.n_real, mesh.n_faces
+    t_end, gamma = info["t_end"], info["gamma"]
+
+    def run(solver, precision, chunk):
+        st = FluxStepper(mesh, prim, gamma=gamma, cfl=0.5, solver=solver, moving=True, precision=precision,
+                         t_end=t_end, device=dev)
+        e0 = st.cons_host()[3, :nr].sum()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        steps, ms = 0, 0.0
+        while True:
+            ev[0].record()
+            st.step(chunk)
+            ev[1].record()
+            c = st.read_clock()                       # synchronises
+            ms += ev[0].elapsed_time(ev[1])
+            steps += chunk
+            if c.t >= t_end * (1.0 - 1e-12) or steps > 200000:
+                break
+        st.check_status()
+        cons = st.cons_host()[:, :nr]
+        return {"steps": steps, "t": c.t, "faces_per_s": F * steps / (ms * 1e-3),
+                "energy_drift": abs(cons[3].sum() - e0) / abs(e0), "rho": cons[0] / mesh.vol[:nr]}
+
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    out = {}
+    for solver in ("hllc", "exact"):
+        r64 = run(solver, "fp64", 10)
+        r32 = run(solver, "fp32", 25)
+        out[solver] = {"fp64": {k: v for k, v in r64.items() if k != "rho"},
+                       "fp32": {k: v for k, v in r32.items() if k != "rho"},
+                       "l1_density_fp32_vs_fp64": float(np.mean(np.abs(r32["rho"] - r64["rho"]))),
+                       "fp32_over_fp64_faces_per_s": r32["faces_per_s"] / r64["faces_per_s"]}
+    clocks = sampler.stop()
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": out["hllc"]["fp32"]["faces_per_s"], "unit": UNIT,
+                          "n_gpus": world, "steps": out["hllc"]["fp32"]["steps"], "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                          "config": {"workload": "point explosion 256x256 jittered periodic, E = 1, gamma 1.4, "
+                                                 "to t = 0.05", "cells": nr, "faces": F,
+                                     "mesh": "fixed across steps (face velocities from the moving-mesh stage)"},
+                          "runs": out, "clocks": clocks}), flush=True)
+
+
 def run_adjoint(args, rank, world):
     """The differentiation workload alone (one replica per rank): adjoint_cost's line
     with the backward/forward time ratio as the value."""
@@ -626,6 +687,8 @@ def main():
             run_ensemble(args, rank, world)
         elif args.workload == "adjoint":
             run_adjoint(args, rank, world)
+        elif args.workload == "explosion":
+            run_explosion(args, rank, world)
         else:
             run_ours(args, rank, world)
     finally:

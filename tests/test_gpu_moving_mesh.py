@@ -71,3 +71,51 @@ def test_moving_mesh_with_remesh_matches_oracle(boundary):
     n = meshes[-1].n_real
     assert rel_rows(gpu_cons[:, :n], c[:, :n]) <= FP64_TOL
     assert rel_rows(gpu_prim, p) <= FP64_TOL
+
+
+def test_shock_tube_full_run_to_t_end_matches_oracle():
+    """The shock-tube configuration in full: 100x100 jittered lattice, reflective box,
+    moving generators re-tessellated after every step, run to t = 0.1 (the last step
+    clipped onto t_end as Simulation.compute_time_step does).  The device plugin
+    integrator against the oracle replaying the same meshes.  Over the whole run the
+    normwise difference stays at round-off level (bound 1e-10: ~50 steps of
+    limiter-switching dynamics on top of the per-step 1e-12)."""
+    mesh, prim, info = pkg.problems.shock_tube(100, seed=3)
+    gamma, t_end = info["gamma"], info["t_end"]
+    meshes = [mesh]
+
+    def remesh(x_moved):
+        m, _ = pkg.meshgen.build_mesh(x_moved.copy(), "reflective", hilbert=False)
+        meshes.append(m)
+        return m
+
+    it = make_integrator(mesh, prim, gamma)
+    t, dts = 0.0, []
+    while t < t_end * (1.0 - 1e-14):
+        dt = it.compute_time_step()
+        if t + dt >= t_end:
+            dt = t_end - t
+        it.dt = dt
+        dts.append(dt)
+        it.evolve_timestep(remesh=remesh)
+        t += dt
+    assert 20 < len(dts) < 400
+    gpu_prim = it.particles.block("primitive").cpu().numpy()
+    gpu_cons = it.particles.block("conservative").cpu().numpy()
+
+    p = prim.copy()
+    c = O.cons_from_prim(mesh, p, gamma)
+    for k, dt in enumerate(dts):
+        mk = meshes[k]
+        dt_o = O.time_step(mk, p, gamma, 0.5, True)
+        if k < len(dts) - 1:
+            assert abs(dt_o - dt) <= 1e-10 * dt
+        O.OracleStepper(mk, gamma=gamma, solver="hllc", moving=True).step(dt, p, c)
+        nxt = meshes[k + 1]
+        c_new = np.zeros((4, nxt.n_cells))
+        c_new[:, :nxt.n_real] = c[:, :mk.n_real]
+        c = O.ghost_refresh_cons(nxt, c_new)
+        p = O.prim_from_cons(nxt, c, gamma)
+    n = meshes[-1].n_real
+    assert rel_rows(gpu_cons[:, :n], c[:, :n]) <= 1e-10
+    assert rel_rows(gpu_prim, p) <= 1e-10
