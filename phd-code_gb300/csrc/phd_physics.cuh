@@ -186,6 +186,44 @@ PHD_HD __forceinline__ double ex_get_pstar(double dl, double ul, double pl, doub
     return p_new;
 }
 
+// The same Newton iteration for the FP32 path (its pressure iteration stays in FP64):
+// on a rarefaction side the function and its derivative share one power,
+// (p/pk)^((-(g+1))/(2g)) = (p/pk)^((g-1)/(2g)) / (p/pk), so each side costs one pow per
+// iteration instead of two.  Results agree with ex_get_pstar to rounding.
+PHD_HD __forceinline__ void ex_side_lean(double d, double p, double c, double gamma, double p_old, double &f,
+                                         double &df) {
+    if (p_old <= p) {
+        const double q = p_old / p;
+        const double qz = pow(q, (gamma - 1.) / (2. * gamma));
+        f = ((2. * c) / (gamma - 1.)) * (qz - 1.);
+        df = (qz / q) / (c * d);
+    } else {
+        const double Ak = 2. / (d * (gamma + 1.));
+        const double Bk = (p * (gamma - 1.)) / (gamma + 1.);
+        const double s = sqrt(Ak / (p_old + Bk));
+        f = (p_old - p) * s;
+        df = s * (1. - ((.5 * (p_old - p)) / (Bk + p_old)));
+    }
+}
+
+PHD_HD __forceinline__ double ex_get_pstar_lean(double dl, double ul, double pl, double cl, double dr,
+                                                double ur, double pr, double cr, double gamma, int max_iter,
+                                                bool *failed) {
+    const double TOL = 1.0e-6;
+    double p_old = ex_p_guess(dl, ul, pl, cl, dr, ur, pr, cr, gamma), p_new = p_old;
+    for (int it = 0; it < max_iter; it++) {
+        double fl, fr, dfl, dfr;
+        ex_side_lean(dl, pl, cl, gamma, p_old, fl, dfl);
+        ex_side_lean(dr, pr, cr, gamma, p_old, fr, dfr);
+        p_new = p_old - ((((fl + fr) + ur) - ul) / (dfl + dfr));
+        if ((2. * fabs((p_new - p_old) / (p_new + p_old))) <= TOL) return p_new;
+        if (p_new < 0.) p_new = TOL;
+        p_old = p_new;
+    }
+    *failed = true;
+    return p_new;
+}
+
 // Exact.riemann_solver riemann.pyx:700-972: exact solution sampled at xi = 0 in the
 // face frame, then deboosted (the Exact solver always boosts, riemann.pyx:695-698).
 template <typename T, int DIM>
@@ -204,12 +242,24 @@ PHD_HD __forceinline__ void exact_flux(const T *L, const T *R, const T *n, const
         vr_sq = vr_sq + R[1 + k] * R[1 + k];
     }
     const double g = double(gamma);
-    const double p_star_d = ex_get_pstar(double(_dl), double(vnl), double(_pl), double(cl), double(_dr),
-                                         double(vnr), double(_pr), double(cr), g, max_iter, failed);
-    const double fl_d = ex_p_func(double(_dl), double(_pl), double(cl), g, p_star_d);
-    const double fr_d = ex_p_func(double(_dr), double(_pr), double(cr), g, p_star_d);
-    const T p_star = T(p_star_d);
-    const T u_star = T(0.5 * (((double(vnl) + double(vnr)) + fr_d) - fl_d));
+    T p_star, u_star;
+    if (sizeof(T) == sizeof(double)) {        // FP64 path: the reference's iteration verbatim
+        const double p_star_d = ex_get_pstar(double(_dl), double(vnl), double(_pl), double(cl), double(_dr),
+                                             double(vnr), double(_pr), double(cr), g, max_iter, failed);
+        const double fl_d = ex_p_func(double(_dl), double(_pl), double(cl), g, p_star_d);
+        const double fr_d = ex_p_func(double(_dr), double(_pr), double(cr), g, p_star_d);
+        p_star = T(p_star_d);
+        u_star = T(0.5 * (((double(vnl) + double(vnr)) + fr_d) - fl_d));
+    } else {                                  // FP32 path: FP64 Newton, one pow per side per step
+        const double p_star_d = ex_get_pstar_lean(double(_dl), double(vnl), double(_pl), double(cl),
+                                                  double(_dr), double(vnr), double(_pr), double(cr), g, max_iter,
+                                                  failed);
+        double fl_d, fr_d, dummy;
+        ex_side_lean(double(_dl), double(_pl), double(cl), g, p_star_d, fl_d, dummy);
+        ex_side_lean(double(_dr), double(_pr), double(cr), g, p_star_d, fr_d, dummy);
+        p_star = T(p_star_d);
+        u_star = T(0.5 * (((double(vnl) + double(vnr)) + fr_d) - fl_d));
+    }
     int kind;            // 0: left data, 1: right data, 2: sampled (d, p, velocity shift)
     T _d = T(0), _p = T(0), ushift = T(0);
     bool right_side = false;
