@@ -109,6 +109,15 @@ class DeviceMesh:
                 nbytes += pinned[nm].numel() * pinned[nm].element_size()
         return nbytes
 
+    def copy_ghost_map(self, pinned, stream=None):
+        """Copy only the ghost part of the image map: real cells keep their order (and
+        therefore their identity map, tags and types) across re-meshes, only the ghosts
+        are re-created.  Returns the bytes copied."""
+        src = pinned["map"][self.n_real:]
+        with (torch.cuda.stream(stream) if stream is not None else _nullctx()):
+            self.map[self.n_real:].copy_(src, non_blocking=True)
+        return src.numel() * src.element_size()
+
     def reset_errors(self, stream=None):
         lib = L.lib()
         with (torch.cuda.stream(stream) if stream is not None else _nullctx()):

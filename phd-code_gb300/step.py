@@ -96,7 +96,9 @@ class FluxStepper:
     def load_mesh(self, pinned):
         """Continue on a new tessellation handed over from pinned host buffers
         (``DeviceMesh.pinned_host`` layout; same cell and face counts, real cells in
-        the same order, as after the host re-mesh of ``integrate.py:410-417``).
+        the same order, as after the host re-mesh of ``integrate.py:410-417`` -- so the
+        real cells' tags, types and identity map do not change and only the ghost part
+        of the map is copied).
 
         The device forms the neighbour lists, flip bits and, for FP32, the periodic twin
         table and FP32 geometry (normals, cell volumes and centroids included, so FP32
@@ -127,7 +129,7 @@ class FluxStepper:
         ev[0].record(main)
         side.wait_event(ev[0])
         dm.build_lists(side)
-        nbytes += dm.copy_fields(pinned, ("x", "map"), main)
+        nbytes += dm.copy_fields(pinned, ("x",), main) + dm.copy_ghost_map(pinned, main)
         ev[1].record(main)
         if fp32:
             side.wait_event(ev[1])
@@ -147,7 +149,8 @@ class FluxStepper:
             L.check(lib.phd_prepare_f32_parts(dm.ref, None, ctypes.byref(out),
                                               L.PREP_FACES | L.PREP_CELLS_FROM_FACES, ss), "phd_prepare_f32_parts")
         ev[3].record(side)
-        nbytes += dm.copy_fields(pinned, ("tag", "type") if fp32 else ("dcom", "vol", "tag", "type"), main)
+        if not fp32:
+            nbytes += dm.copy_fields(pinned, ("dcom", "vol"), main)
         dm.set_flip(main)
         main.wait_event(ev[3])
         L.check(lib.phd_ghost_cons_f64(dm.ref, L.ptr(self.cons), s), "phd_ghost_cons_f64")
