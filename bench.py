@@ -122,6 +122,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def job_rate(units_local, ms_local, device=None):
+    """Whole-job throughput over the ranks of the current process group: the units all
+    ranks processed divided by the slowest rank's time (MAX over ranks).  Returns
+    (units per second, max ms).  One rank (or no process group): local values."""
+    import torch
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        t = torch.tensor([float(ms_local)], dtype=torch.float64, device=device)
+        u = torch.tensor([float(units_local)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        ms_max, units = float(t.item()), float(u.item())
+    else:
+        ms_max, units = float(ms_local), float(units_local)
+    return units / (ms_max * 1e-3), ms_max
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -303,11 +320,7 @@ def run_ours(args, rank, world):
         for q, nm in enumerate(names):
             per[nm] += marks[4 * k + q].elapsed_time(marks[4 * k + q + 1])
     per = {nm: v / args.steps for nm, v in per.items()}
-    t = torch.tensor([ms_total], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * F * args.steps / (ms_max * 1e-3)
+    value, ms_max = job_rate(F * args.steps, ms_total, device=dev)
 
     # roofline of the dominant kernel
     peak, peak_src = measured_peaks()
@@ -556,6 +569,8 @@ def run_ensemble(args, rank, world):
         ens.replay()
     steps = args.steps if args.steps % 2 == 0 else args.steps + 1
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        torch.distributed.barrier()
     torch.cuda.synchronize()
     sampler = ClockSampler(dev.index or 0)
     sampler.start()
@@ -565,9 +580,10 @@ def run_ensemble(args, rank, world):
     e1.record()
     torch.cuda.synchronize()
     clocks = sampler.stop()
+    if world > 1:
+        torch.distributed.barrier()
     ens.check_status()
-    ms = e0.elapsed_time(e1)
-    batched = ens.faces * steps / (ms * 1e-3)
+    batched, ms = job_rate(ens.faces * steps, e0.elapsed_time(e1), device=dev)
     seq = SequentialEnsemble(runs, device=dev)
     seq.step(2)
     q = min(steps, 20)
