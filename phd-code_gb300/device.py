@@ -86,6 +86,11 @@ class DeviceMesh:
         """Pinned host copies of a host mesh's per-step arrays (the face list and the
         cell geometry a host re-mesh writes, ``mesh.pyx:255-323``)."""
         host = self.host if host is None else host
+        nr = self.n_real
+        if (host.n_real != nr or not np.array_equal(host.map[:nr], np.arange(nr)) or
+                not np.array_equal(host.tag, self.host.tag) or not np.array_equal(host.type, self.host.type)):
+            raise ValueError("a re-mesh keeps the real cells (same count and order, identity map) and the "
+                             "tags / types of every row")
         return {nm: torch.from_numpy(np.ascontiguousarray(getattr(host, nm), dtype=dt)).pin_memory()
                 for nm, dt in self.UPLOAD}
 

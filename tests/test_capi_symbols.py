@@ -50,3 +50,29 @@ def test_host_only_calls(lib):
     lib.phd_status_string.restype = ctypes.c_char_p
     lib.phd_status_string.argtypes = [ctypes.c_int]
     assert lib.phd_status_string(1) == b"Mass less than zero in flux update"
+
+
+def test_argument_errors_are_rejected_on_the_host(lib):
+    """Entry points validate their arguments before touching the device: missing
+    pointers and malformed sizes return PHD_ERR_ARG (no GPU is needed to see that)."""
+    L = _lib
+    f = L.lib()                      # argtypes / restypes from the ctypes table
+    assert f.phd_step_f64(None, None, 0, None, None, None, None, None, None, None, None, None) == L.PHD_ERR_ARG
+    assert f.phd_gradients_f64(None, None, 0, None, None, None) == L.PHD_ERR_ARG
+    assert f.phd_build_csr(None, None, None, None, None, None) == L.PHD_ERR_ARG
+    assert f.phd_face_normals_f64(None, None, None, None) == L.PHD_ERR_ARG
+    assert f.phd_prepare_f32(None, None, None, None) == L.PHD_ERR_ARG
+    m = L.PhdMesh()
+    m.dim, m.n_cells, m.n_real, m.n_faces = 2, 10, 10, 5
+    # a mesh with faces but no normals is refused by the FP64 entries that read normals
+    one = ctypes.c_void_p(1)
+    assert f.phd_riemann_f64(ctypes.byref(m), L.HLLC, 1.4, 1, 100, one, one, None, one, one, None) == L.PHD_ERR_ARG
+    # launch shapes out of range, and several runs without a cell-to-run table
+    par = L.PhdParams()
+    geo = L.PhdGeom32()
+    for lch in (L.PhdLaunch(48, 128, 128, 0, 0, 0),       # not a multiple of 32
+                L.PhdLaunch(128, 512, 128, 0, 0, 0)):     # face kernel above its 384-thread bound
+        rc = f.phd_step_f32_batched(ctypes.byref(m), ctypes.byref(geo), ctypes.byref(par), 0, ctypes.byref(lch),
+                                    one, one, one, one, one, one, one, 1, None, None, None)
+        assert rc == L.PHD_ERR_ARG
+    assert f.phd_prim_f32_batched(ctypes.byref(m), ctypes.byref(par), one, one, one, 3, None, None) == L.PHD_ERR_ARG

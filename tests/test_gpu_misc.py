@@ -94,3 +94,38 @@ def test_out_of_range_face_id_is_rejected_not_read():
     st = pkg.FluxStepper(m2, smooth_state(m), solver="hllc")
     st.step(1)
     assert st.read_clock().status & L.STATUS_BAD_INDEX
+
+
+def test_mesh_without_faces():
+    """Empty face list: every entry point returns PHD_OK without launching over faces;
+    gradients of isolated cells are zero and the neighbour lists are empty."""
+    lib = L.lib()
+    s = L.stream_handle()
+    n = 5
+    x = torch.tensor(np.random.default_rng(0).uniform(0, 1, (2, n)), device="cuda")
+    dcom = torch.zeros((2, n), dtype=torch.float64, device="cuda")
+    vol = torch.full((n,), 0.2, dtype=torch.float64, device="cuda")
+    tag = torch.zeros(n, dtype=torch.int8, device="cuda")
+    mp = torch.arange(n, dtype=torch.int32, device="cuda")
+    flip = torch.zeros(n, dtype=torch.int8, device="cuda")
+    ptr = torch.full((n + 1,), 9, dtype=torch.int32, device="cuda")
+    idx = torch.zeros(1, dtype=torch.int32, device="cuda")
+    m = L.PhdMesh()
+    m.dim, m.n_cells, m.n_real, m.n_faces = 2, n, n, 0
+    for name, t in (("tag", tag), ("map", mp), ("flip", flip), ("x", x), ("dcom", dcom), ("vol", vol),
+                    ("nbr_ptr", ptr), ("nbr_idx", idx)):
+        setattr(m, name, t.data_ptr())
+    work = torch.empty(int(lib.phd_csr_work_ints(n)), dtype=torch.int32, device="cuda")
+    L.check(lib.phd_build_csr(ctypes.byref(m), L.ptr(ptr), L.ptr(idx), L.ptr(work), None, s), "csr")
+    prim = torch.tensor(np.random.default_rng(1).uniform(0.5, 1.5, (4, n)), device="cuda")
+    grad = torch.full((8, n), 7.0, dtype=torch.float64, device="cuda")
+    clk = DeviceClock("cuda", dt=1e-3)
+    L.check(lib.phd_gradients_f64(ctypes.byref(m), L.ptr(prim), L.LIMITER_AREPO, L.ptr(grad), clk.ptr, s), "grad")
+    left = torch.zeros((4, 1), dtype=torch.float64, device="cuda")
+    flux = torch.zeros((4, 1), dtype=torch.float64, device="cuda")
+    L.check(lib.phd_riemann_f64(ctypes.byref(m), L.HLLC, 1.4, 1, 100, L.ptr(left), L.ptr(left), None, L.ptr(flux),
+                                clk.ptr, s), "riemann")
+    torch.cuda.synchronize()
+    assert np.array_equal(ptr.cpu().numpy(), np.zeros(n + 1, dtype=np.int32))
+    assert float(grad.abs().max()) == 0.0
+    assert clk.read().status == 0
