@@ -305,6 +305,7 @@ __global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int mo
 // HLLC left / right star branches merged into one (selects instead of divergence).
 struct GasC {
     float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1;
+    ExGas64 X;                 // the exact solver's FP64 Newton constants
 };
 
 inline GasC gas_consts(double gamma) {
@@ -318,6 +319,7 @@ inline GasC gas_consts(double gamma) {
     c.inv_z = 1.f / c.z;
     c.two_gp1 = 2.f / (g + 1.f);
     c.gm1_gp1 = (g - 1.f) / (g + 1.f);
+    c.X = ex_gas64(gamma);
     return c;
 }
 
@@ -470,7 +472,7 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
     }
     float f[4];
     bool failed = false;
-    if (SOLVER == PHD_EXACT) exact_flux<float, 2>(L, R, nrm, w, gamma, P.exact_max_iter, f, &failed);
+    if (SOLVER == PHD_EXACT) exact_flux<float, 2>(L, R, nrm, w, gamma, P.exact_max_iter, f, &failed, &GC.X);
     else hll_family32(SOLVER == PHD_HLLC, L, R, nrm, w, GC, boost, f);
     if (failed) set_status32(clk, PHD_STATUS_RIEMANN_NONCONVERGED);
     // the face's conserved increment dt*A*F (mesh.pyx:519-544), formed once here so both
@@ -481,18 +483,20 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
 
 // At most 384 threads per block and at least 3 blocks per SM: 56 registers per thread,
 // which lets more warps hide the face kernel's gather latency (measured faster than the
-// 61-register build at 512 threads).
+// 61-register build at 512 threads).  The exact solver's kernel is bound by the FP64
+// pipe instead, and at 56 registers its FP64 Newton iteration spills; it takes one block
+// per SM as its minimum (118-138 registers, no spills; measured 4% faster).
 constexpr int FACE_MAX_BLOCK = 384;
 
 template <int SOLVER, bool LINEAR>
-__global__ void __launch_bounds__(FACE_MAX_BLOCK, 3) k_face32(phd_mesh M, phd_params P, int moving,
+__global__ void __launch_bounds__(FACE_MAX_BLOCK, SOLVER == PHD_EXACT ? 1 : 3) k_face32(phd_mesh M, phd_params P, int moving,
                                                 const float4 *__restrict__ face_geo,
                                                 const float2 *__restrict__ face_ar,
                                                 const float4 *__restrict__ cell_geo,
                                                 const float4 *__restrict__ prim4,
                                                 const float4 *__restrict__ grad8, const float2 *__restrict__ w2,
                                                 float4 *__restrict__ flux4, phd_clock *clocks,
-                                                const int32_t *__restrict__ cell_run, const GasC GC) {
+                                                const int32_t *__restrict__ cell_run, const __grid_constant__ GasC GC) {
     for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M.n_faces; m += gridDim.x * blockDim.x)
         face32_face<SOLVER, LINEAR>(m, M, P, moving, face_geo, face_ar, cell_geo, prim4, grad8, w2, flux4, clocks,
                                     cell_run, GC);

@@ -186,49 +186,132 @@ PHD_HD __forceinline__ double ex_get_pstar(double dl, double ul, double pl, doub
     return p_new;
 }
 
-// The same Newton iteration for the FP32 path (its pressure iteration stays in FP64):
-// on a rarefaction side the function and its derivative share one power,
-// (p/pk)^((-(g+1))/(2g)) = (p/pk)^((g-1)/(2g)) / (p/pk), so each side costs one pow per
-// iteration instead of two.  Results agree with ex_get_pstar to rounding.
-PHD_HD __forceinline__ void ex_side_lean(double d, double p, double c, double gamma, double p_old, double &f,
-                                         double &df) {
-    if (p_old <= p) {
-        const double q = p_old / p;
-        const double qz = pow(q, (gamma - 1.) / (2. * gamma));
-        f = ((2. * c) / (gamma - 1.)) * (qz - 1.);
-        df = (qz / q) / (c * d);
+// The same Newton iteration for the FP32 path (its pressure iteration stays in FP64),
+// arranged for GB300's narrow FP64 pipe, where each pow, division and square root is a
+// long instruction sequence:
+//  * gamma-only constants (2/(g-1), 2/(g+1), (g-1)/(g+1), z = (g-1)/(2g)) come from
+//    the host (ExGas64);
+//  * on a rarefaction side the function and its derivative share one power,
+//    (p/p_K)^((-(g+1))/(2g)) = (p/p_K)^z * (p_K/p);
+//  * (1 + d)^z for |d| <= 1/64 is the binomial series sum_{k=0..8} C(z,k) d^k: for
+//    0 < z < 1, |C(z,k)| <= z/k, so the dropped tail is below (1/9)(1/64)^9 / (1 - 1/64)
+//    < 1e-17 relative -- FP64 rounding level;
+//  * each side keeps the reciprocal of the last pressure it evaluated and that power;
+//    the next evaluation multiplies the power by (p_new/p_old)^z when the ratio is
+//    within 1/64 of 1 (every Newton step once the iteration has settled, and the final
+//    evaluation at p*), so a side whose ratio p/p_K stays far from 1 costs one pow for
+//    the whole iteration;
+//  * one reciprocal of the iterate per Newton step serves both sides; the shock side
+//    shares 1/(p + B_K) between its function and derivative; the convergence test
+//    2|dp|/(p_new + p_old) <= TOL is evaluated as 2|dp| <= TOL |p_new + p_old|.
+// Results agree with ex_get_pstar to FP64 rounding (iteration counts can differ by one
+// only where the relative change sits within rounding of TOL).
+struct ExGas64 {
+    double two_gm1, two_gp1, gm1_gp1, z;
+    double c[9];              // C(z, k), k = 0..8
+};
+
+inline ExGas64 ex_gas64(double gamma) {
+    ExGas64 X;
+    X.two_gm1 = 2. / (gamma - 1.);
+    X.two_gp1 = 2. / (gamma + 1.);
+    X.gm1_gp1 = (gamma - 1.) / (gamma + 1.);
+    X.z = (gamma - 1.) / (2. * gamma);
+    X.c[0] = 1.;
+    for (int k = 1; k < 9; k++) X.c[k] = X.c[k - 1] * (X.z - double(k - 1)) / double(k);
+    return X;
+}
+
+constexpr double EX_NEAR_ONE = 0.015625;
+
+// (1 + d)^z, |d| <= 1/64
+PHD_HD __forceinline__ double ex_pow_near_one(const ExGas64 &X, double d) {
+    double s = X.c[8];
+#pragma unroll
+    for (int k = 7; k >= 0; k--) s = fma(s, d, X.c[k]);
+    return s;
+}
+
+struct ExSide {
+    double d, p, c, Bk;
+    double inv_cd, Ak;        // 1/(c d), 2/(d (g+1)); 0 until first needed
+    double inv_ref, qz_ref;   // 1/p and (p/p_K)^z of the last rarefaction evaluation (inv_ref 0: none)
+};
+
+PHD_HD __forceinline__ double ex_side_power(ExSide &S, const ExGas64 &X, double p_old) {
+    const double r = fma(p_old, S.inv_ref, -1.);
+    double qz;
+    if (fabs(r) <= EX_NEAR_ONE) {
+        qz = S.qz_ref * ex_pow_near_one(X, r);
     } else {
-        const double Ak = 2. / (d * (gamma + 1.));
-        const double Bk = (p * (gamma - 1.)) / (gamma + 1.);
-        const double s = sqrt(Ak / (p_old + Bk));
-        f = (p_old - p) * s;
-        df = s * (1. - ((.5 * (p_old - p)) / (Bk + p_old)));
+        const double q = p_old / S.p;
+        qz = (fabs(q - 1.) <= EX_NEAR_ONE) ? ex_pow_near_one(X, q - 1.) : pow(q, X.z);
+    }
+    return qz;
+}
+
+// f_K(p_old) and f_K'(p_old) of ex_p_func / ex_p_func_deriv; inv_pold = 1 / p_old
+PHD_HD __forceinline__ void ex_side_eval(ExSide &S, const ExGas64 &X, double p_old, double inv_pold, double &f,
+                                         double &df) {
+    if (p_old <= S.p) {
+        const double qz = ex_side_power(S, X, p_old);
+        S.inv_ref = inv_pold;
+        S.qz_ref = qz;
+        if (S.inv_cd == 0.) S.inv_cd = 1. / (S.c * S.d);
+        f = (S.c * X.two_gm1) * (qz - 1.);
+        df = (qz * (S.p * inv_pold)) * S.inv_cd;
+    } else {
+        if (S.Ak == 0.) S.Ak = X.two_gp1 / S.d;
+        const double u = 1. / (p_old + S.Bk);
+        const double s = sqrt(S.Ak * u);
+        f = (p_old - S.p) * s;
+        df = s * (1. - (.5 * (p_old - S.p)) * u);
     }
 }
 
+// f_K(p) alone (the final evaluation at p*)
+PHD_HD __forceinline__ double ex_side_f(ExSide &S, const ExGas64 &X, double p) {
+    if (p <= S.p) return (S.c * X.two_gm1) * (ex_side_power(S, X, p) - 1.);
+    if (S.Ak == 0.) S.Ak = X.two_gp1 / S.d;
+    return (p - S.p) * sqrt(S.Ak / (p + S.Bk));
+}
+
+// p* of ex_get_pstar, and the two side functions at p* (for u*).
 PHD_HD __forceinline__ double ex_get_pstar_lean(double dl, double ul, double pl, double cl, double dr,
-                                                double ur, double pr, double cr, double gamma, int max_iter,
-                                                bool *failed) {
+                                                double ur, double pr, double cr, double gamma,
+                                                const ExGas64 &X, int max_iter, bool *failed, double &fl_star,
+                                                double &fr_star) {
     const double TOL = 1.0e-6;
+    ExSide Ls{dl, pl, cl, pl * X.gm1_gp1, 0., 0., 0., 0.};
+    ExSide Rs{dr, pr, cr, pr * X.gm1_gp1, 0., 0., 0., 0.};
     double p_old = ex_p_guess(dl, ul, pl, cl, dr, ur, pr, cr, gamma), p_new = p_old;
     for (int it = 0; it < max_iter; it++) {
         double fl, fr, dfl, dfr;
-        ex_side_lean(dl, pl, cl, gamma, p_old, fl, dfl);
-        ex_side_lean(dr, pr, cr, gamma, p_old, fr, dfr);
+        const double inv_pold = (p_old <= pl || p_old <= pr) ? 1. / p_old : 0.;
+        ex_side_eval(Ls, X, p_old, inv_pold, fl, dfl);
+        ex_side_eval(Rs, X, p_old, inv_pold, fr, dfr);
         p_new = p_old - ((((fl + fr) + ur) - ul) / (dfl + dfr));
-        if ((2. * fabs((p_new - p_old) / (p_new + p_old))) <= TOL) return p_new;
+        const double sum = p_new + p_old;
+        if (2. * fabs(p_new - p_old) <= TOL * fabs(sum) && sum != 0.) {
+            fl_star = ex_side_f(Ls, X, p_new);
+            fr_star = ex_side_f(Rs, X, p_new);
+            return p_new;
+        }
         if (p_new < 0.) p_new = TOL;
         p_old = p_new;
     }
     *failed = true;
+    fl_star = ex_side_f(Ls, X, p_new);
+    fr_star = ex_side_f(Rs, X, p_new);
     return p_new;
 }
 
 // Exact.riemann_solver riemann.pyx:700-972: exact solution sampled at xi = 0 in the
 // face frame, then deboosted (the Exact solver always boosts, riemann.pyx:695-698).
+// X: the FP32 path's gamma constants (unused by the FP64 path).
 template <typename T, int DIM>
 PHD_HD __forceinline__ void exact_flux(const T *L, const T *R, const T *n, const T *w, T gamma,
-                                           int max_iter, T *f, bool *failed) {
+                                           int max_iter, T *f, bool *failed, const ExGas64 *X = nullptr) {
     const int E = DIM + 1;
     const T _dl = L[0], _pl = L[E], _dr = R[0], _pr = R[E];
     const T cl = t_sqrt((gamma * _pl) / _dl);
@@ -243,20 +326,18 @@ PHD_HD __forceinline__ void exact_flux(const T *L, const T *R, const T *n, const
     }
     const double g = double(gamma);
     T p_star, u_star;
-    if (sizeof(T) == sizeof(double)) {        // FP64 path: the reference's iteration verbatim
+    if constexpr (sizeof(T) == sizeof(double)) {   // FP64 path: the reference's iteration verbatim
         const double p_star_d = ex_get_pstar(double(_dl), double(vnl), double(_pl), double(cl), double(_dr),
                                              double(vnr), double(_pr), double(cr), g, max_iter, failed);
         const double fl_d = ex_p_func(double(_dl), double(_pl), double(cl), g, p_star_d);
         const double fr_d = ex_p_func(double(_dr), double(_pr), double(cr), g, p_star_d);
         p_star = T(p_star_d);
         u_star = T(0.5 * (((double(vnl) + double(vnr)) + fr_d) - fl_d));
-    } else {                                  // FP32 path: FP64 Newton, one pow per side per step
+    } else {                                  // FP32 path: FP64 Newton, powers reused across steps
+        double fl_d, fr_d;
         const double p_star_d = ex_get_pstar_lean(double(_dl), double(vnl), double(_pl), double(cl),
-                                                  double(_dr), double(vnr), double(_pr), double(cr), g, max_iter,
-                                                  failed);
-        double fl_d, fr_d, dummy;
-        ex_side_lean(double(_dl), double(_pl), double(cl), g, p_star_d, fl_d, dummy);
-        ex_side_lean(double(_dr), double(_pr), double(cr), g, p_star_d, fr_d, dummy);
+                                                  double(_dr), double(vnr), double(_pr), double(cr), g, *X,
+                                                  max_iter, failed, fl_d, fr_d);
         p_star = T(p_star_d);
         u_star = T(0.5 * (((double(vnl) + double(vnr)) + fr_d) - fl_d));
     }
