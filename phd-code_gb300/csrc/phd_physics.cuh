@@ -188,26 +188,34 @@ PHD_HD __forceinline__ double ex_get_pstar(double dl, double ul, double pl, doub
 
 // The same Newton iteration for the FP32 path (its pressure iteration stays in FP64),
 // arranged for GB300's narrow FP64 pipe, where each pow, division and square root is a
-// long instruction sequence:
-//  * gamma-only constants (2/(g-1), 2/(g+1), (g-1)/(g+1), z = (g-1)/(2g)) come from
-//    the host (ExGas64);
-//  * on a rarefaction side the function and its derivative share one power,
-//    (p/p_K)^((-(g+1))/(2g)) = (p/p_K)^z * (p_K/p);
+// long instruction sequence.  On the face states of smooth and shocked flows alike,
+// 99% of faces converge after one Newton step, so the initial guess and the final
+// evaluation at p* cost as much as the iteration itself; all three are trimmed:
+//  * gamma-only constants (2/(g-1), 2/(g+1), (g-1)/(g+1), (g-1)/2, z = (g-1)/(2g),
+//    1/z) come from the host (ExGas64);
 //  * (1 + d)^z for |d| <= 1/64 is the binomial series sum_{k=0..8} C(z,k) d^k: for
 //    0 < z < 1, |C(z,k)| <= z/k, so the dropped tail is below (1/9)(1/64)^9 / (1 - 1/64)
 //    < 1e-17 relative -- FP64 rounding level;
-//  * each side keeps the reciprocal of the last pressure it evaluated and that power;
-//    the next evaluation multiplies the power by (p_new/p_old)^z when the ratio is
-//    within 1/64 of 1 (every Newton step once the iteration has settled, and the final
-//    evaluation at p*), so a side whose ratio p/p_K stays far from 1 costs one pow for
-//    the whole iteration;
-//  * one reciprocal of the iterate per Newton step serves both sides; the shock side
-//    shares 1/(p + B_K) between its function and derivative; the convergence test
+//  * b^(1/z) in the two-rarefaction guess is a product of squarings when 1/z =
+//    2g/(g-1) is an integer (5 for g = 5/3, 7 for g = 1.4), else pow;
+//  * on a rarefaction side the function and its derivative share one power,
+//    (p/p_K)^((-(g+1))/(2g)) = (p/p_K)^z * (p_K/p), and each side keeps the reciprocal
+//    of the last pressure it evaluated with that power: the next evaluation multiplies
+//    the power by (p_new/p_old)^z (series) when the ratio is within 1/64 of 1;
+//  * on a shock side s(p) = sqrt(A_K/(p + B_K)) takes one division and gives
+//    1/(p + B_K) = s^2 d (g+1)/2 without a second one; the final evaluation at p*
+//    continues from the last Newton point, s(p*) = s(p_old) (1 + e)^(-1/2),
+//    e = (p* - p_old)/(p_old + B_K), by its binomial series (six terms for
+//    |e| <= 2^-12: tail below 1e-19);
+//  * one reciprocal of the iterate per Newton step serves both sides, the shock-branch
+//    guess takes one division and one square root per side, and the convergence test
 //    2|dp|/(p_new + p_old) <= TOL is evaluated as 2|dp| <= TOL |p_new + p_old|.
-// Results agree with ex_get_pstar to FP64 rounding (iteration counts can differ by one
-// only where the relative change sits within rounding of TOL).
+// Results agree with ex_get_pstar to FP64 rounding of the guess (the converged p*
+// within 1e-12 relative; iteration counts can differ by one only where the relative
+// change sits within rounding of TOL).
 struct ExGas64 {
-    double two_gm1, two_gp1, gm1_gp1, z;
+    double two_gm1, two_gp1, gm1_gp1, gm1_2, gp1_2, z, inv_z;
+    int n_inv_z;              // 1/z when it is an integer in [1, 64], else 0
     double c[9];              // C(z, k), k = 0..8
 };
 
@@ -216,7 +224,13 @@ inline ExGas64 ex_gas64(double gamma) {
     X.two_gm1 = 2. / (gamma - 1.);
     X.two_gp1 = 2. / (gamma + 1.);
     X.gm1_gp1 = (gamma - 1.) / (gamma + 1.);
+    X.gm1_2 = .5 * (gamma - 1.);
+    X.gp1_2 = .5 * (gamma + 1.);
     X.z = (gamma - 1.) / (2. * gamma);
+    X.inv_z = (2. * gamma) / (gamma - 1.);
+    const double r = X.inv_z + 0.5;
+    const int n = (r >= 1. && r < 65.) ? int(r) : 0;
+    X.n_inv_z = (n > 0 && fabs(X.inv_z - double(n)) <= 1e-12 * X.inv_z) ? n : 0;
     X.c[0] = 1.;
     for (int k = 1; k < 9; k++) X.c[k] = X.c[k - 1] * (X.z - double(k - 1)) / double(k);
     return X;
@@ -232,22 +246,62 @@ PHD_HD __forceinline__ double ex_pow_near_one(const ExGas64 &X, double d) {
     return s;
 }
 
+// q^z: the series near 1, else pow
+PHD_HD __forceinline__ double ex_pow_z(const ExGas64 &X, double q) {
+    return (fabs(q - 1.) <= EX_NEAR_ONE) ? ex_pow_near_one(X, q - 1.) : pow(q, X.z);
+}
+
+// b^(1/z): squarings for an integer exponent, else pow
+PHD_HD __forceinline__ double ex_pow_inv_z(const ExGas64 &X, double b) {
+    int n = X.n_inv_z;
+    if (n == 0) return pow(b, X.inv_z);
+    double r = 1., x = b;
+    while (n) {
+        if (n & 1) r *= x;
+        n >>= 1;
+        if (n) x *= x;
+    }
+    return r;
+}
+
+// (1 + e)^(-1/2), |e| <= 2^-12
+PHD_HD __forceinline__ double ex_rsqrt_near_one(double e) {
+    return fma(fma(fma(fma(fma(-63. / 256., e, 35. / 128.), e, -5. / 16.), e, 3. / 8.), e, -.5), e, 1.);
+}
+
+// ex_p_guess with the gamma constants of X: PVRS, then the two-rarefaction (TRRS) or
+// two-shock (TSRS) estimate (riemann.pyx p_guess, Toro 9.4.1-9.4.3).
+PHD_HD __forceinline__ double ex_p_guess_lean(double dl, double ul, double pl, double cl, double dr, double ur,
+                                              double pr, double cr, const ExGas64 &X) {
+    const double ppv = (.5 * (pl + pr)) - (((.125 * (ur - ul)) * (dl + dr)) * (cl + cr));
+    const double p_max = (pr > pl) ? pr : pl;
+    const double p_min = (pr < pl) ? pr : pl;
+    if ((p_max <= 2. * p_min) && (p_min <= ppv && ppv <= p_max)) return ppv;
+    if (ppv <= p_min) {
+        const double inv_cl = 1. / cl, inv_cr = 1. / cr;
+        const double p_lr = ex_pow_z(X, pl / pr);
+        const double u_star = (((p_lr * ul) * inv_cl + ur * inv_cr) + X.two_gm1 * (p_lr - 1.)) /
+                              (p_lr * inv_cl + inv_cr);
+        const double p_tl = ex_pow_inv_z(X, 1. + (X.gm1_2 * (ul - u_star)) * inv_cl);
+        const double p_tr = ex_pow_inv_z(X, 1. + (X.gm1_2 * (u_star - ur)) * inv_cr);
+        return .5 * ((pl * p_tl) + (pr * p_tr));
+    }
+    const double gl = sqrt(X.two_gp1 / (dl * (X.gm1_gp1 * pl + ppv)));
+    const double gr = sqrt(X.two_gp1 / (dr * (X.gm1_gp1 * pr + ppv)));
+    return (((gl * pl) + (gr * pr)) - (ur - ul)) / (gr + gl);
+}
+
 struct ExSide {
     double d, p, c, Bk;
-    double inv_cd, Ak;        // 1/(c d), 2/(d (g+1)); 0 until first needed
+    double inv_cd;            // 1/(c d); 0 until first needed
     double inv_ref, qz_ref;   // 1/p and (p/p_K)^z of the last rarefaction evaluation (inv_ref 0: none)
+    double ps_ref, s_ref, u_ref;  // p, s(p) and 1/(p + B_K) of the last shock evaluation (s_ref 0: none)
 };
 
 PHD_HD __forceinline__ double ex_side_power(ExSide &S, const ExGas64 &X, double p_old) {
     const double r = fma(p_old, S.inv_ref, -1.);
-    double qz;
-    if (fabs(r) <= EX_NEAR_ONE) {
-        qz = S.qz_ref * ex_pow_near_one(X, r);
-    } else {
-        const double q = p_old / S.p;
-        qz = (fabs(q - 1.) <= EX_NEAR_ONE) ? ex_pow_near_one(X, q - 1.) : pow(q, X.z);
-    }
-    return qz;
+    if (fabs(r) <= EX_NEAR_ONE) return S.qz_ref * ex_pow_near_one(X, r);
+    return ex_pow_z(X, p_old / S.p);
 }
 
 // f_K(p_old) and f_K'(p_old) of ex_p_func / ex_p_func_deriv; inv_pold = 1 / p_old
@@ -261,9 +315,11 @@ PHD_HD __forceinline__ void ex_side_eval(ExSide &S, const ExGas64 &X, double p_o
         f = (S.c * X.two_gm1) * (qz - 1.);
         df = (qz * (S.p * inv_pold)) * S.inv_cd;
     } else {
-        if (S.Ak == 0.) S.Ak = X.two_gp1 / S.d;
-        const double u = 1. / (p_old + S.Bk);
-        const double s = sqrt(S.Ak * u);
+        const double s = sqrt(X.two_gp1 / (S.d * (p_old + S.Bk)));
+        const double u = ((s * s) * S.d) * X.gp1_2;         // 1/(p_old + B_K)
+        S.ps_ref = p_old;
+        S.s_ref = s;
+        S.u_ref = u;
         f = (p_old - S.p) * s;
         df = s * (1. - (.5 * (p_old - S.p)) * u);
     }
@@ -272,19 +328,19 @@ PHD_HD __forceinline__ void ex_side_eval(ExSide &S, const ExGas64 &X, double p_o
 // f_K(p) alone (the final evaluation at p*)
 PHD_HD __forceinline__ double ex_side_f(ExSide &S, const ExGas64 &X, double p) {
     if (p <= S.p) return (S.c * X.two_gm1) * (ex_side_power(S, X, p) - 1.);
-    if (S.Ak == 0.) S.Ak = X.two_gp1 / S.d;
-    return (p - S.p) * sqrt(S.Ak / (p + S.Bk));
+    const double e = (p - S.ps_ref) * S.u_ref;
+    if (S.s_ref != 0. && fabs(e) <= 0.000244140625) return (p - S.p) * (S.s_ref * ex_rsqrt_near_one(e));
+    return (p - S.p) * sqrt(X.two_gp1 / (S.d * (p + S.Bk)));
 }
 
 // p* of ex_get_pstar, and the two side functions at p* (for u*).
 PHD_HD __forceinline__ double ex_get_pstar_lean(double dl, double ul, double pl, double cl, double dr,
-                                                double ur, double pr, double cr, double gamma,
-                                                const ExGas64 &X, int max_iter, bool *failed, double &fl_star,
-                                                double &fr_star) {
+                                                double ur, double pr, double cr, const ExGas64 &X, int max_iter,
+                                                bool *failed, double &fl_star, double &fr_star) {
     const double TOL = 1.0e-6;
-    ExSide Ls{dl, pl, cl, pl * X.gm1_gp1, 0., 0., 0., 0.};
-    ExSide Rs{dr, pr, cr, pr * X.gm1_gp1, 0., 0., 0., 0.};
-    double p_old = ex_p_guess(dl, ul, pl, cl, dr, ur, pr, cr, gamma), p_new = p_old;
+    ExSide Ls{dl, pl, cl, pl * X.gm1_gp1, 0., 0., 0., 0., 0., 0.};
+    ExSide Rs{dr, pr, cr, pr * X.gm1_gp1, 0., 0., 0., 0., 0., 0.};
+    double p_old = ex_p_guess_lean(dl, ul, pl, cl, dr, ur, pr, cr, X), p_new = p_old;
     for (int it = 0; it < max_iter; it++) {
         double fl, fr, dfl, dfr;
         const double inv_pold = (p_old <= pl || p_old <= pr) ? 1. / p_old : 0.;
@@ -336,8 +392,8 @@ PHD_HD __forceinline__ void exact_flux(const T *L, const T *R, const T *n, const
     } else {                                  // FP32 path: FP64 Newton, powers reused across steps
         double fl_d, fr_d;
         const double p_star_d = ex_get_pstar_lean(double(_dl), double(vnl), double(_pl), double(cl),
-                                                  double(_dr), double(vnr), double(_pr), double(cr), g, *X,
-                                                  max_iter, failed, fl_d, fr_d);
+                                                  double(_dr), double(vnr), double(_pr), double(cr), *X, max_iter,
+                                                  failed, fl_d, fr_d);
         p_star = T(p_star_d);
         u_star = T(0.5 * (((double(vnl) + double(vnr)) + fr_d) - fl_d));
     }

@@ -30,6 +30,7 @@ def test_lean_newton_matches_reference_iteration(tmp_path):
     out = subprocess.run([exe, "200000"], check=True, capture_output=True, text=True).stdout.split()
     n, n_fail, n_flag = int(out[0]), int(out[1]), int(out[2])
     worst_p, worst_u = float(out[3]), float(out[4])
+    assert (int(out[5]), int(out[6])) == (7, 5)
     assert n > 150000
     assert n_flag == 0
     assert n_fail < 0.02 * n
