@@ -11,6 +11,10 @@ shared library exporting the C ABI of ``include/phdflux.h``:
 * ``phd_adj.cu``  hand-written adjoint of the FP64 step, ``--fmad=false`` so its
   recomputed forward branches are those of the forward kernels.
 
+The host tessellation ``phd_tess2d.cpp`` (C ABI of ``include/phdtess.h``) is a plain
+C++ library, ``libphdtess.so``, built with the host compiler and
+``-ffp-contract=off`` (its robust predicates assume separately rounded products).
+
 Usage: ``python phd-code_gb300/build.py`` (or ``__graft_entry__.build()``).
 """
 import os
@@ -33,6 +37,32 @@ UNITS = {
     "phd_util.cu": [],
     "phd_adj.cu": ["--fmad=false"],
 }
+
+
+TESS_SRC = os.path.join(CSRC, "phd_tess2d.cpp")
+TESS_LIB = os.path.join(HERE, "libphdtess.so")
+
+
+def cxx():
+    for c in (os.environ.get("CXX"), "g++", "c++"):
+        if c:
+            return c
+    return "g++"
+
+
+def build_tess(force=False):
+    """Compile the host tessellation library (seconds)."""
+    hdr = os.path.join(INCLUDE, "phdtess.h")
+    if (not force and os.path.exists(TESS_LIB) and
+            os.path.getmtime(TESS_LIB) >= max(os.path.getmtime(TESS_SRC), os.path.getmtime(hdr))):
+        return TESS_LIB
+    cmd = [cxx(), "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I" + INCLUDE,
+           TESS_SRC, "-o", TESS_LIB + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("host compile failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(TESS_LIB + ".tmp", TESS_LIB)
+    return TESS_LIB
 
 
 def nvcc():
@@ -69,8 +99,10 @@ def build(force=False, verbose=False, extra=()):
             os.replace(obj + ".tmp", obj)
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(units)) as ex:
+    with ThreadPoolExecutor(max_workers=len(units) + 1) as ex:
+        tess = ex.submit(build_tess, force)
         objs = list(ex.map(compile_one, units))
+        tess.result()
     if force or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-lcudart"]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -1,0 +1,777 @@
+// phd_tess2d.cpp -- host 2D Delaunay / Voronoi tessellation (libphdtess.so).
+//
+// The reference tessellates on the host with CGAL (phd/mesh/tess.cpp, an exact-
+// predicates Delaunay_triangulation_2) and hands the flux path a face list.  CGAL is
+// not part of this build, so this file provides the same service from scratch:
+//
+//  * Delaunay triangulation by Bowyer-Watson insertion (cavity of triangles whose
+//    circumcircle strictly contains the new point, re-triangulated as a fan), inside
+//    a large enclosing triangle, with points inserted along a Hilbert curve so that
+//    the visibility walk that locates each point stays short;
+//  * robust orientation and in-circle tests: a floating-point evaluation with the
+//    forward error bounds of Shewchuk (1997, "Adaptive precision floating-point
+//    arithmetic and fast robust geometric predicates", ccwerrboundA / iccerrboundA),
+//    and, when the sign is not certain, an exact evaluation with the paper's
+//    expansion arithmetic (Two-Sum, Two-Product via fma, Grow-Expansion,
+//    Scale-Expansion with zero elimination);
+//  * Voronoi extraction in the conventions of Tess2d::extract_geometry
+//    (tess.cpp:238-398) and of the host mesh builder that feeds the flux path: faces
+//    per real cell in counter-clockwise neighbour order from angle -pi, volume and
+//    centroid sums over the incident edges, face lists in ascending face id.
+//
+// Circumcentres use the same closed form as the numpy mesh builder, so faces agree
+// with it to rounding.  Built with -ffp-contract=off: the error-bound filters assume
+// separately rounded products and sums.
+#include "phdtess.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+#include <utility>
+#include <vector>
+
+namespace {
+
+// ---- exact arithmetic (Shewchuk 1997, sections 2.3-2.6) ---------------------------
+inline void two_sum(double a, double b, double &x, double &y) {
+    x = a + b;
+    const double bv = x - a;
+    const double av = x - bv;
+    y = (a - av) + (b - bv);
+}
+
+inline void fast_two_sum(double a, double b, double &x, double &y) {   // |a| >= |b|
+    x = a + b;
+    const double bv = x - a;
+    y = b - bv;
+}
+
+inline void two_diff(double a, double b, double &x, double &y) {
+    x = a - b;
+    const double bv = a - x;
+    const double av = x + bv;
+    y = (a - av) + (bv - b);
+}
+
+inline void two_prod(double a, double b, double &x, double &y) {
+    x = a * b;
+    y = std::fma(a, b, -x);
+}
+
+// nonoverlapping expansion, components in increasing magnitude, zeros removed
+typedef std::vector<double> Exp;
+
+Exp exp_of_diff(double a, double b) {
+    double x, y;
+    two_diff(a, b, x, y);
+    Exp e;
+    if (y != 0.) e.push_back(y);
+    if (x != 0.) e.push_back(x);
+    return e;
+}
+
+// Grow-Expansion: e + b
+Exp exp_grow(const Exp &e, double b) {
+    Exp h;
+    h.reserve(e.size() + 1);
+    double q = b;
+    for (double ei : e) {
+        double qn, hh;
+        two_sum(q, ei, qn, hh);
+        if (hh != 0.) h.push_back(hh);
+        q = qn;
+    }
+    if (q != 0.) h.push_back(q);
+    return h;
+}
+
+Exp exp_add(const Exp &e, const Exp &f) {
+    Exp h = e;
+    for (double fj : f) h = exp_grow(h, fj);
+    return h;
+}
+
+Exp exp_neg(Exp e) {
+    for (double &v : e) v = -v;
+    return e;
+}
+
+// Scale-Expansion: b * e
+Exp exp_scale(const Exp &e, double b) {
+    Exp h;
+    if (e.empty() || b == 0.) return h;
+    h.reserve(2 * e.size());
+    double q, hh;
+    two_prod(e[0], b, q, hh);
+    if (hh != 0.) h.push_back(hh);
+    for (size_t i = 1; i < e.size(); i++) {
+        double T, t, qn;
+        two_prod(e[i], b, T, t);
+        two_sum(q, t, qn, hh);
+        if (hh != 0.) h.push_back(hh);
+        fast_two_sum(T, qn, q, hh);
+        if (hh != 0.) h.push_back(hh);
+    }
+    if (q != 0.) h.push_back(q);
+    return h;
+}
+
+Exp exp_mul(const Exp &e, const Exp &f) {
+    Exp h;
+    for (double fj : f) h = exp_add(h, exp_scale(e, fj));
+    return h;
+}
+
+int exp_sign(const Exp &e) { return e.empty() ? 0 : (e.back() > 0. ? 1 : -1); }
+
+const double EPS = 1.1102230246251565e-16;                 // 2^-53
+const double CCW_ERR_A = (3.0 + 16.0 * EPS) * EPS;
+const double ICC_ERR_A = (10.0 + 96.0 * EPS) * EPS;
+
+// > 0 when a, b, c turn counter-clockwise
+int orient2d(double ax, double ay, double bx, double by, double cx, double cy) {
+    const double detleft = (ax - cx) * (by - cy);
+    const double detright = (ay - cy) * (bx - cx);
+    const double det = detleft - detright;
+    double detsum;
+    if (detleft > 0.) {
+        if (detright <= 0.) return det > 0. ? 1 : (det < 0. ? -1 : 0);
+        detsum = detleft + detright;
+    } else if (detleft < 0.) {
+        if (detright >= 0.) return det > 0. ? 1 : (det < 0. ? -1 : 0);
+        detsum = -detleft - detright;
+    } else {
+        return det > 0. ? 1 : (det < 0. ? -1 : 0);
+    }
+    const double bound = CCW_ERR_A * detsum;
+    if (det >= bound || -det >= bound) return det > 0. ? 1 : -1;
+    const Exp acx = exp_of_diff(ax, cx), bcy = exp_of_diff(by, cy);
+    const Exp acy = exp_of_diff(ay, cy), bcx = exp_of_diff(bx, cx);
+    return exp_sign(exp_add(exp_mul(acx, bcy), exp_neg(exp_mul(acy, bcx))));
+}
+
+// > 0 when d lies strictly inside the circle through the counter-clockwise a, b, c
+int incircle(double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy) {
+    const double adx = ax - dx, bdx = bx - dx, cdx = cx - dx;
+    const double ady = ay - dy, bdy = by - dy, cdy = cy - dy;
+    const double bdxcdy = bdx * cdy, cdxbdy = cdx * bdy;
+    const double alift = adx * adx + ady * ady;
+    const double cdxady = cdx * ady, adxcdy = adx * cdy;
+    const double blift = bdx * bdx + bdy * bdy;
+    const double adxbdy = adx * bdy, bdxady = bdx * ady;
+    const double clift = cdx * cdx + cdy * cdy;
+    const double det = alift * (bdxcdy - cdxbdy) + blift * (cdxady - adxcdy) + clift * (adxbdy - bdxady);
+    const double perm = (std::fabs(bdxcdy) + std::fabs(cdxbdy)) * alift +
+                        (std::fabs(cdxady) + std::fabs(adxcdy)) * blift +
+                        (std::fabs(adxbdy) + std::fabs(bdxady)) * clift;
+    const double bound = ICC_ERR_A * perm;
+    if (det > bound || -det > bound) return det > 0. ? 1 : -1;
+    const Exp eax = exp_of_diff(ax, dx), eay = exp_of_diff(ay, dy);
+    const Exp ebx = exp_of_diff(bx, dx), eby = exp_of_diff(by, dy);
+    const Exp ecx = exp_of_diff(cx, dx), ecy = exp_of_diff(cy, dy);
+    const Exp la = exp_add(exp_mul(eax, eax), exp_mul(eay, eay));
+    const Exp lb = exp_add(exp_mul(ebx, ebx), exp_mul(eby, eby));
+    const Exp lc = exp_add(exp_mul(ecx, ecx), exp_mul(ecy, ecy));
+    const Exp ka = exp_add(exp_mul(ebx, ecy), exp_neg(exp_mul(ecx, eby)));
+    const Exp kb = exp_add(exp_mul(ecx, eay), exp_neg(exp_mul(eax, ecy)));
+    const Exp kc = exp_add(exp_mul(eax, eby), exp_neg(exp_mul(ebx, eay)));
+    return exp_sign(exp_add(exp_add(exp_mul(la, ka), exp_mul(lb, kb)), exp_mul(lc, kc)));
+}
+
+// ---- Hilbert key (phd/hilbert/hilbert.pyx:9-23) -------------------------------------
+const int KEY_INDEX_2D[4] = {0, 1, 3, 2};
+
+int64_t hilbert_key_2d(int32_t x, int32_t y, int order) {
+    int64_t key = 0;
+    for (int i = order - 1; i >= 0; i--) {
+        const int xbit = (x & (int32_t(1) << i)) ? 1 : 0;
+        const int ybit = (y & (int32_t(1) << i)) ? 1 : 0;
+        if (xbit == 0 && ybit == 0) {
+            std::swap(x, y);
+        } else if (xbit == 1 && ybit == 0) {
+            const int32_t nx = ~y, ny = ~x;
+            x = nx;
+            y = ny;
+        }
+        key = (key << 2) + KEY_INDEX_2D[(xbit << 1) + ybit];
+    }
+    return key;
+}
+
+// ---- triangulation --------------------------------------------------------------
+struct Tri {
+    int v[3];      // counter-clockwise; < 0: a vertex of the enclosing triangle
+    int n[3];      // n[k]: triangle across the edge opposite v[k] (-1: none)
+};
+
+struct Geometry {   // one phd_mesh2d_build result
+    int n_real = 0, n_cells = 0, n_faces = 0;
+    double pad_used = 0.;
+    std::vector<double> x, y, vol, dcx, dcy, area, comx, comy, nx, ny;
+    std::vector<int32_t> map, pair_i, pair_j, nbr_ptr, nbr_idx;
+};
+
+}  // namespace
+
+struct phd_tess2d {
+    std::vector<double> X, Y;          // inserted generators, by particle id
+    std::vector<char> inserted;
+    double SX[3] = {0, 0, 0}, SY[3] = {0, 0, 0};
+    std::vector<Tri> tris;
+    std::vector<int> free_tris;
+    std::vector<int> vt;               // one triangle incident to each generator
+    std::vector<int> bad_mark, seen_mark;
+    int stamp = 0;
+    int last = -1;
+    int n_real = 0, n_total = 0;
+    // scratch for one insertion
+    std::vector<int> bad, stack;
+    struct BEdge { int a, b, outer, outer_k; };
+    std::vector<BEdge> bnd;
+    Geometry G;
+
+    double px(int v) const { return v >= 0 ? X[v] : SX[-v - 1]; }
+    double py(int v) const { return v >= 0 ? Y[v] : SY[-v - 1]; }
+
+    void reset() {
+        X.clear(); Y.clear(); inserted.clear(); tris.clear(); free_tris.clear(); vt.clear();
+        bad_mark.clear(); seen_mark.clear(); stamp = 0; last = -1; n_real = n_total = 0;
+    }
+
+    int new_tri() {
+        if (!free_tris.empty()) {
+            const int t = free_tris.back();
+            free_tris.pop_back();
+            return t;
+        }
+        tris.push_back(Tri());
+        bad_mark.push_back(0);
+        seen_mark.push_back(0);
+        return int(tris.size()) - 1;
+    }
+
+    void init_super(double x0, double y0, double x1, double y1) {
+        const double cx = 0.5 * (x0 + x1), cy = 0.5 * (y0 + y1);
+        double ext = std::max(x1 - x0, y1 - y0);
+        if (!(ext > 0.)) ext = 1.;
+        const double M = 1.0e4 * ext;
+        SX[0] = cx - 2. * M; SY[0] = cy - M;
+        SX[1] = cx + 2. * M; SY[1] = cy - M;
+        SX[2] = cx;          SY[2] = cy + 2. * M;
+        tris.clear(); free_tris.clear(); bad_mark.clear(); seen_mark.clear();
+        const int t = new_tri();
+        tris[t].v[0] = -1; tris[t].v[1] = -2; tris[t].v[2] = -3;
+        tris[t].n[0] = tris[t].n[1] = tris[t].n[2] = -1;
+        last = t;
+    }
+
+    bool in_circle(const Tri &T, int p) const {
+        return incircle(px(T.v[0]), py(T.v[0]), px(T.v[1]), py(T.v[1]), px(T.v[2]), py(T.v[2]), X[p], Y[p]) > 0;
+    }
+
+    // visibility walk from the last created triangle
+    int locate(int p) {
+        int t = last;
+        const double x = X[p], y = Y[p];
+        int start = 0;
+        const long max_steps = 4L * long(tris.size()) + 64;
+        for (long step = 0; step < max_steps; step++) {
+            const Tri &T = tris[t];
+            int next = -1;
+            bool outside = false;
+            for (int kk = 0; kk < 3; kk++) {
+                const int k = (kk + start) % 3;
+                const int a = T.v[(k + 1) % 3], b = T.v[(k + 2) % 3];
+                if (orient2d(px(a), py(a), px(b), py(b), x, y) < 0) { next = T.n[k]; outside = true; break; }
+            }
+            if (!outside) return t;
+            if (next < 0) return -1;                      // outside the enclosing triangle
+            t = next;
+            start = (start + 1) % 3;
+        }
+        return -1;
+    }
+
+    // insert generator p (coordinates already in X, Y); 0 or an error code
+    int insert(int p) {
+        const int t0 = locate(p);
+        if (t0 < 0) return -4;
+        {
+            const Tri &T = tris[t0];
+            for (int k = 0; k < 3; k++)
+                if (T.v[k] >= 0 && X[T.v[k]] == X[p] && Y[T.v[k]] == Y[p]) return -3;
+        }
+        if (++stamp == 0x7fffffff) {
+            std::fill(bad_mark.begin(), bad_mark.end(), 0);
+            std::fill(seen_mark.begin(), seen_mark.end(), 0);
+            stamp = 1;
+        }
+        bad.clear();
+        stack.clear();
+        bad_mark[t0] = stamp;
+        seen_mark[t0] = stamp;
+        stack.push_back(t0);
+        while (!stack.empty()) {
+            const int t = stack.back();
+            stack.pop_back();
+            bad.push_back(t);
+            for (int k = 0; k < 3; k++) {
+                const int nb = tris[t].n[k];
+                if (nb < 0 || seen_mark[nb] == stamp) continue;
+                seen_mark[nb] = stamp;
+                if (in_circle(tris[nb], p)) {
+                    bad_mark[nb] = stamp;
+                    stack.push_back(nb);
+                }
+            }
+        }
+        bnd.clear();
+        for (int t : bad) {
+            const Tri &T = tris[t];
+            for (int k = 0; k < 3; k++) {
+                const int nb = T.n[k];
+                if (nb >= 0 && bad_mark[nb] == stamp) continue;
+                int ok = -1;                                   // the outer triangle's edge back to t
+                if (nb >= 0)
+                    for (int m = 0; m < 3; m++)
+                        if (tris[nb].n[m] == t) ok = m;
+                if (nb >= 0 && ok < 0) return -4;
+                bnd.push_back({T.v[(k + 1) % 3], T.v[(k + 2) % 3], nb, ok});
+            }
+        }
+        // the cavity is star-shaped from p: one new triangle (p, a, b) per boundary edge
+        const size_t m = bnd.size();
+        if (m != bad.size() + 2) return -4;
+        std::vector<int> nt(m);
+        for (size_t j = 0; j < m; j++) nt[j] = j < bad.size() ? bad[j] : new_tri();
+        for (size_t j = 0; j < m; j++) {
+            Tri &T = tris[nt[j]];
+            T.v[0] = p; T.v[1] = bnd[j].a; T.v[2] = bnd[j].b;
+            T.n[0] = bnd[j].outer;
+            bad_mark[nt[j]] = 0;
+            if (bnd[j].outer >= 0) tris[bnd[j].outer].n[bnd[j].outer_k] = nt[j];
+        }
+        for (size_t j = 0; j < m; j++) {
+            Tri &T = tris[nt[j]];
+            T.n[1] = T.n[2] = -1;
+            for (size_t q = 0; q < m; q++) {
+                if (bnd[q].a == bnd[j].b) T.n[1] = nt[q];       // across (b, p)
+                if (bnd[q].b == bnd[j].a) T.n[2] = nt[q];       // across (p, a)
+            }
+            if (T.n[1] < 0 || T.n[2] < 0) return -4;
+            if (bnd[j].a >= 0) vt[bnd[j].a] = nt[j];
+            if (bnd[j].b >= 0) vt[bnd[j].b] = nt[j];
+        }
+        vt[p] = nt[0];
+        last = nt[0];
+        inserted[p] = 1;
+        return 0;
+    }
+
+    // insert generators [begin, end) along a Hilbert curve over their bounding box
+    int insert_range(int begin, int end) {
+        if (end <= begin) return 0;
+        double x0 = X[begin], x1 = X[begin], y0 = Y[begin], y1 = Y[begin];
+        for (int i = begin; i < end; i++) {
+            x0 = std::min(x0, X[i]); x1 = std::max(x1, X[i]);
+            y0 = std::min(y0, Y[i]); y1 = std::max(y1, Y[i]);
+        }
+        double box = std::max(x1 - x0, y1 - y0);
+        if (!(box > 0.)) box = 1.;
+        const double scale = double(1 << 16) / box;
+        std::vector<std::pair<int64_t, int>> order(end - begin);
+        for (int i = begin; i < end; i++) {
+            int32_t qx = int32_t((X[i] - x0) * scale), qy = int32_t((Y[i] - y0) * scale);
+            qx = std::min<int32_t>(std::max<int32_t>(qx, 0), 65535);
+            qy = std::min<int32_t>(std::max<int32_t>(qy, 0), 65535);
+            order[i - begin] = std::make_pair(hilbert_key_2d(qx, qy, 16), i);
+        }
+        std::sort(order.begin(), order.end());
+        for (const auto &o : order) {
+            const int rc = insert(o.second);
+            if (rc != 0) return rc;
+        }
+        return 0;
+    }
+
+    // circumcentre of triangle t: the closed form of the numpy mesh builder
+    void circumcentre(int t, double &ux, double &uy) const {
+        const Tri &T = tris[t];
+        const double ax = px(T.v[0]), ay = py(T.v[0]);
+        const double bx = px(T.v[1]) - ax, by = py(T.v[1]) - ay;
+        const double cx = px(T.v[2]) - ax, cy = py(T.v[2]) - ay;
+        const double d = 2.0 * (bx * cy - by * cx);
+        const double b2 = bx * bx + by * by;
+        const double c2 = cx * cx + cy * cy;
+        ux = ax + (cy * b2 - by * c2) / d;
+        uy = ay + (bx * c2 - cx * b2) / d;
+    }
+
+    struct Spoke { int j; int t1, t2; };   // neighbour j, triangles on both sides of edge (i, j)
+
+    // the edges around generator i in circulation order; false where i touches the
+    // enclosing triangle (an unbounded Voronoi cell)
+    bool spokes(int i, std::vector<Spoke> &out) const {
+        out.clear();
+        const int t0 = vt[i];
+        int t = t0;
+        for (int guard = 0; guard < 4096; guard++) {
+            const Tri &T = tris[t];
+            int k = 0;
+            while (k < 3 && T.v[k] != i) k++;
+            if (k == 3) return false;
+            const int b = T.v[(k + 1) % 3];
+            const int across = T.n[(k + 2) % 3];
+            if (b < 0 || T.v[(k + 2) % 3] < 0 || across < 0) return false;
+            out.push_back({b, t, across});
+            t = T.n[(k + 1) % 3];
+            if (t < 0) return false;
+            if (t == t0) return true;
+        }
+        return false;
+    }
+
+    int radius_of(int i, std::vector<Spoke> &sp, double &r) const {
+        if (!spokes(i, sp)) { r = -1.; return 1; }
+        double m = 0.;
+        for (const Spoke &s : sp) {
+            double ux, uy;
+            circumcentre(s.t1, ux, uy);
+            m = std::max(m, (ux - X[i]) * (ux - X[i]) + (uy - Y[i]) * (uy - Y[i]));
+        }
+        r = 2.0 * std::sqrt(m);
+        return 0;
+    }
+};
+
+namespace {
+
+struct Edge1 {                 // one incident edge of a real cell
+    int j;
+    double ang, h, ln, fx, fy, xr, yr;
+};
+
+// incident edges of real cell i sorted counter-clockwise from -pi; false if unbounded
+bool cell_edges(const phd_tess2d &T, int i, std::vector<phd_tess2d::Spoke> &sp, std::vector<Edge1> &E,
+                std::vector<double> &ccx, std::vector<double> &ccy, std::vector<int> &cc_mark, int cc_stamp) {
+    if (!T.spokes(i, sp)) return false;
+    E.clear();
+    auto cc = [&](int t, double &ux, double &uy) {
+        if (cc_mark[t] != cc_stamp) {
+            T.circumcentre(t, ccx[t], ccy[t]);
+            cc_mark[t] = cc_stamp;
+        }
+        ux = ccx[t];
+        uy = ccy[t];
+    };
+    for (const auto &s : sp) {
+        double x1, y1, x2, y2;
+        cc(s.t1, x1, y1);
+        cc(s.t2, x2, y2);
+        Edge1 e;
+        e.j = s.j;
+        e.xr = T.X[s.j] - T.X[i];
+        e.yr = T.Y[s.j] - T.Y[i];
+        e.h = std::sqrt(e.xr * e.xr + e.yr * e.yr);
+        const double xe = x2 - x1, ye = y2 - y1;
+        e.ln = std::sqrt(xe * xe + ye * ye);
+        e.fx = 0.5 * (x1 + x2);
+        e.fy = 0.5 * (y1 + y2);
+        e.ang = std::atan2(e.yr, e.xr);
+        E.push_back(e);
+    }
+    std::sort(E.begin(), E.end(), [](const Edge1 &a, const Edge1 &b) { return a.ang < b.ang; });
+    return E.size() >= 3;
+}
+
+// faces, volumes and centroids of the real cells (extract_geometry); returns the
+// face count or -1.  Face j indices are generator ids (before any ghost pruning).
+int extract(const phd_tess2d &T, std::vector<double> &vol, std::vector<double> &dcx, std::vector<double> &dcy,
+            std::vector<double> &area, std::vector<double> &comx, std::vector<double> &comy,
+            std::vector<double> &nx, std::vector<double> &ny, std::vector<int32_t> &pi, std::vector<int32_t> &pj) {
+    const int n = T.n_real;
+    std::vector<phd_tess2d::Spoke> sp;
+    std::vector<Edge1> E;
+    std::vector<double> ccx(T.tris.size()), ccy(T.tris.size());
+    std::vector<int> cc_mark(T.tris.size(), 0);
+    vol.assign(n, 0.); dcx.assign(n, 0.); dcy.assign(n, 0.);
+    area.clear(); comx.clear(); comy.clear(); nx.clear(); ny.clear(); pi.clear(); pj.clear();
+    for (int i = 0; i < n; i++) {
+        if (!cell_edges(T, i, sp, E, ccx, ccy, cc_mark, 1)) return -1;
+        const double xp = T.X[i], yp = T.Y[i];
+        double v = 0., cx = 0., cy = 0.;
+        for (const Edge1 &e : E) {
+            const double a = 0.25 * e.ln * e.h;
+            const double tx = 2.0 * e.fx / 3.0 + xp / 3.0;
+            const double ty = 2.0 * e.fy / 3.0 + yp / 3.0;
+            v += a;
+            cx += a * tx;
+            cy += a * ty;
+            if (e.j > i) {
+                pi.push_back(i);
+                pj.push_back(e.j);
+                area.push_back(e.ln);
+                comx.push_back(e.fx);
+                comy.push_back(e.fy);
+                nx.push_back(e.xr / e.h);
+                ny.push_back(e.yr / e.h);
+            }
+        }
+        vol[i] = v;
+        dcx[i] = cx / v - xp;
+        dcy[i] = cy / v - yp;
+    }
+    return int(pi.size());
+}
+
+// per-cell face lists in ascending face id (CSR over n_cells)
+void face_lists(int n_cells, const std::vector<int32_t> &pi, const std::vector<int32_t> &pj,
+                std::vector<int32_t> &ptr, std::vector<int32_t> &idx) {
+    const int F = int(pi.size());
+    ptr.assign(n_cells + 1, 0);
+    for (int f = 0; f < F; f++) { ptr[pi[f] + 1]++; ptr[pj[f] + 1]++; }
+    for (int c = 0; c < n_cells; c++) ptr[c + 1] += ptr[c];
+    idx.assign(2 * size_t(F), 0);
+    std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+    for (int f = 0; f < F; f++) {
+        idx[fill[pi[f]]++] = f;
+        idx[fill[pj[f]]++] = f;
+    }
+}
+
+// ghost images of the real generators (the numpy builder's _ghosts)
+void make_ghosts(const double *x, const double *y, int n, int boundary, const double xmin[2], const double xmax[2],
+                 double pad, std::vector<double> &gx, std::vector<double> &gy, std::vector<int32_t> &gmap) {
+    gx.clear(); gy.clear(); gmap.clear();
+    const double L0 = xmax[0] - xmin[0], L1 = xmax[1] - xmin[1];
+    if (boundary == 0) {
+        for (int sx = -1; sx <= 1; sx++)
+            for (int sy = -1; sy <= 1; sy++) {
+                if (sx == 0 && sy == 0) continue;
+                for (int i = 0; i < n; i++) {
+                    const double xs = x[i] + double(sx) * L0, ys = y[i] + double(sy) * L1;
+                    if (xs > xmin[0] - pad && xs < xmax[0] + pad && ys > xmin[1] - pad && ys < xmax[1] + pad) {
+                        gx.push_back(xs); gy.push_back(ys); gmap.push_back(i);
+                    }
+                }
+            }
+    } else {
+        for (int k = 0; k < 2; k++)
+            for (int lo = 1; lo >= 0; lo--) {
+                const double edge = lo ? xmin[k] : xmax[k];
+                for (int i = 0; i < n; i++) {
+                    const double c = k == 0 ? x[i] : y[i];
+                    const bool near = lo ? (c - edge < pad) : (edge - c < pad);
+                    if (!near) continue;
+                    double xs = x[i], ys = y[i];
+                    if (k == 0) xs = xs - 2.0 * (xs - edge);
+                    else ys = ys - 2.0 * (ys - edge);
+                    gx.push_back(xs); gy.push_back(ys); gmap.push_back(i);
+                }
+            }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+phd_tess2d *phd_tess2d_create(void) { return new (std::nothrow) phd_tess2d(); }
+
+void phd_tess2d_destroy(phd_tess2d *t) { delete t; }
+
+int phd_tess2d_build_initial(phd_tess2d *t, const double *x, const double *y, int n_real, double *radius) {
+    if (!t || !x || !y || n_real < 3) return -2;
+    try {
+        t->reset();
+        t->X.assign(x, x + n_real);
+        t->Y.assign(y, y + n_real);
+        t->inserted.assign(n_real, 0);
+        t->vt.assign(n_real, -1);
+        t->n_real = t->n_total = n_real;
+        double x0 = x[0], x1 = x[0], y0 = y[0], y1 = y[0];
+        for (int i = 0; i < n_real; i++) {
+            if (!std::isfinite(x[i]) || !std::isfinite(y[i])) return -2;
+            x0 = std::min(x0, x[i]); x1 = std::max(x1, x[i]);
+            y0 = std::min(y0, y[i]); y1 = std::max(y1, y[i]);
+        }
+        t->init_super(x0, y0, x1, y1);
+        const int rc = t->insert_range(0, n_real);
+        if (rc != 0) return rc;
+        if (radius) {
+            std::vector<phd_tess2d::Spoke> sp;
+            for (int i = 0; i < n_real; i++) t->radius_of(i, sp, radius[i]);
+        }
+        return 0;
+    } catch (...) {
+        return -4;
+    }
+}
+
+int phd_tess2d_update_initial(phd_tess2d *t, const double *x, const double *y, int begin, int end) {
+    if (!t || !x || !y || begin != t->n_total || end < begin) return -2;
+    if (begin == end) return 0;
+    try {
+        for (int i = begin; i < end; i++) {
+            if (!std::isfinite(x[i]) || !std::isfinite(y[i])) return -2;
+            // the enclosing triangle is sized for the real generators' box: far ghosts
+            // would fall outside it
+            const double cx = 0.5 * (t->SX[0] + t->SX[1]);
+            if (std::fabs(x[i] - cx) > 0.25 * (t->SX[1] - t->SX[0]) ||
+                std::fabs(y[i] - t->SY[0]) > 0.5 * (t->SY[2] - t->SY[0]))
+                return -2;
+        }
+        t->X.insert(t->X.end(), x + begin, x + end);
+        t->Y.insert(t->Y.end(), y + begin, y + end);
+        t->inserted.resize(end, 0);
+        t->vt.resize(end, -1);
+        t->n_total = end;
+        return t->insert_range(begin, end);
+    } catch (...) {
+        return -4;
+    }
+}
+
+int phd_tess2d_count_faces(phd_tess2d *t) {
+    if (!t || t->n_real == 0) return -2;
+    std::vector<phd_tess2d::Spoke> sp;
+    int F = 0;
+    for (int i = 0; i < t->n_real; i++) {
+        if (!t->spokes(i, sp)) return -1;
+        for (const auto &s : sp) F += s.j > i;
+    }
+    return F;
+}
+
+int phd_tess2d_update_radius(phd_tess2d *t, const int32_t *ids, int n_ids, double *radius) {
+    if (!t || (n_ids > 0 && (!ids || !radius))) return -2;
+    std::vector<phd_tess2d::Spoke> sp;
+    int open = 0;
+    for (int k = 0; k < n_ids; k++) {
+        const int i = ids[k];
+        if (i < 0 || i >= t->n_total) return -2;
+        open += t->radius_of(i, sp, radius[i]);
+    }
+    return open;
+}
+
+int phd_tess2d_extract_geometry(phd_tess2d *t, double *dcom_x, double *dcom_y, double *volume, double *face_area,
+                                double *com_x, double *com_y, double *normal_x, double *normal_y, int32_t *pair_i,
+                                int32_t *pair_j, int32_t *nbr_ptr, int32_t *nbr_idx) {
+    if (!t || t->n_real == 0) return -2;
+    try {
+        std::vector<double> vol, dcx, dcy, area, comx, comy, nx, ny;
+        std::vector<int32_t> pi, pj, ptr, idx;
+        const int F = extract(*t, vol, dcx, dcy, area, comx, comy, nx, ny, pi, pj);
+        if (F < 0) return F;
+        face_lists(t->n_total, pi, pj, ptr, idx);
+        auto put = [](const auto &v, auto *dst) { if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(v[0])); };
+        put(dcx, dcom_x); put(dcy, dcom_y); put(vol, volume); put(area, face_area);
+        put(comx, com_x); put(comy, com_y); put(nx, normal_x); put(ny, normal_y);
+        put(pi, pair_i); put(pj, pair_j); put(ptr, nbr_ptr); put(idx, nbr_idx);
+        return F;
+    } catch (...) {
+        return -4;
+    }
+}
+
+int phd_mesh2d_build(phd_tess2d *t, const double *x, const double *y, int n_real, int boundary, double xmin0,
+                     double xmin1, double xmax0, double xmax1, double pad) {
+    if (!t || !x || !y || n_real < 3 || (boundary != 0 && boundary != 1) || !(xmax0 > xmin0) ||
+        !(xmax1 > xmin1) || !(pad > 0.))
+        return -2;
+    const double xmin[2] = {xmin0, xmin1}, xmax[2] = {xmax0, xmax1};
+    try {
+        std::vector<double> gx, gy, ax, ay;
+        std::vector<int32_t> gmap;
+        for (int attempt = 0; attempt < 6; attempt++, pad *= 2.0) {
+            make_ghosts(x, y, n_real, boundary, xmin, xmax, pad, gx, gy, gmap);
+            const int n_all = n_real + int(gx.size());
+            ax.assign(x, x + n_real);
+            ax.insert(ax.end(), gx.begin(), gx.end());
+            ay.assign(y, y + n_real);
+            ay.insert(ay.end(), gy.begin(), gy.end());
+            double x0 = ax[0], x1 = ax[0], y0 = ay[0], y1 = ay[0];
+            for (int i = 0; i < n_all; i++) {
+                if (!std::isfinite(ax[i]) || !std::isfinite(ay[i])) return -2;
+                x0 = std::min(x0, ax[i]); x1 = std::max(x1, ax[i]);
+                y0 = std::min(y0, ay[i]); y1 = std::max(y1, ay[i]);
+            }
+            t->reset();
+            t->X = ax;
+            t->Y = ay;
+            t->inserted.assign(n_all, 0);
+            t->vt.assign(n_all, -1);
+            t->n_real = n_real;
+            t->n_total = n_all;
+            t->init_super(x0, y0, x1, y1);
+            int rc;
+            if ((rc = t->insert_range(0, n_real)) != 0) return rc;
+            if ((rc = t->insert_range(n_real, n_all)) != 0) return rc;
+
+            Geometry &G = t->G;
+            std::vector<double> vol, dcx, dcy;
+            const int F = extract(*t, vol, dcx, dcy, G.area, G.comx, G.comy, G.nx, G.ny, G.pair_i, G.pair_j);
+            if (F == -1) continue;                         // a real cell is unbounded: wider pad
+            if (F < 0) return F;
+            // keep ghosts that share a face with a real cell, in creation order
+            std::vector<char> used(n_all, 0);
+            for (int f = 0; f < F; f++) used[G.pair_j[f]] = 1;
+            std::vector<int32_t> newidx(n_all, -1);
+            for (int i = 0; i < n_real; i++) newidx[i] = i;
+            int nc = n_real;
+            for (int g = n_real; g < n_all; g++)
+                if (used[g]) newidx[g] = nc++;
+            for (int f = 0; f < F; f++) G.pair_j[f] = newidx[G.pair_j[f]];
+            G.n_real = n_real;
+            G.n_cells = nc;
+            G.n_faces = F;
+            G.pad_used = pad;
+            G.x.resize(nc); G.y.resize(nc); G.map.resize(nc); G.vol.resize(nc); G.dcx.resize(nc); G.dcy.resize(nc);
+            for (int i = 0; i < n_real; i++) {
+                G.x[i] = x[i]; G.y[i] = y[i]; G.map[i] = i;
+                G.vol[i] = vol[i]; G.dcx[i] = dcx[i]; G.dcy[i] = dcy[i];
+            }
+            for (int g = n_real; g < n_all; g++) {
+                const int c = newidx[g];
+                if (c < 0) continue;
+                const int img = gmap[g - n_real];
+                G.x[c] = ax[g]; G.y[c] = ay[g]; G.map[c] = img;
+                G.vol[c] = vol[img]; G.dcx[c] = dcx[img]; G.dcy[c] = dcy[img];
+            }
+            face_lists(nc, G.pair_i, G.pair_j, G.nbr_ptr, G.nbr_idx);
+            return F;
+        }
+        return -1;
+    } catch (...) {
+        return -4;
+    }
+}
+
+int phd_mesh2d_sizes(const phd_tess2d *t, int32_t *n_cells, int32_t *n_faces, double *pad_used) {
+    if (!t) return -2;
+    if (n_cells) *n_cells = t->G.n_cells;
+    if (n_faces) *n_faces = t->G.n_faces;
+    if (pad_used) *pad_used = t->G.pad_used;
+    return 0;
+}
+
+int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, double *vol, double *dcom_x,
+                    double *dcom_y, int32_t *pair_i, int32_t *pair_j, double *area, double *com_x, double *com_y,
+                    double *normal_x, double *normal_y, int32_t *nbr_ptr, int32_t *nbr_idx) {
+    if (!t || t->G.n_cells == 0) return -2;
+    const Geometry &G = t->G;
+    auto put = [](const auto &v, auto *dst) { if (dst && !v.empty()) std::memcpy(dst, v.data(), v.size() * sizeof(v[0])); };
+    put(G.x, x); put(G.y, y); put(G.map, map); put(G.vol, vol); put(G.dcx, dcom_x); put(G.dcy, dcom_y);
+    put(G.pair_i, pair_i); put(G.pair_j, pair_j); put(G.area, area); put(G.comx, com_x); put(G.comy, com_y);
+    put(G.nx, normal_x); put(G.ny, normal_y); put(G.nbr_ptr, nbr_ptr); put(G.nbr_idx, nbr_idx);
+    return 0;
+}
+
+void phd_hilbert_keys_2d_host(const int32_t *xh, const int32_t *yh, int64_t n, int order, int64_t *keys) {
+    for (int64_t i = 0; i < n; i++) keys[i] = hilbert_key_2d(xh[i], yh[i], order);
+}
+
+}  // extern "C"

@@ -3,8 +3,15 @@
 The reference builds its mesh with CGAL on the host (``phd/mesh/tess.cpp``) and keeps
 it there; the flux path consumes the result.  CGAL is not available in this
 environment, so this module produces the same *kind* of face list from a Delaunay
-triangulation (scipy/Qhull) and our own circumcentre construction, following the
-conventions of ``Tess2d::extract_geometry`` (``tess.cpp:238-398``):
+triangulation and our own circumcentre construction, following the conventions of
+``Tess2d::extract_geometry`` (``tess.cpp:238-398``).  Two builders give the same mesh:
+``backend="native"`` (default) is the C++ tessellation of ``include/phdtess.h``
+(``tess.py``); ``backend="scipy"`` is a numpy construction on scipy/Qhull's Delaunay
+triangulation, kept as the independent check of the native one.  They agree face for
+face (geometry to rounding) except where four generators are exactly cocircular --
+e.g. a generator, its neighbour and their mirror images at a reflective wall -- where
+either diagonal is a valid Delaunay edge and the two builders may emit different
+zero-area faces.  Conventions:
 
 * faces are emitted per REAL cell ``i`` for each Voronoi edge shared with a
   neighbour ``j`` where ``i < j`` -- ghost indices follow all real indices, so
@@ -144,27 +151,36 @@ def _circumcenters(p, simp):
 
 
 def build_mesh(x_real, boundary="periodic", xmin=(0.0, 0.0), xmax=(1.0, 1.0),
-               pad=None, hilbert=True):
+               pad=None, hilbert=True, backend="native"):
     """Tessellate real generators ``x_real`` (2, N) with ghosts for ``boundary``.
 
     With ``hilbert=True`` the real cells are first reordered along the reference's
     Hilbert key (``phd/hilbert``), so neighbouring cells sit close in memory; the
     returned mesh is in that order (``order`` gives original indices).
+    ``backend``: "native" (C++ tessellation, ``tess.py``) or "scipy".
     Returns ``(mesh, order)``.
     """
-    from scipy.spatial import Delaunay
-
+    if backend not in ("native", "scipy"):
+        raise ValueError("backend must be 'native' or 'scipy'")
     x_real = np.ascontiguousarray(x_real, dtype=np.float64)
     n = x_real.shape[1]
     if hilbert:
         box = max(xmax[0] - xmin[0], xmax[1] - xmin[1])
-        order = hilbert_order(x_real[0], x_real[1], xmin, box)
+        if backend == "native":
+            from . import tess
+            from .hilbert import ORDER, quantize
+            keys = tess.hilbert_keys_2d(quantize(x_real[0], xmin[0], box), quantize(x_real[1], xmin[1], box), ORDER)
+            order = np.argsort(keys, kind="stable")
+        else:
+            order = hilbert_order(x_real[0], x_real[1], xmin, box)
         x_real = np.ascontiguousarray(x_real[:, order])
     else:
         order = np.arange(n)
     if pad is None:
         area = (xmax[0] - xmin[0]) * (xmax[1] - xmin[1])
         pad = 3.0 * np.sqrt(area / n)
+    if backend == "native":
+        return _build_native(x_real, boundary, xmin, xmax, pad), order
     for _attempt in range(6):
         try:
             return _build(x_real, boundary, xmin, xmax, pad), order
@@ -175,6 +191,21 @@ def build_mesh(x_real, boundary="periodic", xmin=(0.0, 0.0), xmax=(1.0, 1.0),
 
 class _OpenCell(Exception):
     pass
+
+
+def _build_native(x_real, boundary, xmin, xmax, pad):
+    from . import tess
+    o, _pad_used = tess.build_mesh_native(x_real, boundary, xmin, xmax, pad)
+    n = x_real.shape[1]
+    n_cells = o["x"].shape[1]
+    tag = np.full(n_cells, GHOST, dtype=np.int8)
+    tag[:n] = REAL
+    typ = np.full(n_cells, EXTERIOR, dtype=np.int8)
+    typ[:n] = UNDEFINED
+    return HostMesh(dim=2, n_real=n, x=o["x"], tag=tag, type=typ, map=o["map"], vol=o["vol"], dcom=o["dcom"],
+                    pair_i=o["pair_i"], pair_j=o["pair_j"], area=o["area"], com=o["com"], normal=o["normal"],
+                    nbr_ptr=o["nbr_ptr"], nbr_idx=o["nbr_idx"], xmin=tuple(xmin), xmax=tuple(xmax),
+                    boundary=boundary)
 
 
 def _build(x_real, boundary, xmin, xmax, pad):

@@ -1,0 +1,164 @@
+"""ctypes binding of ``libphdtess.so`` -- the host C++ tessellation of ``include/phdtess.h``.
+
+``Tess2d`` mirrors the reference's ``PyTess2d`` / ``Tess2d`` method set
+(``phd/mesh/pytess.pyx:27-57``, ``phd/mesh/tess.h:53-72``) over numpy arrays;
+``build_mesh_native`` builds a whole box mesh (real cells, ghost images, faces,
+volumes, face lists) in the layout of ``meshgen.HostMesh``.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libphdtess.so")
+
+ERR_INCOMPLETE, ERR_ARG, ERR_DUPLICATE, ERR_INTERNAL = -1, -2, -3, -4
+_MESSAGES = {ERR_INCOMPLETE: "Mesh failed to converged!",      # mesh.pyx:240-241
+             ERR_ARG: "bad argument", ERR_DUPLICATE: "duplicate generator position",
+             ERR_INTERNAL: "internal tessellation failure"}
+
+_lib = None
+_vp, _i32, _f64 = C.c_void_p, C.c_int32, C.c_double
+_SIGNATURES = {
+    "phd_tess2d_create": ([], _vp),
+    "phd_tess2d_destroy": ([_vp], None),
+    "phd_tess2d_build_initial": ([_vp, _vp, _vp, _i32, _vp], C.c_int),
+    "phd_tess2d_update_initial": ([_vp, _vp, _vp, _i32, _i32], C.c_int),
+    "phd_tess2d_count_faces": ([_vp], C.c_int),
+    "phd_tess2d_update_radius": ([_vp, _vp, _i32, _vp], C.c_int),
+    "phd_tess2d_extract_geometry": ([_vp] * 13, C.c_int),
+    "phd_mesh2d_build": ([_vp, _vp, _vp, _i32, _i32, _f64, _f64, _f64, _f64, _f64], C.c_int),
+    "phd_mesh2d_sizes": ([_vp, _vp, _vp, _vp], C.c_int),
+    "phd_mesh2d_copy": ([_vp] * 16, C.c_int),
+    "phd_hilbert_keys_2d_host": ([_vp, _vp, C.c_int64, C.c_int, _vp], None),
+}
+
+
+def lib():
+    """The loaded tessellation library; raises if it was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("phd_code_gb300: %s is missing; run __graft_entry__.build() first" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    for name, (args, res) in _SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def available():
+    return os.path.exists(LIB_PATH)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _check(rc, what):
+    if rc < 0:
+        raise RuntimeError("%s: %s" % (what, _MESSAGES.get(rc, "error %d" % rc)))
+    return rc
+
+
+class Tess2d:
+    """The reference's ``Tess2d`` over numpy arrays (positions ``x`` of shape (2, n))."""
+
+    def __init__(self):
+        self._h = lib().phd_tess2d_create()
+        if not self._h:
+            raise MemoryError("phd_tess2d_create")
+        self.n_real = 0
+        self.n_total = 0
+        self._x = None
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h and _lib is not None:
+            _lib.phd_tess2d_destroy(h)
+
+    def build_initial_tess(self, x, radius, num_real_particles):
+        """tess.cpp:35-142; ``radius`` (float64, length >= n) receives 2 * max distance
+        to the Voronoi vertices, -1 where the cell is unbounded."""
+        self._x = np.ascontiguousarray(x, dtype=np.float64)
+        n = int(num_real_particles)
+        rc = lib().phd_tess2d_build_initial(self._h, _p(self._x[0]), _p(self._x[1]), n,
+                                             _p(radius) if radius is not None else None)
+        self.n_real = self.n_total = n
+        return rc
+
+    def update_initial_tess(self, x, begin_particles, end_particles):
+        """tess.cpp:144-187: insert generators begin..end-1 of ``x``."""
+        self._x = np.ascontiguousarray(x, dtype=np.float64)
+        rc = lib().phd_tess2d_update_initial(self._h, _p(self._x[0]), _p(self._x[1]), int(begin_particles),
+                                              int(end_particles))
+        if rc == 0:
+            self.n_total = int(end_particles)
+        return rc
+
+    def count_number_of_faces(self):
+        """tess.cpp:189-236: faces owned by real cells, -1 while a real cell is unbounded."""
+        return lib().phd_tess2d_count_faces(self._h)
+
+    def update_radius(self, radius, ids):
+        """tess.cpp:400-470 for the generators ``ids``; returns how many stay unbounded."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        return lib().phd_tess2d_update_radius(self._h, _p(ids), int(ids.size), _p(radius))
+
+    def extract_geometry(self):
+        """tess.cpp:238-398.  Returns a dict: ``volume``, ``dcom`` (real cells),
+        ``area``, ``com``, ``normal``, ``pair_i``, ``pair_j``, and the per-cell face lists
+        ``nbr_ptr`` / ``nbr_idx`` over all inserted generators."""
+        F = _check(self.count_number_of_faces(), "count_number_of_faces")
+        n, nt = self.n_real, self.n_total
+        out = {"dcom": np.zeros((2, n)), "volume": np.zeros(n), "area": np.zeros(F), "com": np.zeros((2, F)),
+               "normal": np.zeros((2, F)), "pair_i": np.zeros(F, np.int32), "pair_j": np.zeros(F, np.int32),
+               "nbr_ptr": np.zeros(nt + 1, np.int32), "nbr_idx": np.zeros(2 * F, np.int32)}
+        _check(lib().phd_tess2d_extract_geometry(
+            self._h, _p(out["dcom"][0]), _p(out["dcom"][1]), _p(out["volume"]), _p(out["area"]),
+            _p(out["com"][0]), _p(out["com"][1]), _p(out["normal"][0]), _p(out["normal"][1]),
+            _p(out["pair_i"]), _p(out["pair_j"]), _p(out["nbr_ptr"]), _p(out["nbr_idx"])), "extract_geometry")
+        return out
+
+
+def build_mesh_native(x_real, boundary, xmin, xmax, pad):
+    """Real generators ``x_real`` (2, N) in a periodic or reflective box -> the fields of
+    ``meshgen.HostMesh`` (x, map, vol, dcom, pair_i, pair_j, area, com, normal,
+    nbr_ptr, nbr_idx) and the pad used."""
+    x = np.ascontiguousarray(x_real, dtype=np.float64)
+    n = x.shape[1]
+    L = lib()
+    h = L.phd_tess2d_create()
+    if not h:
+        raise MemoryError("phd_tess2d_create")
+    try:
+        rc = L.phd_mesh2d_build(h, _p(x[0]), _p(x[1]), n, {"periodic": 0, "reflective": 1}[boundary],
+                                float(xmin[0]), float(xmin[1]), float(xmax[0]), float(xmax[1]), float(pad))
+        _check(rc, "tessellate")
+        nc, nf, pad_used = C.c_int32(), C.c_int32(), C.c_double()
+        L.phd_mesh2d_sizes(h, C.byref(nc), C.byref(nf), C.byref(pad_used))
+        nc, F = nc.value, nf.value
+        o = {"x": np.zeros((2, nc)), "map": np.zeros(nc, np.int32), "vol": np.zeros(nc),
+             "dcom": np.zeros((2, nc)), "pair_i": np.zeros(F, np.int32), "pair_j": np.zeros(F, np.int32),
+             "area": np.zeros(F), "com": np.zeros((2, F)), "normal": np.zeros((2, F)),
+             "nbr_ptr": np.zeros(nc + 1, np.int32), "nbr_idx": np.zeros(2 * F, np.int32)}
+        _check(L.phd_mesh2d_copy(h, _p(o["x"][0]), _p(o["x"][1]), _p(o["map"]), _p(o["vol"]), _p(o["dcom"][0]),
+                                 _p(o["dcom"][1]), _p(o["pair_i"]), _p(o["pair_j"]), _p(o["area"]),
+                                 _p(o["com"][0]), _p(o["com"][1]), _p(o["normal"][0]), _p(o["normal"][1]),
+                                 _p(o["nbr_ptr"]), _p(o["nbr_idx"])), "copy")
+        return o, pad_used.value
+    finally:
+        L.phd_tess2d_destroy(h)
+
+
+def hilbert_keys_2d(xh, yh, order):
+    """hilbert_key_2d (phd/hilbert/hilbert.pyx:9-23) in C++ for int32 arrays."""
+    xh = np.ascontiguousarray(xh, dtype=np.int32)
+    yh = np.ascontiguousarray(yh, dtype=np.int32)
+    keys = np.zeros(xh.shape, dtype=np.int64)
+    lib().phd_hilbert_keys_2d_host(_p(xh), _p(yh), int(xh.size), int(order), _p(keys))
+    return keys

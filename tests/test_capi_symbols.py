@@ -1,5 +1,6 @@
-"""The C-ABI library builds for sm_103a, loads, and exports every entry point that
-include/phdflux.h declares (no kernel is launched: this runs without a GPU)."""
+"""The C-ABI libraries build (libphdflux.so for sm_103a, libphdtess.so for the host),
+load, and export every entry point that include/phdflux.h and include/phdtess.h
+declare (no kernel is launched: this runs without a GPU)."""
 import ctypes
 import os
 import re
@@ -12,15 +13,17 @@ from phd_code_gb300 import _lib
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared():
-    names = set()
-    inc = os.path.join(ROOT, "include")
-    for fn in os.listdir(inc):
-        if fn.endswith(".h"):
-            text = open(os.path.join(inc, fn)).read()
-            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-            names |= set(re.findall(r"\b(phd_[a-z0-9_]+)\s*\(", text))
-    return sorted(names)
+HEADERS = {"phdflux.h": "libphdflux.so", "phdtess.h": "libphdtess.so"}
+
+
+def declared(header="phdflux.h"):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(phd_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_header_has_a_library():
+    assert sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h")) == sorted(HEADERS)
 
 
 @pytest.fixture(scope="module")
@@ -38,6 +41,16 @@ def test_every_declared_symbol_is_exported(lib):
     assert len(names) >= 10
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_tessellation_library_exports(lib):
+    from phd_code_gb300 import tess
+    names = declared("phdtess.h")
+    assert len(names) >= 10
+    t = ctypes.CDLL(tess.LIB_PATH)
+    missing = [n for n in names if not hasattr(t, n)]
+    assert not missing, missing
+    assert set(names) <= set(tess._SIGNATURES), set(names) - set(tess._SIGNATURES)
 
 
 def test_binding_covers_declarations(lib):
