@@ -69,13 +69,58 @@ class DeviceMesh:
         L.check(L.lib().phd_flip_mask(self.dim, self.n_cells, L.ptr(self.type), L.ptr(self.x),
                                       xmin, xmax, int(self.boundary == "reflective"),
                                       L.ptr(self.flip), L.stream_handle(stream)), "phd_flip_mask")
+        self._real_type = np.ascontiguousarray(host.type[:self.n_real], dtype=np.int8)
+        self._store = {}
         s = L.PhdMesh()
+        self.struct = s
+        self.ref = C.byref(s)
+        self._point_struct()
+
+    def _point_struct(self):
+        s = self.struct
         s.dim, s.n_cells, s.n_real, s.n_faces = self.dim, self.n_cells, self.n_real, self.n_faces
         for name in ("tag", "map", "flip", "x", "dcom", "vol", "pair_i", "pair_j", "area", "com",
                      "normal", "nbr_ptr", "nbr_idx"):
             setattr(s, name, getattr(self, name).data_ptr())
-        self.struct = s
-        self.ref = C.byref(s)
+
+    # arrays per cell / per face: (name, shape(dim, n_cells, n_faces), dtype)
+    _SIZED = (("tag", lambda d, n, F: (n,), torch.int8), ("type", lambda d, n, F: (n,), torch.int8),
+              ("map", lambda d, n, F: (n,), torch.int32), ("flip", lambda d, n, F: (n,), torch.int8),
+              ("x", lambda d, n, F: (d, n), F64), ("dcom", lambda d, n, F: (d, n), F64),
+              ("vol", lambda d, n, F: (n,), F64), ("pair_i", lambda d, n, F: (F,), torch.int32),
+              ("pair_j", lambda d, n, F: (F,), torch.int32), ("area", lambda d, n, F: (F,), F64),
+              ("com", lambda d, n, F: (d, F), F64), ("normal", lambda d, n, F: (d, F), F64),
+              ("nbr_ptr", lambda d, n, F: (n + 1,), torch.int32),
+              ("nbr_idx", lambda d, n, F: (2 * F,), torch.int32))
+
+    def resize(self, n_cells, n_faces):
+        """Re-shape every per-cell and per-face array for a tessellation with other
+        cell / face counts (the real cells stay: only the ghosts and faces change).
+        Storage grows with 1/8 headroom and is reused while it is large enough; the
+        contents are undefined afterwards (a full upload follows).  Returns True when
+        any array moved to new storage."""
+        n_cells, n_faces = int(n_cells), int(n_faces)
+        if n_cells < self.n_real:
+            raise ValueError("a tessellation holds at least its real cells")
+        moved = False
+        for name, shape_of, dt in self._SIZED:
+            shape = shape_of(self.dim, n_cells, n_faces)
+            need = int(np.prod(shape))
+            store = self._store.get(name)
+            if store is None:
+                store = getattr(self, name).reshape(-1)
+            if store.numel() < max(need, 1):
+                store = torch.empty(need + need // 8 + 16, dtype=dt, device=self.device)
+                moved = True
+            self._store[name] = store
+            setattr(self, name, store[:need].view(shape))
+        if hasattr(self, "_csr_work"):
+            need = int(L.lib().phd_csr_work_ints(n_cells))
+            if self._csr_work.numel() < need:
+                self._csr_work = torch.empty(need + need // 8 + 16, dtype=torch.int32, device=self.device)
+        self.n_cells, self.n_faces = n_cells, n_faces
+        self._point_struct()
+        return moved
 
     # --- per-step hand-over of a new tessellation of the same size -----------------
     UPLOAD = (("tag", np.int8), ("type", np.int8), ("map", np.int32), ("x", np.float64),
@@ -84,15 +129,23 @@ class DeviceMesh:
 
     def pinned_host(self, host=None):
         """Pinned host copies of a host mesh's per-step arrays (the face list and the
-        cell geometry a host re-mesh writes, ``mesh.pyx:255-323``)."""
+        cell geometry a host re-mesh writes, ``mesh.pyx:255-323``).  A re-mesh keeps the
+        real cells -- same count and order, identity map, tags and types -- and re-creates
+        the ghosts (tagged Ghost, type Exterior); the ghost and face counts may change."""
         host = self.host if host is None else host
         nr = self.n_real
         if (host.n_real != nr or not np.array_equal(host.map[:nr], np.arange(nr)) or
-                not np.array_equal(host.tag, self.host.tag) or not np.array_equal(host.type, self.host.type)):
-            raise ValueError("a re-mesh keeps the real cells (same count and order, identity map) and the "
-                             "tags / types of every row")
+                np.any(host.tag[:nr] != 0) or not np.array_equal(host.type[:nr], self._real_type) or
+                np.any(host.tag[nr:] != 1) or np.any(host.type[nr:] != 2)):
+            raise ValueError("a re-mesh keeps the real cells (same count and order, identity map, tags and "
+                             "types) and re-creates the ghosts as Ghost / Exterior rows")
         return {nm: torch.from_numpy(np.ascontiguousarray(getattr(host, nm), dtype=dt)).pin_memory()
                 for nm, dt in self.UPLOAD}
+
+    @staticmethod
+    def pinned_sizes(pinned):
+        """(n_cells, n_faces) of a pinned hand-over."""
+        return int(pinned["map"].shape[0]), int(pinned["pair_i"].shape[0])
 
     def check_upload(self, pinned):
         """Raise unless the pinned arrays have this mesh's cell and face counts."""

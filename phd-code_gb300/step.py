@@ -93,12 +93,76 @@ class FluxStepper:
         L.check(L.lib().phd_time_step_f64(self.dmesh.ref, L.ptr(self.prim), p.gamma, p.cfl, p.boost, 0,
                                           self.clock.ptr, L.stream_handle(self.stream)), "phd_time_step_f64")
 
+    def _resize(self, n_cells, n_faces):
+        """Re-shape the mesh and every state / work array for new ghost and face counts.
+        The real cells' conserved totals are carried over (their rows are re-strided
+        through the second buffer); everything else is recomputed by the hand-over.
+        A captured CUDA graph no longer matches and is dropped."""
+        dm = self.dmesh
+        nr, d = dm.n_real, dm.dim
+        nf = d + 2
+        F1 = max(n_faces, 1)
+        old_cons = self.cons
+        dm.resize(n_cells, n_faces)
+        if not hasattr(self, "_store"):
+            self._store = {}
+
+        def view(name, shape, dtype):
+            need = int(np.prod(shape))
+            store = self._store.get(name)
+            if store is None:
+                store = getattr(self, name).reshape(-1)
+            if store.numel() < need:
+                store = torch.empty(need + need // 8 + 16, dtype=dtype, device=self.device)
+            self._store[name] = store
+            return store[:need].view(shape)
+
+        f64, f32, i32 = torch.float64, torch.float32, torch.int32
+        # the two conserved-state buffers swap every step: find which storage holds the
+        # current state, re-stride its real rows into the other one
+        stores = getattr(self, "_cons_stores", None) or [self.cons.reshape(-1), self.cons_next.reshape(-1)]
+        a, b = stores if stores[0].data_ptr() == old_cons.data_ptr() else stores[::-1]
+        need = nf * n_cells
+        if b.numel() < need:
+            b = torch.empty(need + need // 8 + 16, dtype=f64, device=self.device)
+        nxt = b[:need].view(nf, n_cells)
+        for q in range(nf):
+            nxt[q, :nr].copy_(old_cons[q, :nr])
+        if a.numel() < need:
+            a = torch.empty(need + need // 8 + 16, dtype=f64, device=self.device)
+        self.cons, self.cons_next = nxt, a[:need].view(nf, n_cells)
+        self._cons_stores = [b, a]
+        if self.precision == "fp64":
+            self.prim = view("prim", (nf, n_cells), f64)
+            self.grad = view("grad", (nf * d, n_cells), f64)
+            self.w = view("w", (d, n_cells), f64)
+            self.face_w = view("face_w", (d, n_faces), f64)
+            if not self.moving:
+                self.face_w.zero_()
+            self.flux = view("flux", (nf, F1), f64)
+        else:
+            self.twin = view("twin", (n_faces,), i32)
+            self.face_geo = view("face_geo", (F1, 4), f32)
+            self.face_ar = view("face_ar", (F1, 2), f32)
+            self.csr_face = view("csr_face", (max(2 * n_faces, 1),), i32)
+            self.csr_nbr = view("csr_nbr", (max(2 * n_faces, 1),), i32)
+            self.cell_geo = view("cell_geo", (n_cells, 4), f32)
+            self.prim4 = view("prim4", (n_cells, 4), f32)
+            self.grad8 = view("grad8", (n_cells, 8), f32)
+            self.w2 = view("w2", (n_cells, 2), f32)
+            self.flux4 = view("flux4", (F1, 4), f32)
+            self.geo = L.PhdGeom32(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
+                                                              self.csr_nbr, self.cell_geo)))
+        self._graph = None
+        self._graph_steps = 0
+
     def load_mesh(self, pinned):
         """Continue on a new tessellation handed over from pinned host buffers
-        (``DeviceMesh.pinned_host`` layout; same cell and face counts, real cells in
-        the same order, as after the host re-mesh of ``integrate.py:410-417`` -- so the
-        real cells' tags, types and identity map do not change and only the ghost part
-        of the map is copied).
+        (``DeviceMesh.pinned_host`` layout), as after the host re-mesh of
+        ``integrate.py:410-417``: the real cells keep their order, tags, types and
+        identity map; the ghosts are re-created and their number, like the number of
+        faces, may change -- the arrays are then re-shaped (``_resize``) and the tags,
+        types and whole map copied, otherwise only the ghost part of the map is.
 
         The device forms the neighbour lists, flip bits and, for FP32, the periodic twin
         table and FP32 geometry (normals, cell volumes and centroids included, so FP32
@@ -109,10 +173,16 @@ class FluxStepper:
         codes and face geometry are formed on a second stream while the rest of the mesh
         is still being copied.  Returns the bytes copied."""
         dm, p = self.dmesh, self.params
+        main = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        n_new, f_new = dm.pinned_sizes(pinned)
+        resized = (n_new, f_new) != (dm.n_cells, dm.n_faces)
+        if resized:
+            main.synchronize()            # storage may be released: nothing may still read it
+            with torch.cuda.stream(main):
+                self._resize(n_new, f_new)
         dm.check_upload(pinned)
         lib = L.lib()
         fp32 = self.precision == "fp32"
-        main = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
         if getattr(self, "_side", None) is None:
             self._side = torch.cuda.Stream(self.device)
             self._ev = [torch.cuda.Event() for _ in range(4)]
@@ -129,7 +199,10 @@ class FluxStepper:
         ev[0].record(main)
         side.wait_event(ev[0])
         dm.build_lists(side)
-        nbytes += dm.copy_fields(pinned, ("x",), main) + dm.copy_ghost_map(pinned, main)
+        if resized:
+            nbytes += dm.copy_fields(pinned, ("x", "tag", "type", "map"), main)
+        else:
+            nbytes += dm.copy_fields(pinned, ("x",), main) + dm.copy_ghost_map(pinned, main)
         ev[1].record(main)
         if fp32:
             side.wait_event(ev[1])

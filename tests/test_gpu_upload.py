@@ -178,3 +178,72 @@ def test_cell_geometry_from_faces_matches_host_volumes(boundary):
     assert np.max(np.abs(gb[:, :2] - ga[:, :2])) <= 1e-6 * dx          # dcom
     for k in range(4):                                                 # faces and lists unchanged
         assert torch.equal(a[k], b[k])
+
+
+def _moved_meshes(n, boundary, seed, count):
+    """Tessellations of the same real cells (same count and order) at new generator
+    positions -- a lattice jittered by up to 0.4 spacings, drawn afresh per re-mesh --
+    so the ghost and face counts change from one mesh to the next."""
+    out = []
+    for k in range(count):
+        x = pkg.meshgen.jittered_lattice(n, jitter=0.4, seed=seed + k)
+        m, _ = pkg.meshgen.build_mesh(x, boundary, hilbert=False)
+        out.append(m)
+    return out
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+def test_load_mesh_with_changing_counts_fp64_follows_the_oracle(boundary):
+    meshes = _moved_meshes(18, boundary, 7, 5)
+    assert len({(m.n_cells, m.n_faces) for m in meshes}) > 1
+    prim = smooth_state(meshes[0])
+    st = FluxStepper(meshes[0], prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp64")
+    for k in range(1, len(meshes)):
+        st.step(1)
+        st.load_mesh(st.dmesh.pinned_host(meshes[k]))
+        assert (st.dmesh.n_cells, st.dmesh.n_faces) == (meshes[k].n_cells, meshes[k].n_faces)
+    st.check_status()
+    assert st.dmesh.upload_errors() == 0
+    c, p = _oracle_replay(meshes, prim, 1.4)
+    nr = meshes[0].n_real
+    assert rel_rows(st.cons_host()[:, :nr], c[:, :nr]) <= FP64_TOL
+    assert rel_rows(st.prim_host(), p) <= FP64_TOL
+
+
+def test_load_mesh_with_changing_counts_fp32_conserves_and_replays():
+    """FP32 through re-meshes with changing counts: exact exchange of mass and energy,
+    density close to the FP64 oracle, and a CUDA graph captured after the last
+    re-shape replays the same steps as direct launches."""
+    meshes = _moved_meshes(24, "periodic", 8, 5)
+    assert len({(m.n_cells, m.n_faces) for m in meshes}) > 1
+    prim = smooth_state(meshes[0])
+    st = FluxStepper(meshes[0], prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32")
+    nr = meshes[0].n_real
+    c0 = st.cons_host()[:, :nr].sum(axis=1)
+    for k in range(1, len(meshes)):
+        st.step(1)
+        st.load_mesh(st.dmesh.pinned_host(meshes[k]))
+    st.check_status()
+    cons = st.cons_host()[:, :nr]
+    c1 = cons.sum(axis=1)
+    for q in (0, 3):
+        assert abs(c1[q] - c0[q]) <= 1e-12 * abs(c0[q])
+    c, _ = _oracle_replay(meshes, prim, 1.4)
+    vol = meshes[-1].vol[:nr]
+    assert np.mean(np.abs(cons[0] / vol - c[0, :nr] / vol)) <= 1e-5
+    # graph after the re-shape: 4 captured steps == 4 direct steps
+    clock0 = st.clock.buf.clone()
+    cons0, prim0 = st.cons.clone(), st.prim4.clone()
+    st.step(4)
+    torch.cuda.synchronize()
+    direct = st.cons_host()
+    st.clock.buf.copy_(clock0)
+    st.cons.copy_(cons0)
+    st.prim4.copy_(prim0)
+    st.capture(4)
+    st.clock.buf.copy_(clock0)
+    st.cons.copy_(cons0)
+    st.prim4.copy_(prim0)
+    st.replay()
+    torch.cuda.synchronize()
+    assert np.array_equal(st.cons_host(), direct)
