@@ -507,15 +507,18 @@ def adjoint_cost(dev, n_side=128, n_steps=200, checkpoint=20, n_dirs=16, h=1e-6,
 
 def run_e2e(args, st, mesh, prim, dev):
     """The same step through the public API with host buffers: every step the host
-    hands over its tessellation (face list: pair-i/j, area, centroid; cell geometry:
-    x, dcom, vol, tag, type, map) from pinned memory with FluxStepper.load_mesh, which
-    forms the neighbour lists, flip bits, periodic twins and FP32 geometry on the
-    device, re-creates the ghosts and recovers the primitives; the step runs; the
-    generator velocities (what the host re-mesh needs) and the clock come back."""
+    hands over its tessellation from pinned memory with FluxStepper.load_mesh -- for
+    FP32 the compact hand-over (per-cell face ranges, pair-j, FP32 area and centroid
+    offset, positions, ghost map: 16 B per face), for FP64 the full one (pair-i/j,
+    FP64 area and centroid, x, dcom, vol, map) -- which forms the neighbour lists, flip
+    bits, periodic twins and FP32 geometry on the device, re-creates the ghosts and
+    recovers the primitives; the step runs; the generator velocities (what the host
+    re-mesh needs) and the clock come back."""
     import torch
     from phd_code_gb300 import _lib as L
     dm = st.dmesh
-    pinned = dm.pinned_host(mesh)
+    fp32 = st.precision == "fp32"
+    pinned = dm.pinned_host_compact(mesh) if fp32 else dm.pinned_host(mesh)
     w_host = torch.empty_like(st.w2 if st.precision == "fp32" else st.w, device="cpu").pin_memory()
     clk_host = torch.empty(L.CLOCK_BYTES, dtype=torch.uint8).pin_memory()
     d2h = w_host.numel() * w_host.element_size() + clk_host.numel()
@@ -552,9 +555,11 @@ def run_e2e(args, st, mesh, prim, dev):
     return {"value": rate, "unit": UNIT,
             "h2d_bytes_per_step": int(h2d[0]), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": ms_max / args.e2e_steps, "steps": args.e2e_steps,
-            "what": "per step: host tessellation (face list + cell geometry) H2D from pinned memory; neighbour "
-                    "lists, flip bits, periodic twins, FP32 geometry, ghost refresh and primitives formed on the "
-                    "device; flux step; generator velocities + clock D2H"}
+            "what": "per step: host tessellation H2D from pinned memory (%s); neighbour lists, flip bits, "
+                    "periodic twins, FP32 geometry, ghost refresh and primitives formed on the device; flux step; "
+                    "generator velocities + clock D2H" % ("compact FP32 face list: per-cell face ranges, pair-j, "
+                                                           "FP32 area and centroid offset; FP64 positions, ghost map"
+                                                           if fp32 else "face list + cell geometry, FP64")}
 
 
 def run_ensemble(args, rank, world):

@@ -240,6 +240,22 @@ int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *o
 int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out,
                           int32_t parts, cudaStream_t stream);
 
+/* Compact FP32 hand-over of a re-mesh (the per-step upload of the face list,
+ * mesh.pyx:255-323, in 16 B per face instead of 32): the host sends pair-j, the area
+ * and the centroid offset com - (x_i + x_j)/2 (formed in FP64) rounded once to FP32,
+ * and pair-i as per-real-cell face ranges.
+ *
+ * phd_pair_i_from_face_ptr: pair_i[m] = c for m in [face_ptr[c], face_ptr[c+1]);
+ * face_ptr (n_real + 1 entries) must start at 0, end at n_faces and not decrease --
+ * each real cell whose range breaks that adds 1 to *bad (device) and writes nothing.
+ * phd_prepare_f32_faces_compact: out->face_geo / face_ar as PHD_PREP_FACES forms them,
+ * from area32 [F] and crel32 [F][2] instead of mesh->area / com (needs pair ids and
+ * x); the values equal PHD_PREP_FACES's bit for bit. */
+int phd_pair_i_from_face_ptr(const phd_mesh *mesh, const int32_t *face_ptr, int32_t *pair_i, int32_t *bad,
+                             cudaStream_t stream);
+int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, const float *crel32,
+                                  phd_geom32_out *out, cudaStream_t stream);
+
 /* FP64 totals -> FP32 primitive cells prim4 [n][4] (rho, v_x, v_y, p) and clk->dt from
  * the CFL minimum (clock not advanced). */
 int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4,

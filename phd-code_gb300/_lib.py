@@ -118,6 +118,8 @@ SIGNATURES = {
     "phd_face_normals_f64": ([_PM, _vp, _vp, _vp], C.c_int),
     "phd_csr_work_ints": ([_i32], C.c_size_t),
     "phd_build_csr": ([_PM, _vp, _vp, _vp, _vp, _vp], C.c_int),
+    "phd_pair_i_from_face_ptr": ([_PM, _vp, _vp, _vp, _vp], C.c_int),
+    "phd_prepare_f32_faces_compact": ([_PM, _vp, _vp, C.POINTER(PhdGeom32Out), _vp], C.c_int),
     "phd_periodic_twins": ([_PM, _i32, _f64, _f64, _vp, _vp], C.c_int),
 }
 

@@ -35,6 +35,16 @@ __device__ __forceinline__ void set_status32(phd_clock *clk, int bits) {
 // taken in FP64 and rounded once to FP32; everything formed from them afterwards
 // (separation length, normal when the mesh carries none, 1/V, R) is FP32.  The
 // FP64 -> FP32 roundings use integer arithmetic (narrow_f64), off the FP64 pipe.
+// Separation length and unit normal from the FP32-rounded separation, with the IEEE
+// operations spelled out (fast-math would let each kernel pick its own sqrt /
+// reciprocal sequence): every kernel that forms them gets the same bits.
+__device__ __forceinline__ void face_normal32(float fx, float fy, float &r, float &nx, float &ny) {
+    r = __fsqrt_rn(__fmaf_rn(fx, fx, __fmul_rn(fy, fy)));
+    const float inv = r > 0.f ? __frcp_rn(r) : 0.f;
+    nx = __fmul_rn(fx, inv);
+    ny = __fmul_rn(fy, inv);
+}
+
 __global__ void k_prepare_faces32(phd_mesh M, float4 *__restrict__ face_geo, float2 *__restrict__ face_ar) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M.n_faces) return;
@@ -49,18 +59,54 @@ __global__ void k_prepare_faces32(phd_mesh M, float4 *__restrict__ face_geo, flo
         cy = M.com[(size_t)F + m] - 0.5 * (yi + yj);
     }
     const float fx = narrow_f64(dx), fy = narrow_f64(dy);
-    const float r = sqrtf(fx * fx + fy * fy);
-    float nx, ny;
+    float r, nx, ny;                // n = (x_j - x_i)/|x_j - x_i| (tess.cpp:367-369)
+    face_normal32(fx, fy, r, nx, ny);
     if (M.normal) {
         nx = narrow_f64(M.normal[m]);
         ny = narrow_f64(M.normal[(size_t)F + m]);
-    } else {                       // n = (x_j - x_i)/|x_j - x_i| (tess.cpp:367-369)
-        const float inv = r > 0.f ? 1.f / r : 0.f;
-        nx = fx * inv;
-        ny = fy * inv;
     }
     face_geo[m] = make_float4(nx, ny, narrow_f64(cx), narrow_f64(cy));
     face_ar[m] = make_float2(narrow_f64(M.area[m]), r);
+}
+
+// The same face geometry from the compact FP32 hand-over: the host rounds the area and
+// the centroid offset com - (x_i + x_j)/2 (formed in FP64 as above) once to FP32, so
+// the face record crosses the link in 16 bytes (pair-j, area, offset) instead of 32;
+// separations and normals still come from the FP64 positions.
+__global__ void k_prepare_faces32_compact(phd_mesh M, const float *__restrict__ area32,
+                                          const float2 *__restrict__ crel32, float4 *__restrict__ face_geo,
+                                          float2 *__restrict__ face_ar) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M.n_faces) return;
+    const int n = M.n_cells;
+    const int i = M.pair_i[m], j = M.pair_j[m];
+    double dx = 0, dy = 0;
+    if (i >= 0 && i < n && j >= 0 && j < n) {
+        dx = M.x[j] - M.x[i];
+        dy = M.x[(size_t)n + j] - M.x[(size_t)n + i];
+    }
+    const float fx = narrow_f64(dx), fy = narrow_f64(dy);
+    float r, nx, ny;
+    face_normal32(fx, fy, r, nx, ny);
+    const float2 c = crel32[m];
+    face_geo[m] = make_float4(nx, ny, c.x, c.y);
+    face_ar[m] = make_float2(area32[m], r);
+}
+
+// pair-i of every face from the per-real-cell face ranges (faces are emitted per real
+// cell in ascending cell order, tess.cpp:363): face_ptr[0] = 0, face_ptr[n_real] =
+// n_faces, non-decreasing -- then the ranges tile the face list exactly; a range that
+// breaks this is counted in *bad and left unwritten.
+__global__ void k_pair_i_from_ptr(int n_real, int n_faces, const int32_t *__restrict__ face_ptr,
+                                  int32_t *__restrict__ pair_i, int32_t *bad) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_real) return;
+    const int a = face_ptr[c], b = face_ptr[c + 1];
+    if (a < 0 || b < a || b > n_faces || (c == 0 && a != 0) || (c == n_real - 1 && b != n_faces)) {
+        atomicAdd(bad, 1);
+        return;
+    }
+    for (int m = a; m < b; m++) pair_i[m] = c;
 }
 
 __global__ void k_prepare_cells32(phd_mesh M, float4 *__restrict__ cell_geo) {
@@ -727,6 +773,24 @@ int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_
         k_cells_from_faces32<<<g32(mesh->n_cells), B32, 0, stream>>>(
             *mesh, reinterpret_cast<const float4 *>(out->face_geo), reinterpret_cast<const float2 *>(out->face_ar),
             out->csr_face, reinterpret_cast<float4 *>(out->cell_geo));
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, const float *crel32,
+                                  phd_geom32_out *out, cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || !out || !out->face_geo || !out->face_ar) return PHD_ERR_ARG;
+    if (mesh->n_faces && (!area32 || !crel32 || !mesh->pair_i || !mesh->pair_j || !mesh->x)) return PHD_ERR_ARG;
+    if (mesh->n_faces)
+        k_prepare_faces32_compact<<<g32(mesh->n_faces), B32, 0, stream>>>(
+            *mesh, area32, reinterpret_cast<const float2 *>(crel32), reinterpret_cast<float4 *>(out->face_geo),
+            reinterpret_cast<float2 *>(out->face_ar));
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+int phd_pair_i_from_face_ptr(const phd_mesh *mesh, const int32_t *face_ptr, int32_t *pair_i, int32_t *bad,
+                             cudaStream_t stream) {
+    if (!mesh || !face_ptr || !pair_i || !bad || mesh->n_real < 1 || mesh->n_faces < 0) return PHD_ERR_ARG;
+    k_pair_i_from_ptr<<<g32(mesh->n_real), B32, 0, stream>>>(mesh->n_real, mesh->n_faces, face_ptr, pair_i, bad);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 

@@ -127,33 +127,68 @@ class DeviceMesh:
               ("dcom", np.float64), ("vol", np.float64), ("pair_i", np.int32), ("pair_j", np.int32),
               ("area", np.float64), ("com", np.float64))
 
-    def pinned_host(self, host=None):
-        """Pinned host copies of a host mesh's per-step arrays (the face list and the
-        cell geometry a host re-mesh writes, ``mesh.pyx:255-323``).  A re-mesh keeps the
-        real cells -- same count and order, identity map, tags and types -- and re-creates
-        the ghosts (tagged Ghost, type Exterior); the ghost and face counts may change."""
-        host = self.host if host is None else host
+    def _check_remesh(self, host):
         nr = self.n_real
         if (host.n_real != nr or not np.array_equal(host.map[:nr], np.arange(nr)) or
                 np.any(host.tag[:nr] != 0) or not np.array_equal(host.type[:nr], self._real_type) or
                 np.any(host.tag[nr:] != 1) or np.any(host.type[nr:] != 2)):
             raise ValueError("a re-mesh keeps the real cells (same count and order, identity map, tags and "
                              "types) and re-creates the ghosts as Ghost / Exterior rows")
+
+    def pinned_host(self, host=None):
+        """Pinned host copies of a host mesh's per-step arrays (the face list and the
+        cell geometry a host re-mesh writes, ``mesh.pyx:255-323``).  A re-mesh keeps the
+        real cells -- same count and order, identity map, tags and types -- and re-creates
+        the ghosts (tagged Ghost, type Exterior); the ghost and face counts may change."""
+        host = self.host if host is None else host
+        self._check_remesh(host)
         return {nm: torch.from_numpy(np.ascontiguousarray(getattr(host, nm), dtype=dt)).pin_memory()
                 for nm, dt in self.UPLOAD}
 
+    def pinned_host_compact(self, host):
+        """The compact hand-over of a re-mesh for the FP32 path, 16 B per face instead of
+        32: per-real-cell face ranges ``face_ptr`` instead of pair-i (faces are emitted
+        per real cell in ascending order, tess.cpp:363), pair-j, and the area and the
+        centroid offset com - (x_i + x_j)/2 -- formed in FP64 as the device would --
+        rounded once to FP32 (round to nearest even; magnitudes below 2^-126 to signed
+        zero, as the device's own rounding does), plus the cells' positions and maps.
+        The FP32 face geometry formed from it equals the full hand-over's bit for bit."""
+        self._check_remesh(host)
+        nr = self.n_real
+        pi, pj = np.asarray(host.pair_i), np.asarray(host.pair_j)
+        if pi.size and (np.any(np.diff(pi) < 0) or pi[0] < 0 or pi[-1] >= nr):
+            raise ValueError("faces must be emitted per real cell in ascending cell order")
+        face_ptr = np.searchsorted(pi, np.arange(nr + 1)).astype(np.int32)
+        x = np.asarray(host.x, dtype=np.float64)
+        c64 = np.asarray(host.com, dtype=np.float64) - 0.5 * (x[:, pi] + x[:, pj])
+
+        def round32(a):
+            out = a.astype(np.float32)
+            return np.where(np.abs(a) < 2.0 ** -126, np.copysign(np.float32(0.0), out), out).astype(np.float32)
+
+        arrays = {"face_ptr": face_ptr, "pair_j": np.ascontiguousarray(pj, dtype=np.int32),
+                  "area32": round32(np.asarray(host.area, dtype=np.float64)),
+                  "crel32": np.ascontiguousarray(round32(c64).T),
+                  "x": np.ascontiguousarray(x), "map": np.ascontiguousarray(host.map, dtype=np.int32),
+                  "tag": np.ascontiguousarray(host.tag, dtype=np.int8),
+                  "type": np.ascontiguousarray(host.type, dtype=np.int8)}
+        return {k: torch.from_numpy(v).pin_memory() for k, v in arrays.items()}
+
     @staticmethod
     def pinned_sizes(pinned):
-        """(n_cells, n_faces) of a pinned hand-over."""
-        return int(pinned["map"].shape[0]), int(pinned["pair_i"].shape[0])
+        """(n_cells, n_faces) of a pinned hand-over (full or compact)."""
+        return int(pinned["map"].shape[0]), int(pinned["pair_j"].shape[0])
 
     def check_upload(self, pinned):
         """Raise unless the pinned arrays have this mesh's cell and face counts."""
         shapes = {"tag": (self.n_cells,), "type": (self.n_cells,), "map": (self.n_cells,),
                   "x": (self.dim, self.n_cells), "dcom": (self.dim, self.n_cells), "vol": (self.n_cells,),
                   "pair_i": (self.n_faces,), "pair_j": (self.n_faces,), "area": (self.n_faces,),
-                  "com": (self.dim, self.n_faces)}
-        for nm, _ in self.UPLOAD:
+                  "com": (self.dim, self.n_faces), "face_ptr": (self.n_real + 1,), "area32": (self.n_faces,),
+                  "crel32": (self.n_faces, self.dim)}
+        names = (("face_ptr", "pair_j", "area32", "crel32", "x", "map", "tag", "type") if "face_ptr" in pinned
+                 else [nm for nm, _ in self.UPLOAD])
+        for nm in names:
             if tuple(pinned[nm].shape) != shapes[nm]:
                 raise ValueError("upload: %s has shape %s, this mesh holds %s" % (nm, tuple(pinned[nm].shape),
                                                                                  shapes[nm]))

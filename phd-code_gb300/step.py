@@ -93,6 +93,20 @@ class FluxStepper:
         L.check(L.lib().phd_time_step_f64(self.dmesh.ref, L.ptr(self.prim), p.gamma, p.cfl, p.boost, 0,
                                           self.clock.ptr, L.stream_handle(self.stream)), "phd_time_step_f64")
 
+    def _view(self, name, shape, dtype):
+        """``shape`` view of the named array's storage, which grows (1/8 headroom) when
+        too small; the contents are undefined after growth."""
+        if not hasattr(self, "_store"):
+            self._store = {}
+        need = int(np.prod(shape))
+        store = self._store.get(name)
+        if store is None and hasattr(self, name):
+            store = getattr(self, name).reshape(-1)
+        if store is None or store.numel() < need:
+            store = torch.empty(need + need // 8 + 16, dtype=dtype, device=self.device)
+        self._store[name] = store
+        return store[:need].view(shape)
+
     def _resize(self, n_cells, n_faces):
         """Re-shape the mesh and every state / work array for new ghost and face counts.
         The real cells' conserved totals are carried over (their rows are re-strided
@@ -104,18 +118,7 @@ class FluxStepper:
         F1 = max(n_faces, 1)
         old_cons = self.cons
         dm.resize(n_cells, n_faces)
-        if not hasattr(self, "_store"):
-            self._store = {}
-
-        def view(name, shape, dtype):
-            need = int(np.prod(shape))
-            store = self._store.get(name)
-            if store is None:
-                store = getattr(self, name).reshape(-1)
-            if store.numel() < need:
-                store = torch.empty(need + need // 8 + 16, dtype=dtype, device=self.device)
-            self._store[name] = store
-            return store[:need].view(shape)
+        view = self._view
 
         f64, f32, i32 = torch.float64, torch.float32, torch.int32
         # the two conserved-state buffers swap every step: find which storage holds the
@@ -171,7 +174,10 @@ class FluxStepper:
         primitives recovered with the new volumes and the next dt taken from them
         (steps 6-8 of the moving-mesh step).  The neighbour lists, twin table, FP32 list
         codes and face geometry are formed on a second stream while the rest of the mesh
-        is still being copied.  Returns the bytes copied."""
+        is still being copied.  ``pinned`` is either the full hand-over
+        (``DeviceMesh.pinned_host``) or, for FP32 steppers, the compact one
+        (``DeviceMesh.pinned_host_compact``: 16 B per face, pair-i from per-cell face
+        ranges).  Returns the bytes copied."""
         dm, p = self.dmesh, self.params
         main = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
         n_new, f_new = dm.pinned_sizes(pinned)
@@ -183,6 +189,9 @@ class FluxStepper:
         dm.check_upload(pinned)
         lib = L.lib()
         fp32 = self.precision == "fp32"
+        compact = "face_ptr" in pinned
+        if compact and not fp32:
+            raise ValueError("the compact hand-over carries FP32 face geometry: FP32 steppers only")
         if getattr(self, "_side", None) is None:
             self._side = torch.cuda.Stream(self.device)
             self._ev = [torch.cuda.Event() for _ in range(4)]
@@ -195,7 +204,16 @@ class FluxStepper:
         # copies on the main stream in the order the side stream needs them; the side
         # stream builds the neighbour lists, twins, list codes and face geometry meanwhile
         dm.reset_errors(main)
-        nbytes = dm.copy_fields(pinned, ("pair_i", "pair_j"), main)
+        if compact:
+            # pair-i from the per-real-cell face ranges (phd_pair_i_from_face_ptr)
+            face_ptr = self._view("face_ptr_in", (dm.n_real + 1,), torch.int32)
+            with torch.cuda.stream(main):
+                face_ptr.copy_(pinned["face_ptr"], non_blocking=True)
+            nbytes = face_ptr.numel() * 4 + dm.copy_fields(pinned, ("pair_j",), main)
+            L.check(lib.phd_pair_i_from_face_ptr(dm.ref, L.ptr(face_ptr), L.ptr(dm.pair_i), L.ptr(dm._bad), s),
+                    "phd_pair_i_from_face_ptr")
+        else:
+            nbytes = dm.copy_fields(pinned, ("pair_i", "pair_j"), main)
         ev[0].record(main)
         side.wait_event(ev[0])
         dm.build_lists(side)
@@ -212,15 +230,28 @@ class FluxStepper:
                     "phd_periodic_twins")
             L.check(lib.phd_prepare_f32_parts(dm.ref, L.ptr(self.twin), ctypes.byref(out), L.PREP_LISTS, ss),
                     "phd_prepare_f32_parts")
-        nbytes += dm.copy_fields(pinned, ("com", "area"), main)
+        if compact:
+            area32 = self._view("area32_in", (dm.n_faces,), torch.float32)
+            crel32 = self._view("crel32_in", (dm.n_faces, dm.dim), torch.float32)
+            with torch.cuda.stream(main):
+                area32.copy_(pinned["area32"], non_blocking=True)
+                crel32.copy_(pinned["crel32"], non_blocking=True)
+            nbytes += (area32.numel() + crel32.numel()) * 4
+        else:
+            nbytes += dm.copy_fields(pinned, ("com", "area"), main)
         if fp32:
             # face geometry, then the cells' volumes and centroids from it (the FP32 path
             # needs neither host volumes nor host centroids)
             ev[2].record(main)
             side.wait_event(ev[2])
             dm.set_normals("none", side)
-            L.check(lib.phd_prepare_f32_parts(dm.ref, None, ctypes.byref(out),
-                                              L.PREP_FACES | L.PREP_CELLS_FROM_FACES, ss), "phd_prepare_f32_parts")
+            if compact:
+                L.check(lib.phd_prepare_f32_faces_compact(dm.ref, L.ptr(area32), L.ptr(crel32), ctypes.byref(out),
+                                                          ss), "phd_prepare_f32_faces_compact")
+                parts = L.PREP_CELLS_FROM_FACES
+            else:
+                parts = L.PREP_FACES | L.PREP_CELLS_FROM_FACES
+            L.check(lib.phd_prepare_f32_parts(dm.ref, None, ctypes.byref(out), parts, ss), "phd_prepare_f32_parts")
         ev[3].record(side)
         if not fp32:
             nbytes += dm.copy_fields(pinned, ("dcom", "vol"), main)

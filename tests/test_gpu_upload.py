@@ -247,3 +247,46 @@ def test_load_mesh_with_changing_counts_fp32_conserves_and_replays():
     st.replay()
     torch.cuda.synchronize()
     assert np.array_equal(st.cons_host(), direct)
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+def test_compact_hand_over_equals_the_full_one(boundary):
+    """The compact FP32 hand-over (pair-i from per-cell face ranges, FP32 area and
+    centroid offset rounded on the host) forms the same FP32 geometry bit for bit, so
+    the steps that follow are identical; it moves about half the bytes."""
+    meshes = _moved_meshes(20, boundary, 3, 4)
+    prim = smooth_state(meshes[0])
+    a = FluxStepper(meshes[0], prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32")
+    b = FluxStepper(meshes[0], prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32")
+    for k in range(1, len(meshes)):
+        a.step(1)
+        b.step(1)
+        na = a.load_mesh(a.dmesh.pinned_host(meshes[k]))
+        nb = b.load_mesh(b.dmesh.pinned_host_compact(meshes[k]))
+        assert nb < 0.7 * na
+        torch.cuda.synchronize()
+        assert b.dmesh.upload_errors() == 0
+        for name in ("face_geo", "face_ar", "csr_face", "csr_nbr", "cell_geo", "twin", "prim4"):
+            assert torch.equal(getattr(a, name), getattr(b, name)), name
+        assert torch.equal(a.dmesh.pair_i, b.dmesh.pair_i)
+    a.step(3)
+    b.step(3)
+    a.check_status()
+    b.check_status()
+    assert np.array_equal(a.cons_host(), b.cons_host())
+
+
+def test_compact_hand_over_rejects_broken_face_ranges():
+    """Face ranges that do not tile the face list are counted as upload errors (and
+    never written); the stepper refuses the compact hand-over in FP64."""
+    meshes = _moved_meshes(12, "periodic", 5, 2)
+    prim = smooth_state(meshes[0])
+    st = FluxStepper(meshes[0], prim, gamma=1.4, precision="fp32")
+    pinned = st.dmesh.pinned_host_compact(meshes[1])
+    pinned["face_ptr"][5] = pinned["face_ptr"][6] + 1           # cell 5's range runs backwards
+    st.load_mesh(pinned)
+    torch.cuda.synchronize()
+    assert st.dmesh.upload_errors() >= 1
+    st64 = FluxStepper(meshes[0], prim, gamma=1.4, precision="fp64")
+    with pytest.raises(ValueError, match="FP32"):
+        st64.load_mesh(st64.dmesh.pinned_host_compact(meshes[1]))
