@@ -89,3 +89,8 @@ def test_argument_errors_are_rejected_on_the_host(lib):
                                     one, one, one, one, one, one, one, 1, None, None, None)
         assert rc == L.PHD_ERR_ARG
     assert f.phd_prim_f32_batched(ctypes.byref(m), ctypes.byref(par), one, one, one, 3, None, None) == L.PHD_ERR_ARG
+    # compact hand-over: missing ranges / outputs, and faces without their FP32 geometry
+    assert f.phd_pair_i_from_face_ptr(ctypes.byref(m), None, one, one, None) == L.PHD_ERR_ARG
+    out = L.PhdGeom32Out(1, 1, 1, 1, 1)
+    assert f.phd_prepare_f32_faces_compact(ctypes.byref(m), None, None, ctypes.byref(out), None) == L.PHD_ERR_ARG
+    assert f.phd_prepare_f32_faces_compact(None, one, one, ctypes.byref(out), None) == L.PHD_ERR_ARG
