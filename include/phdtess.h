@@ -73,6 +73,16 @@ int phd_tess2d_extract_geometry(phd_tess2d *t, double *dcom_x, double *dcom_y, d
 int phd_mesh2d_build(phd_tess2d *t, const double *x, const double *y, int n_real, int boundary, double xmin0,
                      double xmin1, double xmax0, double xmax1, double pad);
 
+/* phd_mesh2d_build with the real cells' extraction split into n_strips strips (by the
+ * generators' x quantiles) tessellated on parallel host threads; 0 chooses by the
+ * number of real cells (1 below 65,536, at most 16).  A strip tessellates every
+ * generator within a halo of it and keeps only triangles whose circumcircles lie inside
+ * the x-range its generators cover (widening the halo until they do), so the result is
+ * the whole box's tessellation; circumcentres are formed in a canonical vertex order,
+ * so faces do not depend on the strip that formed them. */
+int phd_mesh2d_build_strips(phd_tess2d *t, const double *x, const double *y, int n_real, int boundary,
+                            double xmin0, double xmin1, double xmax0, double xmax1, double pad, int n_strips);
+
 /* n_cells (real + kept ghosts), n_faces, and the pad the last build used. */
 int phd_mesh2d_sizes(const phd_tess2d *t, int32_t *n_cells, int32_t *n_faces, double *pad_used);
 

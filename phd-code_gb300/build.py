@@ -56,7 +56,7 @@ def build_tess(force=False):
     if (not force and os.path.exists(TESS_LIB) and
             os.path.getmtime(TESS_LIB) >= max(os.path.getmtime(TESS_SRC), os.path.getmtime(hdr))):
         return TESS_LIB
-    cmd = [cxx(), "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I" + INCLUDE,
+    cmd = [cxx(), "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off", "-I" + INCLUDE,
            TESS_SRC, "-o", TESS_LIB + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

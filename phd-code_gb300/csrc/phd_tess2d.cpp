@@ -6,14 +6,16 @@
 //
 //  * Delaunay triangulation by Bowyer-Watson insertion (cavity of triangles whose
 //    circumcircle strictly contains the new point, re-triangulated as a fan), inside
-//    a large enclosing triangle, with points inserted along a Hilbert curve so that
-//    the visibility walk that locates each point stays short;
+//    a large enclosing triangle, with points inserted in a biased randomised order
+//    (rounds of doubling size, each along a Hilbert curve) so that cavities stay small
+//    and the visibility walk that locates each point stays short;
 //  * robust orientation and in-circle tests: a floating-point evaluation with the
 //    forward error bounds of Shewchuk (1997, "Adaptive precision floating-point
 //    arithmetic and fast robust geometric predicates", ccwerrboundA / iccerrboundA),
 //    and, when the sign is not certain, an exact evaluation with the paper's
 //    expansion arithmetic (Two-Sum, Two-Product via fma, Grow-Expansion,
-//    Scale-Expansion with zero elimination);
+//    Scale-Expansion with zero elimination); exactly cocircular points are decided by
+//    a symbolic perturbation of the lift (incircle_sos), so the triangulation is unique;
 //  * Voronoi extraction in the conventions of Tess2d::extract_geometry
 //    (tess.cpp:238-398) and of the host mesh builder that feeds the flux path: faces
 //    per real cell in counter-clockwise neighbour order from angle -pi, volume and
@@ -25,10 +27,12 @@
 #include "phdtess.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <new>
+#include <thread>
 #include <utility>
 #include <vector>
 
@@ -152,7 +156,11 @@ int orient2d(double ax, double ay, double bx, double by, double cx, double cy) {
     return exp_sign(exp_add(exp_mul(acx, bcy), exp_neg(exp_mul(acy, bcx))));
 }
 
-// > 0 when d lies strictly inside the circle through the counter-clockwise a, b, c
+int incircle_sos(double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy);
+
+// > 0 when d lies inside the circle through the counter-clockwise a, b, c; exactly
+// cocircular points are decided by a symbolic perturbation (incircle_sos), so the
+// result is never 0 for four distinct points in general position of the lift
 int incircle(double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy) {
     const double adx = ax - dx, bdx = bx - dx, cdx = cx - dx;
     const double ady = ay - dy, bdy = by - dy, cdy = cy - dy;
@@ -177,7 +185,32 @@ int incircle(double ax, double ay, double bx, double by, double cx, double cy, d
     const Exp ka = exp_add(exp_mul(ebx, ecy), exp_neg(exp_mul(ecx, eby)));
     const Exp kb = exp_add(exp_mul(ecx, eay), exp_neg(exp_mul(eax, ecy)));
     const Exp kc = exp_add(exp_mul(eax, eby), exp_neg(exp_mul(ebx, eay)));
-    return exp_sign(exp_add(exp_add(exp_mul(la, ka), exp_mul(lb, kb)), exp_mul(lc, kc)));
+    const int sgn = exp_sign(exp_add(exp_add(exp_mul(la, ka), exp_mul(lb, kb)), exp_mul(lc, kc)));
+    return sgn != 0 ? sgn : incircle_sos(ax, ay, bx, by, cx, cy, dx, dy);
+}
+
+// Exactly cocircular a, b, c, d (a generator, its neighbour and their mirror images at
+// a wall; four lattice points): lift every point to l = x^2 + y^2 + e_p with
+// infinitesimals e_p ordered by the points' lexicographic (x, y) order (the smallest
+// point's the largest).  The in-circle determinant is linear in the lifts, so its sign
+// is that of the first non-zero coefficient in that order: e_a orient(b,c,d),
+// -e_b orient(a,c,d), e_c orient(a,b,d), -e_d orient(a,b,c).  The triangulation is then
+// the unique Delaunay triangulation of the perturbed lift -- the same whatever the
+// insertion order or the strip that builds it.
+int incircle_sos(double ax, double ay, double bx, double by, double cx, double cy, double dx, double dy) {
+    struct P { double x, y; int k; } pt[4] = {{ax, ay, 0}, {bx, by, 1}, {cx, cy, 2}, {dx, dy, 3}};
+    std::sort(pt, pt + 4, [](const P &u, const P &v) { return u.x < v.x || (u.x == v.x && u.y < v.y); });
+    for (const P &q : pt) {
+        int c = 0;
+        switch (q.k) {
+            case 0: c = orient2d(bx, by, cx, cy, dx, dy); break;
+            case 1: c = -orient2d(ax, ay, cx, cy, dx, dy); break;
+            case 2: c = orient2d(ax, ay, bx, by, dx, dy); break;
+            default: c = -orient2d(ax, ay, bx, by, cx, cy); break;
+        }
+        if (c != 0) return c;
+    }
+    return 0;
 }
 
 // ---- Hilbert key (phd/hilbert/hilbert.pyx:9-23) -------------------------------------
@@ -227,7 +260,7 @@ struct phd_tess2d {
     int last = -1;
     int n_real = 0, n_total = 0;
     // scratch for one insertion
-    std::vector<int> bad, stack;
+    std::vector<int> bad, stack, nt;
     struct BEdge { int a, b, outer, outer_k; };
     std::vector<BEdge> bnd;
     Geometry G;
@@ -344,7 +377,7 @@ struct phd_tess2d {
         // the cavity is star-shaped from p: one new triangle (p, a, b) per boundary edge
         const size_t m = bnd.size();
         if (m != bad.size() + 2) return -4;
-        std::vector<int> nt(m);
+        nt.resize(m);
         for (size_t j = 0; j < m; j++) nt[j] = j < bad.size() ? bad[j] : new_tri();
         for (size_t j = 0; j < m; j++) {
             Tri &T = tris[nt[j]];
@@ -370,7 +403,11 @@ struct phd_tess2d {
         return 0;
     }
 
-    // insert generators [begin, end) along a Hilbert curve over their bounding box
+    // insert generators [begin, end) in a biased randomised insertion order (Amenta,
+    // Choi and Rote 2003): a seeded shuffle split into rounds of doubling size, each
+    // round sorted along a Hilbert curve over the bounding box -- later rounds land inside
+    // the triangulation already built (small cavities), and consecutive points are close
+    // (short walks).  The seed is fixed, so the result is reproducible.
     int insert_range(int begin, int end) {
         if (end <= begin) return 0;
         double x0 = X[begin], x1 = X[begin], y0 = Y[begin], y1 = Y[begin];
@@ -381,17 +418,32 @@ struct phd_tess2d {
         double box = std::max(x1 - x0, y1 - y0);
         if (!(box > 0.)) box = 1.;
         const double scale = double(1 << 16) / box;
-        std::vector<std::pair<int64_t, int>> order(end - begin);
-        for (int i = begin; i < end; i++) {
-            int32_t qx = int32_t((X[i] - x0) * scale), qy = int32_t((Y[i] - y0) * scale);
-            qx = std::min<int32_t>(std::max<int32_t>(qx, 0), 65535);
-            qy = std::min<int32_t>(std::max<int32_t>(qy, 0), 65535);
-            order[i - begin] = std::make_pair(hilbert_key_2d(qx, qy, 16), i);
+        const int n = end - begin;
+        std::vector<int> perm(n);
+        for (int k = 0; k < n; k++) perm[k] = begin + k;
+        uint64_t st = 0x9E3779B97F4A7C15ull;                  // xorshift64* shuffle, fixed seed
+        for (int k = n - 1; k > 0; k--) {
+            st ^= st >> 12; st ^= st << 25; st ^= st >> 27;
+            const uint64_t r = (st * 0x2545F4914F6CDD1Dull) >> 11;
+            std::swap(perm[k], perm[int(r % uint64_t(k + 1))]);
         }
-        std::sort(order.begin(), order.end());
-        for (const auto &o : order) {
-            const int rc = insert(o.second);
-            if (rc != 0) return rc;
+        std::vector<std::pair<int64_t, int>> round;
+        int lo = 0;
+        for (int hi = std::min(n, 64); lo < n; hi = std::min(n, 2 * hi)) {
+            round.resize(hi - lo);
+            for (int k = lo; k < hi; k++) {
+                const int i = perm[k];
+                int32_t qx = int32_t((X[i] - x0) * scale), qy = int32_t((Y[i] - y0) * scale);
+                qx = std::min<int32_t>(std::max<int32_t>(qx, 0), 65535);
+                qy = std::min<int32_t>(std::max<int32_t>(qy, 0), 65535);
+                round[k - lo] = std::make_pair(hilbert_key_2d(qx, qy, 16), i);
+            }
+            std::sort(round.begin(), round.end());
+            for (const auto &o : round) {
+                const int rc = insert(o.second);
+                if (rc != 0) return rc;
+            }
+            lo = hi;
         }
         return 0;
     }
@@ -450,26 +502,76 @@ namespace {
 
 struct Edge1 {                 // one incident edge of a real cell
     int j;
-    double ang, h, ln, fx, fy, xr, yr;
+    double h, ln, fx, fy, xr, yr;
 };
 
-// incident edges of real cell i sorted counter-clockwise from -pi; false if unbounded
-bool cell_edges(const phd_tess2d &T, int i, std::vector<phd_tess2d::Spoke> &sp, std::vector<Edge1> &E,
-                std::vector<double> &ccx, std::vector<double> &ccy, std::vector<int> &cc_mark, int cc_stamp) {
+// angular order of atan2(y, x) in (-pi, pi]: lower half-plane, the positive x axis,
+// upper half-plane, the negative x axis (a signed-zero y there is -pi: first)
+inline int angle_class(double x, double y) {
+    if (y < 0.) return 1;
+    if (y > 0.) return 3;
+    if (x >= 0.) return 2;
+    return std::signbit(y) ? 0 : 4;
+}
+
+inline bool angle_less(double ax, double ay, double bx, double by) {
+    const int ca = angle_class(ax, ay), cb = angle_class(bx, by);
+    if (ca != cb) return ca < cb;
+    return ax * by - ay * bx > 0.;            // same open half-plane: b turns counter-clockwise from a
+}
+
+inline int gid_of(const int *gid, int v) { return gid ? gid[v] : v; }
+
+// circumcentre of triangle t with its vertices rotated so the smallest global id comes
+// first (the closed form of the numpy mesh builder): the same bits whichever
+// triangulation -- the whole box or a strip of it -- holds the triangle
+void circumcentre_canon(const phd_tess2d &T, const int *gid, int t, double &ux, double &uy) {
+    const Tri &tr = T.tris[t];
+    int k0 = 0;
+    for (int k = 1; k < 3; k++)
+        if (gid_of(gid, tr.v[k]) < gid_of(gid, tr.v[k0])) k0 = k;
+    const int va = tr.v[k0], vb = tr.v[(k0 + 1) % 3], vc = tr.v[(k0 + 2) % 3];
+    const double ax = T.px(va), ay = T.py(va);
+    const double bx = T.px(vb) - ax, by = T.py(vb) - ay;
+    const double cx = T.px(vc) - ax, cy = T.py(vc) - ay;
+    const double d = 2.0 * (bx * cy - by * cx);
+    const double b2 = bx * bx + by * by;
+    const double c2 = cx * cx + cy * cy;
+    ux = ax + (cy * b2 - by * c2) / d;
+    uy = ay + (bx * c2 - cx * b2) / d;
+}
+
+struct CCache {                 // circumcentres of one triangulation, formed on first use
+    std::vector<double> x, y;
+    std::vector<char> done;
+    explicit CCache(size_t n) : x(n), y(n), done(n, 0) {}
+};
+
+// incident edges of cell i (local id) sorted counter-clockwise from -pi; false if the
+// cell is unbounded, or -- when lo < hi are finite bounds -- if a circumcircle of one of
+// its triangles reaches outside the x-range [lo, hi] the triangulation's points cover
+// (then the triangle may not be Delaunay for the whole point set)
+bool cell_edges(const phd_tess2d &T, const int *gid, int i, double lo, double hi, std::vector<phd_tess2d::Spoke> &sp,
+                std::vector<Edge1> &E, CCache &C) {
     if (!T.spokes(i, sp)) return false;
     E.clear();
     auto cc = [&](int t, double &ux, double &uy) {
-        if (cc_mark[t] != cc_stamp) {
-            T.circumcentre(t, ccx[t], ccy[t]);
-            cc_mark[t] = cc_stamp;
+        if (!C.done[t]) {
+            circumcentre_canon(T, gid, t, C.x[t], C.y[t]);
+            C.done[t] = 1;
         }
-        ux = ccx[t];
-        uy = ccy[t];
+        ux = C.x[t];
+        uy = C.y[t];
     };
     for (const auto &s : sp) {
         double x1, y1, x2, y2;
         cc(s.t1, x1, y1);
         cc(s.t2, x2, y2);
+        if (lo > -INFINITY || hi < INFINITY) {
+            const double dx = x1 - T.X[i], dy = y1 - T.Y[i];
+            const double R = std::sqrt(dx * dx + dy * dy);
+            if (!(x1 - R > lo && x1 + R < hi)) return false;
+        }
         Edge1 e;
         e.j = s.j;
         e.xr = T.X[s.j] - T.X[i];
@@ -479,29 +581,39 @@ bool cell_edges(const phd_tess2d &T, int i, std::vector<phd_tess2d::Spoke> &sp, 
         e.ln = std::sqrt(xe * xe + ye * ye);
         e.fx = 0.5 * (x1 + x2);
         e.fy = 0.5 * (y1 + y2);
-        e.ang = std::atan2(e.yr, e.xr);
         E.push_back(e);
     }
-    std::sort(E.begin(), E.end(), [](const Edge1 &a, const Edge1 &b) { return a.ang < b.ang; });
+    // the circulation runs counter-clockwise: start it at the smallest angle in (-pi, pi]
+    // (atan2's range), so the edges come in ascending angle without computing one
+    size_t k0 = 0;
+    for (size_t k = 1; k < E.size(); k++)
+        if (angle_less(E[k].xr, E[k].yr, E[k0].xr, E[k0].yr)) k0 = k;
+    std::rotate(E.begin(), E.begin() + k0, E.end());
     return E.size() >= 3;
 }
 
-// faces, volumes and centroids of the real cells (extract_geometry); returns the
-// face count or -1.  Face j indices are generator ids (before any ghost pruning).
-int extract(const phd_tess2d &T, std::vector<double> &vol, std::vector<double> &dcx, std::vector<double> &dcy,
-            std::vector<double> &area, std::vector<double> &comx, std::vector<double> &comy,
-            std::vector<double> &nx, std::vector<double> &ny, std::vector<int32_t> &pi, std::vector<int32_t> &pj) {
-    const int n = T.n_real;
+struct FaceRec {                // a face owned by a real cell, before ghost pruning
+    int j;                      // global id of the other cell
+    double ln, fx, fy, nx, ny;
+};
+
+// faces, volume and centroid offset of the owned real cells (local ids, ascending global
+// ids) of one triangulation (extract_geometry): volume / dcom into the global arrays,
+// faces appended in cell order, face counts into nf[global id].  False if a cell is
+// unbounded or leaves [lo, hi] (see cell_edges).
+bool extract_cells(const phd_tess2d &T, const int *gid, const std::vector<int> &owned, double lo, double hi,
+                   double *vol, double *dcx, double *dcy, std::vector<FaceRec> &faces, int32_t *nf) {
     std::vector<phd_tess2d::Spoke> sp;
     std::vector<Edge1> E;
-    std::vector<double> ccx(T.tris.size()), ccy(T.tris.size());
-    std::vector<int> cc_mark(T.tris.size(), 0);
-    vol.assign(n, 0.); dcx.assign(n, 0.); dcy.assign(n, 0.);
-    area.clear(); comx.clear(); comy.clear(); nx.clear(); ny.clear(); pi.clear(); pj.clear();
-    for (int i = 0; i < n; i++) {
-        if (!cell_edges(T, i, sp, E, ccx, ccy, cc_mark, 1)) return -1;
+    CCache C(T.tris.size());
+    faces.clear();
+    faces.reserve(3 * owned.size() + 64);
+    for (int i : owned) {
+        if (!cell_edges(T, gid, i, lo, hi, sp, E, C)) return false;
+        const int gi = gid_of(gid, i);
         const double xp = T.X[i], yp = T.Y[i];
         double v = 0., cx = 0., cy = 0.;
+        int cnt = 0;
         for (const Edge1 &e : E) {
             const double a = 0.25 * e.ln * e.h;
             const double tx = 2.0 * e.fx / 3.0 + xp / 3.0;
@@ -509,21 +621,42 @@ int extract(const phd_tess2d &T, std::vector<double> &vol, std::vector<double> &
             v += a;
             cx += a * tx;
             cy += a * ty;
-            if (e.j > i) {
-                pi.push_back(i);
-                pj.push_back(e.j);
-                area.push_back(e.ln);
-                comx.push_back(e.fx);
-                comy.push_back(e.fy);
-                nx.push_back(e.xr / e.h);
-                ny.push_back(e.yr / e.h);
+            const int gj = gid_of(gid, e.j);
+            if (gj > gi) {
+                faces.push_back({gj, e.ln, e.fx, e.fy, e.xr / e.h, e.yr / e.h});
+                cnt++;
             }
         }
-        vol[i] = v;
-        dcx[i] = cx / v - xp;
-        dcy[i] = cy / v - yp;
+        vol[gi] = v;
+        dcx[gi] = cx / v - xp;
+        dcy[gi] = cy / v - yp;
+        nf[gi] = cnt;
     }
-    return int(pi.size());
+    return true;
+}
+
+// faces, volumes and centroids of all real cells of one whole triangulation; returns
+// the face count or -1.  Face j indices are generator ids (before any ghost pruning).
+int extract(const phd_tess2d &T, std::vector<double> &vol, std::vector<double> &dcx, std::vector<double> &dcy,
+            std::vector<double> &area, std::vector<double> &comx, std::vector<double> &comy,
+            std::vector<double> &nx, std::vector<double> &ny, std::vector<int32_t> &pi, std::vector<int32_t> &pj) {
+    const int n = T.n_real;
+    std::vector<int> owned(n);
+    for (int i = 0; i < n; i++) owned[i] = i;
+    vol.assign(n, 0.); dcx.assign(n, 0.); dcy.assign(n, 0.);
+    std::vector<int32_t> nf(n, 0);
+    std::vector<FaceRec> faces;
+    if (!extract_cells(T, nullptr, owned, -INFINITY, INFINITY, vol.data(), dcx.data(), dcy.data(), faces, nf.data()))
+        return -1;
+    const size_t F = faces.size();
+    area.resize(F); comx.resize(F); comy.resize(F); nx.resize(F); ny.resize(F); pi.resize(F); pj.resize(F);
+    size_t f = 0;
+    for (int i = 0; i < n; i++)
+        for (int k = 0; k < nf[i]; k++, f++) {
+            const FaceRec &r = faces[f];
+            pi[f] = i; pj[f] = r.j; area[f] = r.ln; comx[f] = r.fx; comy[f] = r.fy; nx[f] = r.nx; ny[f] = r.ny;
+        }
+    return int(F);
 }
 
 // per-cell face lists in ascending face id (CSR over n_cells)
@@ -572,6 +705,140 @@ void make_ghosts(const double *x, const double *y, int n, int boundary, const do
                 }
             }
     }
+}
+
+// ---- strip-parallel extraction ------------------------------------------------------
+// The box is cut into K strips by the real generators' x quantiles.  Each strip is
+// tessellated on its own from every generator (real or ghost) within a halo of it;
+// a triangle of that tessellation is a triangle of the whole one when its circumcircle
+// lies inside the x-range the strip's points cover (no other generator can then fall in
+// it), which extract_cells checks for every triangle around an owned cell -- a strip
+// that fails widens its halo (up to every point).  Circumcentres are formed in a
+// canonical vertex order, so a face gets the same bits from any strip; K depends only
+// on the number of real cells, so the mesh does not depend on the thread count.
+int auto_strips(int n_real) { return n_real >= 65536 ? std::min(16, n_real / 32768) : 1; }
+
+struct StripJob {
+    double s_lo, s_hi;          // owned x-range [s_lo, s_hi)
+    bool first, last;
+    std::vector<int> owned;     // global ids, ascending
+    std::vector<FaceRec> faces;
+};
+
+int strip_pass(StripJob &J, const std::vector<double> &ax, const std::vector<double> &ay,
+               const std::vector<int> &xorder, const std::vector<double> &xsorted, double H0, double *vol,
+               double *dcx, double *dcy, int32_t *nf) {
+    if (J.owned.empty()) return 0;
+    phd_tess2d T;
+    std::vector<int> gids;
+    std::vector<int> owned_local(J.owned.size());
+    for (double H = H0;; H *= 2.0) {
+        const double lo = J.first ? -INFINITY : J.s_lo - H;
+        const double hi = J.last ? INFINITY : J.s_hi + H;
+        const size_t b = std::lower_bound(xsorted.begin(), xsorted.end(), lo) - xsorted.begin();
+        const size_t e = std::upper_bound(xsorted.begin(), xsorted.end(), hi) - xsorted.begin();
+        const bool whole = (b == 0 && e == xsorted.size());
+        gids.assign(xorder.begin() + b, xorder.begin() + e);
+        std::sort(gids.begin(), gids.end());
+        const int m = int(gids.size());
+        T.reset();
+        T.X.resize(m);
+        T.Y.resize(m);
+        double x0 = ax[gids[0]], x1 = x0, y0 = ay[gids[0]], y1 = y0;
+        for (int k = 0; k < m; k++) {
+            T.X[k] = ax[gids[k]];
+            T.Y[k] = ay[gids[k]];
+            x0 = std::min(x0, T.X[k]); x1 = std::max(x1, T.X[k]);
+            y0 = std::min(y0, T.Y[k]); y1 = std::max(y1, T.Y[k]);
+        }
+        T.inserted.assign(m, 0);
+        T.vt.assign(m, -1);
+        T.n_total = m;
+        T.n_real = 0;
+        T.init_super(x0, y0, x1, y1);
+        const int rc = T.insert_range(0, m);
+        if (rc != 0) return rc;
+        size_t q = 0;                                    // owned global ids -> local ids
+        for (size_t k = 0; k < J.owned.size(); k++) {
+            while (gids[q] != J.owned[k]) q++;
+            owned_local[k] = int(q);
+        }
+        if (extract_cells(T, gids.data(), owned_local, whole ? -INFINITY : lo, whole ? INFINITY : hi, vol, dcx,
+                          dcy, J.faces, nf))
+            return 0;
+        if (whole) return -1;                            // a real cell of the whole box is unbounded
+    }
+}
+
+// all real cells' faces, volumes and centroid offsets with K strips on up to K threads;
+// faces in (cell, angle) order with generator ids; returns the face count or an error
+int extract_strips(int K, int n_real, const std::vector<double> &ax, const std::vector<double> &ay, double H0,
+                   std::vector<double> &vol, std::vector<double> &dcx, std::vector<double> &dcy,
+                   std::vector<double> &area, std::vector<double> &comx, std::vector<double> &comy,
+                   std::vector<double> &nx, std::vector<double> &ny, std::vector<int32_t> &pi,
+                   std::vector<int32_t> &pj) {
+    const int n_all = int(ax.size());
+    std::vector<int> xorder(n_all);
+    for (int i = 0; i < n_all; i++) xorder[i] = i;
+    std::sort(xorder.begin(), xorder.end(), [&](int a, int b) { return ax[a] < ax[b] || (ax[a] == ax[b] && a < b); });
+    std::vector<double> xsorted(n_all);
+    for (int i = 0; i < n_all; i++) xsorted[i] = ax[xorder[i]];
+    std::vector<double> xr(ax.begin(), ax.begin() + n_real);
+    std::sort(xr.begin(), xr.end());
+    std::vector<StripJob> jobs(K);
+    for (int k = 0; k < K; k++) {
+        jobs[k].s_lo = k == 0 ? -INFINITY : xr[size_t(k) * n_real / K];
+        jobs[k].s_hi = k == K - 1 ? INFINITY : xr[size_t(k + 1) * n_real / K];
+        jobs[k].first = k == 0;
+        jobs[k].last = k == K - 1;
+    }
+    for (int i = 0; i < n_real; i++) {
+        int k = int(std::upper_bound(xr.begin(), xr.end(), ax[i]) - xr.begin()) * K / n_real;
+        k = std::min(std::max(k, 0), K - 1);
+        while (k > 0 && ax[i] < jobs[k].s_lo) k--;
+        while (k < K - 1 && ax[i] >= jobs[k].s_hi) k++;
+        jobs[k].owned.push_back(i);
+    }
+    vol.assign(n_real, 0.); dcx.assign(n_real, 0.); dcy.assign(n_real, 0.);
+    std::vector<int32_t> nf(n_real, 0);
+    std::atomic<int> next(0), status(0);
+    auto worker = [&]() {
+        for (;;) {
+            const int k = next.fetch_add(1);
+            if (k >= K) return;
+            int rc;
+            try {
+                rc = strip_pass(jobs[k], ax, ay, xorder, xsorted, H0, vol.data(), dcx.data(), dcy.data(), nf.data());
+            } catch (...) {
+                rc = -4;
+            }
+            if (rc != 0) {
+                int expected = 0;
+                status.compare_exchange_strong(expected, rc);
+            }
+        }
+    };
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    const int n_threads = std::min<int>(K, int(hw));
+    std::vector<std::thread> threads;
+    for (int t = 1; t < n_threads; t++) threads.emplace_back(worker);
+    worker();
+    for (auto &th : threads) th.join();
+    if (status.load() != 0) return status.load();
+    std::vector<int64_t> off(size_t(n_real) + 1, 0);
+    for (int i = 0; i < n_real; i++) off[i + 1] = off[i] + nf[i];
+    const size_t F = size_t(off[n_real]);
+    area.resize(F); comx.resize(F); comy.resize(F); nx.resize(F); ny.resize(F); pi.resize(F); pj.resize(F);
+    for (const StripJob &J : jobs) {
+        size_t r = 0;
+        for (int gi : J.owned)
+            for (int64_t f = off[gi]; f < off[gi + 1]; f++, r++) {
+                const FaceRec &rec = J.faces[r];
+                pi[f] = gi; pj[f] = rec.j; area[f] = rec.ln; comx[f] = rec.fx; comy[f] = rec.fy;
+                nx[f] = rec.nx; ny[f] = rec.ny;
+            }
+    }
+    return int(F);
 }
 
 }  // namespace
@@ -679,9 +946,15 @@ int phd_tess2d_extract_geometry(phd_tess2d *t, double *dcom_x, double *dcom_y, d
 
 int phd_mesh2d_build(phd_tess2d *t, const double *x, const double *y, int n_real, int boundary, double xmin0,
                      double xmin1, double xmax0, double xmax1, double pad) {
+    return phd_mesh2d_build_strips(t, x, y, n_real, boundary, xmin0, xmin1, xmax0, xmax1, pad, 0);
+}
+
+int phd_mesh2d_build_strips(phd_tess2d *t, const double *x, const double *y, int n_real, int boundary,
+                            double xmin0, double xmin1, double xmax0, double xmax1, double pad, int n_strips) {
     if (!t || !x || !y || n_real < 3 || (boundary != 0 && boundary != 1) || !(xmax0 > xmin0) ||
-        !(xmax1 > xmin1) || !(pad > 0.))
+        !(xmax1 > xmin1) || !(pad > 0.) || n_strips < 0 || n_strips > 256)
         return -2;
+    const int K = n_strips ? std::min(n_strips, std::max(1, n_real / 64)) : auto_strips(n_real);
     const double xmin[2] = {xmin0, xmin1}, xmax[2] = {xmax0, xmax1};
     try {
         std::vector<double> gx, gy, ax, ay;
@@ -699,21 +972,28 @@ int phd_mesh2d_build(phd_tess2d *t, const double *x, const double *y, int n_real
                 x0 = std::min(x0, ax[i]); x1 = std::max(x1, ax[i]);
                 y0 = std::min(y0, ay[i]); y1 = std::max(y1, ay[i]);
             }
-            t->reset();
-            t->X = ax;
-            t->Y = ay;
-            t->inserted.assign(n_all, 0);
-            t->vt.assign(n_all, -1);
-            t->n_real = n_real;
-            t->n_total = n_all;
-            t->init_super(x0, y0, x1, y1);
-            int rc;
-            if ((rc = t->insert_range(0, n_real)) != 0) return rc;
-            if ((rc = t->insert_range(n_real, n_all)) != 0) return rc;
-
             Geometry &G = t->G;
             std::vector<double> vol, dcx, dcy;
-            const int F = extract(*t, vol, dcx, dcy, G.area, G.comx, G.comy, G.nx, G.ny, G.pair_i, G.pair_j);
+            int F;
+            if (K > 1) {
+                t->reset();
+                const double H0 = 4.0 * std::sqrt((xmax0 - xmin0) * (xmax1 - xmin1) / double(n_real));
+                F = extract_strips(K, n_real, ax, ay, H0, vol, dcx, dcy, G.area, G.comx, G.comy, G.nx, G.ny,
+                                   G.pair_i, G.pair_j);
+            } else {
+                t->reset();
+                t->X = ax;
+                t->Y = ay;
+                t->inserted.assign(n_all, 0);
+                t->vt.assign(n_all, -1);
+                t->n_real = n_real;
+                t->n_total = n_all;
+                t->init_super(x0, y0, x1, y1);
+                int rc;
+                if ((rc = t->insert_range(0, n_real)) != 0) return rc;
+                if ((rc = t->insert_range(n_real, n_all)) != 0) return rc;
+                F = extract(*t, vol, dcx, dcy, G.area, G.comx, G.comy, G.nx, G.ny, G.pair_i, G.pair_j);
+            }
             if (F == -1) continue;                         // a real cell is unbounded: wider pad
             if (F < 0) return F;
             // keep ghosts that share a face with a real cell, in creation order

@@ -29,6 +29,7 @@ _SIGNATURES = {
     "phd_tess2d_update_radius": ([_vp, _vp, _i32, _vp], C.c_int),
     "phd_tess2d_extract_geometry": ([_vp] * 13, C.c_int),
     "phd_mesh2d_build": ([_vp, _vp, _vp, _i32, _i32, _f64, _f64, _f64, _f64, _f64], C.c_int),
+    "phd_mesh2d_build_strips": ([_vp, _vp, _vp, _i32, _i32, _f64, _f64, _f64, _f64, _f64, _i32], C.c_int),
     "phd_mesh2d_sizes": ([_vp, _vp, _vp, _vp], C.c_int),
     "phd_mesh2d_copy": ([_vp] * 16, C.c_int),
     "phd_hilbert_keys_2d_host": ([_vp, _vp, C.c_int64, C.c_int, _vp], None),
@@ -125,10 +126,11 @@ class Tess2d:
         return out
 
 
-def build_mesh_native(x_real, boundary, xmin, xmax, pad):
+def build_mesh_native(x_real, boundary, xmin, xmax, pad, n_strips=0):
     """Real generators ``x_real`` (2, N) in a periodic or reflective box -> the fields of
     ``meshgen.HostMesh`` (x, map, vol, dcom, pair_i, pair_j, area, com, normal,
-    nbr_ptr, nbr_idx) and the pad used."""
+    nbr_ptr, nbr_idx) and the pad used.  ``n_strips``: strips tessellated on parallel
+    host threads (0: chosen by the number of cells)."""
     x = np.ascontiguousarray(x_real, dtype=np.float64)
     n = x.shape[1]
     L = lib()
@@ -136,8 +138,9 @@ def build_mesh_native(x_real, boundary, xmin, xmax, pad):
     if not h:
         raise MemoryError("phd_tess2d_create")
     try:
-        rc = L.phd_mesh2d_build(h, _p(x[0]), _p(x[1]), n, {"periodic": 0, "reflective": 1}[boundary],
-                                float(xmin[0]), float(xmin[1]), float(xmax[0]), float(xmax[1]), float(pad))
+        rc = L.phd_mesh2d_build_strips(h, _p(x[0]), _p(x[1]), n, {"periodic": 0, "reflective": 1}[boundary],
+                                       float(xmin[0]), float(xmin[1]), float(xmax[0]), float(xmax[1]), float(pad),
+                                       int(n_strips))
         _check(rc, "tessellate")
         nc, nf, pad_used = C.c_int32(), C.c_int32(), C.c_double()
         L.phd_mesh2d_sizes(h, C.byref(nc), C.byref(nf), C.byref(pad_used))

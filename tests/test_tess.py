@@ -151,3 +151,42 @@ def test_hilbert_order_same_for_both_backends():
     _, oa = meshgen.build_mesh(x, "periodic", backend="scipy")
     _, ob = meshgen.build_mesh(x, "periodic", backend="native")
     np.testing.assert_array_equal(oa, ob)
+
+
+@pytest.mark.parametrize("jitter", [0.1, 0.0])
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+def test_strip_parallel_build_equals_the_serial_one(boundary, jitter):
+    """Strips tessellated on parallel threads give the whole box's tessellation bit for
+    bit -- also with exactly cocircular generators (a lattice, mirror images at walls),
+    which the symbolic perturbation of the lift decides the same way in every strip."""
+    x = meshgen.jittered_lattice(80, jitter=jitter, seed=6)
+    ref, _ = tess.build_mesh_native(x, boundary, *BOX, pad=3.0 / 80, n_strips=1)
+    for k in (2, 5):
+        o, _ = tess.build_mesh_native(x, boundary, *BOX, pad=3.0 / 80, n_strips=k)
+        for name in o:
+            np.testing.assert_array_equal(o[name], ref[name], err_msg="%s, %d strips" % (name, k))
+
+
+def test_insertion_order_does_not_change_the_mesh():
+    """With the perturbed lift the Delaunay triangulation is unique: the same generators
+    in another order give the same neighbour pairs and volumes, even on an exact lattice
+    with mirror images at the walls."""
+    n = 24
+    nr = n * n
+    x = meshgen.jittered_lattice(n, jitter=0.0)
+    perm = np.random.default_rng(1).permutation(nr)        # b's real cell k is a's cell perm[k]
+    a, _ = tess.build_mesh_native(x, "reflective", *BOX, pad=3.0 / n)
+    b, _ = tess.build_mesh_native(x[:, perm], "reflective", *BOX, pad=3.0 / n)
+
+    def pairs(m, label):
+        out = set()
+        for i, j in zip(m["pair_i"], m["pair_j"]):
+            if j < nr:
+                out.add(("real",) + tuple(sorted((int(label[i]), int(label[j])))))
+            else:
+                out.add(("ghost", int(label[i]), int(label[m["map"][j]]), float(m["x"][0, j]), float(m["x"][1, j])))
+        return out
+
+    assert a["pair_i"].size == b["pair_i"].size
+    assert pairs(a, np.arange(nr)) == pairs(b, perm)
+    np.testing.assert_allclose(b["vol"][:nr], a["vol"][perm], rtol=1e-13)
