@@ -18,9 +18,13 @@ SOLVERS = {"hll": HLL, "hllc": HLLC, "exact": EXACT}
 
 
 def build(force=False):
-    """Compile the restatement with the reference's FP semantics (no FMA contraction)."""
+    """Compile the restatement with the reference's FP semantics (no FMA contraction).
+    C-level ``pow(x, 2.0)`` folds into ``x*x`` here as it does in the reference's
+    compiled Cython; the one square the reference evaluates through Python's float
+    power at run time calls libm through a pointer (phd_oracle.c)."""
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
-            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "phd_oracle.h"))):
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "phd_oracle.h")),
+            os.path.getmtime(os.path.abspath(__file__))):
         return LIB
     subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
                            "-fno-fast-math", "-o", LIB + ".tmp", SRC, "-lm"])

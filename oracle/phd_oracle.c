@@ -8,8 +8,12 @@
  *
  * Every function restates one routine of rickyfernandez/phd-code in FP64 with the
  * reference's operation order (the Cython sources lower Python expressions with
- * their parse-tree grouping; `x**2` lowers to libm pow(x, 2.0), reproduced here).
- * Build with -ffp-contract=off so no multiply-add is fused.
+ * their parse-tree grouping).  Squares: where the reference's typed Cython emits a
+ * C-level pow(x, 2.0) the compiler folds it into the product x*x, here as there; the
+ * face-velocity residual (mesh.pyx:472) squares through Python's float power on boxed
+ * operands, i.e. libm pow at run time, which can differ from x*x by an ulp -- that one
+ * calls libm through a pointer the compiler cannot fold (py_pow).  Build with
+ * -ffp-contract=off so no multiply-add is fused.
  *
  * Layout: structure-of-arrays, row-major [field][index]:
  *   prim  [dim+2][n]  density, velocity-x..., pressure     (particle_creator.pyx:50-55)
@@ -733,6 +737,11 @@ void orc_generator_velocities(const orc_mesh *M, const double *prim, double gamm
     }
 }
 
+/* Python's float power (float_pow -> libm pow), which the reference's mesh.pyx:472
+ * reaches through boxed operands: called through a volatile pointer so the compiler
+ * does not fold pow(x, 2.0) into x*x. */
+static double (*volatile py_pow)(double, double) = pow;
+
 /* Mesh.assign_face_velocities  mesh.pyx:428-477 */
 void orc_face_velocities(const orc_mesh *M, const double *w, double *face_w)
 {
@@ -743,7 +752,7 @@ void orc_face_velocities(const orc_mesh *M, const double *w, double *face_w)
         for (int k = 0; k < dim; k++) {
             factor = factor + ((X(w, k, i, n) - X(w, k, j, n)) *
                                (X(M->com, k, m, F) - (0.5 * (X(M->x, k, i, n) + X(M->x, k, j, n)))));
-            denom = denom + pow(X(M->x, k, j, n) - X(M->x, k, i, n), 2.0);
+            denom = denom + py_pow(X(M->x, k, j, n) - X(M->x, k, i, n), 2.0);
         }
         factor = factor / denom;
         for (int k = 0; k < dim; k++)
