@@ -45,7 +45,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--workload", default="shear", choices=["shear", "ensemble", "adjoint", "explosion"])
+    ap.add_argument("--workload", default="shear", choices=["shear", "ensemble", "adjoint", "explosion", "moving"])
     ap.add_argument("--adj-steps", type=int, default=200, help="adjoint workload: recorded steps")
     ap.add_argument("--adj-dirs", type=int, default=16, help="adjoint workload: finite-difference directions")
     ap.add_argument("--runs", type=int, default=256)
@@ -681,6 +681,72 @@ def run_explosion(args, rank, world):
                           "runs": out, "clocks": clocks}), flush=True)
 
 
+def run_moving(args, rank, world):
+    """The whole moving-mesh loop (integrate.py:385-428) on the shear layer: every step
+    the device takes the flux step, the generator velocities come back, the host moves
+    the real generators by dt*w (wrapped into the periodic box, real cells keep their
+    order), re-tessellates them (C++ Tess2d, strips on the host threads), rounds the
+    compact FP32 hand-over and the device continues on it (FluxStepper.load_mesh).
+    Reports faces/s of the whole loop, the time of each phase, and the mass / energy
+    exchanged across the re-meshes."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    from phd_code_gb300.step import FluxStepper
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    mesh, prim = shear_layer(args.n_side, seed=rank)
+    nr = mesh.n_real
+    st = FluxStepper(mesh, prim, gamma=5.0 / 3.0, cfl=0.5, solver=args.solver, moving=True, precision="fp32",
+                     device=dev)
+    c0 = st.cons_host()[:, :nr].sum(axis=1)
+    x = np.ascontiguousarray(mesh.x[:, :nr])
+    phases = {"device_step": 0.0, "velocities_d2h": 0.0, "tessellation": 0.0, "hand_over_host": 0.0,
+              "load_mesh": 0.0}
+    faces = 0
+    n_steps = max(1, min(args.steps, 20))
+    t_all = time.perf_counter()
+    for k in range(n_steps + 1):                  # the first step is a warm-up
+        if k == 1:
+            t_all = time.perf_counter()
+            faces = 0
+            phases = {p: 0.0 for p in phases}
+        t = time.perf_counter()
+        dt = st.read_clock().dt
+        st.step(1)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        w = st.w2[:nr].double().t().cpu().numpy()
+        t2 = time.perf_counter()
+        faces += st.dmesh.n_faces
+        x = np.mod(x + dt * w, 1.0)
+        m, _ = pkg.meshgen.build_mesh(x, "periodic", hilbert=False)
+        t3 = time.perf_counter()
+        pinned = st.dmesh.pinned_host_compact(m)
+        t4 = time.perf_counter()
+        st.load_mesh(pinned)
+        torch.cuda.synchronize()
+        t5 = time.perf_counter()
+        for name, a, b in (("device_step", t, t1), ("velocities_d2h", t1, t2), ("tessellation", t2, t3),
+                           ("hand_over_host", t3, t4), ("load_mesh", t4, t5)):
+            phases[name] += b - a
+    wall = time.perf_counter() - t_all
+    st.check_status()
+    c1 = st.cons_host()[:, :nr].sum(axis=1)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": faces / wall, "unit": UNIT, "n_gpus": world, "steps": n_steps,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                          "data": "synthetic",
+                          "config": {"workload": "shear layer %dx%d, moving mesh re-tessellated every step" %
+                                                 (args.n_side, args.n_side), "cells": nr, "solver": args.solver,
+                                     "mesh": "host C++ Tess2d every step, compact FP32 hand-over",
+                                     "host_threads": os.cpu_count()},
+                          "ms_per_step": 1e3 * wall / n_steps,
+                          "phases_ms_per_step": {k: round(1e3 * v / n_steps, 3) for k, v in phases.items()},
+                          "mass_drift": float(abs(c1[0] - c0[0]) / abs(c0[0])),
+                          "energy_drift": float(abs(c1[3] - c0[3]) / abs(c0[3]))}), flush=True)
+
+
 def run_adjoint(args, rank, world):
     """The differentiation workload alone (one replica per rank): adjoint_cost's line
     with the backward/forward time ratio as the value."""
@@ -718,6 +784,8 @@ def main():
             run_adjoint(args, rank, world)
         elif args.workload == "explosion":
             run_explosion(args, rank, world)
+        elif args.workload == "moving":
+            run_moving(args, rank, world)
         else:
             run_ours(args, rank, world)
     finally:
