@@ -93,6 +93,16 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
                     double *dcom_y, int32_t *pair_i, int32_t *pair_j, double *area, double *com_x, double *com_y,
                     double *normal_x, double *normal_y, int32_t *nbr_ptr, int32_t *nbr_idx);
 
+/* The last phd_mesh2d_build result as the flux path's compact FP32 hand-over
+ * (phd_pair_i_from_face_ptr / phd_prepare_f32_faces_compact of phdflux.h): per-real-cell
+ * face ranges face_ptr[n_real + 1], pair_j[n_faces], the area and the centroid offset
+ * com - (x_i + x_j)/2 (formed in FP64) rounded to FP32 -- area32[n_faces],
+ * crel32[n_faces][2] -- and the cells' positions x[2][n_cells] (x row then y row), image
+ * map, tags (Real 0 / Ghost 1) and types (Undefined 4 for real cells, Exterior 2 for
+ * ghosts), written into caller buffers (e.g. pinned host memory reused across steps). */
+int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *crel32,
+                            double *x, int32_t *map, int8_t *tag, int8_t *type);
+
 /* hilbert_key_2d (phd/hilbert/hilbert.pyx:9-23) for n integer coordinate pairs. */
 void phd_hilbert_keys_2d_host(const int32_t *xh, const int32_t *yh, int64_t n, int order, int64_t *keys);
 

@@ -1050,6 +1050,38 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
     return 0;
 }
 
+int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *crel32,
+                            double *x, int32_t *map, int8_t *tag, int8_t *type) {
+    if (!t || t->G.n_cells == 0 || !face_ptr || !pair_j || !area32 || !crel32 || !x || !map || !tag || !type)
+        return -2;
+    const Geometry &G = t->G;
+    const int nr = G.n_real, n = G.n_cells, F = G.n_faces;
+    // FP64 -> FP32, round to nearest even; magnitudes below 2^-126 to signed zero (the
+    // device's own rounding of the same quantities)
+    auto round32 = [](double v) -> float {
+        return std::fabs(v) < 1.1754943508222875e-38 ? std::copysign(0.0f, float(v)) : float(v);
+    };
+    int c = 0;
+    face_ptr[0] = 0;
+    for (int f = 0; f < F; f++) {
+        const int i = G.pair_i[f], j = G.pair_j[f];
+        while (c < i) face_ptr[++c] = f;
+        pair_j[f] = j;
+        area32[f] = round32(G.area[f]);
+        crel32[2 * size_t(f)] = round32(G.comx[f] - 0.5 * (G.x[i] + G.x[j]));
+        crel32[2 * size_t(f) + 1] = round32(G.comy[f] - 0.5 * (G.y[i] + G.y[j]));
+    }
+    while (c < nr) face_ptr[++c] = F;
+    std::memcpy(x, G.x.data(), sizeof(double) * n);
+    std::memcpy(x + n, G.y.data(), sizeof(double) * n);
+    std::memcpy(map, G.map.data(), sizeof(int32_t) * n);
+    for (int k = 0; k < n; k++) {
+        tag[k] = k < nr ? 0 : 1;                        // Real / Ghost (particle_tags.py:1-6)
+        type[k] = k < nr ? 4 : 2;                       // Undefined / Exterior
+    }
+    return 0;
+}
+
 void phd_hilbert_keys_2d_host(const int32_t *xh, const int32_t *yh, int64_t n, int order, int64_t *keys) {
     for (int64_t i = 0; i < n; i++) keys[i] = hilbert_key_2d(xh[i], yh[i], order);
 }

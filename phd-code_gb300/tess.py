@@ -32,6 +32,7 @@ _SIGNATURES = {
     "phd_mesh2d_build_strips": ([_vp, _vp, _vp, _i32, _i32, _f64, _f64, _f64, _f64, _f64, _i32], C.c_int),
     "phd_mesh2d_sizes": ([_vp, _vp, _vp, _vp], C.c_int),
     "phd_mesh2d_copy": ([_vp] * 16, C.c_int),
+    "phd_mesh2d_copy_compact": ([_vp] * 9, C.c_int),
     "phd_hilbert_keys_2d_host": ([_vp, _vp, C.c_int64, C.c_int, _vp], None),
 }
 
@@ -156,6 +157,63 @@ def build_mesh_native(x_real, boundary, xmin, xmax, pad, n_strips=0):
         return o, pad_used.value
     finally:
         L.phd_tess2d_destroy(h)
+
+
+class CompactMesher:
+    """Re-tessellation of the real generators straight into the flux path's compact FP32
+    hand-over (``FluxStepper.load_mesh``; ``phd_mesh2d_copy_compact``): the real cells
+    keep their order, the ghosts are re-created.  The hand-over lives in pinned host
+    buffers reused across calls (grown by 1/8 when a mesh needs more), so the next call
+    overwrites them: let the copies of the previous hand-over finish (any
+    synchronisation of the stepper's stream) before calling again."""
+
+    def __init__(self, boundary, xmin=(0.0, 0.0), xmax=(1.0, 1.0), n_strips=0):
+        if boundary not in ("periodic", "reflective"):
+            raise ValueError("boundary must be 'periodic' or 'reflective'")
+        self.boundary, self.xmin, self.xmax, self.n_strips = boundary, tuple(xmin), tuple(xmax), int(n_strips)
+        self._h = lib().phd_tess2d_create()
+        if not self._h:
+            raise MemoryError("phd_tess2d_create")
+        self._buf = {}
+
+    def __del__(self):
+        h, self._h = getattr(self, "_h", None), None
+        if h and _lib is not None:
+            _lib.phd_tess2d_destroy(h)
+
+    def _pinned(self, name, shape, dtype):
+        import torch
+        need = int(np.prod(shape))
+        b = self._buf.get(name)
+        if b is None or b.numel() < need:
+            b = torch.empty(need + need // 8 + 16, dtype=dtype, pin_memory=True)
+            self._buf[name] = b
+        return b[:need].view(shape)
+
+    def __call__(self, x_real, pad=None):
+        """Pinned compact hand-over of the tessellation of ``x_real`` (2, N)."""
+        import torch
+        x = np.ascontiguousarray(x_real, dtype=np.float64)
+        n = x.shape[1]
+        if pad is None:
+            pad = 3.0 * np.sqrt((self.xmax[0] - self.xmin[0]) * (self.xmax[1] - self.xmin[1]) / n)
+        L = lib()
+        _check(L.phd_mesh2d_build_strips(self._h, _p(x[0]), _p(x[1]), n, {"periodic": 0, "reflective": 1}[self.boundary],
+                                         float(self.xmin[0]), float(self.xmin[1]), float(self.xmax[0]),
+                                         float(self.xmax[1]), float(pad), self.n_strips), "tessellate")
+        nc, nf, pad_used = C.c_int32(), C.c_int32(), C.c_double()
+        L.phd_mesh2d_sizes(self._h, C.byref(nc), C.byref(nf), C.byref(pad_used))
+        nc, F = nc.value, nf.value
+        out = {"face_ptr": self._pinned("face_ptr", (n + 1,), torch.int32),
+               "pair_j": self._pinned("pair_j", (F,), torch.int32),
+               "area32": self._pinned("area32", (F,), torch.float32),
+               "crel32": self._pinned("crel32", (F, 2), torch.float32),
+               "x": self._pinned("x", (2, nc), torch.float64), "map": self._pinned("map", (nc,), torch.int32),
+               "tag": self._pinned("tag", (nc,), torch.int8), "type": self._pinned("type", (nc,), torch.int8)}
+        _check(L.phd_mesh2d_copy_compact(self._h, *(C.c_void_p(out[k].data_ptr()) for k in
+                                                    ("face_ptr", "pair_j", "area32", "crel32", "x", "map", "tag",
+                                                     "type"))), "copy_compact")
+        return out
 
 
 def hilbert_keys_2d(xh, yh, order):

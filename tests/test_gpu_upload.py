@@ -290,3 +290,22 @@ def test_compact_hand_over_rejects_broken_face_ranges():
     st64 = FluxStepper(meshes[0], prim, gamma=1.4, precision="fp64")
     with pytest.raises(ValueError, match="FP32"):
         st64.load_mesh(st64.dmesh.pinned_host_compact(meshes[1]))
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+def test_compact_mesher_equals_the_host_mesh_path(boundary):
+    """tess.CompactMesher writes the compact hand-over straight from the C++
+    tessellation into reused pinned buffers: the same arrays, bit for bit, as building
+    the host mesh and rounding it in DeviceMesh.pinned_host_compact."""
+    meshes = _moved_meshes(22, boundary, 9, 3)
+    st = FluxStepper(meshes[0], smooth_state(meshes[0]), gamma=1.4, precision="fp32")
+    mesher = pkg.tess.CompactMesher(boundary)
+    for m in meshes[1:]:
+        a = st.dmesh.pinned_host_compact(m)
+        b = mesher(m.x[:, :m.n_real])
+        assert sorted(a) == sorted(b)
+        for k in a:
+            assert torch.equal(a[k], b[k]), k
+        st.load_mesh(b)
+        torch.cuda.synchronize()
+        assert st.dmesh.upload_errors() == 0
