@@ -725,9 +725,12 @@ struct StripJob {
     std::vector<FaceRec> faces;
 };
 
-int strip_pass(StripJob &J, const std::vector<double> &ax, const std::vector<double> &ay,
-               const std::vector<int> &xorder, const std::vector<double> &xsorted, double H0, double *vol,
-               double *dcx, double *dcy, int32_t *nf) {
+int strip_pass(StripJob &J, int n_real, const std::vector<double> &ax, const std::vector<double> &ay, double H0,
+               double *vol, double *dcx, double *dcy, int32_t *nf) {
+    const int n_all = int(ax.size());
+    J.owned.clear();                                     // the real cells in [s_lo, s_hi), ascending
+    for (int i = 0; i < n_real; i++)
+        if (ax[i] >= J.s_lo && ax[i] < J.s_hi) J.owned.push_back(i);
     if (J.owned.empty()) return 0;
     phd_tess2d T;
     std::vector<int> gids;
@@ -735,11 +738,10 @@ int strip_pass(StripJob &J, const std::vector<double> &ax, const std::vector<dou
     for (double H = H0;; H *= 2.0) {
         const double lo = J.first ? -INFINITY : J.s_lo - H;
         const double hi = J.last ? INFINITY : J.s_hi + H;
-        const size_t b = std::lower_bound(xsorted.begin(), xsorted.end(), lo) - xsorted.begin();
-        const size_t e = std::upper_bound(xsorted.begin(), xsorted.end(), hi) - xsorted.begin();
-        const bool whole = (b == 0 && e == xsorted.size());
-        gids.assign(xorder.begin() + b, xorder.begin() + e);
-        std::sort(gids.begin(), gids.end());
+        gids.clear();                                    // every generator within the halo, ascending
+        for (int i = 0; i < n_all; i++)
+            if (ax[i] >= lo && ax[i] <= hi) gids.push_back(i);
+        const bool whole = (int(gids.size()) == n_all);
         const int m = int(gids.size());
         T.reset();
         T.X.resize(m);
@@ -777,27 +779,19 @@ int extract_strips(int K, int n_real, const std::vector<double> &ax, const std::
                    std::vector<double> &area, std::vector<double> &comx, std::vector<double> &comy,
                    std::vector<double> &nx, std::vector<double> &ny, std::vector<int32_t> &pi,
                    std::vector<int32_t> &pj) {
-    const int n_all = int(ax.size());
-    std::vector<int> xorder(n_all);
-    for (int i = 0; i < n_all; i++) xorder[i] = i;
-    std::sort(xorder.begin(), xorder.end(), [&](int a, int b) { return ax[a] < ax[b] || (ax[a] == ax[b] && a < b); });
-    std::vector<double> xsorted(n_all);
-    for (int i = 0; i < n_all; i++) xsorted[i] = ax[xorder[i]];
-    std::vector<double> xr(ax.begin(), ax.begin() + n_real);
+    // strip bounds at x quantiles of a regular sample of the real generators (any bounds
+    // give the same mesh; these only balance the strips)
+    const int stride = std::max(1, n_real / 65536);
+    std::vector<double> xr;
+    for (int i = 0; i < n_real; i += stride) xr.push_back(ax[i]);
     std::sort(xr.begin(), xr.end());
+    const size_t ns = xr.size();
     std::vector<StripJob> jobs(K);
     for (int k = 0; k < K; k++) {
-        jobs[k].s_lo = k == 0 ? -INFINITY : xr[size_t(k) * n_real / K];
-        jobs[k].s_hi = k == K - 1 ? INFINITY : xr[size_t(k + 1) * n_real / K];
+        jobs[k].s_lo = k == 0 ? -INFINITY : xr[size_t(k) * ns / K];
+        jobs[k].s_hi = k == K - 1 ? INFINITY : xr[size_t(k + 1) * ns / K];
         jobs[k].first = k == 0;
         jobs[k].last = k == K - 1;
-    }
-    for (int i = 0; i < n_real; i++) {
-        int k = int(std::upper_bound(xr.begin(), xr.end(), ax[i]) - xr.begin()) * K / n_real;
-        k = std::min(std::max(k, 0), K - 1);
-        while (k > 0 && ax[i] < jobs[k].s_lo) k--;
-        while (k < K - 1 && ax[i] >= jobs[k].s_hi) k++;
-        jobs[k].owned.push_back(i);
     }
     vol.assign(n_real, 0.); dcx.assign(n_real, 0.); dcy.assign(n_real, 0.);
     std::vector<int32_t> nf(n_real, 0);
@@ -808,7 +802,7 @@ int extract_strips(int K, int n_real, const std::vector<double> &ax, const std::
             if (k >= K) return;
             int rc;
             try {
-                rc = strip_pass(jobs[k], ax, ay, xorder, xsorted, H0, vol.data(), dcx.data(), dcy.data(), nf.data());
+                rc = strip_pass(jobs[k], n_real, ax, ay, H0, vol.data(), dcx.data(), dcy.data(), nf.data());
             } catch (...) {
                 rc = -4;
             }
@@ -829,15 +823,25 @@ int extract_strips(int K, int n_real, const std::vector<double> &ax, const std::
     for (int i = 0; i < n_real; i++) off[i + 1] = off[i] + nf[i];
     const size_t F = size_t(off[n_real]);
     area.resize(F); comx.resize(F); comy.resize(F); nx.resize(F); ny.resize(F); pi.resize(F); pj.resize(F);
-    for (const StripJob &J : jobs) {
-        size_t r = 0;
-        for (int gi : J.owned)
-            for (int64_t f = off[gi]; f < off[gi + 1]; f++, r++) {
-                const FaceRec &rec = J.faces[r];
-                pi[f] = gi; pj[f] = rec.j; area[f] = rec.ln; comx[f] = rec.fx; comy[f] = rec.fy;
-                nx[f] = rec.nx; ny[f] = rec.ny;
-            }
-    }
+    std::atomic<int> next_copy(0);
+    auto copier = [&]() {                               // each strip fills its own cells' face ranges
+        for (;;) {
+            const int k = next_copy.fetch_add(1);
+            if (k >= K) return;
+            const StripJob &J = jobs[k];
+            size_t r = 0;
+            for (int gi : J.owned)
+                for (int64_t f = off[gi]; f < off[gi + 1]; f++, r++) {
+                    const FaceRec &rec = J.faces[r];
+                    pi[f] = gi; pj[f] = rec.j; area[f] = rec.ln; comx[f] = rec.fx; comy[f] = rec.fy;
+                    nx[f] = rec.nx; ny[f] = rec.ny;
+                }
+        }
+    };
+    threads.clear();
+    for (int t = 1; t < n_threads; t++) threads.emplace_back(copier);
+    copier();
+    for (auto &th : threads) th.join();
     return int(F);
 }
 
