@@ -1,0 +1,90 @@
+"""The headline workloads at their full sizes, through size-independent properties:
+the 1024x1024 shear layer (1,048,576 cells, 3.15 M faces) and the 256x256 point
+explosion (65,536 cells).  At full size the oracle still takes one FP64 step (a few
+seconds on the host), so FP64 parity is checked there too; the rest are properties
+that hold at any size -- exact exchange of mass and energy, FP32 tracking FP64,
+device-built neighbour lists equal to the host's, the compact hand-over equal to the
+full one, bitwise-repeatable steps."""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+import phd_code_gb300 as pkg
+from phd_code_gb300.step import FluxStepper
+from _util import FP64_TOL, rel_rows
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def shear():
+    mesh, prim, info = pkg.problems.shear_layer(1024, seed=0)
+    assert mesh.n_real == 1024 * 1024
+    return mesh, prim, info["gamma"]
+
+
+def test_shear_1024_fp64_step_matches_the_oracle(shear):
+    mesh, prim, gamma = shear
+    st = FluxStepper(mesh, prim, gamma=gamma, cfl=0.5, solver="hllc", moving=True, precision="fp64")
+    st.step(1)
+    st.check_status()
+    p = prim.copy()
+    c = O.cons_from_prim(mesh, p, gamma)
+    dt = O.time_step(mesh, p, gamma, 0.5, True)
+    assert O.OracleStepper(mesh, gamma=gamma, solver="hllc", moving=True).step(dt, p, c) == 0
+    nr = mesh.n_real
+    assert rel_rows(st.cons_host()[:, :nr], c[:, :nr]) <= FP64_TOL
+    assert rel_rows(st.prim_host(), p) <= FP64_TOL
+
+
+def test_shear_1024_fp32_conserves_tracks_fp64_and_repeats(shear):
+    mesh, prim, gamma = shear
+    nr = mesh.n_real
+    runs = []
+    for precision in ("fp32", "fp32", "fp64"):
+        st = FluxStepper(mesh, prim, gamma=gamma, cfl=0.5, solver="hllc", moving=True, precision=precision)
+        c0 = st.cons_host()[:, :nr].sum(axis=1)
+        st.step(10)
+        st.check_status()
+        runs.append((st.cons_host()[:, :nr], c0))
+    (a, c0), (b, _), (ref, _) = runs
+    assert np.array_equal(a, b)                                  # bitwise repeatable
+    c1 = a.sum(axis=1)
+    for q in (0, 3):                                             # exact exchange, periodic box
+        assert abs(c1[q] - c0[q]) <= 1e-12 * abs(c0[q])
+    vol = mesh.vol[:nr]
+    assert np.mean(np.abs(a[0] / vol - ref[0] / vol)) <= 1e-5   # L1 density, FP32 vs FP64
+
+
+def test_shear_1024_device_mesh_data_and_compact_hand_over(shear):
+    mesh, prim, gamma = shear
+    st = FluxStepper(mesh, prim, gamma=gamma, precision="fp32")
+    geo = [t.clone() for t in (st.face_geo, st.face_ar, st.csr_face, st.csr_nbr, st.cell_geo)]
+    st.load_mesh(st.dmesh.pinned_host_compact(mesh))             # lists, twins, geometry on the device
+    torch.cuda.synchronize()
+    assert st.dmesh.upload_errors() == 0
+    assert np.array_equal(st.dmesh.nbr_ptr.cpu().numpy(), mesh.nbr_ptr)
+    assert np.array_equal(st.dmesh.nbr_idx.cpu().numpy(), mesh.nbr_idx)
+    assert np.array_equal(st.dmesh.pair_i.cpu().numpy(), mesh.pair_i)
+    # the first preparation rounds the host's FP64 normals, the hand-over forms them from
+    # the rounded separation: equal to FP32 rounding; everything else bit for bit
+    assert torch.equal(geo[0][:, 2:], st.face_geo[:, 2:])
+    assert torch.max(torch.abs(geo[0][:, :2] - st.face_geo[:, :2])).item() <= 4e-7
+    for old, new in zip(geo[1:4], (st.face_ar, st.csr_face, st.csr_nbr)):
+        assert torch.equal(old, new)
+
+
+def test_explosion_256_fp32_tracks_fp64():
+    mesh, prim, info = pkg.problems.point_explosion(256, seed=0)
+    nr, gamma = mesh.n_real, info["gamma"]
+    out = {}
+    for precision in ("fp32", "fp64"):
+        st = FluxStepper(mesh, prim, gamma=gamma, cfl=0.5, solver="hllc", moving=True, precision=precision)
+        e0 = st.cons_host()[3, :nr].sum()
+        st.step(40)
+        st.check_status()
+        cons = st.cons_host()[:, :nr]
+        assert abs(cons[3].sum() - e0) <= 1e-12 * abs(e0)
+        out[precision] = cons[0] / mesh.vol[:nr]
+    assert np.mean(np.abs(out["fp32"] - out["fp64"])) <= 1e-5
