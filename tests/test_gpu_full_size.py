@@ -88,3 +88,23 @@ def test_explosion_256_fp32_tracks_fp64():
         assert abs(cons[3].sum() - e0) <= 1e-12 * abs(e0)
         out[precision] = cons[0] / mesh.vol[:nr]
     assert np.mean(np.abs(out["fp32"] - out["fp64"])) <= 1e-5
+
+
+def test_ensemble_256_runs_batch_equals_single_runs():
+    """The batching workload at its full size (256 runs, 1,000-65,536 generators each,
+    about 4.6 M cells in one batch): runs never interact -- a sample of them, the
+    smallest and largest included, evolves bit for bit as it does alone."""
+    from phd_code_gb300.ensemble import EnsembleStepper
+    runs, _ = pkg.problems.riemann_ensemble(n_runs=256, seed=0)
+    sizes = [m.n_real for m, _ in runs]
+    assert sum(sizes) > 4_000_000
+    ens = EnsembleStepper(runs)
+    ens.step(5)
+    ens.check_status()
+    sample = sorted({int(np.argmin(sizes)), int(np.argmax(sizes)), 7, 100, 200})
+    for r in sample:
+        m, p = runs[r]
+        st = FluxStepper(m, p, precision="fp32", solver="hllc")
+        st.step(5)
+        assert np.array_equal(ens.run_cons(r), st.cons_host()[:, :m.n_real])
+        assert ens.read_clocks()[r].dt == st.read_clock().dt
