@@ -683,9 +683,9 @@ def run_explosion(args, rank, world):
 
 def run_moving(args, rank, world):
     """The whole moving-mesh loop (integrate.py:385-428) on the shear layer: every step
-    the device takes the flux step, the generator velocities come back, the host moves
-    the real generators by dt*w (wrapped into the periodic box, real cells keep their
-    order), re-tessellates them (C++ Tess2d, strips on the host threads), rounds the
+    the device takes the flux step and moves the real generators by dt*w (wrapped into
+    the periodic box; real cells keep their order), the positions come back, the host
+    re-tessellates them (C++ Tess2d, strips on the host threads) straight into the
     compact FP32 hand-over and the device continues on it (FluxStepper.load_mesh).
     Reports faces/s of the whole loop, the time of each phase, and the mass / energy
     exchanged across the re-meshes."""
@@ -702,7 +702,7 @@ def run_moving(args, rank, world):
     c0 = st.cons_host()[:, :nr].sum(axis=1)
     x = np.ascontiguousarray(mesh.x[:, :nr])
     mesher = pkg.tess.CompactMesher("periodic")
-    phases = {"device_step": 0.0, "velocities_d2h": 0.0, "tessellation_to_hand_over": 0.0, "load_mesh": 0.0}
+    phases = {"device_step_and_move": 0.0, "positions_d2h": 0.0, "tessellation_to_hand_over": 0.0, "load_mesh": 0.0}
     faces = 0
     n_steps = max(1, min(args.steps, 20))
     t_all = time.perf_counter()
@@ -712,21 +712,20 @@ def run_moving(args, rank, world):
             faces = 0
             phases = {p: 0.0 for p in phases}
         t = time.perf_counter()
-        dt = st.read_clock().dt
         st.step(1)
+        xd = st.move_generators()                 # x + dt*w, periodic wrap, on the device
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        w = st.w2[:nr].double().t().cpu().numpy()
+        x = xd.cpu().numpy()
         t2 = time.perf_counter()
         faces += st.dmesh.n_faces
-        x = np.mod(x + dt * w, 1.0)
         pinned = mesher(x)
         t3 = time.perf_counter()
         st.load_mesh(pinned)
         torch.cuda.synchronize()
         t4 = time.perf_counter()
-        for name, a, b in (("device_step", t, t1), ("velocities_d2h", t1, t2), ("tessellation_to_hand_over", t2, t3),
-                           ("load_mesh", t3, t4)):
+        for name, a, b in (("device_step_and_move", t, t1), ("positions_d2h", t1, t2),
+                           ("tessellation_to_hand_over", t2, t3), ("load_mesh", t3, t4)):
             phases[name] += b - a
     wall = time.perf_counter() - t_all
     st.check_status()

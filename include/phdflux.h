@@ -41,6 +41,7 @@ extern "C" {
 #define PHD_STATUS_NEG_ENERGY 2            /* "Energy less than zero in flux update" mesh.pyx:549-551 */
 #define PHD_STATUS_RIEMANN_NONCONVERGED 4  /* "No convergence in Exact Riemann Solver" riemann.pyx:1088-1090 */
 #define PHD_STATUS_BAD_INDEX 8             /* "ERROR: incorrect neighbors!" reconstruction.pyx:651-652 */
+#define PHD_STATUS_LEFT_DOMAIN 16          /* "particle left domain in reflective boundary condition!!" boundary.pyx:262-263 */
 
 /* solver / reconstruction selectors */
 #define PHD_HLL 0                          /* riemann.pyx:225-504 */
@@ -80,6 +81,7 @@ typedef struct phd_clock {
     unsigned int arrive;      /* accumulator; initialise to 0 */
     int status;               /* PHD_STATUS_* bits, OR-ed by kernels */
     long long step;           /* completed steps */
+    double dt_last;           /* time step of the last completed step */
 } phd_clock;
 
 /* Physics parameters of a run. */
@@ -239,6 +241,18 @@ int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *o
 #define PHD_PREP_CELLS_FROM_FACES 8
 int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out,
                           int32_t parts, cudaStream_t stream);
+
+/* DomainManager.move_generators + BoundaryCondition.migrate_particles
+ * (domain_manager.pyx:566-590, boundary.pyx:236-263, 502-538) after a step: for every
+ * real cell x_out[k][i] = x[k][i] + dt_last * w[k][i] (FP64, the product and the sum
+ * rounded separately, as the reference does) with the step's generator velocities --
+ * w2 [n][2] FP32 from the FP32 step, or w [2][n] FP64 from the FP64 step (exactly one
+ * of them non-NULL) -- and clk->dt_last.  A generator outside [xmin, xmax] in some
+ * axis is wrapped (periodic != 0: +L where it is <= xmin, -L where >= xmax, L = xmax -
+ * xmin) or, for reflective walls, flagged PHD_STATUS_LEFT_DOMAIN in clk->status.
+ * x_out is [2][n_real]. */
+int phd_move_generators(const phd_mesh *mesh, const float *w2, const double *w, phd_clock *clk, int32_t periodic,
+                        double xmin0, double xmin1, double xmax0, double xmax1, double *x_out, cudaStream_t stream);
 
 /* Compact FP32 hand-over of a re-mesh (the per-step upload of the face list,
  * mesh.pyx:255-323, in 16 B per face instead of 32): the host sends pair-j, the area

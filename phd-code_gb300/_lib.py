@@ -15,6 +15,7 @@ PHD_OK, PHD_ERR_ARG, PHD_ERR_LAUNCH, PHD_ERR_UNSUPPORTED, PHD_ERR_SCRATCH_TOO_SM
 ADJ_NOALLOC_MAX_DOUBLES = 4194304
 GRAD_TAPE_F64_ROWS, GRAD_TAPE_I32_ROWS = 12, 13
 STATUS_NEG_MASS, STATUS_NEG_ENERGY, STATUS_RIEMANN_NONCONVERGED, STATUS_BAD_INDEX = 1, 2, 4, 8
+STATUS_LEFT_DOMAIN = 16
 HLL, HLLC, EXACT = 0, 1, 2
 PREP_FACES, PREP_CELLS, PREP_LISTS, PREP_ALL, PREP_CELLS_FROM_FACES = 1, 2, 4, 7, 8
 CONSTANT, LINEAR = 0, 1
@@ -26,6 +27,7 @@ STATUS_MESSAGES = {
     STATUS_NEG_ENERGY: "Energy less than zero in flux update",
     STATUS_RIEMANN_NONCONVERGED: "No convergence in Exact Riemann Solver",
     STATUS_BAD_INDEX: "ERROR: incorrect neighbors!",
+    STATUS_LEFT_DOMAIN: "particle left domain in reflective boundary condition!!",
 }
 
 
@@ -42,7 +44,7 @@ class PhdMesh(C.Structure):
 class PhdClock(C.Structure):
     _fields_ = [("dt", C.c_double), ("t", C.c_double), ("t_end", C.c_double),
                 ("dt_hydro", C.c_double), ("dtmin_bits", C.c_uint64), ("arrive", C.c_uint32),
-                ("status", C.c_int32), ("step", C.c_int64)]
+                ("status", C.c_int32), ("step", C.c_int64), ("dt_last", C.c_double)]
 
 
 class PhdParams(C.Structure):
@@ -119,6 +121,7 @@ SIGNATURES = {
     "phd_csr_work_ints": ([_i32], C.c_size_t),
     "phd_build_csr": ([_PM, _vp, _vp, _vp, _vp, _vp], C.c_int),
     "phd_pair_i_from_face_ptr": ([_PM, _vp, _vp, _vp, _vp], C.c_int),
+    "phd_move_generators": ([_PM, _vp, _vp, _vp, _i32, _f64, _f64, _f64, _f64, _vp, _vp], C.c_int),
     "phd_prepare_f32_faces_compact": ([_PM, _vp, _vp, C.POINTER(PhdGeom32Out), _vp], C.c_int),
     "phd_periodic_twins": ([_PM, _i32, _f64, _f64, _vp, _vp], C.c_int),
 }

@@ -133,6 +133,7 @@ __device__ __forceinline__ void finalize_clock(phd_clock *clk, double cfl, bool 
     const double mn = __longlong_as_double(static_cast<long long>(bits));
     if (advance) {
         clk->t = clk->t + clk->dt;
+        clk->dt_last = clk->dt;
         clk->step = clk->step + 1;
     }
     double dt = cfl * mn;

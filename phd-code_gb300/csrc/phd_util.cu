@@ -256,6 +256,45 @@ __global__ void k_periodic_twins(phd_mesh M, int periodic, double Lx, double Ly,
     twin[a] = out;
 }
 
+
+// DomainManager.move_generators (domain_manager.pyx:566-590) and the boundary
+// conditions' migrate_particles (boundary.pyx:236-263 reflective, 502-538 periodic) for
+// the real cells, after a step, with the step's own dt (clk->dt_last).  The product and
+// the sum are rounded separately (no contraction), as in the reference.
+__global__ void k_move_generators(int n_real, int n, const double *__restrict__ x, const float2 *__restrict__ w2,
+                                  const double *__restrict__ w, const phd_clock *clk, int periodic, double lo0,
+                                  double lo1, double hi0, double hi1, double *__restrict__ x_out, int *status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_real) return;
+    const double dt = clk->dt_last;
+    double wx, wy;
+    if (w2) {
+        const float2 v = w2[i];
+        wx = v.x;
+        wy = v.y;
+    } else {
+        wx = w[i];
+        wy = w[(size_t)n + i];
+    }
+    double xs[2] = {__dadd_rn(x[i], __dmul_rn(dt, wx)), __dadd_rn(x[(size_t)n + i], __dmul_rn(dt, wy))};
+    const double lo[2] = {lo0, lo1}, hi[2] = {hi0, hi1};
+    const bool inside = !(xs[0] < lo[0] || xs[0] > hi[0] || xs[1] < lo[1] || xs[1] > hi[1]);   // intersect_bounds
+    double xo[2] = {xs[0], xs[1]};
+    if (!inside) {
+        if (periodic) {
+            for (int k = 0; k < 2; k++) {
+                const double L = __dsub_rn(hi[k], lo[k]);            // domain_manager.translate
+                if (xs[k] <= lo[k]) xo[k] = __dadd_rn(xo[k], L);
+                if (xs[k] >= hi[k]) xo[k] = __dsub_rn(xo[k], L);
+            }
+        } else {
+            atomicOr(status, PHD_STATUS_LEFT_DOMAIN);
+        }
+    }
+    x_out[i] = xo[0];
+    x_out[(size_t)n_real + i] = xo[1];
+}
+
 }  // namespace phd
 
 extern "C" {
@@ -323,6 +362,18 @@ int phd_periodic_twins(const phd_mesh *mesh, int32_t periodic, double box_x, dou
         return PHD_ERR_ARG;
     phd::k_periodic_twins<<<(mesh->n_faces + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(
         *mesh, periodic != 0, box_x, box_y, twin);
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+int phd_move_generators(const phd_mesh *mesh, const float *w2, const double *w, phd_clock *clk, int32_t periodic,
+                        double xmin0, double xmin1, double xmax0, double xmax1, double *x_out, cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || !mesh->x || !clk || !x_out || (!w2) == (!w) || mesh->n_real < 0 ||
+        mesh->n_real > mesh->n_cells || !(xmax0 > xmin0) || !(xmax1 > xmin1))
+        return PHD_ERR_ARG;
+    if (mesh->n_real == 0) return PHD_OK;
+    phd::k_move_generators<<<(mesh->n_real + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(
+        mesh->n_real, mesh->n_cells, mesh->x, reinterpret_cast<const float2 *>(w2), w, clk, periodic, xmin0, xmin1,
+        xmax0, xmax1, x_out, &clk->status);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 

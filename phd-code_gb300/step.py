@@ -287,6 +287,24 @@ class FluxStepper:
         L.check(rc, "phd_step_" + self.precision)
         self.cons, self.cons_next = self.cons_next, self.cons
 
+    def move_generators(self):
+        """DomainManager.move_generators + migrate_particles (domain_manager.pyx:566-590,
+        boundary.pyx:236-263, 502-538) on the device after a moving step: x + dt * w for the
+        real cells with the step's dt and generator velocities, wrapped into a periodic box
+        or flagged (PHD_STATUS_LEFT_DOMAIN, raised by check_status) when a generator leaves
+        a reflective one.  Returns the [2][n_real] FP64 positions (a device tensor, reused
+        by the next call) -- what the host re-tessellation needs."""
+        if not self.moving:
+            raise RuntimeError("generator velocities exist only in moving-mesh steps")
+        dm = self.dmesh
+        out = self._view("x_moved", (dm.dim, dm.n_real), torch.float64)
+        w2, w = (self.w2, None) if self.precision == "fp32" else (None, self.w)
+        L.check(L.lib().phd_move_generators(dm.ref, L.ptr(w2), L.ptr(w), self.clock.ptr,
+                                            int(dm.boundary == "periodic"), float(dm.xmin[0]), float(dm.xmin[1]),
+                                            float(dm.xmax[0]), float(dm.xmax[1]), L.ptr(out),
+                                            L.stream_handle(self.stream)), "phd_move_generators")
+        return out
+
     def step(self, n=1):
         """Launch n steps (asynchronous; read the clock or state to synchronise)."""
         for _ in range(n):

@@ -309,3 +309,43 @@ def test_compact_mesher_equals_the_host_mesh_path(boundary):
         st.load_mesh(b)
         torch.cuda.synchronize()
         assert st.dmesh.upload_errors() == 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_device_generator_move_follows_the_reference(precision):
+    """move_generators (domain_manager.pyx:566-590 + the periodic wrap of
+    boundary.pyx:502-538) on the device equals the host evaluation with the step's dt and
+    generator velocities, bit for bit."""
+    m = lattice_mesh(24, "periodic", seed=4)
+    prim = smooth_state(m)
+    prim[1] += 0.8                                   # drift right so generators cross x = 1
+    st = FluxStepper(m, prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision=precision)
+    st.step(1)
+    c = st.read_clock()
+    c.dt_last = 0.05                                 # a long move, so that generators cross the box
+    dt = c.dt_last
+    st.clock.buf.copy_(torch.frombuffer(bytearray(bytes(c)), dtype=torch.uint8))
+    xd = st.move_generators().cpu().numpy()
+    st.check_status()
+    nr = m.n_real
+    w = (st.w2[:nr].double().t() if precision == "fp32" else st.w[:, :nr]).cpu().numpy()
+    xs = m.x[:, :nr] + dt * w
+    out = (xs < 0.0) | (xs > 1.0)
+    outside = out[0] | out[1]
+    expect = xs.copy()
+    for k in range(2):
+        expect[k] = np.where(outside & (xs[k] <= 0.0), expect[k] + 1.0, expect[k])
+        expect[k] = np.where(outside & (xs[k] >= 1.0), expect[k] - 1.0, expect[k])
+    assert outside.any()
+    assert np.array_equal(xd, expect)
+
+
+def test_generator_leaving_a_reflective_box_is_flagged():
+    m = lattice_mesh(16, "reflective", seed=2)
+    prim = smooth_state(m)
+    prim[1] -= 3.0                                   # everything rushes to the x = 0 wall: with
+    st = FluxStepper(m, prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32")
+    st.step(1)                                       # boost the CFL step ignores |v|, so the
+    st.move_generators()                             # cells at the wall cross it in one step
+    with pytest.raises(RuntimeError, match="particle left domain in reflective boundary condition"):
+        st.check_status()
