@@ -95,5 +95,6 @@ def test_argument_errors_are_rejected_on_the_host(lib):
     assert f.phd_prepare_f32_faces_compact(ctypes.byref(m), None, None, ctypes.byref(out), None) == L.PHD_ERR_ARG
     assert f.phd_prepare_f32_faces_compact(None, one, one, ctypes.byref(out), None) == L.PHD_ERR_ARG
     # generator move: exactly one velocity array, and a real box
+    m.x = 1
     assert f.phd_move_generators(ctypes.byref(m), None, None, one, 1, 0.0, 0.0, 1.0, 1.0, one, None) == L.PHD_ERR_ARG
     assert f.phd_move_generators(ctypes.byref(m), one, one, one, 1, 0.0, 0.0, 1.0, 1.0, one, None) == L.PHD_ERR_ARG
