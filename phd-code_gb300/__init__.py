@@ -11,7 +11,7 @@ Importable as ``phd_code_gb300`` (the directory name carries a hyphen; see
 """
 __version__ = "0.1.0"
 
-from . import meshgen, hilbert, problems, tess                   # noqa: F401  (host only)
+from . import meshgen, hilbert, problems, tess, io               # noqa: F401  (host only)
 from .containers import CarrayContainer, HydroParticleCreator    # noqa: F401
 from .equation_state import EquationStateBase, IdealGas           # noqa: F401
 from .domain import DomainManager, Reflective, Periodic           # noqa: F401
