@@ -23,9 +23,10 @@ def _sm_count(device):
     return torch.cuda.get_device_properties(device).multi_processor_count
 
 
-def tune(stepper, blocks=BLOCKS, cap_waves=CAP_WAVES, reps=3):
+def tune(stepper, blocks=BLOCKS, cap_waves=CAP_WAVES, reps=9):
     """Pick a PhdLaunch for an EnsembleStepper or an fp32 FluxStepper; returns
-    (launch, table) where table maps (block, waves) to per-kernel milliseconds."""
+    (launch, table) where table maps (block, waves) to per-kernel milliseconds (the
+    median over ``reps`` timed steps, which keeps a noisy step from deciding)."""
     dev = stepper.device
     sms = _sm_count(dev)
     saved = {k: getattr(stepper, k).clone() for k in ("cons", "cons_next", "prim4", "grad8", "w2", "flux4")}
@@ -55,11 +56,8 @@ def tune(stepper, blocks=BLOCKS, cap_waves=CAP_WAVES, reps=3):
                                               L.ptr(clk_buf), n_runs, L.ptr(cell_run), L.stream_handle(), arr)
                 L.check(rc, "tune step")
             torch.cuda.synchronize(dev)
-            t = [0.0, 0.0, 0.0]
-            for k in range(reps):
-                for q in range(3):
-                    t[q] += ev[4 * k + q].elapsed_time(ev[4 * k + q + 1]) / reps
-            table[(b, w)] = t
+            samples = [[ev[4 * k + q].elapsed_time(ev[4 * k + q + 1]) for k in range(reps)] for q in range(3)]
+            table[(b, w)] = [sorted(v)[len(v) // 2] for v in samples]
     for k, v in saved.items():
         getattr(stepper, k).copy_(v)
     clk_buf.copy_(clk_saved)

@@ -423,6 +423,7 @@ static int adjoint_step(const phd_mesh *mesh, const phd_adj_index *index, const 
 int phd_adjoint_step_f64(const phd_mesh *mesh, const phd_adj_index *index, const phd_params *par, double dt,
                          const double *cons, const double *prim, const double *grad, const double *face_w,
                          const double *lam_next, double *lam, double *work, cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_adjoint_step_f64");
     return adjoint_step(mesh, index, par, dt, cons, prim, grad, face_w, lam_next, lam, work, nullptr, nullptr,
                         stream);
 }
@@ -431,6 +432,7 @@ int phd_adjoint_step_f64_taped(const phd_mesh *mesh, const phd_adj_index *index,
                                double dt, const double *cons, const double *prim, const double *grad,
                                const double *face_w, const double *lam_next, double *lam, double *work,
                                const double *tape_f64, const int32_t *tape_i32, cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_adjoint_step_f64_taped");
     if (!tape_f64 || !tape_i32) return PHD_ERR_ARG;
     return adjoint_step(mesh, index, par, dt, cons, prim, grad, face_w, lam_next, lam, work, tape_f64, tape_i32,
                         stream);
@@ -515,6 +517,7 @@ extern "C" {
 int phd_adjoint_step_f64_noalloc(const phd_mesh *mesh, const phd_adj_index *index, const phd_params *par,
                                  double dt, const double *cons, const double *prim, const double *grad,
                                  const double *face_w, const double *lam_next, double *lam, cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_adjoint_step_f64_noalloc");
     if (!mesh || mesh->n_cells < 0 || mesh->n_faces < 0) return PHD_ERR_ARG;
     if (phd_adjoint_work_doubles(mesh->n_cells, mesh->n_faces) > (size_t)PHD_ADJ_NOALLOC_MAX_DOUBLES)
         return PHD_ERR_SCRATCH_TOO_SMALL;

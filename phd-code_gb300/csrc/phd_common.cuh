@@ -3,6 +3,7 @@
 #include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include "../../include/phdflux.h"
 
 #define PHD_REAL_TAG 0
@@ -13,6 +14,16 @@
 #endif
 
 namespace phd {
+
+// A named NVTX range over the launches one entry point issues (Nsight tools can select
+// kernels by it, e.g. ncu --nvtx --nvtx-include "phd_step_f32/"); header-only NVTX costs
+// nothing when no tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange &) = delete;
+    NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Threads per block for a launch over n items with at most max_block threads: halved
 // (down to one warp) while the grid would not cover every SM twice, so small meshes

@@ -752,6 +752,7 @@ extern "C" {
 
 int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out, int32_t parts,
                           cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_prepare_f32");
     if (!mesh || mesh->dim != 2 || !out || parts < 0 || parts > (PHD_PREP_ALL | PHD_PREP_CELLS_FROM_FACES))
         return PHD_ERR_ARG;
     if ((parts & PHD_PREP_CELLS) && (parts & PHD_PREP_CELLS_FROM_FACES)) return PHD_ERR_ARG;
@@ -778,6 +779,7 @@ int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_
 
 int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, const float *crel32,
                                   phd_geom32_out *out, cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_prepare_f32_faces_compact");
     if (!mesh || mesh->dim != 2 || !out || !out->face_geo || !out->face_ar) return PHD_ERR_ARG;
     if (mesh->n_faces && (!area32 || !crel32 || !mesh->pair_i || !mesh->pair_j || !mesh->x)) return PHD_ERR_ARG;
     if (mesh->n_faces)
@@ -789,6 +791,7 @@ int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, con
 
 int phd_pair_i_from_face_ptr(const phd_mesh *mesh, const int32_t *face_ptr, int32_t *pair_i, int32_t *bad,
                              cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_pair_i_from_face_ptr");
     if (!mesh || !face_ptr || !pair_i || !bad || mesh->n_real < 1 || mesh->n_faces < 0) return PHD_ERR_ARG;
     k_pair_i_from_ptr<<<g32(mesh->n_real), B32, 0, stream>>>(mesh->n_real, mesh->n_faces, face_ptr, pair_i, bad);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
@@ -824,6 +827,7 @@ int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_
                          const phd_launch *launch, float *prim4, const double *cons, double *cons_next, float *grad8,
                          float *w2, float *flux4, phd_clock *clocks, int32_t n_runs, const int32_t *cell_run,
                          cudaStream_t stream, cudaEvent_t *marks) {
+    phd::NvtxRange nvtx_range("phd_step_f32");
     if (!mesh || mesh->dim != 2 || !geo || !par || !prim4 || !cons || !cons_next || !flux4 || !clocks)
         return PHD_ERR_ARG;
     const bool linear = par->reconstruction == PHD_LINEAR;

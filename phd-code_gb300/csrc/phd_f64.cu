@@ -665,6 +665,7 @@ static int step_f64(const phd_mesh *mesh, const phd_params *par, int32_t moving,
 int phd_step_f64_marked(const phd_mesh *mesh, const phd_params *par, int32_t moving, double *prim,
                         const double *cons, double *cons_next, double *grad, double *w, double *face_w,
                         double *flux, phd_clock *clk, cudaStream_t stream, cudaEvent_t *marks) {
+    phd::NvtxRange nvtx_range("phd_step_f64");
     return step_f64(mesh, par, moving, prim, cons, cons_next, grad, w, face_w, flux, clk, stream, marks,
                     GradTape{nullptr, nullptr});
 }
@@ -672,6 +673,7 @@ int phd_step_f64_marked(const phd_mesh *mesh, const phd_params *par, int32_t mov
 int phd_step_f64_taped(const phd_mesh *mesh, const phd_params *par, int32_t moving, double *prim,
                        const double *cons, double *cons_next, double *grad, double *w, double *face_w,
                        double *flux, double *tape_f64, int32_t *tape_i32, phd_clock *clk, cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_step_f64_taped");
     if (!tape_f64 || !tape_i32) return PHD_ERR_ARG;
     return step_f64(mesh, par, moving, prim, cons, cons_next, grad, w, face_w, flux, clk, stream, nullptr,
                     GradTape{tape_f64, tape_i32});
@@ -708,6 +710,7 @@ static int step_f64(const phd_mesh *mesh, const phd_params *par, int32_t moving,
 int phd_step_f64(const phd_mesh *mesh, const phd_params *par, int32_t moving, double *prim, const double *cons,
                  double *cons_next, double *grad, double *w, double *face_w, double *flux, phd_clock *clk,
                  cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_step_f64");
     return phd_step_f64_marked(mesh, par, moving, prim, cons, cons_next, grad, w, face_w, flux, clk, stream,
                                nullptr);
 }

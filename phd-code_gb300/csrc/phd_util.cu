@@ -334,6 +334,7 @@ size_t phd_csr_work_ints(int32_t n_cells) {
 
 int phd_build_csr(const phd_mesh *mesh, int32_t *nbr_ptr, int32_t *nbr_idx, int32_t *work, int32_t *bad,
                   cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_build_csr");
     if (!mesh || mesh->n_cells <= 0 || mesh->n_faces < 0 || !nbr_ptr || !work) return PHD_ERR_ARG;
     if (mesh->n_faces && (!mesh->pair_i || !mesh->pair_j || !nbr_idx)) return PHD_ERR_ARG;
     const int n = mesh->n_cells, F = mesh->n_faces;
@@ -367,6 +368,7 @@ int phd_periodic_twins(const phd_mesh *mesh, int32_t periodic, double box_x, dou
 
 int phd_move_generators(const phd_mesh *mesh, const float *w2, const double *w, phd_clock *clk, int32_t periodic,
                         double xmin0, double xmin1, double xmax0, double xmax1, double *x_out, cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_move_generators");
     if (!mesh || mesh->dim != 2 || !mesh->x || !clk || !x_out || (!w2) == (!w) || mesh->n_real < 0 ||
         mesh->n_real > mesh->n_cells || !(xmax0 > xmin0) || !(xmax1 > xmin1))
         return PHD_ERR_ARG;
