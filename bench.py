@@ -509,16 +509,17 @@ def run_e2e(args, st, mesh, prim, dev):
     """The same step through the public API with host buffers: every step the host
     hands over its tessellation from pinned memory with FluxStepper.load_mesh -- for
     FP32 the compact hand-over (per-cell face ranges, pair-j, FP32 area and centroid
-    offset, positions, ghost map: 16 B per face), for FP64 the full one (pair-i/j,
-    FP64 area and centroid, x, dcom, vol, map) -- which forms the neighbour lists, flip
-    bits, periodic twins and FP32 geometry on the device, re-creates the ghosts and
-    recovers the primitives; the step runs; the generator velocities (what the host
-    re-mesh needs) and the clock come back."""
+    offset: 16 B per face, plus the ghost map and ghost codes; the real cells' positions
+    are the device's own, as after its generator move), for FP64 the full one (pair-i/j,
+    FP64 area and centroid, x, dcom, vol, map) -- which forms the neighbour lists, ghost
+    positions, flip bits, periodic twins and FP32 geometry on the device, re-creates the
+    ghosts and recovers the primitives; the step runs; the generator velocities (what the
+    host re-mesh needs) and the clock come back."""
     import torch
     from phd_code_gb300 import _lib as L
     dm = st.dmesh
     fp32 = st.precision == "fp32"
-    pinned = dm.pinned_host_compact(mesh) if fp32 else dm.pinned_host(mesh)
+    pinned = dm.pinned_host_compact(mesh, resident=True) if fp32 else dm.pinned_host(mesh)
     w_host = torch.empty_like(st.w2 if st.precision == "fp32" else st.w, device="cpu").pin_memory()
     clk_host = torch.empty(L.CLOCK_BYTES, dtype=torch.uint8).pin_memory()
     d2h = w_host.numel() * w_host.element_size() + clk_host.numel()
@@ -558,7 +559,8 @@ def run_e2e(args, st, mesh, prim, dev):
             "what": "per step: host tessellation H2D from pinned memory (%s); neighbour lists, flip bits, "
                     "periodic twins, FP32 geometry, ghost refresh and primitives formed on the device; flux step; "
                     "generator velocities + clock D2H" % ("compact FP32 face list: per-cell face ranges, pair-j, "
-                                                           "FP32 area and centroid offset; FP64 positions, ghost map"
+                                                           "FP32 area and centroid offset; ghost map and codes (real "
+                                                           "positions stay on the device)"
                                                            if fp32 else "face list + cell geometry, FP64")}
 
 
@@ -701,7 +703,7 @@ def run_moving(args, rank, world):
                      device=dev)
     c0 = st.cons_host()[:, :nr].sum(axis=1)
     x = np.ascontiguousarray(mesh.x[:, :nr])
-    mesher = pkg.tess.CompactMesher("periodic")
+    mesher = pkg.tess.CompactMesher("periodic", resident=True)
     phases = {"device_step_and_move": 0.0, "positions_d2h": 0.0, "tessellation_to_hand_over": 0.0, "load_mesh": 0.0}
     faces = 0
     n_steps = max(1, min(args.steps, 20))

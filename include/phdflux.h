@@ -254,6 +254,17 @@ int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_
 int phd_move_generators(const phd_mesh *mesh, const float *w2, const double *w, phd_clock *clk, int32_t periodic,
                         double xmin0, double xmin1, double xmax0, double xmax1, double *x_out, cudaStream_t stream);
 
+/* The ghost rows of mesh->x from their images' rows (the real rows already hold the
+ * current positions, e.g. from phd_move_generators): per ghost g, ghost_code[g - n_real]
+ * = 1 + 3 (sx + 1) + (sy + 1) for a periodic copy shifted by (sx, sy) box lengths
+ * (x + s (xmax - xmin)), 16 + 2 k + h for a mirror image across axis k at its low
+ * (h = 0) or high (h = 1) wall (x - 2 (x - wall)) -- the host tessellation's own
+ * arithmetic, so the positions equal the host's bit for bit.  Invalid codes or images
+ * add to *bad (device) and leave the row unwritten.  With it a re-mesh hands over no
+ * positions at all (mesh->x is written through the const mesh view). */
+int phd_ghost_positions(const phd_mesh *mesh, const int8_t *ghost_code, double xmin0, double xmin1, double xmax0,
+                        double xmax1, int32_t *bad, cudaStream_t stream);
+
 /* Compact FP32 hand-over of a re-mesh (the per-step upload of the face list,
  * mesh.pyx:255-323, in 16 B per face instead of 32): the host sends pair-j, the area
  * and the centroid offset com - (x_i + x_j)/2 (formed in FP64) rounded once to FP32,

@@ -99,9 +99,15 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
  * com - (x_i + x_j)/2 (formed in FP64) rounded to FP32 -- area32[n_faces],
  * crel32[n_faces][2] -- and the cells' positions x[2][n_cells] (x row then y row), image
  * map, tags (Real 0 / Ghost 1) and types (Undefined 4 for real cells, Exterior 2 for
- * ghosts), written into caller buffers (e.g. pinned host memory reused across steps). */
+ * ghosts), written into caller buffers (e.g. pinned host memory reused across steps).
+ * x may be NULL (the device already holds the real cells' positions, e.g. from its own
+ * generator move); ghost_code[n_cells - n_real] (may be NULL) says how each ghost images
+ * its real cell, so the device can form the ghost positions itself
+ * (phd_ghost_positions of phdflux.h): 1 + 3 (sx + 1) + (sy + 1) for a periodic copy
+ * shifted by (sx, sy) box lengths, 16 + 2 k + h for a mirror image across axis k at its
+ * low (h = 0) or high (h = 1) wall. */
 int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *crel32,
-                            double *x, int32_t *map, int8_t *tag, int8_t *type);
+                            double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code);
 
 /* hilbert_key_2d (phd/hilbert/hilbert.pyx:9-23) for n integer coordinate pairs. */
 void phd_hilbert_keys_2d_host(const int32_t *xh, const int32_t *yh, int64_t n, int order, int64_t *keys);

@@ -122,6 +122,7 @@ SIGNATURES = {
     "phd_build_csr": ([_PM, _vp, _vp, _vp, _vp, _vp], C.c_int),
     "phd_pair_i_from_face_ptr": ([_PM, _vp, _vp, _vp, _vp], C.c_int),
     "phd_move_generators": ([_PM, _vp, _vp, _vp, _i32, _f64, _f64, _f64, _f64, _vp, _vp], C.c_int),
+    "phd_ghost_positions": ([_PM, _vp, _f64, _f64, _f64, _f64, _vp, _vp], C.c_int),
     "phd_prepare_f32_faces_compact": ([_PM, _vp, _vp, C.POINTER(PhdGeom32Out), _vp], C.c_int),
     "phd_periodic_twins": ([_PM, _i32, _f64, _f64, _vp, _vp], C.c_int),
 }

@@ -244,6 +244,7 @@ struct Geometry {   // one phd_mesh2d_build result
     double pad_used = 0.;
     std::vector<double> x, y, vol, dcx, dcy, area, comx, comy, nx, ny;
     std::vector<int32_t> map, pair_i, pair_j, nbr_ptr, nbr_idx;
+    std::vector<int8_t> gcode;      // per kept ghost: how it images its real cell (ghost_code)
 };
 
 }  // namespace
@@ -675,9 +676,12 @@ void face_lists(int n_cells, const std::vector<int32_t> &pi, const std::vector<i
 }
 
 // ghost images of the real generators (the numpy builder's _ghosts)
+// Ghost codes (phdtess.h): periodic shift (sx, sy) -> 1 + 3 (sx + 1) + (sy + 1);
+// reflective mirror across axis k at its low / high wall -> 16 + 2 k + (high).
 void make_ghosts(const double *x, const double *y, int n, int boundary, const double xmin[2], const double xmax[2],
-                 double pad, std::vector<double> &gx, std::vector<double> &gy, std::vector<int32_t> &gmap) {
-    gx.clear(); gy.clear(); gmap.clear();
+                 double pad, std::vector<double> &gx, std::vector<double> &gy, std::vector<int32_t> &gmap,
+                 std::vector<int8_t> &gcode) {
+    gx.clear(); gy.clear(); gmap.clear(); gcode.clear();
     const double L0 = xmax[0] - xmin[0], L1 = xmax[1] - xmin[1];
     if (boundary == 0) {
         for (int sx = -1; sx <= 1; sx++)
@@ -687,6 +691,7 @@ void make_ghosts(const double *x, const double *y, int n, int boundary, const do
                     const double xs = x[i] + double(sx) * L0, ys = y[i] + double(sy) * L1;
                     if (xs > xmin[0] - pad && xs < xmax[0] + pad && ys > xmin[1] - pad && ys < xmax[1] + pad) {
                         gx.push_back(xs); gy.push_back(ys); gmap.push_back(i);
+                        gcode.push_back(int8_t(1 + 3 * (sx + 1) + (sy + 1)));
                     }
                 }
             }
@@ -702,6 +707,7 @@ void make_ghosts(const double *x, const double *y, int n, int boundary, const do
                     if (k == 0) xs = xs - 2.0 * (xs - edge);
                     else ys = ys - 2.0 * (ys - edge);
                     gx.push_back(xs); gy.push_back(ys); gmap.push_back(i);
+                    gcode.push_back(int8_t(16 + 2 * k + (lo ? 0 : 1)));
                 }
             }
     }
@@ -963,8 +969,9 @@ int phd_mesh2d_build_strips(phd_tess2d *t, const double *x, const double *y, int
     try {
         std::vector<double> gx, gy, ax, ay;
         std::vector<int32_t> gmap;
+        std::vector<int8_t> gcode;
         for (int attempt = 0; attempt < 6; attempt++, pad *= 2.0) {
-            make_ghosts(x, y, n_real, boundary, xmin, xmax, pad, gx, gy, gmap);
+            make_ghosts(x, y, n_real, boundary, xmin, xmax, pad, gx, gy, gmap, gcode);
             const int n_all = n_real + int(gx.size());
             ax.assign(x, x + n_real);
             ax.insert(ax.end(), gx.begin(), gx.end());
@@ -1014,6 +1021,7 @@ int phd_mesh2d_build_strips(phd_tess2d *t, const double *x, const double *y, int
             G.n_faces = F;
             G.pad_used = pad;
             G.x.resize(nc); G.y.resize(nc); G.map.resize(nc); G.vol.resize(nc); G.dcx.resize(nc); G.dcy.resize(nc);
+            G.gcode.assign(nc - n_real, 0);
             for (int i = 0; i < n_real; i++) {
                 G.x[i] = x[i]; G.y[i] = y[i]; G.map[i] = i;
                 G.vol[i] = vol[i]; G.dcx[i] = dcx[i]; G.dcy[i] = dcy[i];
@@ -1023,6 +1031,7 @@ int phd_mesh2d_build_strips(phd_tess2d *t, const double *x, const double *y, int
                 if (c < 0) continue;
                 const int img = gmap[g - n_real];
                 G.x[c] = ax[g]; G.y[c] = ay[g]; G.map[c] = img;
+                G.gcode[c - n_real] = gcode[g - n_real];
                 G.vol[c] = vol[img]; G.dcx[c] = dcx[img]; G.dcy[c] = dcy[img];
             }
             face_lists(nc, G.pair_i, G.pair_j, G.nbr_ptr, G.nbr_idx);
@@ -1055,8 +1064,8 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
 }
 
 int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *crel32,
-                            double *x, int32_t *map, int8_t *tag, int8_t *type) {
-    if (!t || t->G.n_cells == 0 || !face_ptr || !pair_j || !area32 || !crel32 || !x || !map || !tag || !type)
+                            double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
+    if (!t || t->G.n_cells == 0 || !face_ptr || !pair_j || !area32 || !crel32 || !map || !tag || !type)
         return -2;
     const Geometry &G = t->G;
     const int nr = G.n_real, n = G.n_cells, F = G.n_faces;
@@ -1076,8 +1085,11 @@ int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pai
         crel32[2 * size_t(f) + 1] = round32(G.comy[f] - 0.5 * (G.y[i] + G.y[j]));
     }
     while (c < nr) face_ptr[++c] = F;
-    std::memcpy(x, G.x.data(), sizeof(double) * n);
-    std::memcpy(x + n, G.y.data(), sizeof(double) * n);
+    if (x) {
+        std::memcpy(x, G.x.data(), sizeof(double) * n);
+        std::memcpy(x + n, G.y.data(), sizeof(double) * n);
+    }
+    if (ghost_code && n > nr) std::memcpy(ghost_code, G.gcode.data(), sizeof(int8_t) * (n - nr));
     std::memcpy(map, G.map.data(), sizeof(int32_t) * n);
     for (int k = 0; k < n; k++) {
         tag[k] = k < nr ? 0 : 1;                        // Real / Ghost (particle_tags.py:1-6)

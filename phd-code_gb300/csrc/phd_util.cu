@@ -295,6 +295,41 @@ __global__ void k_move_generators(int n_real, int n, const double *__restrict__ 
     x_out[(size_t)n_real + i] = xo[1];
 }
 
+
+// Ghost positions from the real cells' (domain_manager.pyx:712-774 ghost copies;
+// boundary.pyx:66-130 mirror images, 351-400 periodic copies), with the host
+// tessellation's arithmetic: x + s L for a periodic copy, x - 2 (x - wall) across a
+// mirror.  code (per ghost): 1 + 3 (sx + 1) + (sy + 1) periodic, 16 + 2 k + h mirror.
+__global__ void k_ghost_positions(int n_real, int n, const int32_t *__restrict__ map,
+                                  const int8_t *__restrict__ code, double lo0, double lo1, double hi0, double hi1,
+                                  double *__restrict__ x, int *bad) {
+    const int g = n_real + blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int img = map[g];
+    const int c = code[g - n_real];
+    if (img < 0 || img >= n_real) { atomicAdd(bad, 1); return; }
+    double px = x[img], py = x[(size_t)n + img];
+    if (c >= 1 && c <= 9 && c != 5) {
+        const int sx = (c - 1) / 3 - 1, sy = (c - 1) % 3 - 1;
+        px = __dadd_rn(px, __dmul_rn(double(sx), __dsub_rn(hi0, lo0)));
+        py = __dadd_rn(py, __dmul_rn(double(sy), __dsub_rn(hi1, lo1)));
+    } else if (c >= 16 && c <= 19) {
+        const int k = (c - 16) >> 1, high = (c - 16) & 1;
+        if (k == 0) {
+            const double wall = high ? hi0 : lo0;
+            px = __dsub_rn(px, __dmul_rn(2.0, __dsub_rn(px, wall)));
+        } else {
+            const double wall = high ? hi1 : lo1;
+            py = __dsub_rn(py, __dmul_rn(2.0, __dsub_rn(py, wall)));
+        }
+    } else {
+        atomicAdd(bad, 1);
+        return;
+    }
+    x[g] = px;
+    x[(size_t)n + g] = py;
+}
+
 }  // namespace phd
 
 extern "C" {
@@ -376,6 +411,22 @@ int phd_move_generators(const phd_mesh *mesh, const float *w2, const double *w, 
     phd::k_move_generators<<<(mesh->n_real + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(
         mesh->n_real, mesh->n_cells, mesh->x, reinterpret_cast<const float2 *>(w2), w, clk, periodic, xmin0, xmin1,
         xmax0, xmax1, x_out, &clk->status);
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+
+int phd_ghost_positions(const phd_mesh *mesh, const int8_t *ghost_code, double xmin0, double xmin1, double xmax0,
+                        double xmax1, int32_t *bad, cudaStream_t stream) {
+    phd::NvtxRange nvtx_range("phd_ghost_positions");
+    if (!mesh || mesh->dim != 2 || !mesh->x || !mesh->map || !bad || mesh->n_real < 0 ||
+        mesh->n_real > mesh->n_cells || !(xmax0 > xmin0) || !(xmax1 > xmin1))
+        return PHD_ERR_ARG;
+    const int ng = mesh->n_cells - mesh->n_real;
+    if (ng == 0) return PHD_OK;
+    if (!ghost_code) return PHD_ERR_ARG;
+    phd::k_ghost_positions<<<(ng + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(
+        mesh->n_real, mesh->n_cells, mesh->map, ghost_code, xmin0, xmin1, xmax0, xmax1, const_cast<double *>(mesh->x),
+        bad);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 

@@ -145,14 +145,35 @@ class DeviceMesh:
         return {nm: torch.from_numpy(np.ascontiguousarray(getattr(host, nm), dtype=dt)).pin_memory()
                 for nm, dt in self.UPLOAD}
 
-    def pinned_host_compact(self, host):
+    def ghost_codes(self, host):
+        """How each ghost of ``host`` images its real cell (phd_ghost_positions): a
+        periodic shift (sx, sy) -> 1 + 3 (sx + 1) + (sy + 1); a mirror across axis k at
+        its low / high wall -> 16 + 2 k + (high)."""
+        nr = host.n_real
+        g = np.arange(nr, host.n_cells)
+        img = host.map[g]
+        x = np.asarray(host.x)
+        lo, hi = np.asarray(host.xmin, dtype=np.float64), np.asarray(host.xmax, dtype=np.float64)
+        d = x[:, g] - x[:, img]
+        if host.boundary == "periodic":
+            s = np.rint(d / (hi - lo)[:, None]).astype(np.int64)
+            code = 1 + 3 * (s[0] + 1) + (s[1] + 1)
+        else:
+            k = (d[1] != 0.0).astype(np.int64)                 # the mirrored axis
+            high = x[k, g] > 0.5 * (lo[k] + hi[k])
+            code = 16 + 2 * k + high.astype(np.int64)
+        return code.astype(np.int8)
+
+    def pinned_host_compact(self, host, resident=False):
         """The compact hand-over of a re-mesh for the FP32 path, 16 B per face instead of
         32: per-real-cell face ranges ``face_ptr`` instead of pair-i (faces are emitted
         per real cell in ascending order, tess.cpp:363), pair-j, and the area and the
         centroid offset com - (x_i + x_j)/2 -- formed in FP64 as the device would --
         rounded once to FP32 (round to nearest even; magnitudes below 2^-126 to signed
         zero, as the device's own rounding does), plus the cells' positions and maps.
-        The FP32 face geometry formed from it equals the full hand-over's bit for bit."""
+        The FP32 face geometry formed from it equals the full hand-over's bit for bit.
+        ``resident``: the device already holds the real cells' positions (its own
+        generator move); ghost codes replace the positions (``phd_ghost_positions``)."""
         self._check_remesh(host)
         nr = self.n_real
         pi, pj = np.asarray(host.pair_i), np.asarray(host.pair_j)
@@ -169,9 +190,13 @@ class DeviceMesh:
         arrays = {"face_ptr": face_ptr, "pair_j": np.ascontiguousarray(pj, dtype=np.int32),
                   "area32": round32(np.asarray(host.area, dtype=np.float64)),
                   "crel32": np.ascontiguousarray(round32(c64).T),
-                  "x": np.ascontiguousarray(x), "map": np.ascontiguousarray(host.map, dtype=np.int32),
+                  "map": np.ascontiguousarray(host.map, dtype=np.int32),
                   "tag": np.ascontiguousarray(host.tag, dtype=np.int8),
                   "type": np.ascontiguousarray(host.type, dtype=np.int8)}
+        if resident:            # the device holds the real positions; ghosts from their codes
+            arrays["ghost_code"] = self.ghost_codes(host)
+        else:
+            arrays["x"] = np.ascontiguousarray(x)
         return {k: torch.from_numpy(v).pin_memory() for k, v in arrays.items()}
 
     @staticmethod
@@ -185,9 +210,12 @@ class DeviceMesh:
                   "x": (self.dim, self.n_cells), "dcom": (self.dim, self.n_cells), "vol": (self.n_cells,),
                   "pair_i": (self.n_faces,), "pair_j": (self.n_faces,), "area": (self.n_faces,),
                   "com": (self.dim, self.n_faces), "face_ptr": (self.n_real + 1,), "area32": (self.n_faces,),
-                  "crel32": (self.n_faces, self.dim)}
-        names = (("face_ptr", "pair_j", "area32", "crel32", "x", "map", "tag", "type") if "face_ptr" in pinned
-                 else [nm for nm, _ in self.UPLOAD])
+                  "crel32": (self.n_faces, self.dim), "ghost_code": (self.n_cells - self.n_real,)}
+        if "face_ptr" in pinned:
+            names = ("face_ptr", "pair_j", "area32", "crel32", "map", "tag", "type") + \
+                (("x",) if "x" in pinned else ("ghost_code",))
+        else:
+            names = [nm for nm, _ in self.UPLOAD]
         for nm in names:
             if tuple(pinned[nm].shape) != shapes[nm]:
                 raise ValueError("upload: %s has shape %s, this mesh holds %s" % (nm, tuple(pinned[nm].shape),

@@ -176,10 +176,17 @@ class FluxStepper:
         codes and face geometry are formed on a second stream while the rest of the mesh
         is still being copied.  ``pinned`` is either the full hand-over
         (``DeviceMesh.pinned_host``) or, for FP32 steppers, the compact one
-        (``DeviceMesh.pinned_host_compact``: 16 B per face, pair-i from per-cell face
-        ranges).  Returns the bytes copied."""
+        (``DeviceMesh.pinned_host_compact`` / ``tess.CompactMesher``: 16 B per face, pair-i
+        from per-cell face ranges); a compact hand-over without positions keeps the real
+        cells' positions on the device -- the last generator move's (``move_generators``)
+        or the current ones -- and forms the ghosts' from their codes
+        (``phd_ghost_positions``).  Returns the bytes copied."""
         dm, p = self.dmesh, self.params
         main = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        resident = "x" not in pinned          # positions stay on the device (ghost codes come instead)
+        if resident:
+            with torch.cuda.stream(main):
+                xr = self._real_positions()
         n_new, f_new = dm.pinned_sizes(pinned)
         resized = (n_new, f_new) != (dm.n_cells, dm.n_faces)
         if resized:
@@ -218,9 +225,22 @@ class FluxStepper:
         side.wait_event(ev[0])
         dm.build_lists(side)
         if resized:
-            nbytes += dm.copy_fields(pinned, ("x", "tag", "type", "map"), main)
+            nbytes += dm.copy_fields(pinned, ("tag", "type", "map"), main)
         else:
-            nbytes += dm.copy_fields(pinned, ("x",), main) + dm.copy_ghost_map(pinned, main)
+            nbytes += dm.copy_ghost_map(pinned, main)
+        if resident:
+            code = self._view("ghost_code_in", (dm.n_cells - dm.n_real,), torch.int8)
+            with torch.cuda.stream(main):
+                for k in range(dm.dim):                       # row by row: plain device copies
+                    dm.x[k, :dm.n_real].copy_(xr[k])
+                code.copy_(pinned["ghost_code"], non_blocking=True)
+            nbytes += code.numel()
+            L.check(lib.phd_ghost_positions(dm.ref, L.ptr(code), float(dm.xmin[0]), float(dm.xmin[1]),
+                                            float(dm.xmax[0]), float(dm.xmax[1]), L.ptr(dm._bad), s),
+                    "phd_ghost_positions")
+        else:
+            nbytes += dm.copy_fields(pinned, ("x",), main)
+            self._x_real_valid = False
         ev[1].record(main)
         if fp32:
             side.wait_event(ev[1])
@@ -303,6 +323,18 @@ class FluxStepper:
                                             int(dm.boundary == "periodic"), float(dm.xmin[0]), float(dm.xmin[1]),
                                             float(dm.xmax[0]), float(dm.xmax[1]), L.ptr(out),
                                             L.stream_handle(self.stream)), "phd_move_generators")
+        self._x_real_valid = True
+        return out
+
+    def _real_positions(self):
+        """The [2][n_real] positions of the real cells the next hand-over starts from: the
+        last generator move's, else (copied once) the mesh's own."""
+        dm = self.dmesh
+        out = self._view("x_moved", (dm.dim, dm.n_real), torch.float64)
+        if not getattr(self, "_x_real_valid", False):
+            for k in range(dm.dim):
+                out[k].copy_(dm.x[k, :dm.n_real])
+            self._x_real_valid = True
         return out
 
     def step(self, n=1):

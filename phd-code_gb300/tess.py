@@ -32,7 +32,7 @@ _SIGNATURES = {
     "phd_mesh2d_build_strips": ([_vp, _vp, _vp, _i32, _i32, _f64, _f64, _f64, _f64, _f64, _i32], C.c_int),
     "phd_mesh2d_sizes": ([_vp, _vp, _vp, _vp], C.c_int),
     "phd_mesh2d_copy": ([_vp] * 16, C.c_int),
-    "phd_mesh2d_copy_compact": ([_vp] * 9, C.c_int),
+    "phd_mesh2d_copy_compact": ([_vp] * 10, C.c_int),
     "phd_hilbert_keys_2d_host": ([_vp, _vp, C.c_int64, C.c_int, _vp], None),
 }
 
@@ -167,10 +167,14 @@ class CompactMesher:
     overwrites them: let the copies of the previous hand-over finish (any
     synchronisation of the stepper's stream) before calling again."""
 
-    def __init__(self, boundary, xmin=(0.0, 0.0), xmax=(1.0, 1.0), n_strips=0):
+    def __init__(self, boundary, xmin=(0.0, 0.0), xmax=(1.0, 1.0), n_strips=0, resident=False):
+        """``resident``: the device already holds the real cells' positions (from its own
+        generator move, ``FluxStepper.move_generators``): hand over ghost codes instead of
+        positions (``phd_ghost_positions``)."""
         if boundary not in ("periodic", "reflective"):
             raise ValueError("boundary must be 'periodic' or 'reflective'")
         self.boundary, self.xmin, self.xmax, self.n_strips = boundary, tuple(xmin), tuple(xmax), int(n_strips)
+        self.resident = bool(resident)
         self._h = lib().phd_tess2d_create()
         if not self._h:
             raise MemoryError("phd_tess2d_create")
@@ -208,11 +212,19 @@ class CompactMesher:
                "pair_j": self._pinned("pair_j", (F,), torch.int32),
                "area32": self._pinned("area32", (F,), torch.float32),
                "crel32": self._pinned("crel32", (F, 2), torch.float32),
-               "x": self._pinned("x", (2, nc), torch.float64), "map": self._pinned("map", (nc,), torch.int32),
+               "map": self._pinned("map", (nc,), torch.int32),
                "tag": self._pinned("tag", (nc,), torch.int8), "type": self._pinned("type", (nc,), torch.int8)}
-        _check(L.phd_mesh2d_copy_compact(self._h, *(C.c_void_p(out[k].data_ptr()) for k in
-                                                    ("face_ptr", "pair_j", "area32", "crel32", "x", "map", "tag",
-                                                     "type"))), "copy_compact")
+        if self.resident:
+            out["ghost_code"] = self._pinned("ghost_code", (nc - n,), torch.int8)
+        else:
+            out["x"] = self._pinned("x", (2, nc), torch.float64)
+
+        def ptr(k):
+            return C.c_void_p(out[k].data_ptr()) if k in out else None
+
+        _check(L.phd_mesh2d_copy_compact(self._h, *(ptr(k) for k in ("face_ptr", "pair_j", "area32", "crel32", "x",
+                                                                      "map", "tag", "type", "ghost_code"))),
+               "copy_compact")
         return out
 
 

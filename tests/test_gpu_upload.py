@@ -349,3 +349,44 @@ def test_generator_leaving_a_reflective_box_is_flagged():
     st.move_generators()                             # cells at the wall cross it in one step
     with pytest.raises(RuntimeError, match="particle left domain in reflective boundary condition"):
         st.check_status()
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+def test_resident_positions_hand_over_equals_the_full_one(boundary):
+    """A compact hand-over without positions: the real positions stay on the device and
+    the ghosts' come from their codes (phd_ghost_positions) -- equal to the host's bit
+    for bit, so the steps are identical to the full hand-over's; with the device's own
+    generator move in the loop, positions never cross the link to the device."""
+    meshes = _moved_meshes(20, boundary, 11, 3)
+    prim = smooth_state(meshes[0])
+    a = FluxStepper(meshes[0], prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32")
+    b = FluxStepper(meshes[0], prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32")
+    nb_full = a.load_mesh(a.dmesh.pinned_host(meshes[0]))
+    nb = b.load_mesh(b.dmesh.pinned_host_compact(meshes[0], resident=True))
+    assert nb < 0.55 * nb_full
+    torch.cuda.synchronize()
+    assert b.dmesh.upload_errors() == 0
+    assert torch.equal(a.dmesh.x, b.dmesh.x)                    # ghosts formed on the device
+    a.step(2)
+    b.step(2)
+    assert np.array_equal(a.cons_host(), b.cons_host())
+    # the whole loop: device move, host tessellation of the moved generators, resident hand-over
+    mesher = pkg.tess.CompactMesher(boundary, resident=True)
+    full = pkg.tess.CompactMesher(boundary)
+    for _ in range(3):
+        a.step(1)
+        b.step(1)
+        xa = a.move_generators()
+        xb = b.move_generators()
+        a.check_status()
+        x_host = xa.cpu().numpy()
+        assert np.array_equal(x_host, xb.cpu().numpy())
+        a.load_mesh(full(x_host))
+        b.load_mesh(mesher(x_host))
+        torch.cuda.synchronize()
+        assert b.dmesh.upload_errors() == 0
+        assert torch.equal(a.dmesh.x, b.dmesh.x)
+    a.step(2)
+    b.step(2)
+    a.check_status()
+    assert np.array_equal(a.cons_host(), b.cons_host())
