@@ -122,7 +122,7 @@ class DeviceMesh:
         self._point_struct()
         return moved
 
-    # --- per-step hand-over of a new tessellation of the same size -----------------
+    # --- per-step hand-over of a new tessellation (resize first when its counts differ)
     UPLOAD = (("tag", np.int8), ("type", np.int8), ("map", np.int32), ("x", np.float64),
               ("dcom", np.float64), ("vol", np.float64), ("pair_i", np.int32), ("pair_j", np.int32),
               ("area", np.float64), ("com", np.float64))
@@ -273,7 +273,8 @@ class DeviceMesh:
             raise ValueError("normals must be 'device' or 'none'")
 
     def upload(self, pinned, normals="device", stream=None):
-        """Hand over a new tessellation with this mesh's cell and face counts.
+        """Hand over a new tessellation with this mesh's cell and face counts (``resize``
+        first for other counts).
 
         Copies the face list (pair-i/j, area, centroid) and the cell geometry (x, dcom,
         vol, tag, type, map) from pinned host buffers, then forms on the device what
