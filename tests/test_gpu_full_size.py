@@ -108,3 +108,50 @@ def test_ensemble_256_runs_batch_equals_single_runs():
         st.step(5)
         assert np.array_equal(ens.run_cons(r), st.cons_host()[:, :m.n_real])
         assert ens.read_clocks()[r].dt == st.read_clock().dt
+
+
+def test_differentiation_workload_gradient_vs_autograd():
+    """The differentiation workload at its full size (128x128 periodic, HLLC, CFL 0.4,
+    200 recorded steps, checkpoint every 20; start: the background with 1e-3 seeded
+    noise; loss: squared distance of the final density to the evolved Gaussian bump):
+    the hand-written adjoint's gradient against PyTorch autograd through the independent
+    FP64 step (oracle/torch_step.py) over the same 200 steps.  Autograd follows the
+    branches its own forward pass takes, as the adjoint does, so this measures the
+    derivative of the piecewise-smooth map on the branch actually taken -- which central
+    differences cannot, once the perturbation crosses a limiter switch."""
+    import torch_step as T
+    from phd_code_gb300.adjoint import FluxRun, FluxRunRecord, StepRecord
+    from phd_code_gb300.device import DeviceMesh
+    mesh, prim_bump, _ = pkg.problems.gaussian_bump(128, background=False)
+    _, prim_bg, _ = pkg.problems.gaussian_bump(128, background=True)
+    nr = mesh.n_real
+    dm = DeviceMesh(mesh)
+    st_t = FluxStepper(dm, prim_bump, gamma=1.4, cfl=0.4, solver="hllc", moving=False)
+    st_t.step(200)
+    target = st_t.prim[0, :nr].clone()
+    rng = np.random.default_rng(3)
+    p_init = prim_bg.copy()
+    p_init[:, :nr] += 1e-3 * rng.uniform(-1.0, 1.0, (4, nr))
+    p_init = pkg.meshgen.fill_ghosts(mesh, p_init)
+    st = FluxStepper(dm, p_init, gamma=1.4, cfl=0.4, solver="hllc", moving=False)
+    fw = torch.zeros((2, mesh.n_faces), dtype=torch.float64, device="cuda")
+    recs = []
+    for _ in range(200):
+        recs.append(StepRecord(dm, fw, st.read_clock().dt))
+        st.step(1)
+    run = FluxRunRecord(recs, gamma=1.4, solver="hllc", checkpoint=20)
+    p0 = torch.as_tensor(p_init[:, :nr]).cuda().requires_grad_(True)
+    ((FluxRun.apply(p0, run) - target) ** 2).sum().backward()
+    g = p0.grad.detach()
+    # autograd through the PyTorch FP64 step on the device, same dt schedule
+    tm = T.TorchMesh(mesh, device="cuda")
+    vol = torch.as_tensor(mesh.vol[:nr]).cuda()
+    pp = torch.as_tensor(p_init[:, :nr]).cuda().requires_grad_(True)
+    U = T.cons_from_prim(pp, vol, 1.4)
+    for rec in recs:
+        U = T.step(tm, U, fw, rec.dt, 1.4)
+    ((U[0] / vol - target) ** 2).sum().backward()
+    gr = pp.grad.detach()
+    rel = (torch.linalg.norm(g - gr) / torch.linalg.norm(gr)).item()
+    print("differentiation workload: adjoint vs autograd, normwise relative difference %.3e" % rel)
+    assert rel <= 1e-10, rel
