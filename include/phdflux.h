@@ -337,7 +337,9 @@ int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_p
 
 /* ---- adjoint of one FP64 step ----------------------------------------------------
  * Reverse mode of U' = step(U) with the mesh, the face velocities and dt held fixed
- * (HLL / HLLC, constant or linear reconstruction, both limiters).  Index tables:
+ * (HLL / HLLC / exact -- the exact solver's p* by implicit differentiation of its
+ * converged Newton root --, constant or linear reconstruction, both limiters).  Index
+ * tables:
  *   partner [2F]          for each nbr_idx entry, the entry of the same face in the
  *                         other cell's list
  *   ghost_ptr [n_real+1], ghost_idx: the ghosts of each real cell (CSR by image).

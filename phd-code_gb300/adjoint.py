@@ -102,8 +102,8 @@ class FluxRunRecord:
 
     def __init__(self, steps, gamma=1.4, solver="hllc", limiter="arepo", gizmo=True, boost=True,
                  reconstruction="linear", checkpoint=20, final_vol=None):
-        if solver not in ("hll", "hllc"):
-            raise ValueError("the adjoint covers the HLL and HLLC solvers")
+        if solver not in ("hll", "hllc", "exact"):
+            raise ValueError("solver must be 'hll', 'hllc' or 'exact'")
         self.steps = steps
         self.params = make_params(gamma=gamma, solver=solver, limiter=limiter, gizmo=gizmo, boost=boost,
                                   reconstruction=reconstruction)

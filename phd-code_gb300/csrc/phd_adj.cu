@@ -105,6 +105,9 @@ __device__ __forceinline__ void spatial_rev_f64(const SpatialTape &t, const doub
     }
 }
 
+// EXACT: the exact solver's reverse (exact_flux_adj); otherwise HLL / HLLC -- separate
+// instantiations, so the HLL-family kernel carries none of the exact solver's registers.
+template <bool EXACT>
 __global__ void __launch_bounds__(BA) k_adj_face(phd_mesh M, phd_params P, double dt, const double *__restrict__ prim,
                                                  const double *__restrict__ grad, const double *__restrict__ face_w,
                                                  const double *__restrict__ lam_next, double *__restrict__ out) {
@@ -145,7 +148,8 @@ __global__ void __launch_bounds__(BA) k_adj_face(phd_mesh M, phd_params P, doubl
             if (boost) for (int k = 0; k < 2; k++) { L[1 + k] -= w[k]; R[1 + k] -= w[k]; }
         }
         double aL[4] = {0, 0, 0, 0}, aR[4] = {0, 0, 0, 0};
-        hll_family_adj<double>(P.solver == PHD_HLLC, L, R, nrm, w, P.gamma, boost, aF, aL, aR);
+        if (EXACT) exact_flux_adj(L, R, nrm, w, P.gamma, P.exact_max_iter, aF, aL, aR);
+        else hll_family_adj<double>(P.solver == PHD_HLLC, L, R, nrm, w, P.gamma, boost, aF, aL, aR);
         double *api = res, *apj = res + 4, *agi = res + 8, *agj = res + 16;
         if (linear) {
             double aLs[4] = {0, 0, 0, 0}, aRs[4] = {0, 0, 0, 0};
@@ -445,7 +449,7 @@ static int adjoint_step(const phd_mesh *mesh, const phd_adj_index *index, const 
     if (!mesh || mesh->dim != 2 || !index || !par || !cons || !prim || !lam_next || !lam || !work)
         return PHD_ERR_ARG;
     if (mesh->n_faces && !mesh->normal) return PHD_ERR_ARG;
-    if (par->solver != PHD_HLL && par->solver != PHD_HLLC) return PHD_ERR_UNSUPPORTED;
+    if (par->solver < PHD_HLL || par->solver > PHD_EXACT) return PHD_ERR_ARG;
     if (par->reconstruction == PHD_LINEAR && !grad) return PHD_ERR_ARG;
     const phd_mesh &M = *mesh;
     const size_t n = M.n_cells, F = M.n_faces;
@@ -456,7 +460,10 @@ static int adjoint_step(const phd_mesh *mesh, const phd_adj_index *index, const 
     double *prim_adj = self_adj + 4 * n;           // [4][n]
     cudaMemsetAsync(entry_adj, 0, sizeof(double) * 8 * F, stream);
     cudaMemsetAsync(self_adj, 0, sizeof(double) * 4 * n, stream);
-    if (F) k_adj_face<<<ga((int)F), ba((int)F), 0, stream>>>(M, *par, dt, prim, grad, face_w, lam_next, face_adj);
+    if (F && par->solver == PHD_EXACT)
+        k_adj_face<true><<<ga((int)F), ba((int)F), 0, stream>>>(M, *par, dt, prim, grad, face_w, lam_next, face_adj);
+    else if (F)
+        k_adj_face<false><<<ga((int)F), ba((int)F), 0, stream>>>(M, *par, dt, prim, grad, face_w, lam_next, face_adj);
     k_adj_gather<<<ga((int)n), ba((int)n), 0, stream>>>(M, face_adj, cell_adj);
     if (par->reconstruction == PHD_LINEAR)
     {

@@ -386,6 +386,208 @@ PHD_HD void hll_family_adj(bool hllc, const T *L, const T *R, const T *n, const 
     }
 }
 
+// ---- Exact Riemann solver (riemann.pyx:700-1090), FP64 --------------------------------
+// Partial derivatives of the pressure function f_K(p) of ex_p_func (riemann.pyx:1015-1040)
+// in p and in the side's data (d_K, p_K, c_K), c_K treated as its own input:
+//   rarefaction (p <= p_K): f = 2 c/(g-1) ((p/p_K)^z - 1), z = (g-1)/(2g);
+//   shock (p > p_K): f = (p - p_K) sqrt(A/(p + B)), A = 2/((g+1) d_K), B = (g-1) p_K/(g+1).
+PHD_HD __forceinline__ void ex_p_func_partials(double d, double pk, double c, double gamma, double p,
+                                               double &f_p, double &f_d, double &f_pk, double &f_c) {
+    if (p <= pk) {
+        const double z = (gamma - 1.) / (2. * gamma);
+        const double q = p / pk;
+        const double qz = pow(q, z);
+        f_c = (2. / (gamma - 1.)) * (qz - 1.);
+        f_pk = -((c / gamma) * qz) / pk;
+        f_d = 0.;
+        f_p = ((c / gamma) * (qz / q)) / pk;
+    } else {
+        const double A = 2. / (d * (gamma + 1.));
+        const double B = (pk * (gamma - 1.)) / (gamma + 1.);
+        const double s = sqrt(A / (p + B));
+        const double ds = -0.5 * s / (p + B);              // d s / d(p + B)
+        f_p = s + (p - pk) * ds;
+        f_pk = -s + (p - pk) * ds * ((gamma - 1.) / (gamma + 1.));
+        f_d = -0.5 * (p - pk) * s / d;
+        f_c = 0.;
+    }
+}
+
+// Adjoint of exact_flux<double, 2> (the FP64 path's solver: ex_get_pstar, ex_p_func at
+// p*, sampling at xi = 0 in the face frame, deboost).  The forward is recomputed with the
+// same arithmetic, so every branch (rarefaction / shock per side, the sampled region) is
+// the forward's; p* enters through the implicit function F(p*) = f_L(p*) + f_R(p*) +
+// (u_R - u_L) = 0 at the converged root: dp* = -dF / F'(p*).  aF: adjoint of the
+// deboosted flux; accumulates into aL, aR.
+PHD_HD void exact_flux_adj(const double *L, const double *R, const double *n, const double *w, double gamma,
+                           int max_iter, const double *aFin, double *aL, double *aR) {
+    const double _dl = L[0], _pl = L[3], _dr = R[0], _pr = R[3];
+    const double cl = sqrt((gamma * _pl) / _dl), cr = sqrt((gamma * _pr) / _dr);
+    double vnl = 0., vnr = 0.;
+    for (int k = 0; k < 2; k++) {
+        vnl = vnl + L[1 + k] * n[k];
+        vnr = vnr + R[1 + k] * n[k];
+    }
+    bool failed = false;
+    const double p_star = ex_get_pstar(_dl, vnl, _pl, cl, _dr, vnr, _pr, cr, gamma, max_iter, &failed);
+    const double fl_d = ex_p_func(_dl, _pl, cl, gamma, p_star);
+    const double fr_d = ex_p_func(_dr, _pr, cr, gamma, p_star);
+    const double u_star = 0.5 * (((vnl + vnr) + fr_d) - fl_d);
+    const double g1 = gamma - 1., gp = gamma + 1.;
+    // sampling (the forward's branch, with what its reverse needs)
+    int kind = 0, how = 0;     // kind 0/1: left/right data; 2: sampled; how: 1 raref. star, 2 fan, 3 shock star
+    bool right = false;
+    double _d = 0., _p = 0., ushift = 0., c_fan = 0.;
+    if (0. <= u_star) {
+        if (p_star <= _pl) {
+            if (!(0. <= vnl - cl)) {
+                const double c_star_l = cl * pow(p_star / _pl, g1 / (2. * gamma));
+                if (0. >= u_star - c_star_l) {
+                    kind = 2; how = 1; _d = _dl * pow(p_star / _pl, 1. / gamma); _p = p_star; ushift = u_star - vnl;
+                } else {
+                    c_fan = (2. / gp) * (cl + ((0.5 * g1) * vnl));
+                    kind = 2; how = 2; _d = _dl * pow(c_fan / cl, 2. / g1);
+                    _p = _pl * pow(c_fan / cl, (2. * gamma) / g1); ushift = c_fan - vnl;
+                }
+            }
+        } else {
+            const double sl = vnl - (cl * sqrt((((gp * p_star) / ((2. * gamma) * _pl)) + (g1 / (2. * gamma)))));
+            if (!(0. <= sl)) {
+                kind = 2; how = 3;
+                _d = (_dl * ((p_star / _pl) + (g1 / gp))) / (((p_star * g1) / (gp * _pl)) + 1.);
+                _p = p_star; ushift = u_star - vnl;
+            }
+        }
+    } else {
+        right = true;
+        kind = 1;
+        if (p_star >= _pr) {
+            const double sr = vnr + (cr * sqrt((((gp * p_star) / ((2. * gamma) * _pr)) + (g1 / (2. * gamma)))));
+            if (!(0. >= sr)) {
+                kind = 2; how = 3;
+                _d = (_dr * ((p_star / _pr) + (g1 / gp))) / (((p_star * g1) / (gp * _pr)) + 1.);
+                _p = p_star; ushift = u_star - vnr;
+            }
+        } else {
+            if (!(0. >= vnr + cr)) {
+                const double c_star_r = cr * pow(p_star / _pr, g1 / (2. * gamma));
+                if (0. <= u_star + c_star_r) {
+                    kind = 2; how = 1; _d = _dr * pow(p_star / _pr, 1. / gamma); _p = p_star; ushift = u_star - vnr;
+                } else {
+                    c_fan = (2. / gp) * (cr - ((0.5 * g1) * vnr));
+                    kind = 2; how = 2; _d = _dr * pow(c_fan / cr, 2. / g1);
+                    _p = _pr * pow(c_fan / cr, (2. * gamma) / g1);
+                    ushift = ((2. / gp) * ((-cr) + ((0.5 * g1) * vnr))) - vnr;
+                }
+            }
+        }
+    }
+    // deboost reverse (the exact solver always boosts)
+    double aF[4];
+    aF[0] = aFin[0] + w[0] * aFin[1] + w[1] * aFin[2] + 0.5 * (w[0] * w[0] + w[1] * w[1]) * aFin[3];
+    aF[1] = aFin[1] + w[0] * aFin[3];
+    aF[2] = aFin[2] + w[1] * aFin[3];
+    aF[3] = aFin[3];
+    // adjoints of the side data (d, p, c, vn, velocity) and of p*, u*
+    double a_d[2] = {0., 0.}, a_p[2] = {0., 0.}, a_c[2] = {0., 0.}, a_vn[2] = {0., 0.};
+    double a_v[2][2] = {{0., 0.}, {0., 0.}};
+    double a_ps = 0., a_us = 0.;
+    const double *side[2] = {L, R};
+    const double dK[2] = {_dl, _dr}, pK[2] = {_pl, _pr}, cK[2] = {cl, cr}, vnK[2] = {vnl, vnr};
+    if (kind != 2) {                                   // one side's data flux
+        const int s = kind;
+        const double vs[2] = {side[s][1], side[s][2]};
+        const double v2 = vs[0] * vs[0] + vs[1] * vs[1];
+        double ad = 0., av[2] = {0., 0.}, ap = 0., aVn = 0., av2 = 0.;
+        data_flux_adj<double>(dK[s], vs, pK[s], vnK[s], v2, n, 0., gamma, aF, ad, av, ap, aVn, av2);
+        a_d[s] += ad; a_p[s] += ap; a_vn[s] += aVn;
+        for (int k = 0; k < 2; k++) a_v[s][k] += av[k] + 2. * vs[k] * av2;
+    } else {
+        const int s = right ? 1 : 0;
+        double v[2], vn = 0., v_sq = 0.;
+        for (int k = 0; k < 2; k++) {
+            v[k] = side[s][1 + k] + (ushift * n[k]);
+            vn = vn + v[k] * n[k];
+            v_sq = v_sq + v[k] * v[k];
+        }
+        double ad = 0., av[2] = {0., 0.}, ap = 0., aVn = 0., av2 = 0.;
+        data_flux_adj<double>(_d, v, _p, vn, v_sq, n, 0., gamma, aF, ad, av, ap, aVn, av2);
+        double a_ush = 0.;
+        for (int k = 0; k < 2; k++) {
+            const double avk = av[k] + aVn * n[k] + 2. * v[k] * av2;
+            a_v[s][k] += avk;
+            a_ush += avk * n[k];
+        }
+        const double dk = dK[s], pk = pK[s], ck = cK[s];
+        if (how == 1) {                                // rarefaction star: d = d_K (p*/p_K)^(1/g)
+            const double q = p_star / pk;
+            const double aq = ad * dk * (1. / gamma) * pow(q, 1. / gamma - 1.);
+            a_d[s] += ad * pow(q, 1. / gamma);
+            a_ps += aq / pk + ap;
+            a_p[s] += -aq * q / pk;
+            a_us += a_ush;
+            a_vn[s] -= a_ush;
+        } else if (how == 3) {                         // shock star
+            const double q = p_star / pk, gg = g1 / gp;
+            const double num = dk * (q + gg), den = gg * q + 1.;
+            const double anum = ad / den, aden = -ad * num / (den * den);
+            a_d[s] += anum * (q + gg);
+            const double aq = anum * dk + aden * gg;
+            a_ps += aq / pk + ap;
+            a_p[s] += -aq * q / pk;
+            a_us += a_ush;
+            a_vn[s] -= a_ush;
+        } else {                                       // inside the rarefaction fan
+            const double r = c_fan / ck, e1 = 2. / g1, e2 = (2. * gamma) / g1;
+            const double ar = ad * dk * e1 * pow(r, e1 - 1.) + ap * pk * e2 * pow(r, e2 - 1.);
+            a_d[s] += ad * pow(r, e1);
+            a_p[s] += ap * pow(r, e2);
+            double a_cfan = ar / ck;
+            a_c[s] += -ar * c_fan / (ck * ck);
+            if (s == 0) {                              // c = 2/(g+1) (c_L + (g-1)/2 u_L); shift = c - u_L
+                a_cfan += a_ush;
+                a_vn[0] -= a_ush;
+                a_c[0] += a_cfan * (2. / gp);
+                a_vn[0] += a_cfan * (2. / gp) * (0.5 * g1);
+            } else {                                   // c = 2/(g+1) (c_R - (g-1)/2 u_R);
+                a_c[1] += a_cfan * (2. / gp);          // shift = 2/(g+1) (-c_R + (g-1)/2 u_R) - u_R
+                a_vn[1] += -a_cfan * (2. / gp) * (0.5 * g1);
+                a_c[1] += -a_ush * (2. / gp);
+                a_vn[1] += a_ush * ((2. / gp) * (0.5 * g1) - 1.);
+            }
+        }
+    }
+    // u* = ((u_L + u_R) + f_R(p*) - f_L(p*)) / 2
+    double fpL, fdL, fpkL, fcL, fpR, fdR, fpkR, fcR;
+    ex_p_func_partials(_dl, _pl, cl, gamma, p_star, fpL, fdL, fpkL, fcL);
+    ex_p_func_partials(_dr, _pr, cr, gamma, p_star, fpR, fdR, fpkR, fcR);
+    if (a_us != 0.) {
+        a_vn[0] += 0.5 * a_us;
+        a_vn[1] += 0.5 * a_us;
+        const double afr = 0.5 * a_us, afl = -0.5 * a_us;
+        a_ps += afr * fpR + afl * fpL;
+        a_d[0] += afl * fdL; a_p[0] += afl * fpkL; a_c[0] += afl * fcL;
+        a_d[1] += afr * fdR; a_p[1] += afr * fpkR; a_c[1] += afr * fcR;
+    }
+    // p*: the converged root of F(p) = f_L(p) + f_R(p) + (u_R - u_L)
+    if (a_ps != 0.) {
+        const double sgm = a_ps / (fpL + fpR);
+        a_vn[0] += sgm;
+        a_vn[1] -= sgm;
+        a_d[0] -= sgm * fdL; a_p[0] -= sgm * fpkL; a_c[0] -= sgm * fcL;
+        a_d[1] -= sgm * fdR; a_p[1] -= sgm * fpkR; a_c[1] -= sgm * fcR;
+    }
+    // c_K = sqrt(g p_K / d_K), u_K = v_K . n
+    for (int s = 0; s < 2; s++) {
+        double *aS = s == 0 ? aL : aR;
+        a_p[s] += a_c[s] * 0.5 * cK[s] / pK[s];
+        a_d[s] += -a_c[s] * 0.5 * cK[s] / dK[s];
+        aS[0] += a_d[s];
+        aS[3] += a_p[s];
+        for (int k = 0; k < 2; k++) aS[1 + k] += a_v[s][k] + a_vn[s] * n[k];
+    }
+}
+
 // Adjoint of the GIZMO pair limit of one field (gizmo_pair in phd_physics.cuh).
 // Returns adjoints of (sl, sr, xl, xr) given adjoints of the limited (xl, xr).
 // si = |sep_i| / |x_j - x_i|, sj = |sep_j| / |x_j - x_i| (the same quotients the forward

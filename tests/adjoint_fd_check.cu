@@ -1,6 +1,7 @@
 // Host-side check of the hand-written reverse routines (phd_adjoint.cuh) against
 // central finite differences of the forward routines (phd_physics.cuh), compiled for the
-// host: the HLL / HLLC flux with and without boost (hll_family_adj), the wave-speed
+// host: the HLL / HLLC flux with and without boost (hll_family_adj), the exact solver
+// (exact_flux_adj: Newton root by implicit differentiation, every sampled region), the wave-speed
 // estimate (get_waves_adj), the GIZMO pair limiter (gizmo_pair_adj) and the
 // MUSCL-Hancock half step (temporal_adj).
 //
@@ -52,7 +53,7 @@ int main(int argc, char **argv) {
     std::uniform_real_distribution<double> U(0., 1.);
     auto u = [&](double a, double b) { return a + (b - a) * U(rng); };
     const double gamma = 1.4;
-    Stat hllc{"hllc"}, hll{"hll"}, hllc_lab{"hllc_lab"}, waves{"get_waves"}, gizmo{"gizmo_pair"},
+    Stat hllc{"hllc"}, hll{"hll"}, hllc_lab{"hllc_lab"}, exact{"exact"}, waves{"get_waves"}, gizmo{"gizmo_pair"},
         temp{"temporal"};
 
     for (long c = 0; c < cases; c++) {
@@ -78,6 +79,27 @@ int main(int argc, char **argv) {
                 for (int k = 0; k < 4; k++) dot += aL[k] * v[k] + aR[k] * v[4 + k];
                 check(variant == 0 ? hllc : (variant == 1 ? hll : hllc_lab), x, v, f, dot);
             }
+        }
+        // ---- exact solver + deboost (states spanning shocks, rarefactions and fans) ----
+        {
+            std::vector<double> x = {u(0.2, 2.), u(-2., 2.), u(-2., 2.), u(0.1, 3.),
+                                     u(0.2, 2.), u(-2., 2.), u(-2., 2.), u(0.1, 3.)};
+            const double th = u(0., 6.283185307179586);
+            const double n[2] = {std::cos(th), std::sin(th)}, w[2] = {u(-.5, .5), u(-.5, .5)};
+            std::vector<double> v(8), a(4);
+            for (auto &e : v) e = u(-1., 1.);
+            for (auto &e : a) e = u(-1., 1.);
+            auto f = [&](const std::vector<double> &y) {
+                double F[4];
+                bool failed = false;
+                exact_flux<double, 2>(y.data(), y.data() + 4, n, w, gamma, 1000, F, &failed);
+                return a[0] * F[0] + a[1] * F[1] + a[2] * F[2] + a[3] * F[3];
+            };
+            double aL[4] = {0, 0, 0, 0}, aR[4] = {0, 0, 0, 0};
+            exact_flux_adj(x.data(), x.data() + 4, n, w, gamma, 1000, a.data(), aL, aR);
+            double dot = 0.;
+            for (int k = 0; k < 4; k++) dot += aL[k] * v[k] + aR[k] * v[4 + k];
+            check(exact, x, v, f, dot);
         }
         // ---- wave speeds -------------------------------------------------------------
         {
@@ -147,7 +169,7 @@ int main(int argc, char **argv) {
             check(temp, x, v, f, dot);
         }
     }
-    for (const Stat &S : {hllc, hll, hllc_lab, waves, gizmo, temp})
+    for (const Stat &S : {hllc, hll, hllc_lab, exact, waves, gizmo, temp})
         printf("%s %ld %ld %.6e\n", S.name, S.n, S.compared, S.worst);
     return 0;
 }

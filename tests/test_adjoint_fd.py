@@ -1,5 +1,6 @@
 """The hand-written reverse routines of the adjoint (phd_adjoint.cuh: HLL / HLLC with and
-without boost, wave speeds, GIZMO pair limiter, MUSCL-Hancock half step) against central
+without boost, the exact solver, wave speeds, GIZMO pair limiter, MUSCL-Hancock half
+step) against central
 finite differences of the forward routines (phd_physics.cuh) on seeded random cases,
 compiled for the host with nvcc.  No GPU needed."""
 import os
@@ -29,7 +30,7 @@ def test_reverse_routines_match_finite_differences(tmp_path):
                     os.path.join(HERE, "adjoint_fd_check.cu"), "-o", exe], check=True)
     out = subprocess.run([exe, "4000"], check=True, capture_output=True, text=True).stdout
     rows = {r.split()[0]: r.split()[1:] for r in out.strip().splitlines()}
-    assert set(rows) == {"hllc", "hll", "hllc_lab", "get_waves", "gizmo_pair", "temporal"}
+    assert set(rows) == {"hllc", "hll", "hllc_lab", "exact", "get_waves", "gizmo_pair", "temporal"}
     for name, (n, compared, worst) in rows.items():
         n, compared, worst = int(n), int(compared), float(worst)
         assert n == 4000

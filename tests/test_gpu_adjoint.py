@@ -55,10 +55,10 @@ def test_one_step_adjoint_lab_frame(boundary):
     assert one_step_case(boundary, "hllc", "arepo", False, seed=3) <= 1e-9
 
 
-def record_static_run(m, prim, n_steps, cfl=0.4, gamma=1.4):
+def record_static_run(m, prim, n_steps, cfl=0.4, gamma=1.4, solver="hllc"):
     """Forward FP64 run on a fixed mesh recording its dt schedule (static mesh: w = 0)."""
     dm = DeviceMesh(m)
-    st = pkg.FluxStepper(dm, prim, gamma=gamma, cfl=cfl, solver="hllc", moving=False)
+    st = pkg.FluxStepper(dm, prim, gamma=gamma, cfl=cfl, solver=solver, moving=False)
     recs = []
     fw = torch.zeros((2, m.n_faces), dtype=torch.float64, device="cuda")
     for _ in range(n_steps):
@@ -82,9 +82,9 @@ def generic_state(m):
     return pkg.meshgen.fill_ghosts(m, prim)
 
 
-def multistep_case(m, prim, n_steps, limiter="arepo", checkpoint=5):
-    recs = record_static_run(m, prim, n_steps)
-    run = FluxRunRecord(recs, gamma=1.4, solver="hllc", limiter=limiter, checkpoint=checkpoint)
+def multistep_case(m, prim, n_steps, limiter="arepo", checkpoint=5, solver="hllc"):
+    recs = record_static_run(m, prim, n_steps, solver=solver)
+    run = FluxRunRecord(recs, gamma=1.4, solver=solver, limiter=limiter, checkpoint=checkpoint)
     p0 = torch.tensor(prim[:, :m.n_real], device="cuda")
     tgt = torch.tensor(1.0 + 0.02 * np.sin(2 * np.pi * m.x[0, :m.n_real]), device="cuda")
 
@@ -163,3 +163,27 @@ def test_taped_adjoint_equals_recomputing_adjoint(limiter):
         b = run._adjoint(recs[k], (cons, prim_k, grad, None), lam)
         assert torch.equal(a, b)
         lam = a
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+def test_exact_solver_gradient_vs_finite_differences(boundary):
+    """The exact solver's reverse (p* by implicit differentiation of the converged Newton
+    root, every sampled region) through recorded multi-step runs against central
+    differences.  The forward's Newton stops at a relative change of 1e-6, so its p*
+    carries a ~1e-12 convergence error that a difference quotient at h = 1e-6 turns into
+    ~1e-6 noise; the bound allows for that."""
+    m = lattice_mesh(16, boundary, seed=9)
+    prim = generic_state(m)
+    run, recs, p0, tgt, loss, g = multistep_case(m, prim, 6, solver="exact", checkpoint=3)
+    rng = np.random.default_rng(13)
+    h = 1e-6
+    errs = []
+    for _ in range(8):
+        d = torch.tensor(rng.standard_normal(p0.shape), device="cuda")
+        d = d / torch.linalg.norm(d)
+        with torch.no_grad():
+            fd = (loss(p0 + h * d) - loss(p0 - h * d)).item() / (2 * h)
+        ad = float((g * d).sum())
+        errs.append(abs(fd - ad) / max(abs(fd), 1e-12))
+    assert np.median(errs) <= 1e-5, errs
+    assert max(errs) <= 1e-4, errs
