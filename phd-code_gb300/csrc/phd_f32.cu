@@ -452,6 +452,68 @@ __device__ __forceinline__ void hll_family32(bool hllc, const float *L, const fl
 }
 
 // ---- fused face kernel ------------------------------------------------------------
+
+// FP32 MUSCL-Hancock half step (temporal of phd_physics.cuh, 2D) with each side's
+// 1/rho formed once and the divergence / advection terms written out per side.
+__device__ __forceinline__ void temporal32(float *L, float *R, const float *pi, const float *pj, const float *gi,
+                                           const float *gj, const float *w, float gamma, float dt, bool boost) {
+    float sl[4], sr[4];
+#pragma unroll
+    for (int f = 0; f < 4; f++) { sl[f] = L[f]; sr[f] = R[f]; }
+    const float vi[2] = {boost ? pi[1] - w[0] : pi[1], boost ? pi[2] - w[1] : pi[2]};
+    const float vj[2] = {boost ? pj[1] - w[0] : pj[1], boost ? pj[2] - w[1] : pj[2]};
+    const float ri = dt / pi[0], rj = dt / pj[0];
+    // grad rows: rho (0, 1), vx (2, 3), vy (4, 5), p (6, 7)
+    const float divi = gi[2] + gi[5], divj = gj[2] + gj[5];
+    L[0] -= dt * (pi[0] * divi + vi[0] * gi[0] + vi[1] * gi[1]);
+    R[0] -= dt * (pj[0] * divj + vj[0] * gj[0] + vj[1] * gj[1]);
+    L[1] -= ri * gi[6] + dt * (vi[0] * gi[2] + vi[1] * gi[3]);
+    R[1] -= rj * gj[6] + dt * (vj[0] * gj[2] + vj[1] * gj[3]);
+    L[2] -= ri * gi[7] + dt * (vi[0] * gi[4] + vi[1] * gi[5]);
+    R[2] -= rj * gj[7] + dt * (vj[0] * gj[4] + vj[1] * gj[5]);
+    L[3] -= dt * (gamma * pi[3] * divi + vi[0] * gi[6] + vi[1] * gi[7]);
+    R[3] -= dt * (gamma * pj[3] * divj + vj[0] * gj[6] + vj[1] * gj[7]);
+    if (L[0] < 0.f || L[3] < 0.f) {
+#pragma unroll
+        for (int f = 0; f < 4; f++) L[f] = sl[f];
+    }
+    if (R[0] < 0.f || R[3] < 0.f) {
+#pragma unroll
+        for (int f = 0; f < 4; f++) R[f] = sr[f];
+    }
+}
+
+// FP32 GIZMO pair limit (gizmo_pair of phd_physics.cuh) with the separation quotients
+// formed once per face and the sign-changing bound phi / (1 + delta/|phi|) written as
+// phi |phi| / (|phi| + delta): one division on that (rare) branch.
+__device__ __forceinline__ void gizmo_pair32(float sl, float sr, float ci, float cj, float qi, float qj,
+                                             float &xl, float &xr) {
+    const float ad = fabsf(sl - sr);
+    const float delta1 = 0.5f * ad, delta2 = 0.25f * ad;
+    const float phi_min = fminf(sl, sr), phi_max = fmaxf(sl, sr);
+    const float phibar_l = sl + qi * (sr - sl);
+    const float phibar_r = sr + qj * (sl - sr);
+    float phi_plus = phi_max + delta1, phi_minus = phi_min - delta1;
+    if (__builtin_expect(phi_plus * phi_max < 0.f, 0)) {
+        const float a = fabsf(phi_max);
+        phi_plus = (phi_max * a) / (a + delta1);
+    }
+    if (__builtin_expect(phi_minus * phi_min < 0.f, 0)) {
+        const float a = fabsf(phi_min);
+        phi_minus = (phi_min * a) / (a + delta1);
+    }
+    if (ci < cj) {
+        xl = fmaxf(phi_minus, fminf(phibar_l + delta2, xl));
+        xr = fminf(phi_plus, fmaxf(phibar_r - delta2, xr));
+    } else if (ci > cj) {
+        xl = fminf(phi_plus, fmaxf(phibar_l - delta2, xl));
+        xr = fmaxf(phi_minus, fminf(phibar_r + delta2, xr));
+    } else {
+        xl = sl;
+        xr = sr;
+    }
+}
+
 template <int SOLVER, bool LINEAR>
 __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_params &P, int moving,
                                             const float4 *__restrict__ face_geo,
@@ -504,7 +566,8 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
         if (P.gizmo) {
             const float smi = sqrtf(six * six + siy * siy), smj = sqrtf(sjx * sjx + sjy * sjy);
 #pragma unroll
-            for (int f = 0; f < 4; f++) gizmo_pair<float>(sl[f], sr[f], pi[f], pj[f], smi, smj, ar.y, L[f], R[f]);
+            const float qi = smi / ar.y, qj = smj / ar.y;
+            for (int f = 0; f < 4; f++) gizmo_pair32(sl[f], sr[f], pi[f], pj[f], qi, qj, L[f], R[f]);
             if (L[0] < 0.f || L[3] < 0.f) {
 #pragma unroll
                 for (int f = 0; f < 4; f++) L[f] = sl[f];
@@ -514,7 +577,7 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
                 for (int f = 0; f < 4; f++) R[f] = sr[f];
             }
         }
-        temporal<float, 2>(L, R, pi, pj, gi, gj, w, gamma, dt_half, boost);
+        temporal32(L, R, pi, pj, gi, gj, w, gamma, dt_half, boost);
     }
     float f[4];
     bool failed = false;
