@@ -281,6 +281,55 @@ int phd_pair_i_from_face_ptr(const phd_mesh *mesh, const int32_t *face_ptr, int3
 int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, const float *crel32,
                                   phd_geom32_out *out, cudaStream_t stream);
 
+/* One hand-over of a re-mesh to an FP32 stepper in one call: the host tessellation of
+ * integrate.py:410-417 arrives in the compact format and the device forms everything
+ * else (steps 6-8 of the moving-mesh step) -- pair-i from the face ranges
+ * (phd_pair_i_from_face_ptr), the neighbour lists (phd_build_csr), the ghost rows of
+ * mesh->x (phd_ghost_positions) or all of mesh->x from the host, the periodic twins,
+ * the FP32 list codes, face geometry and cell geometry (phd_prepare_f32_parts,
+ * phd_prepare_f32_faces_compact), the flip bits (phd_flip_mask), the ghost totals
+ * (phd_ghost_cons_f64) and the primitives with the next dt (phd_prim_f32_cells).
+ *
+ * The copies run on `stream` with the large ones (area, centroid offset) issued right
+ * after the small ones the lists need; the derivations run on side[0] (pair-i,
+ * positions, lists, twins, list codes, flip bits, then the cell geometry) and side[1]
+ * (the face geometry, as soon as the face records have landed) while the copies are in
+ * flight, and are joined back into `stream` at the end.  events: 6 CUDA events
+ * (created by the caller, reused across calls).  The mesh's own arrays (pair_i, pair_j, map
+ * ghost rows, x, nbr_ptr/nbr_idx, flip) are written through the const view; mesh->normal
+ * must be NULL (the FP32 geometry forms its own normals).  The counts are the mesh's:
+ * a tessellation with other counts needs the arrays re-sized first.  Faces or ghosts
+ * whose indices are out of range add to *bad (device; read it after the call). */
+typedef struct phd_handover32 {
+    /* host arrays (pinned, for the copies to overlap the derivations) */
+    const int32_t *face_ptr;      /* [n_real + 1] faces of each real cell */
+    const int32_t *pair_j;        /* [n_faces] */
+    const float *area32;          /* [n_faces] face areas, FP32 */
+    const float *crel32;          /* [n_faces][2] centroid - (x_i + x_j)/2, FP32 */
+    const int32_t *ghost_map;     /* [n_cells - n_real] images of the ghosts; NULL: mesh->map holds them */
+    const int8_t *ghost_code;     /* [n_cells - n_real] phd_ghost_positions codes (with x == NULL) */
+    const double *x;              /* [2][n_cells] every position; NULL: real rows from x_real, ghost
+                                     rows from ghost_code */
+    /* device arrays */
+    const double *x_real;         /* [2][n_real] real positions (phd_move_generators' x_out); NULL:
+                                     mesh->x already holds them.  Ignored when x != NULL. */
+    const int8_t *type;           /* [n_cells] particle types (the flip bits' Exterior test) */
+    int32_t *d_face_ptr;          /* [n_real + 1] staging */
+    float *d_area32;              /* [n_faces] staging */
+    float *d_crel32;              /* [n_faces][2] staging */
+    int8_t *d_ghost_code;         /* [n_cells - n_real] staging (with x == NULL) */
+    int32_t *twin;                /* [n_faces] periodic twin table */
+    int32_t *csr_work;            /* phd_csr_work_ints(n_cells) */
+    int32_t *bad;                 /* [1] error counter, zeroed by the call */
+    int32_t periodic;             /* 1: periodic box, 0: reflective walls */
+    int32_t dedup_periodic;       /* 1: periodic twin faces counted once (phd_periodic_twins) */
+    double xmin[2], xmax[2];      /* the box */
+} phd_handover32;
+
+int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_params *par, phd_geom32_out *out,
+                      double *cons, float *prim4, phd_clock *clk, cudaStream_t stream, const cudaStream_t *side,
+                      cudaEvent_t *events);
+
 /* FP64 totals -> FP32 primitive cells prim4 [n][4] (rho, v_x, v_y, p) and clk->dt from
  * the CFL minimum (clock not advanced). */
 int phd_prim_f32(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4,

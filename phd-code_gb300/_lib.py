@@ -72,6 +72,14 @@ class PhdGeom32Out(C.Structure):
     _fields_ = PhdGeom32._fields_
 
 
+class PhdHandover32(C.Structure):
+    """phd_handover32: one compact re-mesh hand-over to an FP32 stepper (phd_load_mesh_f32)."""
+    _fields_ = [(nm, C.c_void_p) for nm in ("face_ptr", "pair_j", "area32", "crel32", "ghost_map", "ghost_code", "x",
+                                            "x_real", "type", "d_face_ptr", "d_area32", "d_crel32", "d_ghost_code",
+                                            "twin", "csr_work", "bad")] + \
+        [("periodic", C.c_int32), ("dedup_periodic", C.c_int32), ("xmin", C.c_double * 2), ("xmax", C.c_double * 2)]
+
+
 CLOCK_BYTES = C.sizeof(PhdClock)
 
 _lib = None
@@ -124,6 +132,8 @@ SIGNATURES = {
     "phd_move_generators": ([_PM, _vp, _vp, _vp, _i32, _f64, _f64, _f64, _f64, _vp, _vp], C.c_int),
     "phd_ghost_positions": ([_PM, _vp, _f64, _f64, _f64, _f64, _vp, _vp], C.c_int),
     "phd_prepare_f32_faces_compact": ([_PM, _vp, _vp, C.POINTER(PhdGeom32Out), _vp], C.c_int),
+    "phd_load_mesh_f32": ([_PM, C.POINTER(PhdHandover32), C.POINTER(PhdParams), C.POINTER(PhdGeom32Out), _vp, _vp,
+                           _vp, _vp, _vp, _vp], C.c_int),
     "phd_periodic_twins": ([_PM, _i32, _f64, _f64, _vp, _vp], C.c_int),
 }
 

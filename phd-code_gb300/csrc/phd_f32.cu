@@ -204,16 +204,25 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
                                             const float4 *__restrict__ cell_geo,
                                             const float4 *__restrict__ prim4, float4 *__restrict__ grad8,
                                             float2 *__restrict__ w2, phd_clock *clk) {
+    // the cell's own row is loaded before its tag is known: for a real cell it is the
+    // row the gradient needs; a ghost reloads its twin's
     const bool real = M.tag[i] == PHD_REAL_TAG;
-    const int c = real ? i : M.map[i];
-    if (c < 0 || c >= M.n_cells) { set_status32(clk, PHD_STATUS_BAD_INDEX); return; }
-    const float4 pc = prim4[c];
-    const float4 gc = cell_geo[c];
+    float4 pc = prim4[i];
+    float4 gc = cell_geo[i];
+    int e0 = M.nbr_ptr[i], e1 = M.nbr_ptr[i + 1];
+    int c = i;
+    if (!real) {
+        c = M.map[i];
+        if (c < 0 || c >= M.n_cells) { set_status32(clk, PHD_STATUS_BAD_INDEX); return; }
+        pc = prim4[c];
+        gc = cell_geo[c];
+        e0 = M.nbr_ptr[c];
+        e1 = M.nbr_ptr[c + 1];
+    }
     const float P0[4] = {pc.x, pc.y, pc.z, pc.w};
     float mx[4], mn[4], df[4][2];
 #pragma unroll
     for (int f = 0; f < 4; f++) { mx[f] = mn[f] = P0[f]; df[f][0] = df[f][1] = 0.f; }
-    const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
     // entries in chunks of CH: all of a chunk's dependent loads are issued before any
     // arithmetic, so their latencies overlap (lanes past the end reload entry e0)
     constexpr int CH = 4;
@@ -310,7 +319,7 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
     grad8[2 * (size_t)i + 1] = make_float4(gv[4], gv[5], gv[6], gv[7]);
 
     if (moving) {   // Mesh.assign_generator_velocities mesh.pyx:397-426, own (ghost) cell data
-        const float4 p = prim4[i];
+        const float4 p = (i == c) ? pc : prim4[i];
         const float4 gi = (i == c) ? gc : cell_geo[i];
         float wx = p.y, wy = p.z;
         if (P.regularize) {

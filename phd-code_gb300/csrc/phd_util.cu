@@ -300,15 +300,23 @@ __global__ void k_move_generators(int n_real, int n, const double *__restrict__ 
 // boundary.pyx:66-130 mirror images, 351-400 periodic copies), with the host
 // tessellation's arithmetic: x + s L for a periodic copy, x - 2 (x - wall) across a
 // mirror.  code (per ghost): 1 + 3 (sx + 1) + (sy + 1) periodic, 16 + 2 k + h mirror.
-__global__ void k_ghost_positions(int n_real, int n, const int32_t *__restrict__ map,
-                                  const int8_t *__restrict__ code, double lo0, double lo1, double hi0, double hi1,
-                                  double *__restrict__ x, int *bad) {
-    const int g = n_real + blockIdx.x * blockDim.x + threadIdx.x;
+// Rows of x: the real rows copied from src (rows of stride src_stride) when copy_real,
+// and every ghost row from its image's row of src by its code.  src may be x itself
+// (stride n, copy_real = 0).
+__global__ void k_positions(int n_real, int n, int copy_real, const int32_t *__restrict__ map,
+                            const int8_t *__restrict__ code, double lo0, double lo1, double hi0, double hi1,
+                            const double *src, size_t src_stride, double *x, int *bad) {
+    const int g = (copy_real ? 0 : n_real) + blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n) return;
+    if (g < n_real) {
+        x[g] = src[g];
+        x[(size_t)n + g] = src[src_stride + g];
+        return;
+    }
     const int img = map[g];
     const int c = code[g - n_real];
     if (img < 0 || img >= n_real) { atomicAdd(bad, 1); return; }
-    double px = x[img], py = x[(size_t)n + img];
+    double px = src[img], py = src[src_stride + img];
     if (c >= 1 && c <= 9 && c != 5) {
         const int sx = (c - 1) / 3 - 1, sy = (c - 1) % 3 - 1;
         px = __dadd_rn(px, __dmul_rn(double(sx), __dsub_rn(hi0, lo0)));
@@ -328,6 +336,55 @@ __global__ void k_ghost_positions(int n_real, int n, const int32_t *__restrict__
     }
     x[g] = px;
     x[(size_t)n + g] = py;
+}
+
+// Neighbour lists of a hand-over whose faces come grouped by pair-i in per-real-cell
+// ranges [face_ptr[c], face_ptr[c+1]) (the compact format): pair-i is written from the
+// ranges, a cell's count is its own range plus the faces naming it as pair-j, and its
+// own range goes to the tail of its list without atomics; the pair-j side is scattered
+// with a cursor, and k_csr_sort orders every list.  A broken range (face_ptr not
+// starting at 0, decreasing, or not ending at n_faces) and faces with out-of-range or
+// equal cells add to *bad, as phd_pair_i_from_face_ptr and phd_build_csr count them.
+__device__ __forceinline__ bool range_ok(int c, int n_real, int F, int a, int b) {
+    return !(a < 0 || b < a || b > F || (c == 0 && a != 0) || (c == n_real - 1 && b != F));
+}
+
+__global__ void k_csr_count_ranges(int n_real, int n, int F, const int32_t *__restrict__ face_ptr,
+                                   const int32_t *__restrict__ pair_j, int32_t *__restrict__ pair_i,
+                                   int32_t *__restrict__ cnt, int32_t *__restrict__ bad) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_real) return;
+    const int a = face_ptr[c], b = face_ptr[c + 1];
+    if (!range_ok(c, n_real, F, a, b)) { atomicAdd(bad, 1); return; }
+    int own = 0;
+    for (int m = a; m < b; m++) {
+        pair_i[m] = c;
+        const int j = pair_j[m];
+        if (j >= 0 && j < n && j != c) {
+            atomicAdd(&cnt[j], 1);
+            own++;
+        } else {
+            atomicAdd(bad, 1);
+        }
+    }
+    if (own) atomicAdd(&cnt[c], own);
+}
+
+__global__ void k_csr_scatter_ranges(int n_real, int n, int F, const int32_t *__restrict__ face_ptr,
+                                     const int32_t *__restrict__ pair_j, const int32_t *__restrict__ ptr,
+                                     int32_t *__restrict__ cursor, int32_t *__restrict__ idx) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n_real) return;
+    const int a = face_ptr[c], b = face_ptr[c + 1];
+    if (!range_ok(c, n_real, F, a, b)) return;
+    int end = ptr[c + 1];
+    for (int m = b - 1; m >= a; m--) {
+        const int j = pair_j[m];
+        if (j >= 0 && j < n && j != c) {
+            idx[--end] = m;
+            idx[ptr[j] + atomicAdd(&cursor[j], 1)] = m;
+        }
+    }
 }
 
 }  // namespace phd
@@ -424,10 +481,115 @@ int phd_ghost_positions(const phd_mesh *mesh, const int8_t *ghost_code, double x
     const int ng = mesh->n_cells - mesh->n_real;
     if (ng == 0) return PHD_OK;
     if (!ghost_code) return PHD_ERR_ARG;
-    phd::k_ghost_positions<<<(ng + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(
-        mesh->n_real, mesh->n_cells, mesh->map, ghost_code, xmin0, xmin1, xmax0, xmax1, const_cast<double *>(mesh->x),
-        bad);
+    phd::k_positions<<<(ng + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, stream>>>(
+        mesh->n_real, mesh->n_cells, 0, mesh->map, ghost_code, xmin0, xmin1, xmax0, xmax1, mesh->x,
+        (size_t)mesh->n_cells, const_cast<double *>(mesh->x), bad);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
+
+int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_params *par, phd_geom32_out *out,
+                      double *cons, float *prim4, phd_clock *clk, cudaStream_t stream, const cudaStream_t *side,
+                      cudaEvent_t *events) {
+    phd::NvtxRange nvtx_range("phd_load_mesh_f32");
+    if (!mesh || !h || !par || !out || !cons || !prim4 || !clk || !side || !events || mesh->dim != 2 ||
+        mesh->normal || mesh->n_cells <= 0 || mesh->n_real < 0 || mesh->n_real > mesh->n_cells ||
+        mesh->n_faces < 0)
+        return PHD_ERR_ARG;
+    if (!mesh->pair_i || !mesh->pair_j || !mesh->map || !mesh->x || !mesh->flip || !mesh->nbr_ptr || !mesh->nbr_idx)
+        return PHD_ERR_ARG;
+    if (!h->face_ptr || !h->pair_j || !h->area32 || !h->crel32 || !h->d_face_ptr || !h->d_area32 || !h->d_crel32 ||
+        !h->type || !h->twin || !h->csr_work || !h->bad || !(h->xmax[0] > h->xmin[0]) || !(h->xmax[1] > h->xmin[1]))
+        return PHD_ERR_ARG;
+    const int n = mesh->n_cells, nr = mesh->n_real, F = mesh->n_faces, ng = n - nr;
+    if (!h->x && ng > 0 && (!h->ghost_code || !h->d_ghost_code)) return PHD_ERR_ARG;
+    int32_t *pair_i = const_cast<int32_t *>(mesh->pair_i);
+    int32_t *pair_j = const_cast<int32_t *>(mesh->pair_j);
+    double *x = const_cast<double *>(mesh->x);
+    const cudaMemcpyKind H2D = cudaMemcpyHostToDevice;
+    const cudaStream_t lists = side[0], geom = side[1];
+    int rc = PHD_OK;
+#define PHD_TRY(call)                                                      \
+    do {                                                                   \
+        if ((rc = (call)) != PHD_OK) return rc;                            \
+    } while (0)
+#define PHD_TRY_CUDA(call)                                                 \
+    do {                                                                   \
+        if ((call) != cudaSuccess) return PHD_ERR_LAUNCH;                  \
+    } while (0)
+    // stream: the face ranges and pair-j, then the per-ghost arrays, then the large FP32
+    // face records; each group's event releases the work that needs it
+    PHD_TRY_CUDA(cudaMemsetAsync(h->bad, 0, sizeof(int32_t), stream));
+    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_face_ptr, h->face_ptr, (size_t)(nr + 1) * sizeof(int32_t), H2D, stream));
+    PHD_TRY_CUDA(cudaMemcpyAsync(pair_j, h->pair_j, (size_t)F * sizeof(int32_t), H2D, stream));
+    PHD_TRY_CUDA(cudaEventRecord(events[0], stream));
+    if (h->ghost_map && ng > 0)
+        PHD_TRY_CUDA(cudaMemcpyAsync(const_cast<int32_t *>(mesh->map) + nr, h->ghost_map, (size_t)ng * sizeof(int32_t),
+                                     H2D, stream));
+    if (h->x)
+        PHD_TRY_CUDA(cudaMemcpyAsync(x, h->x, (size_t)2 * n * sizeof(double), H2D, stream));
+    else if (ng > 0)
+        PHD_TRY_CUDA(cudaMemcpyAsync(h->d_ghost_code, h->ghost_code, (size_t)ng, H2D, stream));
+    PHD_TRY_CUDA(cudaEventRecord(events[1], stream));
+    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_area32, h->area32, (size_t)F * sizeof(float), H2D, stream));
+    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_crel32, h->crel32, (size_t)F * 2 * sizeof(float), H2D, stream));
+    PHD_TRY_CUDA(cudaEventRecord(events[2], stream));
+
+    // lists stream, while the face records are in flight: pair-i with the list counts,
+    // every position, the neighbour lists, periodic twins, FP32 list codes, flip bits
+    const int32_t *nbr_ptr = mesh->nbr_ptr;
+    int32_t *cnt = h->csr_work, *cursor = h->csr_work + n, *tile_sum = h->csr_work + 2 * (size_t)n;
+    const int n_tiles = (n + phd::SCAN_TILE - 1) / phd::SCAN_TILE;
+    const int gr = nr > 0 ? (nr + phd::UBLOCK - 1) / phd::UBLOCK : 1;
+    PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[0], 0));
+    PHD_TRY_CUDA(cudaMemsetAsync(h->csr_work, 0, sizeof(int32_t) * phd_csr_work_ints(n), lists));
+    if (nr > 0)
+        phd::k_csr_count_ranges<<<gr, phd::UBLOCK, 0, lists>>>(nr, n, F, h->d_face_ptr, pair_j, pair_i, cnt, h->bad);
+    PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[1], 0));
+    if (!h->x && n > 0) {
+        const bool copy_real = h->x_real != nullptr;
+        const int first = copy_real ? 0 : nr;
+        if (n > first)
+            phd::k_positions<<<(n - first + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, lists>>>(
+                nr, n, copy_real, mesh->map, h->d_ghost_code, h->xmin[0], h->xmin[1], h->xmax[0], h->xmax[1],
+                copy_real ? h->x_real : x, copy_real ? (size_t)nr : (size_t)n, x, h->bad);
+    }
+    PHD_TRY_CUDA(cudaEventRecord(events[3], lists));
+    phd::k_scan_tiles<<<n_tiles, phd::SCAN_THREADS, 0, lists>>>(n, cnt, tile_sum);
+    phd::k_scan_tile_sums<<<1, phd::SCAN_THREADS, 0, lists>>>(n_tiles, tile_sum);
+    phd::k_scan_offsets<<<n_tiles, phd::SCAN_THREADS, 0, lists>>>(n, cnt, tile_sum, const_cast<int32_t *>(nbr_ptr));
+    if (nr > 0 && F > 0) {
+        phd::k_csr_scatter_ranges<<<gr, phd::UBLOCK, 0, lists>>>(nr, n, F, h->d_face_ptr, pair_j, nbr_ptr, cursor,
+                                                                 const_cast<int32_t *>(mesh->nbr_idx));
+        phd::k_csr_sort<<<(n + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, lists>>>(
+            n, nbr_ptr, const_cast<int32_t *>(mesh->nbr_idx));
+    }
+    PHD_TRY_CUDA(cudaPeekAtLastError());
+    PHD_TRY(phd_periodic_twins(mesh, h->periodic && h->dedup_periodic, h->xmax[0] - h->xmin[0],
+                               h->xmax[1] - h->xmin[1], h->twin, lists));
+    PHD_TRY(phd_prepare_f32_parts(mesh, h->twin, out, PHD_PREP_LISTS, lists));
+    const double lo[3] = {h->xmin[0], h->xmin[1], 0.}, hi[3] = {h->xmax[0], h->xmax[1], 0.};
+    PHD_TRY(phd_flip_mask(2, n, h->type, x, lo, hi, !h->periodic, const_cast<int8_t *>(mesh->flip), lists));
+
+    // geometry stream: the FP32 face geometry as soon as the records and the positions
+    // are there, beside the lists
+    PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[2], 0));
+    PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[3], 0));
+    PHD_TRY(phd_prepare_f32_faces_compact(mesh, h->d_area32, h->d_crel32, out, geom));
+    PHD_TRY_CUDA(cudaEventRecord(events[4], geom));
+
+    // lists stream: the cells' volumes and centroids from faces and lists
+    PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[4], 0));
+    PHD_TRY(phd_prepare_f32_parts(mesh, nullptr, out, PHD_PREP_CELLS_FROM_FACES, lists));
+    PHD_TRY_CUDA(cudaEventRecord(events[5], lists));
+
+    // stream: ghost totals from their images, primitives and the next dt
+    PHD_TRY_CUDA(cudaStreamWaitEvent(stream, events[5], 0));
+    PHD_TRY(phd_ghost_cons_f64(mesh, cons, stream));
+    PHD_TRY(phd_prim_f32_cells(mesh, out->cell_geo, par, cons, prim4, clk, stream));
+#undef PHD_TRY
+#undef PHD_TRY_CUDA
+    return PHD_OK;
 }
 
 }  // extern "C"

@@ -201,8 +201,13 @@ class FluxStepper:
             raise ValueError("the compact hand-over carries FP32 face geometry: FP32 steppers only")
         if getattr(self, "_side", None) is None:
             self._side = torch.cuda.Stream(self.device)
-            self._ev = [torch.cuda.Event() for _ in range(4)]
+            self._side2 = torch.cuda.Stream(self.device)
+            self._ev = [torch.cuda.Event() for _ in range(6)]
+            for e in self._ev:                        # creates the events' handles
+                e.record(main)
         side, ev = self._side, self._ev
+        if compact:
+            return self._load_mesh_compact(pinned, resized, xr if resident else None, main)
         s, ss = L.stream_handle(main), L.stream_handle(side)
         out = None
         if fp32:
@@ -211,16 +216,7 @@ class FluxStepper:
         # copies on the main stream in the order the side stream needs them; the side
         # stream builds the neighbour lists, twins, list codes and face geometry meanwhile
         dm.reset_errors(main)
-        if compact:
-            # pair-i from the per-real-cell face ranges (phd_pair_i_from_face_ptr)
-            face_ptr = self._view("face_ptr_in", (dm.n_real + 1,), torch.int32)
-            with torch.cuda.stream(main):
-                face_ptr.copy_(pinned["face_ptr"], non_blocking=True)
-            nbytes = face_ptr.numel() * 4 + dm.copy_fields(pinned, ("pair_j",), main)
-            L.check(lib.phd_pair_i_from_face_ptr(dm.ref, L.ptr(face_ptr), L.ptr(dm.pair_i), L.ptr(dm._bad), s),
-                    "phd_pair_i_from_face_ptr")
-        else:
-            nbytes = dm.copy_fields(pinned, ("pair_i", "pair_j"), main)
+        nbytes = dm.copy_fields(pinned, ("pair_i", "pair_j"), main)
         ev[0].record(main)
         side.wait_event(ev[0])
         dm.build_lists(side)
@@ -228,19 +224,8 @@ class FluxStepper:
             nbytes += dm.copy_fields(pinned, ("tag", "type", "map"), main)
         else:
             nbytes += dm.copy_ghost_map(pinned, main)
-        if resident:
-            code = self._view("ghost_code_in", (dm.n_cells - dm.n_real,), torch.int8)
-            with torch.cuda.stream(main):
-                for k in range(dm.dim):                       # row by row: plain device copies
-                    dm.x[k, :dm.n_real].copy_(xr[k])
-                code.copy_(pinned["ghost_code"], non_blocking=True)
-            nbytes += code.numel()
-            L.check(lib.phd_ghost_positions(dm.ref, L.ptr(code), float(dm.xmin[0]), float(dm.xmin[1]),
-                                            float(dm.xmax[0]), float(dm.xmax[1]), L.ptr(dm._bad), s),
-                    "phd_ghost_positions")
-        else:
-            nbytes += dm.copy_fields(pinned, ("x",), main)
-            self._x_real_valid = False
+        nbytes += dm.copy_fields(pinned, ("x",), main)
+        self._x_real_valid = False
         ev[1].record(main)
         if fp32:
             side.wait_event(ev[1])
@@ -250,28 +235,15 @@ class FluxStepper:
                     "phd_periodic_twins")
             L.check(lib.phd_prepare_f32_parts(dm.ref, L.ptr(self.twin), ctypes.byref(out), L.PREP_LISTS, ss),
                     "phd_prepare_f32_parts")
-        if compact:
-            area32 = self._view("area32_in", (dm.n_faces,), torch.float32)
-            crel32 = self._view("crel32_in", (dm.n_faces, dm.dim), torch.float32)
-            with torch.cuda.stream(main):
-                area32.copy_(pinned["area32"], non_blocking=True)
-                crel32.copy_(pinned["crel32"], non_blocking=True)
-            nbytes += (area32.numel() + crel32.numel()) * 4
-        else:
-            nbytes += dm.copy_fields(pinned, ("com", "area"), main)
+        nbytes += dm.copy_fields(pinned, ("com", "area"), main)
         if fp32:
             # face geometry, then the cells' volumes and centroids from it (the FP32 path
             # needs neither host volumes nor host centroids)
             ev[2].record(main)
             side.wait_event(ev[2])
             dm.set_normals("none", side)
-            if compact:
-                L.check(lib.phd_prepare_f32_faces_compact(dm.ref, L.ptr(area32), L.ptr(crel32), ctypes.byref(out),
-                                                          ss), "phd_prepare_f32_faces_compact")
-                parts = L.PREP_CELLS_FROM_FACES
-            else:
-                parts = L.PREP_FACES | L.PREP_CELLS_FROM_FACES
-            L.check(lib.phd_prepare_f32_parts(dm.ref, None, ctypes.byref(out), parts, ss), "phd_prepare_f32_parts")
+            L.check(lib.phd_prepare_f32_parts(dm.ref, None, ctypes.byref(out), L.PREP_FACES | L.PREP_CELLS_FROM_FACES,
+                                              ss), "phd_prepare_f32_parts")
         ev[3].record(side)
         if not fp32:
             nbytes += dm.copy_fields(pinned, ("dcom", "vol"), main)
@@ -286,6 +258,50 @@ class FluxStepper:
             L.check(lib.phd_prim_from_cons_f64(dm.dim, dm.n_cells, p.gamma, L.ptr(dm.vol), L.ptr(self.cons),
                                                L.ptr(self.prim), s), "phd_prim_from_cons_f64")
             self.initial_time_step()
+        return nbytes
+
+    def _load_mesh_compact(self, pinned, resized, xr, main):
+        """load_mesh for the compact FP32 hand-over as one C call (phd_load_mesh_f32):
+        the copies on the main stream, the derivations on two side streams while the
+        face records are in flight.  xr: the real cells' device positions when the
+        hand-over carries none."""
+        dm, lib = self.dmesh, L.lib()
+        nr, ng, nf = dm.n_real, dm.n_cells - dm.n_real, dm.n_faces
+        nbytes = 0
+        if resized:                                   # tags, types and the whole map are new
+            nbytes += dm.copy_fields(pinned, ("tag", "type", "map"), main)
+        if not hasattr(dm, "_bad"):
+            dm.reset_errors(main)
+        stage = {"face_ptr": self._view("face_ptr_in", (nr + 1,), torch.int32),
+                 "area32": self._view("area32_in", (nf,), torch.float32),
+                 "crel32": self._view("crel32_in", (nf, dm.dim), torch.float32)}
+        if xr is not None:
+            stage["ghost_code"] = self._view("ghost_code_in", (ng,), torch.int8)
+        dm.set_normals("none")
+        hp = lambda k: pinned[k].data_ptr() if k in pinned else None
+        h = L.PhdHandover32(face_ptr=hp("face_ptr"), pair_j=hp("pair_j"), area32=hp("area32"), crel32=hp("crel32"),
+                            ghost_map=None if resized else pinned["map"][nr:].data_ptr(),
+                            ghost_code=hp("ghost_code") if xr is not None else None,
+                            x=None if xr is not None else hp("x"),
+                            x_real=xr.data_ptr() if xr is not None else None, type=dm.type.data_ptr(),
+                            d_face_ptr=stage["face_ptr"].data_ptr(), d_area32=stage["area32"].data_ptr(),
+                            d_crel32=stage["crel32"].data_ptr(),
+                            d_ghost_code=stage["ghost_code"].data_ptr() if xr is not None else None,
+                            twin=self.twin.data_ptr(), csr_work=dm._csr_work.data_ptr(), bad=dm._bad.data_ptr(),
+                            periodic=int(dm.boundary == "periodic"), dedup_periodic=int(self.dedup_periodic),
+                            xmin=(ctypes.c_double * 2)(*dm.xmin[:2]),
+                            xmax=(ctypes.c_double * 2)(*dm.xmax[:2]))
+        out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face, self.csr_nbr,
+                                                        self.cell_geo)))
+        events = (ctypes.c_void_p * 6)(*(e.cuda_event for e in self._ev))
+        sides = (ctypes.c_void_p * 2)(self._side.cuda_stream, self._side2.cuda_stream)
+        L.check(lib.phd_load_mesh_f32(dm.ref, ctypes.byref(h), ctypes.byref(self.params), ctypes.byref(out),
+                                      L.ptr(self.cons), L.ptr(self.prim4), self.clock.ptr, L.stream_handle(main),
+                                      sides, events), "phd_load_mesh_f32")
+        if xr is None:
+            self._x_real_valid = False
+        nbytes += 4 * (nr + 1) + 4 * nf + 12 * nf + (0 if resized else 4 * ng)
+        nbytes += ng if xr is not None else 8 * dm.dim * dm.n_cells
         return nbytes
 
     def _launch_step(self, marks=None):

@@ -98,3 +98,29 @@ def test_argument_errors_are_rejected_on_the_host(lib):
     m.x = 1
     assert f.phd_move_generators(ctypes.byref(m), None, None, one, 1, 0.0, 0.0, 1.0, 1.0, one, None) == L.PHD_ERR_ARG
     assert f.phd_move_generators(ctypes.byref(m), one, one, one, 1, 0.0, 0.0, 1.0, 1.0, one, None) == L.PHD_ERR_ARG
+    # one-call compact hand-over: incomplete hand-over, a mesh that still carries FP64
+    # normals, an empty box, ghosts without their codes
+    h = L.PhdHandover32(face_ptr=1, pair_j=1, area32=1, crel32=1, type=1, d_face_ptr=1, d_area32=1, d_crel32=1,
+                        twin=1, csr_work=1, bad=1, periodic=1, dedup_periodic=1,
+                        xmin=(ctypes.c_double * 2)(0.0, 0.0), xmax=(ctypes.c_double * 2)(1.0, 1.0))
+    ev = (ctypes.c_void_p * 6)(1, 1, 1, 1, 1, 1)
+    sides = (ctypes.c_void_p * 2)(None, None)
+    m.x, m.normal, m.n_real = 1, None, 8
+    m.pair_i = m.pair_j = m.map = m.flip = m.nbr_ptr = m.nbr_idx = 1
+
+    def load(mesh, hh):
+        return f.phd_load_mesh_f32(ctypes.byref(mesh), ctypes.byref(hh), ctypes.byref(par), ctypes.byref(out), one,
+                                   one, one, None, sides, ev)
+
+    assert load(m, h) == L.PHD_ERR_ARG                    # 2 ghosts, neither positions nor ghost codes
+    h.ghost_code, h.d_ghost_code = 1, 1
+    m.normal = 1
+    assert load(m, h) == L.PHD_ERR_ARG                    # FP64 normals still attached
+    m.normal = None
+    h.xmax = (ctypes.c_double * 2)(0.0, 1.0)
+    assert load(m, h) == L.PHD_ERR_ARG                    # empty box
+    h.xmax = (ctypes.c_double * 2)(1.0, 1.0)
+    h.twin = None
+    assert load(m, h) == L.PHD_ERR_ARG                    # no twin table
+    assert f.phd_load_mesh_f32(None, ctypes.byref(h), ctypes.byref(par), ctypes.byref(out), one, one, one, None,
+                               sides, ev) == L.PHD_ERR_ARG
