@@ -536,7 +536,7 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     PHD_TRY_CUDA(cudaEventRecord(events[2], stream));
 
     // lists stream, while the face records are in flight: pair-i with the list counts,
-    // every position, the neighbour lists, periodic twins, FP32 list codes, flip bits
+    // every position, the neighbour lists, periodic twins and FP32 list codes
     const int32_t *nbr_ptr = mesh->nbr_ptr;
     int32_t *cnt = h->csr_work, *cursor = h->csr_work + n, *tile_sum = h->csr_work + 2 * (size_t)n;
     const int n_tiles = (n + phd::SCAN_TILE - 1) / phd::SCAN_TILE;
@@ -568,13 +568,13 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     PHD_TRY(phd_periodic_twins(mesh, h->periodic && h->dedup_periodic, h->xmax[0] - h->xmin[0],
                                h->xmax[1] - h->xmin[1], h->twin, lists));
     PHD_TRY(phd_prepare_f32_parts(mesh, h->twin, out, PHD_PREP_LISTS, lists));
-    const double lo[3] = {h->xmin[0], h->xmin[1], 0.}, hi[3] = {h->xmax[0], h->xmax[1], 0.};
-    PHD_TRY(phd_flip_mask(2, n, h->type, x, lo, hi, !h->periodic, const_cast<int8_t *>(mesh->flip), lists));
 
-    // geometry stream: the FP32 face geometry as soon as the records and the positions
-    // are there, beside the lists
-    PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[2], 0));
+    // geometry stream, beside the lists: the flip bits once the positions are there,
+    // the FP32 face geometry once the face records are too
+    const double lo[3] = {h->xmin[0], h->xmin[1], 0.}, hi[3] = {h->xmax[0], h->xmax[1], 0.};
     PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[3], 0));
+    PHD_TRY(phd_flip_mask(2, n, h->type, x, lo, hi, !h->periodic, const_cast<int8_t *>(mesh->flip), geom));
+    PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[2], 0));
     PHD_TRY(phd_prepare_f32_faces_compact(mesh, h->d_area32, h->d_crel32, out, geom));
     PHD_TRY_CUDA(cudaEventRecord(events[4], geom));
 
