@@ -292,10 +292,11 @@ int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, con
  *
  * The copies run on `stream` with the large ones (area, centroid offset) issued right
  * after the small ones the lists need; the derivations run on side[0] (pair-i,
- * positions, lists, twins, list codes, then the cell geometry) and side[1] (the flip
- * bits, and the face geometry as soon as the face records have landed) while the
- * copies are in flight, and are joined back into `stream` at the end.  events: 6 CUDA events
- * (created by the caller, reused across calls).  The mesh's own arrays (pair_i, pair_j, map
+ * positions, neighbour lists, list codes, then the cell geometry) and side[1] (flip
+ * bits, periodic twins from the face ranges, and the face geometry as soon as the face
+ * records have landed, in two halves) while the copies are in flight, and are joined
+ * back into `stream` at the end.  events: 8 CUDA events (created by the caller, reused
+ * across calls).  The mesh's own arrays (pair_i, pair_j, map
  * ghost rows, x, nbr_ptr/nbr_idx, flip) are written through the const view; mesh->normal
  * must be NULL (the FP32 geometry forms its own normals).  The counts are the mesh's:
  * a tessellation with other counts needs the arrays re-sized first.  Faces or ghosts

@@ -257,6 +257,39 @@ __global__ void k_periodic_twins(phd_mesh M, int periodic, double Lx, double Ly,
 }
 
 
+// k_periodic_twins for a hand-over whose faces come in per-real-cell ranges: the
+// candidates of image cell k are its own faces [face_ptr[k], face_ptr[k+1]) -- in
+// ascending order, as they stand in k's sorted neighbour list, so the table is the same
+// -- and the neighbour lists are not needed.
+__global__ void k_periodic_twins_ranges(phd_mesh M, const int32_t *__restrict__ face_ptr, double Lx, double Ly,
+                                        int32_t *__restrict__ twin) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= M.n_faces) return;
+    const int n = M.n_cells, nr = M.n_real, F = M.n_faces;
+    int32_t out = -1;
+    const int i = M.pair_i[a], g = M.pair_j[a];
+    if (i >= 0 && i < nr && g >= nr && g < n) {
+        const int k = M.map[g];
+        if (k >= 0 && k < nr && k != i) {
+            const int sx = shift_of(M.x[g] - M.x[k], Lx);
+            const int sy = shift_of(M.x[(size_t)n + g] - M.x[(size_t)n + k], Ly);
+            const int b0 = max(face_ptr[k], 0), b1 = min(face_ptr[k + 1], F);
+            for (int b = b0; b < b1; b++) {
+                if (b == a || M.pair_i[b] != k) continue;
+                const int g2 = M.pair_j[b];
+                if (g2 < nr || g2 >= n || M.map[g2] != i) continue;
+                const int tx = shift_of(M.x[g2] - M.x[i], Lx);
+                const int ty = shift_of(M.x[(size_t)n + g2] - M.x[(size_t)n + i], Ly);
+                if (tx == -sx && ty == -sy) {
+                    if (b < a) out = b;
+                    break;
+                }
+            }
+        }
+    }
+    twin[a] = out;
+}
+
 // DomainManager.move_generators (domain_manager.pyx:566-590) and the boundary
 // conditions' migrate_particles (boundary.pyx:236-263 reflective, 502-538 periodic) for
 // the real cells, after a step, with the step's own dt (clk->dt_last).  The product and
@@ -531,12 +564,19 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     else if (ng > 0)
         PHD_TRY_CUDA(cudaMemcpyAsync(h->d_ghost_code, h->ghost_code, (size_t)ng, H2D, stream));
     PHD_TRY_CUDA(cudaEventRecord(events[1], stream));
-    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_area32, h->area32, (size_t)F * sizeof(float), H2D, stream));
-    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_crel32, h->crel32, (size_t)F * 2 * sizeof(float), H2D, stream));
+    // the face records in two halves: the first half's geometry is formed while the
+    // second half is in flight
+    const int F0 = F / 2;
+    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_area32, h->area32, (size_t)F0 * sizeof(float), H2D, stream));
+    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_crel32, h->crel32, (size_t)F0 * 2 * sizeof(float), H2D, stream));
+    PHD_TRY_CUDA(cudaEventRecord(events[7], stream));
+    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_area32 + F0, h->area32 + F0, (size_t)(F - F0) * sizeof(float), H2D, stream));
+    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_crel32 + 2 * (size_t)F0, h->crel32 + 2 * (size_t)F0,
+                                 (size_t)(F - F0) * 2 * sizeof(float), H2D, stream));
     PHD_TRY_CUDA(cudaEventRecord(events[2], stream));
 
     // lists stream, while the face records are in flight: pair-i with the list counts,
-    // every position, the neighbour lists, periodic twins and FP32 list codes
+    // every position, the neighbour lists
     const int32_t *nbr_ptr = mesh->nbr_ptr;
     int32_t *cnt = h->csr_work, *cursor = h->csr_work + n, *tile_sum = h->csr_work + 2 * (size_t)n;
     const int n_tiles = (n + phd::SCAN_TILE - 1) / phd::SCAN_TILE;
@@ -565,20 +605,39 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
             n, nbr_ptr, const_cast<int32_t *>(mesh->nbr_idx));
     }
     PHD_TRY_CUDA(cudaPeekAtLastError());
-    PHD_TRY(phd_periodic_twins(mesh, h->periodic && h->dedup_periodic, h->xmax[0] - h->xmin[0],
-                               h->xmax[1] - h->xmin[1], h->twin, lists));
-    PHD_TRY(phd_prepare_f32_parts(mesh, h->twin, out, PHD_PREP_LISTS, lists));
 
-    // geometry stream, beside the lists: the flip bits once the positions are there,
-    // the FP32 face geometry once the face records are too
+    // geometry stream, beside the lists: the flip bits and periodic twins once the
+    // positions are there, the FP32 face geometry once the face records are too
     const double lo[3] = {h->xmin[0], h->xmin[1], 0.}, hi[3] = {h->xmax[0], h->xmax[1], 0.};
     PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[3], 0));
     PHD_TRY(phd_flip_mask(2, n, h->type, x, lo, hi, !h->periodic, const_cast<int8_t *>(mesh->flip), geom));
-    PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[2], 0));
-    PHD_TRY(phd_prepare_f32_faces_compact(mesh, h->d_area32, h->d_crel32, out, geom));
+    if (F > 0) {
+        if (h->periodic && h->dedup_periodic)
+            phd::k_periodic_twins_ranges<<<(F + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, geom>>>(
+                *mesh, h->d_face_ptr, h->xmax[0] - h->xmin[0], h->xmax[1] - h->xmin[1], h->twin);
+        else
+            PHD_TRY_CUDA(cudaMemsetAsync(h->twin, 0xff, (size_t)F * sizeof(int32_t), geom));
+    }
+    PHD_TRY_CUDA(cudaEventRecord(events[6], geom));
+    for (int half = 0; half < 2; half++) {        // faces [0, F0), then [F0, F)
+        const int m0 = half ? F0 : 0, cnt = half ? F - F0 : F0;
+        phd_mesh part = *mesh;
+        part.pair_i += m0;
+        part.pair_j += m0;
+        part.n_faces = cnt;
+        phd_geom32_out po = *out;
+        po.face_geo += 4 * (size_t)m0;
+        po.face_ar += 2 * (size_t)m0;
+        PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[half ? 2 : 7], 0));
+        if (cnt > 0)
+            PHD_TRY(phd_prepare_f32_faces_compact(&part, h->d_area32 + m0, h->d_crel32 + 2 * (size_t)m0, &po, geom));
+    }
     PHD_TRY_CUDA(cudaEventRecord(events[4], geom));
 
-    // lists stream: the cells' volumes and centroids from faces and lists
+    // lists stream: the FP32 list codes once the twins are there, then the cells'
+    // volumes and centroids from faces and lists
+    PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[6], 0));
+    PHD_TRY(phd_prepare_f32_parts(mesh, h->twin, out, PHD_PREP_LISTS, lists));
     PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[4], 0));
     PHD_TRY(phd_prepare_f32_parts(mesh, nullptr, out, PHD_PREP_CELLS_FROM_FACES, lists));
     PHD_TRY_CUDA(cudaEventRecord(events[5], lists));

@@ -202,7 +202,7 @@ class FluxStepper:
         if getattr(self, "_side", None) is None:
             self._side = torch.cuda.Stream(self.device)
             self._side2 = torch.cuda.Stream(self.device)
-            self._ev = [torch.cuda.Event() for _ in range(6)]
+            self._ev = [torch.cuda.Event() for _ in range(8)]
             for e in self._ev:                        # creates the events' handles
                 e.record(main)
         side, ev = self._side, self._ev
@@ -293,7 +293,7 @@ class FluxStepper:
                             xmax=(ctypes.c_double * 2)(*dm.xmax[:2]))
         out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face, self.csr_nbr,
                                                         self.cell_geo)))
-        events = (ctypes.c_void_p * 6)(*(e.cuda_event for e in self._ev))
+        events = (ctypes.c_void_p * 8)(*(e.cuda_event for e in self._ev))
         sides = (ctypes.c_void_p * 2)(self._side.cuda_stream, self._side2.cuda_stream)
         L.check(lib.phd_load_mesh_f32(dm.ref, ctypes.byref(h), ctypes.byref(self.params), ctypes.byref(out),
                                       L.ptr(self.cons), L.ptr(self.prim4), self.clock.ptr, L.stream_handle(main),

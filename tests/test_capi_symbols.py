@@ -103,7 +103,7 @@ def test_argument_errors_are_rejected_on_the_host(lib):
     h = L.PhdHandover32(face_ptr=1, pair_j=1, area32=1, crel32=1, type=1, d_face_ptr=1, d_area32=1, d_crel32=1,
                         twin=1, csr_work=1, bad=1, periodic=1, dedup_periodic=1,
                         xmin=(ctypes.c_double * 2)(0.0, 0.0), xmax=(ctypes.c_double * 2)(1.0, 1.0))
-    ev = (ctypes.c_void_p * 6)(1, 1, 1, 1, 1, 1)
+    ev = (ctypes.c_void_p * 8)(1, 1, 1, 1, 1, 1, 1, 1)
     sides = (ctypes.c_void_p * 2)(None, None)
     m.x, m.normal, m.n_real = 1, None, 8
     m.pair_i = m.pair_j = m.map = m.flip = m.nbr_ptr = m.nbr_idx = 1
