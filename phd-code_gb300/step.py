@@ -323,6 +323,32 @@ class FluxStepper:
         L.check(rc, "phd_step_" + self.precision)
         self.cons, self.cons_next = self.cons_next, self.cons
 
+    def step_and_fetch(self, host_w):
+        """One step whose generator velocities (w2 [n][2] FP32, or w [2][n] FP64) are
+        copied into the pinned host buffer ``host_w`` as soon as the step's first stage
+        has formed them, on a copy stream that overlaps the rest of the step -- what the
+        host needs for the next re-mesh (integrate.py:410-417), without waiting for the
+        flux and update kernels.  Returns the copy's CUDA event; ``host_w`` holds the
+        velocities once it has completed.  Later work on the stepper's stream waits for
+        the copy (the next step overwrites the velocities)."""
+        if not self.moving:
+            raise RuntimeError("generator velocities exist only in moving-mesh steps")
+        main = self.stream if self.stream is not None else torch.cuda.current_stream(self.device)
+        if getattr(self, "_fetch", None) is None:
+            evs = [torch.cuda.Event() for _ in range(4)]
+            for e in evs:                              # creates the events' handles
+                e.record(main)
+            self._fetch = (torch.cuda.Stream(self.device), evs, torch.cuda.Event())
+        copy_stream, evs, done = self._fetch
+        w = self.w2 if self.precision == "fp32" else self.w
+        self._launch_step(marks=(ctypes.c_void_p * 4)(*(e.cuda_event for e in evs)))
+        copy_stream.wait_event(evs[1])                 # recorded after the gradient stage
+        with torch.cuda.stream(copy_stream):
+            host_w.copy_(w, non_blocking=True)
+            done.record(copy_stream)
+        main.wait_event(done)
+        return done
+
     def move_generators(self):
         """DomainManager.move_generators + migrate_particles (domain_manager.pyx:566-590,
         boundary.pyx:236-263, 502-538) on the device after a moving step: x + dt * w for the

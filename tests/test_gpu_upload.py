@@ -390,3 +390,27 @@ def test_resident_positions_hand_over_equals_the_full_one(boundary):
     b.step(2)
     a.check_status()
     assert np.array_equal(a.cons_host(), b.cons_host())
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_step_and_fetch_returns_the_step_velocities_early(precision):
+    """step_and_fetch copies the generator velocities to pinned host memory on a copy
+    stream as soon as the step's first stage has formed them: the same velocities and
+    the same state as a plain step followed by a copy, several steps in a row."""
+    m = lattice_mesh(24, "periodic", seed=4)
+    prim = smooth_state(m)
+    a = FluxStepper(m, prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision=precision)
+    b = FluxStepper(m, prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision=precision)
+    wa = a.w2 if precision == "fp32" else a.w
+    host = torch.empty_like(wa, device="cpu").pin_memory()
+    for _ in range(3):
+        a.step(1)
+        ev = b.step_and_fetch(host)
+        ev.synchronize()
+        assert torch.equal(host, wa.cpu())
+    a.check_status()
+    b.check_status()
+    assert np.array_equal(a.cons_host(), b.cons_host())
+    fixed = FluxStepper(m, prim, gamma=1.4, cfl=0.5, solver="hllc", moving=False, precision=precision)
+    with pytest.raises(RuntimeError, match="moving-mesh"):
+        fixed.step_and_fetch(host)
