@@ -182,4 +182,10 @@ __device__ __forceinline__ void finish_cfl(phd_clock *clk, double cfl, bool adva
     finish_cfl_multi(clk, 1, cfl, advance);
 }
 
+// The tail of an FP32 mesh hand-over in one kernel (defined with the FP32 kernels):
+// cell geometry from the prepared faces and lists, ghost totals from their images,
+// primitives and the next dt.
+int cells_prim_f32(const phd_mesh *mesh, const phd_params *par, const phd_geom32_out *out, double *cons,
+                   float *prim4, phd_clock *clk, cudaStream_t stream);
+
 }  // namespace phd

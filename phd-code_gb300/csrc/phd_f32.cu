@@ -126,11 +126,9 @@ __global__ void k_prepare_cells32(phd_mesh M, float4 *__restrict__ cell_geo) {
 // with f - x = c + r n / 2 from pair-i and c - r n / 2 from pair-j.  Ghost rows take
 // their image's values (dcom unflipped, as the ghost copies do).  FP32 throughout: the
 // relative vectors have no cancellation left.
-__global__ void k_cells_from_faces32(phd_mesh M, const float4 *__restrict__ face_geo,
-                                     const float2 *__restrict__ face_ar, const int32_t *__restrict__ csr_face,
-                                     float4 *__restrict__ cell_geo) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= M.n_cells) return;
+__device__ __forceinline__ float4 cell_geo_of(const phd_mesh &M, int i, const float4 *__restrict__ face_geo,
+                                              const float2 *__restrict__ face_ar,
+                                              const int32_t *__restrict__ csr_face) {
     const int c = (M.tag[i] == PHD_REAL_TAG) ? i : M.map[i];
     float vol = 0.f, sx = 0.f, sy = 0.f;
     if (c >= 0 && c < M.n_cells) {
@@ -147,7 +145,15 @@ __global__ void k_cells_from_faces32(phd_mesh M, const float4 *__restrict__ face
         }
     }
     const float inv = vol > 0.f ? 1.f / vol : 0.f;
-    cell_geo[i] = make_float4((2.f / 3.f) * sx * inv, (2.f / 3.f) * sy * inv, inv, sqrtf(vol * 0.3183098861837907f));
+    return make_float4((2.f / 3.f) * sx * inv, (2.f / 3.f) * sy * inv, inv, sqrtf(vol * 0.3183098861837907f));
+}
+
+__global__ void k_cells_from_faces32(phd_mesh M, const float4 *__restrict__ face_geo,
+                                     const float2 *__restrict__ face_ar, const int32_t *__restrict__ csr_face,
+                                     float4 *__restrict__ cell_geo) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M.n_cells) return;
+    cell_geo[i] = cell_geo_of(M, i, face_geo, face_ar, csr_face);
 }
 
 // CSR entries with the side folded into the face id, plus the neighbour cell.  Where a
@@ -732,6 +738,24 @@ __global__ void __launch_bounds__(512) k_update32(phd_mesh M, phd_params P, cons
     finish_cfl_multi(clocks, cell_run ? n_runs : 1, P.cfl, true);
 }
 
+// IdealGas.primitive_from_conservative equation_state.pyx:106-117 in FP32 from the FP64
+// totals U (internal energy formed in FP64) and the CFL candidate riemann.pyx:170-187
+// of a real cell (INFINITY for a ghost); R = sqrt(vol/pi).
+__device__ __forceinline__ float prim32_of(const double (&U)[4], float inv_v, float R, bool real,
+                                           const phd_params &P, float gam, float4 &out) {
+    const float m = narrow_f64(U[0]), mx = narrow_f64(U[1]), my = narrow_f64(U[2]);
+    const float rm = 1.f / m;
+    const float vx = mx * rm, vy = my * rm;
+    const float ke = 0.5f * (mx * vx + my * vy);
+    const float p = (gam - 1.f) * narrow_f64(U[3] - widen_f32(ke)) * inv_v;
+    const float4 pr = make_float4(m * inv_v, vx, vy, p);
+    out = pr;
+    if (!real) return INFINITY;
+    const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
+    const float cs = sqrtf(gam * pr.w / pr.x);
+    return R / (boost ? cs : cs + sqrtf(pr.y * pr.y + pr.z * pr.z));
+}
+
 // FP64 conserved totals -> FP32 primitive cells and each run's CFL step (clocks not
 // advanced).  Same per-run reduction as k_update32.
 __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const double *__restrict__ cons,
@@ -749,30 +773,18 @@ __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const 
         int run = 0;
         if (i < n) {
             // the primitive recovery of k_update32 (FP32, internal energy formed in FP64)
-            const double U3 = cons[3 * (size_t)n + i];
-            const float m = narrow_f64(cons[i]), mx = narrow_f64(cons[(size_t)n + i]);
-            const float my = narrow_f64(cons[2 * (size_t)n + i]);
-            float v, inv_v, R;
+            const double U[4] = {cons[i], cons[(size_t)n + i], cons[2 * (size_t)n + i], cons[3 * (size_t)n + i]};
+            float inv_v, R;
             if (cell_geo) {                    // volumes formed on the device from the faces
                 const float4 cg = cell_geo[i];
                 inv_v = cg.z;
                 R = cg.w;
             } else {
-                v = narrow_f64(M.vol[i]);
+                const float v = narrow_f64(M.vol[i]);
                 inv_v = 1.f / v;
                 R = sqrtf(v * 0.3183098861837907f);
             }
-            const float rm = 1.f / m;
-            const float vx = mx * rm, vy = my * rm;
-            const float ke = 0.5f * (mx * vx + my * vy);
-            const float p = (gam - 1.f) * narrow_f64(U3 - widen_f32(ke)) * inv_v;
-            const float4 pr = make_float4(m * inv_v, vx, vy, p);
-            prim4[i] = pr;
-            if (M.tag[i] == PHD_REAL_TAG) {
-                const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
-                const float cs = sqrtf(gam * pr.w / pr.x);
-                cand = R / (boost ? cs : cs + sqrtf(pr.y * pr.y + pr.z * pr.z));
-            }
+            cand = prim32_of(U, inv_v, R, M.tag[i] == PHD_REAL_TAG, P, gam, prim4[i]);
             if (cell_run) run = cell_run[i];
         }
         if (!cell_run) {
@@ -789,6 +801,56 @@ __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const 
     }
     if (!cell_run) block_min_to_f(cand_all, &clocks[0].dtmin_bits);
     finish_cfl_multi(clocks, cell_run ? n_runs : 1, P.cfl, false);
+}
+
+// The tail of a mesh hand-over in one pass per cell: the cell geometry from the faces
+// (k_cells_from_faces32), a ghost's FP64 totals from its image with the momentum
+// flipped across reflective walls (k_ghost_cons), the primitives and the CFL step
+// (k_prim32) -- the same expressions as the three kernels, so the same bits.
+__global__ void __launch_bounds__(512) k_cells_prim32(phd_mesh M, phd_params P, const float4 *__restrict__ face_geo,
+                                                      const float2 *__restrict__ face_ar,
+                                                      const int32_t *__restrict__ csr_face,
+                                                      float4 *__restrict__ cell_geo, double *__restrict__ cons,
+                                                      float4 *__restrict__ prim4, phd_clock *clocks) {
+    const int n = M.n_cells;
+    const int stride = gridDim.x * blockDim.x;
+    const int n_iter = (n + stride - 1) / stride;
+    const float gam = narrow_f64(P.gamma);
+    float cand_all = INFINITY;
+    for (int it = 0; it < n_iter; it++) {
+        const int i = blockIdx.x * blockDim.x + threadIdx.x + it * stride;
+        if (i >= n) continue;
+        const float4 cg = cell_geo_of(M, i, face_geo, face_ar, csr_face);
+        cell_geo[i] = cg;
+        const bool real = M.tag[i] == PHD_REAL_TAG;
+        const int c = real ? i : M.map[i];
+        double U[4];
+        if (real || c < 0 || c >= n) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) U[q] = cons[(size_t)q * n + i];
+        } else {
+            const int fl = M.flip ? M.flip[i] : 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                double u = cons[(size_t)q * n + c];
+                if (q >= 1 && q <= 2 && (fl & (1 << (q - 1)))) u *= -1;
+                U[q] = u;
+                cons[(size_t)q * n + i] = u;
+            }
+        }
+        cand_all = fminf(cand_all, prim32_of(U, cg.z, cg.w, real, P, gam, prim4[i]));
+    }
+    block_min_to_f(cand_all, &clocks[0].dtmin_bits);
+    finish_cfl_multi(clocks, 1, P.cfl, false);
+}
+
+int cells_prim_f32(const phd_mesh *mesh, const phd_params *par, const phd_geom32_out *out, double *cons,
+                   float *prim4, phd_clock *clk, cudaStream_t stream) {
+    if (!mesh || mesh->dim != 2 || mesh->n_cells <= 0 || !par || !out || !out->cell_geo || !cons || !prim4 || !clk) return PHD_ERR_ARG;
+    k_cells_prim32<<<(mesh->n_cells + B32 - 1) / B32, B32, 0, stream>>>(
+        *mesh, *par, reinterpret_cast<const float4 *>(out->face_geo), reinterpret_cast<const float2 *>(out->face_ar),
+        out->csr_face, reinterpret_cast<float4 *>(out->cell_geo), cons, reinterpret_cast<float4 *>(prim4), clk);
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
 template <int SOLVER>

@@ -634,18 +634,16 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     }
     PHD_TRY_CUDA(cudaEventRecord(events[4], geom));
 
-    // lists stream: the FP32 list codes once the twins are there, then the cells'
-    // volumes and centroids from faces and lists
+    // lists stream: the FP32 list codes once the twins are there
     PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[6], 0));
     PHD_TRY(phd_prepare_f32_parts(mesh, h->twin, out, PHD_PREP_LISTS, lists));
-    PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[4], 0));
-    PHD_TRY(phd_prepare_f32_parts(mesh, nullptr, out, PHD_PREP_CELLS_FROM_FACES, lists));
     PHD_TRY_CUDA(cudaEventRecord(events[5], lists));
 
-    // stream: ghost totals from their images, primitives and the next dt
+    // stream, once the lists and the faces are in: cell geometry, ghost totals from
+    // their images, primitives and the next dt in one pass
     PHD_TRY_CUDA(cudaStreamWaitEvent(stream, events[5], 0));
-    PHD_TRY(phd_ghost_cons_f64(mesh, cons, stream));
-    PHD_TRY(phd_prim_f32_cells(mesh, out->cell_geo, par, cons, prim4, clk, stream));
+    PHD_TRY_CUDA(cudaStreamWaitEvent(stream, events[4], 0));
+    PHD_TRY(phd::cells_prim_f32(mesh, par, out, cons, prim4, clk, stream));
 #undef PHD_TRY
 #undef PHD_TRY_CUDA
     return PHD_OK;
