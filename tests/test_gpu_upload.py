@@ -414,3 +414,27 @@ def test_step_and_fetch_returns_the_step_velocities_early(precision):
     fixed = FluxStepper(m, prim, gamma=1.4, cfl=0.5, solver="hllc", moving=False, precision=precision)
     with pytest.raises(RuntimeError, match="moving-mesh"):
         fixed.step_and_fetch(host)
+
+
+def test_compact_hand_over_without_periodic_dedup():
+    """With periodic twin de-duplication off, the one-call compact hand-over leaves the
+    twin table empty (every entry -1) and forms the same lists, geometry and state as
+    the full hand-over with de-duplication off."""
+    meshes = _moved_meshes(20, "periodic", 5, 3)
+    prim = smooth_state(meshes[0])
+    kw = dict(gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32", dedup_periodic=False)
+    a = FluxStepper(meshes[0], prim, **kw)
+    b = FluxStepper(meshes[0], prim, **kw)
+    for k in range(1, len(meshes)):
+        a.step(1)
+        b.step(1)
+        a.load_mesh(a.dmesh.pinned_host(meshes[k]))
+        b.load_mesh(b.dmesh.pinned_host_compact(meshes[k]))
+        torch.cuda.synchronize()
+        assert b.dmesh.upload_errors() == 0
+        assert bool((b.twin == -1).all())
+        for name in ("face_geo", "face_ar", "csr_face", "csr_nbr", "cell_geo", "twin", "prim4"):
+            assert torch.equal(getattr(a, name), getattr(b, name)), name
+    a.step(2)
+    b.step(2)
+    assert np.array_equal(a.cons_host(), b.cons_host())
