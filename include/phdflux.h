@@ -42,6 +42,8 @@ extern "C" {
 #define PHD_STATUS_RIEMANN_NONCONVERGED 4  /* "No convergence in Exact Riemann Solver" riemann.pyx:1088-1090 */
 #define PHD_STATUS_BAD_INDEX 8             /* "ERROR: incorrect neighbors!" reconstruction.pyx:651-652 */
 #define PHD_STATUS_LEFT_DOMAIN 16          /* "particle left domain in reflective boundary condition!!" boundary.pyx:262-263 */
+#define PHD_STATUS_NONFINITE 32            /* FP32 path: a recovered primitive is NaN or infinite (no reference
+                                              counterpart: the FP64 reference carries such values on silently) */
 
 /* solver / reconstruction selectors */
 #define PHD_HLL 0                          /* riemann.pyx:225-504 */

@@ -26,7 +26,8 @@ Cython directives: ``language_level=2`` (the reference is Python 2 code),
 ``cpow=True`` (so ``range(3**dim)`` stays an int, ``boundary.pyx:378``) and
 ``legacy_implicit_noexcept=True`` (``tree.pyx:606``).
 
-Usage:  python oracle/build_ref.py [--reference /root/reference] [--jobs 8]
+Usage:  python oracle/build_ref.py [--reference DIR] [--jobs 8]
+        (DIR defaults to $PHD_REFERENCE_DIR, else /root/reference)
         python oracle/build_ref.py --compile-staged   (compile the staged C++ on this machine)
 """
 import argparse
@@ -38,6 +39,7 @@ import sys
 import textwrap
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_REFERENCE = "/root/reference"
 OUT = os.path.join(HERE, "_ref")
 BUILD = os.path.join(OUT, "build")
 
@@ -73,6 +75,9 @@ STAGE = {
     "mesh": ["mesh.pyx", "mesh.pxd", "pytess.pyx", "pytess.pxd", "tess.h", "__init__.py"],
     "riemann": ["riemann.pyx", "riemann.pxd", "__init__.py"],
     "reconstruction": ["reconstruction.pyx", "reconstruction.pxd", "__init__.py"],
+    # the integrator, for the drop-in test that installs plugin subclasses through its
+    # check_class setters (integrate.py:148-161) and steps StaticMeshMUSCLHancock
+    "integrate": ["integrate.py", "__init__.py"],
 }
 
 # Python-3 edits: (file, regex, replacement).  Container bookkeeping only.
@@ -202,6 +207,11 @@ def stage(reference):
         fh.write(REFHELPER)
 
 
+def reference_dir():
+    """Where the reference tree is read from: $PHD_REFERENCE_DIR, else the default."""
+    return os.environ.get("PHD_REFERENCE_DIR", DEFAULT_REFERENCE)
+
+
 def build(reference, jobs):
     stage(reference)
     with open(os.path.join(BUILD, "setup_ref.py"), "w") as fh:
@@ -249,7 +259,7 @@ def compile_staged(jobs=None):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=reference_dir())
     ap.add_argument("--jobs", type=int, default=os.cpu_count() or 4)
     ap.add_argument("--compile-staged", action="store_true",
                     help="compile the already staged sources for this machine (no reference tree needed)")

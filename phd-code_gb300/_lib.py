@@ -16,6 +16,7 @@ ADJ_NOALLOC_MAX_DOUBLES = 4194304
 GRAD_TAPE_F64_ROWS, GRAD_TAPE_I32_ROWS = 12, 13
 STATUS_NEG_MASS, STATUS_NEG_ENERGY, STATUS_RIEMANN_NONCONVERGED, STATUS_BAD_INDEX = 1, 2, 4, 8
 STATUS_LEFT_DOMAIN = 16
+STATUS_NONFINITE = 32
 HLL, HLLC, EXACT = 0, 1, 2
 PREP_FACES, PREP_CELLS, PREP_LISTS, PREP_ALL, PREP_CELLS_FROM_FACES = 1, 2, 4, 7, 8
 CONSTANT, LINEAR = 0, 1
@@ -28,6 +29,7 @@ STATUS_MESSAGES = {
     STATUS_RIEMANN_NONCONVERGED: "No convergence in Exact Riemann Solver",
     STATUS_BAD_INDEX: "ERROR: incorrect neighbors!",
     STATUS_LEFT_DOMAIN: "particle left domain in reflective boundary condition!!",
+    STATUS_NONFINITE: "Non-finite primitive state after flux update",
 }
 
 

@@ -94,8 +94,20 @@ __device__ __forceinline__ void block_min_to(double v, unsigned long long *slot)
 
 // FP32 <-> FP64 conversions done with integer operations, for kernels whose FP64
 // pipe is the bottleneck (GB300 issues FP64 at a small fraction of the FP32 rate).
-// Zero / denormal inputs map to signed zero; values are finite.
+// Zero / denormal inputs map to signed zero; infinities stay infinite and NaN stays NaN.
 __device__ __forceinline__ double widen_f32(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu;
+    const unsigned e64 = (ex == 0xffu) ? 0x7ffu : ex + 896u;
+    const unsigned hi = (u & 0x80000000u) | (e64 << 20) | ((u & 0x7fffffu) >> 3);
+    const unsigned lo = u << 29;
+    return __hiloint2double((int)(ex ? hi : (u & 0x80000000u)), (int)(ex ? lo : 0u));
+}
+
+// The same for finite inputs only (an infinity or NaN comes out as a finite value of
+// magnitude >= 2^128): the hot update path, which range-checks its FP64 results instead
+// (fp64_beyond_f32).
+__device__ __forceinline__ double widen_f32_finite(float f) {
     const unsigned u = __float_as_uint(f);
     const unsigned ex = (u >> 23) & 0xffu;
     const unsigned hi = (u & 0x80000000u) | ((ex + 896u) << 20) | ((u & 0x7fffffu) >> 3);
@@ -103,9 +115,10 @@ __device__ __forceinline__ double widen_f32(float f) {
     return __hiloint2double((int)(ex ? hi : (u & 0x80000000u)), (int)(ex ? lo : 0u));
 }
 
-// Round-to-nearest-even FP64 -> FP32 (finite, normal-range results; smaller
-// magnitudes flush to signed zero).
-__device__ __forceinline__ float narrow_f64(double d) {
+// Round-to-nearest-even FP64 -> FP32 for magnitudes below 2^128 (smaller magnitudes
+// than the FP32 normal range flush to signed zero): the hot update path, after
+// fp64_beyond_f32 has ruled out everything else.
+__device__ __forceinline__ float narrow_f64_finite(double d) {
     const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(d));
     const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
     const int ex = static_cast<int>((b >> 52) & 0x7ffull) - 896;
@@ -114,6 +127,31 @@ __device__ __forceinline__ float narrow_f64(double d) {
     const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (m23 & 1u));
     const unsigned mag = ((static_cast<unsigned>(ex) << 23) | m23) + up;
     return __uint_as_float(ex > 0 ? (sign | mag) : sign);
+}
+
+// True when |d| >= 2^127 (so it may round beyond FLT_MAX), or d is infinite or NaN:
+// one look at the exponent field.
+__device__ __forceinline__ bool fp64_beyond_f32(double d) {
+    return (static_cast<unsigned>(__double2hiint(d)) & 0x7ff00000u) >= ((1023u + 127u) << 20);
+}
+
+// Round-to-nearest-even FP64 -> FP32.  Magnitudes below the FP32 normal range flush
+// to signed zero; magnitudes that round above FLT_MAX, and infinities, give signed
+// infinity; NaN gives NaN -- so a blown-up FP64 total never turns into a plausible
+// finite float.
+__device__ __forceinline__ float narrow_f64(double d) {
+    const unsigned long long b = static_cast<unsigned long long>(__double_as_longlong(d));
+    const unsigned sign = static_cast<unsigned>(b >> 32) & 0x80000000u;
+    const int ex = static_cast<int>((b >> 52) & 0x7ffull) - 896;
+    const unsigned m23 = static_cast<unsigned>((b >> 29) & 0x7fffffull);
+    const unsigned rem = static_cast<unsigned>(b & 0x1fffffffull);
+    const unsigned up = (rem > 0x10000000u) || (rem == 0x10000000u && (m23 & 1u));
+    // exponents 1..254: a carry out of the mantissa lands on the next binade, and out
+    // of binade 254 on the infinity pattern 0x7f800000
+    const unsigned mag = ((static_cast<unsigned>(ex) << 23) | m23) + up;
+    const bool nan = (b & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+    const unsigned big = nan ? 0x7fc00000u : (sign | 0x7f800000u);
+    return __uint_as_float(ex >= 255 ? big : (ex > 0 ? (sign | mag) : sign));
 }
 
 __device__ __forceinline__ float warp_min_f(float v) {
@@ -159,12 +197,16 @@ __device__ __forceinline__ void finalize_clock(phd_clock *clk, double cfl, bool 
 // Finish a grid-wide CFL reduction over n_runs clocks: the last block to arrive
 // finalises every run.  No block waits on another: every block reads the clocks'
 // dt before its arrival is counted (clocks[0].arrive), and only the last arrival
-// writes them.
+// writes them.  The block's minimum reached L2 through an atomic issued by thread 0
+// (block_min_to / block_min_to_f); thread 0 alone fences before counting the arrival
+// (release), so the block's other threads never wait for their own outstanding stores.
+// Per-run minima issued by other threads (the batched path) are fenced where they are
+// issued (atomic_min_fenced).
 __device__ __forceinline__ void finish_cfl_multi(phd_clock *clocks, int n_runs, double cfl, bool advance) {
     __shared__ bool s_last;
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
+        __threadfence();
         const unsigned int prev = atomicAdd(&clocks[0].arrive, 1u);
         s_last = (prev == gridDim.x - 1);
     }
@@ -176,6 +218,13 @@ __device__ __forceinline__ void finish_cfl_multi(phd_clock *clocks, int n_runs, 
         if (threadIdx.x == 0) clocks[0].arrive = 0u;
         __threadfence();
     }
+}
+
+// A per-run CFL candidate merged by a thread other than the block's thread 0: the
+// fence orders it before the block's arrival (finish_cfl_multi).
+__device__ __forceinline__ void atomic_min_fenced(unsigned long long *slot, unsigned long long v) {
+    atomicMin(slot, v);
+    __threadfence();
 }
 
 __device__ __forceinline__ void finish_cfl(phd_clock *clk, double cfl, bool advance) {

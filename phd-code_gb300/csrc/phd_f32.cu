@@ -200,7 +200,16 @@ __global__ void k_prepare_csr32(phd_mesh M, const int32_t *__restrict__ twin, in
 // Same estimator and limiter as cell_gradient_f64 (reconstruction.pyx:620-736) in
 // the relative geometry: with sigma = +1 for pair-i and -1 for pair-j,
 //   d phi/dx_k = 1/V sum_faces [ (A/r) (phi_j - phi_i) c_k + sigma A/2 (phi_j + phi_i) n_k ]
-//   limiter separation  f - (x + dcom) = c + sigma r/2 n - dcom.
+//              = 1/V sum_faces (phi_j - phi_i) w_k + (2 phi_i / V) sum_faces sigma A/2 n_k,
+//   w = (A/r) c + sigma (A/2) n,
+// and the last sum is the cell's closure sum, zero for a closed Voronoi cell (it is
+// FP32 rounding noise of the face geometry here; the FP64 path keeps the reference's
+// form), so the FP32 estimate is sum (phi_j - phi_i) w / V: one difference and two
+// FMAs per face and field, and no cancellation between the two terms.  The neighbour
+// extrema enter the limiter only through phi_max - phi_i and phi_min - phi_i, tracked
+// directly as the extrema of the same differences (fl(x - phi_i) is monotonic in x, so
+// these are the bits of the reference's max - phi_i).  Limiter separation
+//   f - (x + dcom) = t - dcom,  t = c + sigma r/2 n.
 template <int LIMITER>
 __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_params &P, int moving,
                                             const float4 *__restrict__ face_geo,
@@ -226,9 +235,9 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
         e1 = M.nbr_ptr[c + 1];
     }
     const float P0[4] = {pc.x, pc.y, pc.z, pc.w};
-    float mx[4], mn[4], df[4][2];
+    float dmx[4], dmn[4], df[4][2];
 #pragma unroll
-    for (int f = 0; f < 4; f++) { mx[f] = mn[f] = P0[f]; df[f][0] = df[f][1] = 0.f; }
+    for (int f = 0; f < 4; f++) { dmx[f] = dmn[f] = 0.f; df[f][0] = df[f][1] = 0.f; }
     // entries in chunks of CH: all of a chunk's dependent loads are issued before any
     // arithmetic, so their latencies overlap (lanes past the end reload entry e0)
     constexpr int CH = 4;
@@ -255,14 +264,14 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
             const float Pj[4] = {pj[k].x, pj[k].y, pj[k].z, pj[k].w};
             const float a_r = ar[k].x / ar[k].y;
             const float ha = (code[k] < 0 ? -0.5f : 0.5f) * ar[k].x;
+            const float wx = a_r * g[k].z + ha * g[k].x, wy = a_r * g[k].w + ha * g[k].y;
 #pragma unroll
             for (int f = 0; f < 4; f++) {
-                mx[f] = fmaxf(mx[f], Pj[f]);
-                mn[f] = fminf(mn[f], Pj[f]);
-                const float dd = (Pj[f] - P0[f]) * a_r;
-                const float ds = (Pj[f] + P0[f]) * ha;
-                df[f][0] += dd * g[k].z + ds * g[k].x;
-                df[f][1] += dd * g[k].w + ds * g[k].y;
+                const float d = Pj[f] - P0[f];
+                dmx[f] = fmaxf(dmx[f], d);
+                dmn[f] = fminf(dmn[f], d);
+                df[f][0] += d * wx;
+                df[f][1] += d * wy;
             }
         }
     }
@@ -273,27 +282,45 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
         // alpha_f = min over faces of max(psi, 0), psi = (phi_max - phi)/dphi for dphi > 0
         // and (phi_min - phi)/dphi for dphi < 0: the numerators do not depend on the
         // face, so the minimum is reached at the largest |dphi| of each sign -- two
-        // divisions per field instead of one per face and field.
-        float dpos[4] = {0.f, 0.f, 0.f, 0.f}, dneg[4] = {0.f, 0.f, 0.f, 0.f};
-        for (int e = e0; e < e1; e++) {
-            const int code = csr_face[e];
-            const int fid = code < 0 ? ~code : code;
-            const float hs = code < 0 ? -0.5f : 0.5f;
-            const float4 g = face_geo[fid];
-            const float r = face_ar[fid].y;
-            const float sx = g.z + hs * r * g.x - gc.x;
-            const float sy = g.w + hs * r * g.y - gc.y;
+        // divisions per field instead of one per face and field.  dphi = grad . t - grad . dcom,
+        // the second term once per field.
+        float dpos[4], dneg[4], gd[4];
 #pragma unroll
-            for (int f = 0; f < 4; f++) {
-                const float dphi = df[f][0] * sx + df[f][1] * sy;
-                dpos[f] = fmaxf(dpos[f], dphi);
-                dneg[f] = fminf(dneg[f], dphi);
+        for (int f = 0; f < 4; f++) {
+            gd[f] = df[f][0] * gc.x + df[f][1] * gc.y;
+            dpos[f] = dneg[f] = gd[f];          // the offset is taken out after the loop
+        }
+        // the same chunks again (L1 hits), each chunk's loads issued together
+        for (int eb = e0; eb < e1; eb += CH) {
+            int code[CH];
+#pragma unroll
+            for (int k = 0; k < CH; k++) code[k] = csr_face[(eb + k < e1) ? eb + k : e0];
+            float4 g[CH];
+            float r[CH];
+#pragma unroll
+            for (int k = 0; k < CH; k++) {
+                const int fid = code[k] < 0 ? ~code[k] : code[k];
+                g[k] = face_geo[fid];
+                r[k] = face_ar[fid].y;
+            }
+#pragma unroll
+            for (int k = 0; k < CH; k++) {
+                if (eb + k >= e1) break;
+                const float hr = (code[k] < 0 ? -0.5f : 0.5f) * r[k];
+                const float tx = g[k].z + hr * g[k].x, ty = g[k].w + hr * g[k].y;
+#pragma unroll
+                for (int f = 0; f < 4; f++) {
+                    const float dphi = df[f][0] * tx + df[f][1] * ty;
+                    dpos[f] = fmaxf(dpos[f], dphi);
+                    dneg[f] = fminf(dneg[f], dphi);
+                }
             }
         }
 #pragma unroll
         for (int f = 0; f < 4; f++) {
-            if (dpos[f] > 0.f) alpha[f] = fminf(alpha[f], fmaxf((mx[f] - P0[f]) / dpos[f], 0.f));
-            if (dneg[f] < 0.f) alpha[f] = fminf(alpha[f], fmaxf((mn[f] - P0[f]) / dneg[f], 0.f));
+            const float hi = dpos[f] - gd[f], lo = dneg[f] - gd[f];
+            if (hi > 0.f) alpha[f] = fminf(alpha[f], dmx[f] / hi);
+            if (lo < 0.f) alpha[f] = fminf(alpha[f], dmn[f] / lo);
         }
     } else {
         for (int e = e0; e < e1; e++) {
@@ -361,11 +388,15 @@ __global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int mo
 
 // ---- FP32 Riemann solver with the gas constants formed once on the host -------------
 // HLL.get_waves riemann.pyx:375-504 and HLL/HLLC.riemann_solver riemann.pyx:243-373,
-// 521-682 in FP32: the same formulas as hll_family<float> with every quantity that
-// depends only on gamma ((g-1)/(2g), 1/(g-1), (g+1)/(2g), ...) precomputed, and the
-// HLLC left / right star branches merged into one (selects instead of divergence).
+// 521-682 in FP32: the same formulas and branch structure as hll_family<float>, with
+// every quantity that depends only on gamma ((g-1)/(2g), 1/(g-1), (g+1)/2, ...)
+// precomputed, and the divisions and square roots rewritten so that each side needs
+// one reciprocal of its density (shared by its sound speed, its shock speed and the
+// HLLC star flux): the face kernel is bound by its issue rate, and every FP32 division
+// or square root is a multi-function-unit instruction plus fix-ups.  The HLLC left /
+// right star branches are merged into one (selects instead of divergence).
 struct GasC {
-    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1;
+    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1, gp1_half, half_gm1;
     ExGas64 X;                 // the exact solver's FP64 Newton constants
 };
 
@@ -380,39 +411,49 @@ inline GasC gas_consts(double gamma) {
     c.inv_z = 1.f / c.z;
     c.two_gp1 = 2.f / (g + 1.f);
     c.gm1_gp1 = (g - 1.f) / (g + 1.f);
+    c.gp1_half = 0.5f * (g + 1.f);
+    c.half_gm1 = 0.5f * (g - 1.f);
     c.X = ex_gas64(gamma);
     return c;
 }
 
-__device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float dr, float ur, float pr,
-                                            const GasC &C, float &sl, float &sc, float &sr) {
-    float p_star;
-    const float cl = fmaxf(sqrtf((C.g * pl) / dl), 1.0e-10f);
-    const float cr = fmaxf(sqrtf((C.g * pr) / dr), 1.0e-10f);
+// idl, idr: 1/dl, 1/dr.
+__device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float dr, float ur, float pr, float idl,
+                                            float idr, const GasC &C, float &sl, float &sc, float &sr) {
+    // c^2 = g p / d (riemann.pyx:404-405), floored at c = 1e-10 as the reference does
+    const float cl2 = (C.g * pl) * idl, cr2 = (C.g * pr) * idr;
+    const float cl = fmaxf(sqrtf(cl2), 1.0e-10f);
+    const float cr = fmaxf(sqrtf(cr2), 1.0e-10f);
     const float d_avg = 0.5f * (dl + dr);
     const float c_avg = 0.5f * (cl + cr);
-    p_star = fmaxf(0.f, ((0.5f * (pl + pr)) + (((0.5f * (ul - ur)) * d_avg) * c_avg)));
+    float p_star = fmaxf(0.f, ((0.5f * (pl + pr)) + (((0.5f * (ul - ur)) * d_avg) * c_avg)));
     const float p_min = fminf(pl, pr);
     const float p_max = fmaxf(pl, pr);
-    if (((p_max / p_min) < 2.f) && ((p_min < p_star) && (p_star < p_max))) {
+    // p_max / p_min < 2 without the division (dividing by a negative p_min flips it)
+    const bool ratio2 = (p_min > 0.f) ? (p_max < 2.f * p_min) : (p_min < 0.f && p_max > 2.f * p_min);
+    if (ratio2 && ((p_min < p_star) && (p_star < p_max))) {
         // PVRS estimate stands
     } else if (p_star <= p_min) {          // two-rarefaction (TRRS)
+        const float icl = 1.f / cl, icr = 1.f / cr;
         const float plr = __powf(pl / pr, C.z);
-        const float u_star = ((((plr * ul) / cl) + (ur / cr)) + ((2.f * (plr - 1.f)) * C.inv_gm1)) /
-                             ((plr / cl) + (1.f / cr));
-        p_star = (0.5f * pl) * __powf((1.f + ((C.gm1 * (ul - u_star)) / (2.f * cl))), C.inv_z);
-        p_star = p_star + ((0.5f * pr) * __powf((1.f + ((C.gm1 * (u_star - ur)) / (2.f * cr))), C.inv_z));
+        const float u_star = ((((plr * ul) * icl) + (ur * icr)) + ((2.f * (plr - 1.f)) * C.inv_gm1)) /
+                             ((plr * icl) + icr);
+        p_star = (0.5f * pl) * __powf(1.f + (C.half_gm1 * (ul - u_star)) * icl, C.inv_z);
+        p_star = p_star + ((0.5f * pr) * __powf(1.f + (C.half_gm1 * (u_star - ur)) * icr, C.inv_z));
     } else {                               // two-shock (TSRS)
-        const float Al = C.two_gp1 / dl;
-        const float Ar = C.two_gp1 / dr;
-        const float gl = sqrtf(Al / (p_star + pl * C.gm1_gp1));
-        const float gr = sqrtf(Ar / (p_star + pr * C.gm1_gp1));
+        // sqrt(A / (p + B)) with A = 2/((g+1) d) as one reciprocal square root
+        const float gl = rsqrtf((C.gp1_half * dl) * (p_star + pl * C.gm1_gp1));
+        const float gr = rsqrtf((C.gp1_half * dr) * (p_star + pr * C.gm1_gp1));
         p_star = (((gl * pl) + (gr * pr)) - (ur - ul)) / (gl + gr);
     }
-    if (p_star <= pl) sl = ul - cl;
-    else sl = ul - (cl * sqrtf((1.f + (C.gp1_2g * ((p_star / pl) - 1.f)))));
-    if (p_star <= pr) sr = ur + cr;
-    else sr = ur + (cr * sqrtf((1.f + (C.gp1_2g * ((p_star / pr) - 1.f)))));
+    // shock speeds c sqrt(1 + (g+1)/(2g) (p*/p - 1)) = sqrt(c^2 + (g+1)/2 (p* - p) / d);
+    // a floored sound speed (vacuum-like side) keeps the reference's form
+    float ql = cl2 + (C.gp1_half * (p_star - pl)) * idl;
+    float qr = cr2 + (C.gp1_half * (p_star - pr)) * idr;
+    if (__builtin_expect(!(cl2 >= 1.0e-20f), 0)) ql = (cl * cl) * (1.f + (C.gp1_2g * ((p_star / pl) - 1.f)));
+    if (__builtin_expect(!(cr2 >= 1.0e-20f), 0)) qr = (cr * cr) * (1.f + (C.gp1_2g * ((p_star / pr) - 1.f)));
+    sl = (p_star <= pl) ? ul - cl : ul - sqrtf(ql);
+    sr = (p_star <= pr) ? ur + cr : ur + sqrtf(qr);
     sc = (((pr - pl) + ((dl * ul) * (sl - ul))) - ((dr * ur) * (sr - ur))) /
          ((dl * (sl - ul)) - (dr * (sr - ur)));
 }
@@ -420,11 +461,12 @@ __device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float 
 __device__ __forceinline__ void hll_family32(bool hllc, const float *L, const float *R, const float *n,
                                              const float *w, const GasC &C, bool boost, float *f) {
     const float _dl = L[0], _pl = L[3], _dr = R[0], _pr = R[3];
+    const float idl = 1.f / _dl, idr = 1.f / _dr;
     const float vl_sq = L[1] * L[1] + L[2] * L[2], vr_sq = R[1] * R[1] + R[2] * R[2];
     const float Vnl = L[1] * n[0] + L[2] * n[1], Vnr = R[1] * n[0] + R[2] * n[1];
     const float wn = boost ? 0.f : (w[0] * n[0] + w[1] * n[1]);
     float sl, sc, sr;
-    get_waves32(_dl, Vnl, _pl, _dr, Vnr, _pr, C, sl, sc, sr);
+    get_waves32(_dl, Vnl, _pl, _dr, Vnr, _pr, idl, idr, C, sl, sc, sr);
     if (wn <= sl) {
         f[0] = _dl * (Vnl - wn);
         f[3] = ((((0.5f * _dl) * vl_sq) + (_pl * C.inv_gm1)) * (Vnl - wn)) + (_pl * Vnl);
@@ -447,15 +489,17 @@ __device__ __forceinline__ void hll_family32(bool hllc, const float *L, const fl
         } else {                           // star region on the side of the contact
             const bool left = wn <= sc;
             const float d = left ? _dl : _dr, p = left ? _pl : _pr, Vn = left ? Vnl : Vnr, s = left ? sl : sr;
+            const float id = left ? idl : idr;
             const float vsq = left ? vl_sq : vr_sq;
             const float *S = left ? L : R;
-            const float factor_1 = (d * (s - Vn)) / (s - sc);
+            const float a = s - Vn;
+            const float factor_1 = (d * a) / (s - sc);
             const float factor_2 = ((factor_1 * (s - wn)) * (sc - Vn)) + p;
             const float frho = (d * (Vn - s)) + (factor_1 * (s - wn));
             const float e = ((0.5f * d) * vsq) + (p * C.inv_gm1);
             f[0] = frho;
-            f[3] = (((e + p) * Vn) - (s * e)) +
-                   (((s - wn) * factor_1) * ((e / d) + ((sc - Vn) * (sc + (p / (d * (s - Vn)))))));
+            // e/d and p/(d (s - Vn)) with the side's density reciprocal
+            f[3] = (((e + p) * Vn) - (s * e)) + (((s - wn) * factor_1) * ((e * id) + ((sc - Vn) * (sc + (p * id) / a))));
             for (int k = 0; k < 2; k++) f[1 + k] = (frho * S[1 + k]) + (factor_2 * n[k]);
         }
     } else {
@@ -548,12 +592,13 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
     const float4 g = face_geo[m];
     const float2 ar = face_ar[m];
     const float nrm[2] = {g.x, g.y};
+    const float inv_r = 1.f / ar.y;
     const float4 a = prim4[i], b = prim4[j];
     const float pi[4] = {a.x, a.y, a.z, a.w}, pj[4] = {b.x, b.y, b.z, b.w};
     float w[2] = {0.f, 0.f};
     if (moving) {   // Mesh.assign_face_velocities mesh.pyx:462-477: (w_i+w_j)/2 + ((w_i-w_j).c / r) n
         const float2 wi = w2[i], wj = w2[j];
-        const float fac = ((wi.x - wj.x) * g.z + (wi.y - wj.y) * g.w) / ar.y;
+        const float fac = ((wi.x - wj.x) * g.z + (wi.y - wj.y) * g.w) * inv_r;
         w[0] = 0.5f * (wi.x + wj.x) + fac * g.x;
         w[1] = 0.5f * (wi.y + wj.y) + fac * g.y;
     }
@@ -580,8 +625,8 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
         }
         if (P.gizmo) {
             const float smi = sqrtf(six * six + siy * siy), smj = sqrtf(sjx * sjx + sjy * sjy);
+            const float qi = smi * inv_r, qj = smj * inv_r;
 #pragma unroll
-            const float qi = smi / ar.y, qj = smj / ar.y;
             for (int f = 0; f < 4; f++) gizmo_pair32(sl[f], sr[f], pi[f], pj[f], qi, qj, L[f], R[f]);
             if (L[0] < 0.f || L[3] < 0.f) {
 #pragma unroll
@@ -660,7 +705,8 @@ __device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const p
 #pragma unroll
         for (int k = 0; k < CH; k++) {
             if (eb + k >= e1) break;
-            // the face's increment dt*A*F, identical for both of its cells
+            // the face's increment dt*A*F, identical for both of its cells (compensated
+            // sum; packed FP32 pairs measured slower here: more registers, lower occupancy)
             const float inc[4] = {fl[k].x, fl[k].y, fl[k].z, fl[k].w};
 #pragma unroll
             for (int q = 0; q < 4; q++) {
@@ -674,8 +720,14 @@ __device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const p
     // FP64 totals: the only FP64 arithmetic of the step (two adds per field)
     double U[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) U[q] = (cons[(size_t)q * n + c] + widen_f32(hs[q])) + widen_f32(lo[q]);
-    float m = narrow_f64(U[0]), mx = narrow_f64(U[1]), my = narrow_f64(U[2]);
+    for (int q = 0; q < 4; q++)
+        U[q] = (cons[(size_t)q * n + c] + widen_f32_finite(hs[q])) + widen_f32_finite(lo[q]);
+    // a blow-up (a total beyond the FP32 range, an infinite or NaN flux sum, which the
+    // fast widening turns into a magnitude >= 2^128) is reported, and the cell's
+    // primitives become NaN rather than a plausible finite value
+    const bool blown = fp64_beyond_f32(U[0]) || fp64_beyond_f32(U[1]) || fp64_beyond_f32(U[2]) ||
+                       fp64_beyond_f32(U[3]);
+    float m = narrow_f64_finite(U[0]), mx = narrow_f64_finite(U[1]), my = narrow_f64_finite(U[2]);
     if (!(U[0] > 0.0)) set_status32(clk, PHD_STATUS_NEG_MASS);
     if (!(U[3] > 0.0)) set_status32(clk, PHD_STATUS_NEG_ENERGY);
     if (!real) {
@@ -688,12 +740,15 @@ __device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const p
     // IdealGas.primitive_from_conservative equation_state.pyx:106-117 with the
     // internal energy E - m v^2/2 formed in FP64
     const float4 cg = cell_geo[i];
-    const float rho = m * cg.z;
+    float rho = m * cg.z;
     const float rm = 1.f / m;
-    const float vx = mx * rm, vy = my * rm;
+    float vx = mx * rm, vy = my * rm;
     const float ke = 0.5f * (mx * vx + my * vy);
-    const float eint = narrow_f64(U[3] - widen_f32(ke));
-    const float p = (gam - 1.f) * eint * cg.z;
+    float p = (gam - 1.f) * narrow_f64_finite(U[3] - widen_f32_finite(ke)) * cg.z;
+    if (blown || !(fabsf(rho) + fabsf(p) + fabsf(vx) + fabsf(vy) < INFINITY)) {
+        set_status32(clk, PHD_STATUS_NONFINITE);
+        rho = vx = vy = p = __uint_as_float(0x7fc00000u);
+    }
     prim4[i] = make_float4(rho, vx, vy, p);
     if (!real) return INFINITY;
     // riemann.pyx:170-187, R = sqrt(vol/pi) precomputed
@@ -728,9 +783,9 @@ __global__ void __launch_bounds__(512) k_update32(phd_mesh M, phd_params P, cons
             const int r0 = __shfl_sync(0xffffffffu, run, 0);
             if (__all_sync(0xffffffffu, run == r0 || cand == INFINITY)) {
                 const float wm = warp_min_f(cand);
-                if ((threadIdx.x & 31) == 0 && wm < INFINITY) atomicMin(&clocks[r0].dtmin_bits, dbits((double)wm));
+                if ((threadIdx.x & 31) == 0 && wm < INFINITY) atomic_min_fenced(&clocks[r0].dtmin_bits, dbits((double)wm));
             } else if (cand < INFINITY) {
-                atomicMin(&clocks[run].dtmin_bits, dbits((double)cand));
+                atomic_min_fenced(&clocks[run].dtmin_bits, dbits((double)cand));
             }
         }
     }
@@ -742,7 +797,7 @@ __global__ void __launch_bounds__(512) k_update32(phd_mesh M, phd_params P, cons
 // totals U (internal energy formed in FP64) and the CFL candidate riemann.pyx:170-187
 // of a real cell (INFINITY for a ghost); R = sqrt(vol/pi).
 __device__ __forceinline__ float prim32_of(const double (&U)[4], float inv_v, float R, bool real,
-                                           const phd_params &P, float gam, float4 &out) {
+                                           const phd_params &P, float gam, float4 &out, bool &nonfinite) {
     const float m = narrow_f64(U[0]), mx = narrow_f64(U[1]), my = narrow_f64(U[2]);
     const float rm = 1.f / m;
     const float vx = mx * rm, vy = my * rm;
@@ -750,6 +805,7 @@ __device__ __forceinline__ float prim32_of(const double (&U)[4], float inv_v, fl
     const float p = (gam - 1.f) * narrow_f64(U[3] - widen_f32(ke)) * inv_v;
     const float4 pr = make_float4(m * inv_v, vx, vy, p);
     out = pr;
+    if (!(fabsf(pr.x) + fabsf(p) + fabsf(vx) + fabsf(vy) < INFINITY)) nonfinite = true;
     if (!real) return INFINITY;
     const bool boost = (P.solver == PHD_EXACT) ? true : (P.boost != 0);
     const float cs = sqrtf(gam * pr.w / pr.x);
@@ -784,8 +840,10 @@ __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const 
                 inv_v = 1.f / v;
                 R = sqrtf(v * 0.3183098861837907f);
             }
-            cand = prim32_of(U, inv_v, R, M.tag[i] == PHD_REAL_TAG, P, gam, prim4[i]);
+            bool bad = false;
+            cand = prim32_of(U, inv_v, R, M.tag[i] == PHD_REAL_TAG, P, gam, prim4[i], bad);
             if (cell_run) run = cell_run[i];
+            if (bad) set_status32(clocks + run, PHD_STATUS_NONFINITE);
         }
         if (!cell_run) {
             cand_all = fminf(cand_all, cand);
@@ -793,9 +851,9 @@ __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const 
             const int r0 = __shfl_sync(0xffffffffu, run, 0);
             if (__all_sync(0xffffffffu, run == r0 || cand == INFINITY)) {
                 const float wm = warp_min_f(cand);
-                if ((threadIdx.x & 31) == 0 && wm < INFINITY) atomicMin(&clocks[r0].dtmin_bits, dbits((double)wm));
+                if ((threadIdx.x & 31) == 0 && wm < INFINITY) atomic_min_fenced(&clocks[r0].dtmin_bits, dbits((double)wm));
             } else if (cand < INFINITY) {
-                atomicMin(&clocks[run].dtmin_bits, dbits((double)cand));
+                atomic_min_fenced(&clocks[run].dtmin_bits, dbits((double)cand));
             }
         }
     }
@@ -838,7 +896,9 @@ __global__ void __launch_bounds__(512) k_cells_prim32(phd_mesh M, phd_params P, 
                 cons[(size_t)q * n + i] = u;
             }
         }
-        cand_all = fminf(cand_all, prim32_of(U, cg.z, cg.w, real, P, gam, prim4[i]));
+        bool bad = false;
+        cand_all = fminf(cand_all, prim32_of(U, cg.z, cg.w, real, P, gam, prim4[i], bad));
+        if (bad) set_status32(clocks, PHD_STATUS_NONFINITE);
     }
     block_min_to_f(cand_all, &clocks[0].dtmin_bits);
     finish_cfl_multi(clocks, 1, P.cfl, false);

@@ -566,6 +566,7 @@ const char *phd_status_string(int bit) {
         case PHD_STATUS_RIEMANN_NONCONVERGED: return "No convergence in Exact Riemann Solver";
         case PHD_STATUS_BAD_INDEX: return "ERROR: incorrect neighbors!";
         case PHD_STATUS_LEFT_DOMAIN: return "particle left domain in reflective boundary condition!!";
+        case PHD_STATUS_NONFINITE: return "Non-finite primitive state after flux update";
         default: return "unknown status";
     }
 }
