@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--adj-dirs", type=int, default=16, help="adjoint workload: finite-difference directions")
     ap.add_argument("--runs", type=int, default=256)
     ap.add_argument("--no-tune", action="store_true", help="FP32: default launch shapes instead of autotuned")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="leave out the explosion and ensemble summaries of the default line")
     return ap.parse_args()
 
 
@@ -162,12 +164,26 @@ def ncu_traffic():
 
 # Compulsory ("algorithmic") bytes per launch of each FP32 step kernel in this
 # layout: every array touched by the kernel counted once, no re-reads.
+#   k_grad32:   per cell tag 1, list bounds 4, prim4 16 (the neighbours' rows are the
+#               same array), cell_geo 16, flip 1, cellrec written 64, w2 written 8; per
+#               list entry entry_rec 16 + csr_nbr 4
+#   k_face32:   per face pair ids 8, face_geo 16, face_ar 8, flux4 written 16; per cell
+#               its cellrec 64 (gathered from both sides; each row counted once)
+#   k_update32: per cell tag 1, list bounds 4, cell_geo 16, FP64 totals 32 read + 32
+#               written, prim4 written 16; per entry csr_face 4; per face flux4 16
 def algorithmic_bytes(n, F, n_real):
     e = 2 * F
-    grad = n * (16 + 16 + 4 + 1 + 32 + 8) + e * 8 + F * (16 + 8)
-    face = F * (8 + 16 + 8 + 16) + n * (16 + 32 + 16 + 8)
-    update = n * (4 + 1 + 32 + 32 + 8 + 16) + e * 4 + F * 16
+    grad = n * (1 + 4 + 16 + 16 + 1 + 64 + 8) + e * (16 + 4)
+    face = F * (8 + 16 + 8 + 16) + n * 64
+    update = n * (1 + 4 + 16 + 32 + 32 + 16) + e * 4 + F * 16
     return {"k_grad32": grad, "k_face32": face, "k_update32": update}
+
+
+# The layout-independent count of the flux step (compulsory traffic with each array
+# read or written once: 64 B of face record and 8 B of list per face, 204 B per cell),
+# about 140 B per face at F/N = 3.
+def step_bytes_layout_free(n, F):
+    return F * (64 + 8) + n * 204
 
 
 def algorithmic_bytes_f64(n, F, n_real):
@@ -289,7 +305,8 @@ def run_ours(args, rank, world):
         lch, _ = tune(st)
         st.launch = lch
         launch_cfg = {"blocks": [lch.block_grad, lch.block_face, lch.block_update],
-                      "grid_caps": [lch.grid_cap_grad, lch.grid_cap_face, lch.grid_cap_update]}
+                      "grid_caps": [lch.grid_cap_grad, lch.grid_cap_face, lch.grid_cap_update],
+                      "items_per_thread": [lch.items_grad, lch.items_face, lch.items_update]}
     # the timed steps replay a CUDA graph of GRAPH_CHUNK steps (an even count, so the
     # double-buffered conserved state returns to the buffer the graph was recorded
     # on); a remainder of steps % GRAPH_CHUNK runs as direct launches after the replays
@@ -350,10 +367,17 @@ def run_ours(args, rank, world):
     if tr and dom in tr.get("kernels", {}):
         k = tr["kernels"][dom]
         traffic = k["dram_bytes_per_face"] * F if "dram_bytes_per_face" in k else None
+    step_ms = ms_max / args.steps
+    free = step_bytes_layout_free(n, F)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic, "kernel": dom,
                 "peak_source": peak_src, "algorithmic_bytes": algo[dom],
-                "kernel_ms": {k: round(v, 5) for k, v in per.items()}}
+                "kernel_ms": {k: round(v, 5) for k, v in per.items()},
+                "kernel_frac": {k: round(algo[k] / (per[k] * 1e-3) / 1e9 / peak, 4) for k in per},
+                "step": {"bytes_per_face_layout_free": round(free / F, 1), "bytes_layout_free": free,
+                         "bytes_this_layout": sum(algo.values()), "ms": round(step_ms, 5),
+                         "frac_layout_free": round(free / (step_ms * 1e-3) / 1e9 / peak, 4),
+                         "frac_this_layout": round(sum(algo.values()) / (step_ms * 1e-3) / 1e9 / peak, 4)}}
 
     # end to end through the public API with host buffers: the host mesh hands over
     # its face list and cell geometry each step (pinned host -> device), the step runs,
@@ -372,6 +396,11 @@ def run_ours(args, rank, world):
     adjoint = None
     if not args.no_adjoint and rank == 0:
         adjoint = adjoint_cost(dev)
+
+    explosion = ensemble = None
+    if rank == 0 and not args.no_extra:
+        explosion = explosion_summary(dev)
+        ensemble = ensemble_summary(dev)
 
     if rank == 0:
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -395,6 +424,9 @@ def run_ours(args, rank, world):
                                                              args.steps)},
                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "accuracy": accuracy,
                "adjoint": adjoint,
+               "fp64_value": accuracy["fp64_faces_per_s"] if accuracy else None,
+               "fp32_over_fp64": (value / accuracy["fp64_faces_per_s"]) if accuracy else None,
+               "explosion": explosion, "ensemble": ensemble,
                # per step: FP32 k_grad32 (with the generator velocities), k_face32, k_update32;
                # FP64 k_gen_vel, k_face_vel, k_gradients, k_face_flux, k_update_step
                "gpu_launches": (3 if st.precision == "fp32" else 5) * args.steps, "clocks": clocks}
@@ -409,8 +441,14 @@ def fp32_accuracy(st, mesh, prim, n_steps, dev, solver):
     from phd_code_gb300.step import FluxStepper
     ref = FluxStepper(st.dmesh, prim, gamma=5.0 / 3.0, cfl=0.5, solver=solver, moving=True, precision="fp64",
                       device=dev)
-    ref.step(n_steps)
+    ref.step(2)                                   # warm-up (timed below: the FP64 path's own throughput)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
     torch.cuda.synchronize()
+    ev[0].record()
+    ref.step(n_steps - 2)
+    ev[1].record()
+    torch.cuda.synchronize()
+    fp64_ms = ev[0].elapsed_time(ev[1]) / (n_steps - 2)
     nr = mesh.n_real
     r32 = st.prim4[:nr, 0].double()
     r64 = ref.prim[0, :nr]
@@ -425,7 +463,10 @@ def fp32_accuracy(st, mesh, prim, n_steps, dev, solver):
             "energy_drift": abs(float(c[3].sum()) - e0) / e0,
             "fp64_mass_drift": abs(float(c64[0].sum()) - m0) / m0,
             "fp64_energy_drift": abs(float(c64[3].sum()) - e0) / e0,
-            "t_fp32": st.read_clock().t, "t_fp64": ref.read_clock().t}
+            "t_fp32": st.read_clock().t, "t_fp64": ref.read_clock().t,
+            "fp64_ms_per_step": fp64_ms, "fp64_faces_per_s": mesh.n_faces / (fp64_ms * 1e-3),
+            "fp64_timing": "CUDA events around %d directly launched FP64 steps (the reference-parity path), after "
+                           "2 warm-up steps" % (n_steps - 2)}
 
 
 def adjoint_cost(dev, n_side=128, n_steps=200, checkpoint=20, n_dirs=16, h=1e-6, h_small=1e-10, noise=1e-3):
@@ -585,81 +626,89 @@ def run_e2e(args, st, mesh, prim, dev):
                                                            if fp32 else "face list + cell geometry, FP64")}
 
 
-def run_ensemble(args, rank, world):
-    """Batched two-state Riemann ensemble: all runs advance through one launch per stage
-    (CUDA graph per step, autotuned launch shapes) vs the same runs launched one after
-    another; aggregate faces/s."""
+def ensemble_summary(dev, n_runs=256, steps=20, warmup=3, seed=0, seq_steps=10):
+    """The batching workload: n_runs independent two-state Riemann runs (N log-uniform in
+    [1000, 65536]) advanced together, one launch per stage, a CUDA graph of two steps,
+    autotuned launch shapes; against the same runs as separate single-run steppers
+    launched one after another.  Returns the aggregate faces/s of both."""
     import torch
     import __graft_entry__ as ge
     pkg = ge.load_package()
     from phd_code_gb300.autotune import tune
     from phd_code_gb300.ensemble import EnsembleStepper, SequentialEnsemble
-    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
-    torch.cuda.set_device(dev)
-    runs, info = pkg.problems.riemann_ensemble(n_runs=args.runs, seed=rank)
+    runs, info = pkg.problems.riemann_ensemble(n_runs=n_runs, seed=seed)
     ens = EnsembleStepper(runs, device=dev)
     launch, table = tune(ens)
     ens.launch = launch
     ens.capture(2)
-    for _ in range(max(3, args.warmup)):
+    for _ in range(max(3, warmup)):
         ens.replay()
-    steps = args.steps if args.steps % 2 == 0 else args.steps + 1
+    steps = steps if steps % 2 == 0 else steps + 1
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    if world > 1:
-        torch.distributed.barrier()
     torch.cuda.synchronize()
-    sampler = ClockSampler(dev.index or 0)
-    sampler.start()
     e0.record()
     for _ in range(steps // 2):
         ens.replay()
     e1.record()
     torch.cuda.synchronize()
-    clocks = sampler.stop()
-    if world > 1:
-        torch.distributed.barrier()
     ens.check_status()
-    batched, ms = job_rate(ens.faces * steps, e0.elapsed_time(e1), device=dev)
+    ms = e0.elapsed_time(e1)
     seq = SequentialEnsemble(runs, device=dev)
     seq.step(2)
-    q = min(steps, 20)
     torch.cuda.synchronize()
     e0.record()
-    seq.step(q)
+    seq.step(seq_steps)
     e1.record()
     torch.cuda.synchronize()
-    seq_rate = seq.faces * q / (e0.elapsed_time(e1) * 1e-3)
+    seq_rate = seq.faces * seq_steps / (e0.elapsed_time(e1) * 1e-3)
+    batched = ens.faces * steps / (ms * 1e-3)
+    return {"runs": n_runs, "cells": int(ens.dmesh.n_real), "faces": int(ens.faces), "steps": steps,
+            "faces_per_s": batched, "ms_per_step": ms / steps, "sequential_faces_per_s": seq_rate,
+            "sequential_steps": seq_steps, "speedup_vs_sequential": batched / seq_rate,
+            "launch": {"block": [launch.block_grad, launch.block_face, launch.block_update],
+                       "grid_cap": [launch.grid_cap_grad, launch.grid_cap_face, launch.grid_cap_update],
+                       "items_per_thread": [launch.items_grad, launch.items_face, launch.items_update]}}
+
+
+def run_ensemble(args, rank, world):
+    """Batched two-state Riemann ensemble as its own line (one replica per rank)."""
+    import torch
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    r = ensemble_summary(dev, n_runs=args.runs, steps=args.steps, warmup=args.warmup, seed=rank,
+                         seq_steps=min(args.steps, 20))
+    clocks = sampler.stop()
+    batched, ms = job_rate(r["faces"] * r["steps"], r["ms_per_step"] * r["steps"], device=dev)
     if rank == 0:
-        out = {"metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": world, "steps": steps,
-               "warmup": max(3, args.warmup), "ms_per_step": ms / steps, "higher_is_better": True,
+        out = {"metric": METRIC, "value": batched, "unit": UNIT, "n_gpus": world, "steps": r["steps"],
+               "warmup": max(3, args.warmup), "ms_per_step": ms / r["steps"], "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": {"workload": "ensemble of %d two-state Riemann runs, N log-uniform in [1000, 65536], "
                                       "reflective unit boxes, gamma 1.4, FP32+FP64-accumulate HLLC" % args.runs,
-                          "cells": int(ens.dmesh.n_real), "faces": int(ens.faces),
-                          "launch": {"block": [launch.block_grad, launch.block_face, launch.block_update],
-                                     "grid_cap": [launch.grid_cap_grad, launch.grid_cap_face,
-                                                  launch.grid_cap_update]}},
-               "sequential": {"value": seq_rate, "unit": UNIT, "steps": q,
+                          "cells": r["cells"], "faces": r["faces"], "launch": r["launch"]},
+               "sequential": {"value": r["sequential_faces_per_s"], "unit": UNIT, "steps": r["sequential_steps"],
                               "what": "the same runs as separate single-run steppers launched in turn"},
-               "speedup_vs_sequential": batched / seq_rate, "gpu_launches": 3 * steps, "clocks": clocks}
+               "speedup_vs_sequential": r["speedup_vs_sequential"], "gpu_launches": 3 * r["steps"],
+               "clocks": clocks}
         print(json.dumps(out), flush=True)
 
 
-def run_explosion(args, rank, world):
-    """The point-explosion workload: 256x256 jittered periodic box, rho = 1, p = 1e-5,
+def explosion_summary(dev, n_side=256, seed=0, solvers=("hllc", "exact")):
+    """The point-explosion workload: n_side^2 jittered periodic box, rho = 1, p = 1e-5,
     E = 1 deposited within two lattice spacings of the centre, gamma 1.4, run to
-    t = 0.05 (the clock clips the last step onto t_end) with HLLC and with the exact
-    solver, each in FP64 and in FP32 + FP64 accumulation (moving-mesh stage order, mesh
-    held fixed).  Reports each run's faces/s, the FP32 run's L1 density error against
-    the FP64 run (the FP64 path matches the reference to 1e-12, tests/) and both runs'
-    total-energy drift."""
+    t = 0.05 (the clock clips the last step onto t_end) with each solver in FP64 and in
+    FP32 + FP64 accumulation (moving-mesh stage order, mesh held fixed).  Reports each
+    run's faces/s, the FP32 run's L1 density error against the FP64 run (the FP64 path
+    matches the reference to 1e-12, tests/) and both runs' total-energy drift."""
     import torch
     import __graft_entry__ as ge
     pkg = ge.load_package()
     from phd_code_gb300.step import FluxStepper
-    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
-    torch.cuda.set_device(dev)
-    mesh, prim, info = pkg.problems.point_explosion(256, seed=rank)
+    mesh, prim, info = pkg.problems.point_explosion(n_side, seed=seed)
     nr, F = mesh.n_real, mesh.n_faces
     t_end, gamma = info["t_end"], info["gamma"]
 
@@ -683,25 +732,35 @@ def run_explosion(args, rank, world):
         return {"steps": steps, "t": c.t, "faces_per_s": F * steps / (ms * 1e-3),
                 "energy_drift": abs(cons[3].sum() - e0) / abs(e0), "rho": cons[0] / mesh.vol[:nr]}
 
-    sampler = ClockSampler(dev.index or 0)
-    sampler.start()
-    out = {}
-    for solver in ("hllc", "exact"):
+    out = {"workload": "point explosion %dx%d jittered periodic, E = 1, gamma 1.4, to t = 0.05" % (n_side, n_side),
+           "cells": nr, "faces": F}
+    for solver in solvers:
         r64 = run(solver, "fp64", 10)
         r32 = run(solver, "fp32", 25)
         out[solver] = {"fp64": {k: v for k, v in r64.items() if k != "rho"},
                        "fp32": {k: v for k, v in r32.items() if k != "rho"},
                        "l1_density_fp32_vs_fp64": float(np.mean(np.abs(r32["rho"] - r64["rho"]))),
                        "fp32_over_fp64_faces_per_s": r32["faces_per_s"] / r64["faces_per_s"]}
+    return out
+
+
+def run_explosion(args, rank, world):
+    """The point-explosion workload as its own line."""
+    import torch
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", 0)))
+    torch.cuda.set_device(dev)
+    sampler = ClockSampler(dev.index or 0)
+    sampler.start()
+    out = explosion_summary(dev, seed=rank)
     clocks = sampler.stop()
     if rank == 0:
         print(json.dumps({"metric": METRIC, "value": out["hllc"]["fp32"]["faces_per_s"], "unit": UNIT,
                           "n_gpus": world, "steps": out["hllc"]["fp32"]["steps"], "higher_is_better": True,
                           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                          "config": {"workload": "point explosion 256x256 jittered periodic, E = 1, gamma 1.4, "
-                                                 "to t = 0.05", "cells": nr, "faces": F,
+                          "config": {"workload": out["workload"], "cells": out["cells"], "faces": out["faces"],
                                      "mesh": "fixed across steps (face velocities from the moving-mesh stage)"},
-                          "runs": out, "clocks": clocks}), flush=True)
+                          "runs": {k: v for k, v in out.items() if k in ("hllc", "exact")}, "clocks": clocks}),
+              flush=True)
 
 
 def run_moving(args, rank, world):

@@ -206,6 +206,11 @@ int phd_step_f64_taped(const phd_mesh *mesh, const phd_params *par, int32_t movi
  *                   pair-i, ~face id where it is pair-j
  *   csr_nbr  [2F]   the other cell of each listed face
  *   cell_geo [n][4] (dcom_x, dcom_y, 1/vol, sqrt(vol/pi))
+ *   entry_rec [2F][4] per list entry (sigma = +1 where the cell is pair-i, -1 where it is
+ *                   pair-j): (w_x, w_y, t_x, t_y), w = (area/r) c + sigma (area/2) n the
+ *                   gradient weight, t = c + sigma (r/2) n the face centroid minus the
+ *                   generator (r = |x_j - x_i|); the gradient kernel reads its geometry in
+ *                   list order through it (PHD_PREP_RECORDS)
  * twin (optional, [F]): for periodic faces the reference computes twice (once from each
  * side, mesh.pyx:529-544), twin[f] = the kept copy's id for the dropped copy f, else -1;
  * both cells then exchange the same FP32 flux and the totals are conserved exactly. */
@@ -215,6 +220,7 @@ typedef struct phd_geom32 {
     const int32_t *csr_face;
     const int32_t *csr_nbr;
     const float *cell_geo;
+    const float *entry_rec;
 } phd_geom32;
 
 typedef struct phd_geom32_out {
@@ -223,8 +229,10 @@ typedef struct phd_geom32_out {
     int32_t *csr_face;
     int32_t *csr_nbr;
     float *cell_geo;
+    float *entry_rec;           /* may be NULL where no part writes it */
 } phd_geom32_out;
 
+/* All parts (PHD_PREP_ALL, plus PHD_PREP_RECORDS when out->entry_rec is given). */
 int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out,
                     cudaStream_t stream);
 
@@ -241,6 +249,9 @@ int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *o
  * PHD_PREP_LISTS done before it (same call or earlier on the stream); excludes
  * PHD_PREP_CELLS.  The FP32 path then needs no volumes or centroids from the host. */
 #define PHD_PREP_CELLS_FROM_FACES 8
+/* entry_rec from the prepared faces and list codes; needs PHD_PREP_FACES and
+ * PHD_PREP_LISTS done before it (same call or earlier on the stream). */
+#define PHD_PREP_RECORDS 16
 int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out,
                           int32_t parts, cudaStream_t stream);
 
@@ -352,20 +363,28 @@ int phd_prim_f32_batched(const phd_mesh *mesh, const phd_params *par, const doub
 /* One fused step (same order as phd_step_f64): gradients (+ generator velocities when
  * moving) -> per-face states, Riemann flux and deboost (face velocities formed on the
  * fly) -> segmented update into cons_next, FP32 primitives, next dt.
- * prim4 [n][4], grad8 [n][8], w2 [n][2], flux4 [F][4] (FP32; each face's conserved
- * increment dt*A*F, applied with opposite signs to its two cells); cons, cons_next [4][n]
- * (FP64). */
+ * prim4 [n][4], w2 [n][2], flux4 [F][4] (FP32; each face's conserved increment dt*A*F,
+ * applied with opposite signs to its two cells); cons, cons_next [4][n] (FP64);
+ * cellrec [n][16] (FP32, 32-byte aligned) the record the gradient stage writes for the
+ * face stage: the cell's primitives, its limited gradient (d/dx, d/dy of rho, v_x,
+ * v_y, p, the reference's grad[f*dim+k] order), dcom and generator velocity.  With
+ * linear reconstruction or a moving mesh geo->entry_rec, geo->csr_nbr and cellrec are
+ * required. */
 int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par,
-                 int32_t moving, float *prim4, const double *cons, double *cons_next, float *grad8,
+                 int32_t moving, float *prim4, const double *cons, double *cons_next, float *cellrec,
                  float *w2, float *flux4, phd_clock *clk, cudaStream_t stream);
 
 /* Launch shape of the three step kernels (chosen by an autotuner): threads per block
- * (multiple of 32, <= 512; the face kernel <= 384) and a cap on blocks per grid (0: one
- * thread per item; > 0: that many blocks, each looping over items -- a persistent
- * launch). */
+ * (multiple of 32, <= 512; the face kernel <= 384), a cap on blocks per grid (0: enough
+ * blocks for every item; > 0: that many blocks, each looping over items -- a persistent
+ * launch) and items per thread (0 or 1, 2, 4: a block covers block * items consecutive
+ * cells or faces, thread t taking items t, t + block, ...; a warp then handles 32 *
+ * items faces).  The exact solver's face kernel always runs one face per thread.  Every
+ * shape gives the same bits. */
 typedef struct phd_launch {
     int32_t block_grad, block_face, block_update;
     int32_t grid_cap_grad, grid_cap_face, grid_cap_update;
+    int32_t items_grad, items_face, items_update;
 } phd_launch;
 
 /* Batched step: n_runs independent runs concatenated into one mesh (disjoint cell and
@@ -375,7 +394,7 @@ typedef struct phd_launch {
  * bits of a run go to clocks[run] (index errors of the gradient stage to clocks[0]). */
 int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par,
                          int32_t moving, const phd_launch *launch, float *prim4,
-                         const double *cons, double *cons_next, float *grad8, float *w2,
+                         const double *cons, double *cons_next, float *cellrec, float *w2,
                          float *flux4, phd_clock *clocks, int32_t n_runs,
                          const int32_t *cell_run, cudaStream_t stream, cudaEvent_t *marks);
 
@@ -384,7 +403,7 @@ int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_
  * so a caller can time each kernel inside a timed run; marks may be NULL. */
 int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par,
                         int32_t moving, float *prim4, const double *cons, double *cons_next,
-                        float *grad8, float *w2, float *flux4, phd_clock *clk,
+                        float *cellrec, float *w2, float *flux4, phd_clock *clk,
                         cudaStream_t stream, cudaEvent_t *marks);
 
 /* ---- adjoint of one FP64 step ----------------------------------------------------

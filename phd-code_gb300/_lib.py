@@ -18,7 +18,7 @@ STATUS_NEG_MASS, STATUS_NEG_ENERGY, STATUS_RIEMANN_NONCONVERGED, STATUS_BAD_INDE
 STATUS_LEFT_DOMAIN = 16
 STATUS_NONFINITE = 32
 HLL, HLLC, EXACT = 0, 1, 2
-PREP_FACES, PREP_CELLS, PREP_LISTS, PREP_ALL, PREP_CELLS_FROM_FACES = 1, 2, 4, 7, 8
+PREP_FACES, PREP_CELLS, PREP_LISTS, PREP_ALL, PREP_CELLS_FROM_FACES, PREP_RECORDS = 1, 2, 4, 7, 8, 16
 CONSTANT, LINEAR = 0, 1
 LIMITER_AREPO, LIMITER_TESS = 0, 1
 STAGE_SPATIAL, STAGE_TEMPORAL = 1, 2
@@ -58,12 +58,13 @@ class PhdParams(C.Structure):
 
 class PhdGeom32(C.Structure):
     _fields_ = [("face_geo", C.c_void_p), ("face_ar", C.c_void_p), ("csr_face", C.c_void_p),
-                ("csr_nbr", C.c_void_p), ("cell_geo", C.c_void_p)]
+                ("csr_nbr", C.c_void_p), ("cell_geo", C.c_void_p), ("entry_rec", C.c_void_p)]
 
 
 class PhdLaunch(C.Structure):
     _fields_ = [("block_grad", C.c_int32), ("block_face", C.c_int32), ("block_update", C.c_int32),
-                ("grid_cap_grad", C.c_int32), ("grid_cap_face", C.c_int32), ("grid_cap_update", C.c_int32)]
+                ("grid_cap_grad", C.c_int32), ("grid_cap_face", C.c_int32), ("grid_cap_update", C.c_int32),
+                ("items_grad", C.c_int32), ("items_face", C.c_int32), ("items_update", C.c_int32)]
 
 
 class PhdAdjIndex(C.Structure):
@@ -175,6 +176,13 @@ def raise_status(status):
     if status:
         msgs = [m for b, m in STATUS_MESSAGES.items() if status & b]
         raise RuntimeError("; ".join(msgs) or ("status %d" % status))
+
+
+def geom32(tensors, out=False):
+    """PhdGeom32 (or PhdGeom32Out) over the FP32 geometry tensors (face_geo, face_ar,
+    csr_face, csr_nbr, cell_geo, entry_rec)."""
+    cls = PhdGeom32Out if out else PhdGeom32
+    return cls(*(t.data_ptr() for t in tensors))
 
 
 def ptr(t):

@@ -25,6 +25,15 @@ struct NvtxRange {
     NvtxRange &operator=(const NvtxRange &) = delete;
 };
 
+// Programmatic dependent launch (sm_90 and later).  pdl_launch_dependents lets the
+// runtime schedule the next kernel of the stream (launched with programmatic stream
+// serialization) into SM slots this grid frees; pdl_wait blocks until every
+// prerequisite grid has completed and its memory operations are visible.  A kernel
+// reads only data that no earlier kernel of the step writes (the mesh) before pdl_wait.
+// Launched without the attribute, both are no-ops in effect.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Threads per block for a launch over n items with at most max_block threads: halved
 // (down to one warp) while the grid would not cover every SM twice, so small meshes
 // (16k cells) still spread FP64-bound work over the whole GPU.

@@ -14,11 +14,19 @@
 //   face_ar   float2 [F]  (area, r = |x_j - x_i|)
 //   csr_face  int32 [2F]  face id where the cell is pair-i, ~face id where it is pair-j
 //   csr_nbr   int32 [2F]  the other cell of that face
+//   entry_rec float4 [2F] per list entry, sigma = +1 (pair-i) / -1 (pair-j):
+//                         (w_x, w_y, t_x, t_y), w = (A/r) c + sigma (A/2) n (the
+//                         gradient weight), t = c + sigma (r/2) n (face centroid minus
+//                         the generator): the gradient kernel reads its geometry in list
+//                         order instead of gathering two face records per entry
 //   cell_geo  float4 [n]  (dcom_x, dcom_y, 1/vol, R = sqrt(vol/pi))
 //   prim4     float4 [n]  (rho, v_x, v_y, p)
-//   grad8     float4 [2n] (d rho/dx, d rho/dy, d vx/dx, d vx/dy) (d vy/dx, d vy/dy, d p/dx, d p/dy)
-//   w2        float2 [n]  generator velocity
+//   cellrec   float4 [4n] what the face kernel needs of a cell, 64 B (two 256-bit
+//                         loads): prim4 | d/dx, d/dy of rho, v_x | of v_y, p |
+//                         (dcom_x, dcom_y, w_x, w_y); written by the gradient kernel
+//   w2        float2 [n]  generator velocity (the host re-mesh reads it)
 //   flux4     float4 [F]  dt*A*F: the face's conserved increment (mass, mom_x, mom_y, energy)
+#include <utility>
 #include "phd_common.cuh"
 #include "phd_physics.cuh"
 
@@ -126,10 +134,26 @@ __global__ void k_prepare_cells32(phd_mesh M, float4 *__restrict__ cell_geo) {
 // with f - x = c + r n / 2 from pair-i and c - r n / 2 from pair-j.  Ghost rows take
 // their image's values (dcom unflipped, as the ghost copies do).  FP32 throughout: the
 // relative vectors have no cancellation left.
+// The gradient record of one list entry (see entry_rec): minus = the cell is pair-j.
+// The roundings are spelled out (IEEE quotient, explicit FMAs) so every kernel that
+// forms a record gets the same bits (the full and compact hand-overs form them in
+// different kernels).
+__device__ __forceinline__ float4 entry_record(float4 g, float2 ar, bool minus) {
+    const float a_r = __fdiv_rn(ar.x, ar.y);
+    const float ha = (minus ? -0.5f : 0.5f) * ar.x;
+    const float hr = (minus ? -0.5f : 0.5f) * ar.y;
+    return make_float4(__fmaf_rn(a_r, g.z, __fmul_rn(ha, g.x)), __fmaf_rn(a_r, g.w, __fmul_rn(ha, g.y)),
+                       __fmaf_rn(hr, g.x, g.z), __fmaf_rn(hr, g.y, g.w));
+}
+
+// entry_rec, when given, receives the gradient records of a real cell's list entries
+// (a ghost's gradient is its image's, formed from the image's entries).
 __device__ __forceinline__ float4 cell_geo_of(const phd_mesh &M, int i, const float4 *__restrict__ face_geo,
                                               const float2 *__restrict__ face_ar,
-                                              const int32_t *__restrict__ csr_face) {
-    const int c = (M.tag[i] == PHD_REAL_TAG) ? i : M.map[i];
+                                              const int32_t *__restrict__ csr_face,
+                                              float4 *__restrict__ entry_rec = nullptr) {
+    const bool real = M.tag[i] == PHD_REAL_TAG;
+    const int c = real ? i : M.map[i];
     float vol = 0.f, sx = 0.f, sy = 0.f;
     if (c >= 0 && c < M.n_cells) {
         for (int e = M.nbr_ptr[c]; e < M.nbr_ptr[c + 1]; e++) {
@@ -142,10 +166,26 @@ __device__ __forceinline__ float4 cell_geo_of(const phd_mesh &M, int i, const fl
             vol += w;
             sx += w * (g.z + hr * g.x);
             sy += w * (g.w + hr * g.y);
+            if (entry_rec && real) entry_rec[e] = entry_record(g, ar, code < 0);
         }
     }
     const float inv = vol > 0.f ? 1.f / vol : 0.f;
     return make_float4((2.f / 3.f) * sx * inv, (2.f / 3.f) * sy * inv, inv, sqrtf(vol * 0.3183098861837907f));
+}
+
+// entry_rec of every real cell's list from the prepared faces and list codes (a
+// ghost's gradient is its image's, formed from the image's entries).
+__global__ void k_entry_rec32(phd_mesh M, const float4 *__restrict__ face_geo, const float2 *__restrict__ face_ar,
+                              const int32_t *__restrict__ csr_face, float4 *__restrict__ entry_rec) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M.n_cells || M.tag[c] != PHD_REAL_TAG) return;
+    const int F = M.n_faces;
+    for (int e = M.nbr_ptr[c]; e < M.nbr_ptr[c + 1]; e++) {
+        const int code = csr_face[e];
+        const int fid = code < 0 ? ~code : code;
+        if (fid < 0 || fid >= F) { entry_rec[e] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
+        entry_rec[e] = entry_record(face_geo[fid], face_ar[fid], code < 0);
+    }
 }
 
 __global__ void k_cells_from_faces32(phd_mesh M, const float4 *__restrict__ face_geo,
@@ -210,21 +250,43 @@ __global__ void k_prepare_csr32(phd_mesh M, const int32_t *__restrict__ twin, in
 // directly as the extrema of the same differences (fl(x - phi_i) is monotonic in x, so
 // these are the bits of the reference's max - phi_i).  Limiter separation
 //   f - (x + dcom) = t - dcom,  t = c + sigma r/2 n.
+// w and t of every list entry come precomputed in list order (entry_rec), so the only
+// gather left is the neighbour's primitive row.
+// The mesh rows of a cell that no kernel of the step writes (its tag, list bounds and
+// cell geometry), issued together at the start of the cell.  (Loading the next cell's
+// rows during the current one measured about 1 us slower: more live registers.)
+struct GradHead {
+    int real, e0, e1;
+    float4 gc;
+};
+
+__device__ __forceinline__ GradHead grad_head(int i, const phd_mesh &M, const float4 *__restrict__ cell_geo) {
+    GradHead h;
+    h.real = 0;
+    h.e0 = h.e1 = 0;
+    h.gc = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < M.n_cells) {
+        h.real = M.tag[i] == PHD_REAL_TAG;
+        h.e0 = M.nbr_ptr[i];
+        h.e1 = M.nbr_ptr[i + 1];
+        h.gc = cell_geo[i];
+    }
+    return h;
+}
+
 template <int LIMITER>
-__device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_params &P, int moving,
-                                            const float4 *__restrict__ face_geo,
-                                            const float2 *__restrict__ face_ar,
-                                            const int32_t *__restrict__ csr_face,
+__device__ __forceinline__ void grad32_cell(int i, const GradHead &H, const phd_mesh &M, const phd_params &P,
+                                            int moving, const float4 *__restrict__ entry_rec,
                                             const int32_t *__restrict__ csr_nbr,
                                             const float4 *__restrict__ cell_geo,
-                                            const float4 *__restrict__ prim4, float4 *__restrict__ grad8,
+                                            const float4 *__restrict__ prim4, float4 *__restrict__ cellrec,
                                             float2 *__restrict__ w2, phd_clock *clk) {
-    // the cell's own row is loaded before its tag is known: for a real cell it is the
-    // row the gradient needs; a ghost reloads its twin's
-    const bool real = M.tag[i] == PHD_REAL_TAG;
+    // the cell's own rows were loaded before its tag was known: for a real cell they are
+    // the rows the gradient needs; a ghost reloads its twin's
+    const bool real = H.real;
     float4 pc = prim4[i];
-    float4 gc = cell_geo[i];
-    int e0 = M.nbr_ptr[i], e1 = M.nbr_ptr[i + 1];
+    float4 gc = H.gc;
+    int e0 = H.e0, e1 = H.e1;
     int c = i;
     if (!real) {
         c = M.map[i];
@@ -238,40 +300,32 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
     float dmx[4], dmn[4], df[4][2];
 #pragma unroll
     for (int f = 0; f < 4; f++) { dmx[f] = dmn[f] = 0.f; df[f][0] = df[f][1] = 0.f; }
-    // entries in chunks of CH: all of a chunk's dependent loads are issued before any
-    // arithmetic, so their latencies overlap (lanes past the end reload entry e0)
+    // entries in chunks of CH: all of a chunk's loads are issued before any arithmetic,
+    // so their latencies overlap (lanes past the end reload entry e0)
     constexpr int CH = 4;
     for (int eb = e0; eb < e1; eb += CH) {
-        int code[CH], nb[CH];
+        int nb[CH];
+        float4 rw[CH];
 #pragma unroll
         for (int k = 0; k < CH; k++) {
             const int e = (eb + k < e1) ? eb + k : e0;
-            code[k] = csr_face[e];
             nb[k] = csr_nbr[e];
+            rw[k] = entry_rec[e];
         }
-        float4 g[CH], pj[CH];
-        float2 ar[CH];
+        float4 pj[CH];
 #pragma unroll
-        for (int k = 0; k < CH; k++) {
-            const int fid = code[k] < 0 ? ~code[k] : code[k];
-            g[k] = face_geo[fid];
-            ar[k] = face_ar[fid];
-            pj[k] = prim4[nb[k]];
-        }
+        for (int k = 0; k < CH; k++) pj[k] = prim4[nb[k]];
 #pragma unroll
         for (int k = 0; k < CH; k++) {
             if (eb + k >= e1) break;
             const float Pj[4] = {pj[k].x, pj[k].y, pj[k].z, pj[k].w};
-            const float a_r = ar[k].x / ar[k].y;
-            const float ha = (code[k] < 0 ? -0.5f : 0.5f) * ar[k].x;
-            const float wx = a_r * g[k].z + ha * g[k].x, wy = a_r * g[k].w + ha * g[k].y;
 #pragma unroll
             for (int f = 0; f < 4; f++) {
                 const float d = Pj[f] - P0[f];
                 dmx[f] = fmaxf(dmx[f], d);
                 dmn[f] = fminf(dmn[f], d);
-                df[f][0] += d * wx;
-                df[f][1] += d * wy;
+                df[f][0] += d * rw[k].x;
+                df[f][1] += d * rw[k].y;
             }
         }
     }
@@ -282,35 +336,25 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
         // alpha_f = min over faces of max(psi, 0), psi = (phi_max - phi)/dphi for dphi > 0
         // and (phi_min - phi)/dphi for dphi < 0: the numerators do not depend on the
         // face, so the minimum is reached at the largest |dphi| of each sign -- two
-        // divisions per field instead of one per face and field.  dphi = grad . t - grad . dcom,
-        // the second term once per field.
+        // divisions per field instead of one per face and field.  dphi = grad . t -
+        // grad . dcom, the second term once per field.
         float dpos[4], dneg[4], gd[4];
 #pragma unroll
         for (int f = 0; f < 4; f++) {
             gd[f] = df[f][0] * gc.x + df[f][1] * gc.y;
             dpos[f] = dneg[f] = gd[f];          // the offset is taken out after the loop
         }
-        // the same chunks again (L1 hits), each chunk's loads issued together
+        // the same entries again (L1 hits), each chunk's loads issued together
         for (int eb = e0; eb < e1; eb += CH) {
-            int code[CH];
+            float4 rt[CH];
 #pragma unroll
-            for (int k = 0; k < CH; k++) code[k] = csr_face[(eb + k < e1) ? eb + k : e0];
-            float4 g[CH];
-            float r[CH];
-#pragma unroll
-            for (int k = 0; k < CH; k++) {
-                const int fid = code[k] < 0 ? ~code[k] : code[k];
-                g[k] = face_geo[fid];
-                r[k] = face_ar[fid].y;
-            }
+            for (int k = 0; k < CH; k++) rt[k] = entry_rec[(eb + k < e1) ? eb + k : e0];
 #pragma unroll
             for (int k = 0; k < CH; k++) {
                 if (eb + k >= e1) break;
-                const float hr = (code[k] < 0 ? -0.5f : 0.5f) * r[k];
-                const float tx = g[k].z + hr * g[k].x, ty = g[k].w + hr * g[k].y;
 #pragma unroll
                 for (int f = 0; f < 4; f++) {
-                    const float dphi = df[f][0] * tx + df[f][1] * ty;
+                    const float dphi = df[f][0] * rt[k].z + df[f][1] * rt[k].w;
                     dpos[f] = fmaxf(dpos[f], dphi);
                     dneg[f] = fminf(dneg[f], dphi);
                 }
@@ -324,13 +368,8 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
         }
     } else {
         for (int e = e0; e < e1; e++) {
-            const int code = csr_face[e];
-            const int fid = code < 0 ? ~code : code;
-            const float hs = code < 0 ? -0.5f : 0.5f;
-            const float4 g = face_geo[fid];
-            const float r = face_ar[fid].y;
-            const float sx = g.z + hs * r * g.x - gc.x;
-            const float sy = g.w + hs * r * g.y - gc.y;
+            const float4 rt = entry_rec[e];
+            const float sx = rt.z - gc.x, sy = rt.w - gc.y;
             const float4 pj = prim4[csr_nbr[e]];
             const float Pj[4] = {pj.x, pj.y, pj.z, pj.w};
 #pragma unroll
@@ -348,13 +387,14 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
     const int fl = M.flip[i];
     if (fl & 1) gv[2] = -gv[2];        // d vx / dx
     if (fl & 2) gv[5] = -gv[5];        // d vy / dy
-    grad8[2 * (size_t)i] = make_float4(gv[0], gv[1], gv[2], gv[3]);
-    grad8[2 * (size_t)i + 1] = make_float4(gv[4], gv[5], gv[6], gv[7]);
 
+    // the cell's own row (a ghost's, not its image's) for the face kernel
+    const float4 p = (i == c) ? pc : prim4[i];
+    const float4 gi = (i == c) ? gc : cell_geo[i];
+    float wx = 0.f, wy = 0.f;
     if (moving) {   // Mesh.assign_generator_velocities mesh.pyx:397-426, own (ghost) cell data
-        const float4 p = (i == c) ? pc : prim4[i];
-        const float4 gi = (i == c) ? gc : cell_geo[i];
-        float wx = p.y, wy = p.z;
+        wx = p.y;
+        wy = p.z;
         if (P.regularize) {
             const float cs = sqrtf(narrow_f64(P.gamma) * p.w / p.x);
             const float d = sqrtf(gi.x * gi.x + gi.y * gi.y);
@@ -371,19 +411,34 @@ __device__ __forceinline__ void grad32_cell(int i, const phd_mesh &M, const phd_
         }
         w2[i] = make_float2(wx, wy);
     }
+    float4 *rec = cellrec + 4 * (size_t)i;
+    rec[0] = p;
+    rec[1] = make_float4(gv[0], gv[1], gv[2], gv[3]);
+    rec[2] = make_float4(gv[4], gv[5], gv[6], gv[7]);
+    rec[3] = make_float4(gi.x, gi.y, wx, wy);
 }
 
-template <int LIMITER>
+// ITEMS cells per thread: a block covers blockDim * ITEMS consecutive cells, thread t
+// taking cells t, t + blockDim, ... of each tile (the autotuner picks 1, 2 or 4).
+template <int LIMITER, int ITEMS>
 __global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int moving,
-                                                const float4 *__restrict__ face_geo,
-                                                const float2 *__restrict__ face_ar,
-                                                const int32_t *__restrict__ csr_face,
+                                                const float4 *__restrict__ entry_rec,
                                                 const int32_t *__restrict__ csr_nbr,
                                                 const float4 *__restrict__ cell_geo,
-                                                const float4 *__restrict__ prim4, float4 *__restrict__ grad8,
+                                                const float4 *__restrict__ prim4, float4 *__restrict__ cellrec,
                                                 float2 *__restrict__ w2, phd_clock *clk) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < M.n_cells; i += gridDim.x * blockDim.x)
-        grad32_cell<LIMITER>(i, M, P, moving, face_geo, face_ar, csr_face, csr_nbr, cell_geo, prim4, grad8, w2, clk);
+    pdl_launch_dependents();
+    const int tile = blockDim.x * ITEMS;
+    pdl_wait();                                  // prim4: written by the previous step's update
+    for (int base = blockIdx.x * tile; base < M.n_cells; base += gridDim.x * tile) {
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const int i = base + k * blockDim.x + threadIdx.x;
+            if (i < M.n_cells)
+                grad32_cell<LIMITER>(i, grad_head(i, M, cell_geo), M, P, moving, entry_rec, csr_nbr, cell_geo, prim4,
+                                     cellrec, w2, clk);
+        }
+    }
 }
 
 // ---- FP32 Riemann solver with the gas constants formed once on the host -------------
@@ -573,45 +628,88 @@ __device__ __forceinline__ void gizmo_pair32(float sl, float sr, float ci, float
     }
 }
 
+// 64 bytes of a cell record in two 256-bit loads through the read-only path (the
+// record is not written while the face kernel runs).
+__device__ __forceinline__ void load_cellrec(const float4 *__restrict__ p, float4 &r0, float4 &r1, float4 &r2,
+                                             float4 &r3) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r0.x), "=f"(r0.y), "=f"(r0.z), "=f"(r0.w), "=f"(r1.x), "=f"(r1.y), "=f"(r1.z), "=f"(r1.w)
+        : "l"(p));
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(r2.x), "=f"(r2.y), "=f"(r2.z), "=f"(r2.w), "=f"(r3.x), "=f"(r3.y), "=f"(r3.z), "=f"(r3.w)
+        : "l"(p + 2));
+}
+
+// One face.  Linear reconstruction reads both cells' records (cellrec: primitives,
+// limited gradient, centre offset, generator velocity); constant reconstruction reads
+// the primitive rows (and the generator velocities when moving).
+// A face's mesh record (pair ids and FP32 geometry).
+struct FaceHead {
+    int i, j;
+    float4 g;
+    float2 ar;
+};
+
+__device__ __forceinline__ FaceHead face_head(int m, const phd_mesh &M, const float4 *__restrict__ face_geo,
+                                              const float2 *__restrict__ face_ar) {
+    FaceHead h;
+    h.i = h.j = -1;
+    h.g = make_float4(0.f, 0.f, 0.f, 0.f);
+    h.ar = make_float2(0.f, 0.f);
+    if (m < M.n_faces) {
+        h.i = M.pair_i[m];
+        h.j = M.pair_j[m];
+        h.g = face_geo[m];
+        h.ar = face_ar[m];
+    }
+    return h;
+}
+
 template <int SOLVER, bool LINEAR>
-__device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_params &P, int moving,
-                                            const float4 *__restrict__ face_geo,
-                                            const float2 *__restrict__ face_ar,
-                                            const float4 *__restrict__ cell_geo,
-                                            const float4 *__restrict__ prim4,
-                                            const float4 *__restrict__ grad8, const float2 *__restrict__ w2,
+__device__ __forceinline__ void face32_face(int m, const FaceHead &H, const phd_mesh &M, const phd_params &P,
+                                            int moving, const float4 *__restrict__ prim4,
+                                            const float4 *__restrict__ cellrec, const float2 *__restrict__ w2,
                                             float4 *__restrict__ flux4, phd_clock *clocks,
                                             const int32_t *__restrict__ cell_run, const GasC &GC) {
-    const int i = M.pair_i[m], j = M.pair_j[m];
+    const int i = H.i, j = H.j;
     if (i < 0 || i >= M.n_cells || j < 0 || j >= M.n_cells) { set_status32(clocks, PHD_STATUS_BAD_INDEX); return; }
     phd_clock *clk = cell_run ? clocks + cell_run[i] : clocks;
     const bool boost = (SOLVER == PHD_EXACT) ? true : (P.boost != 0);
     const float gamma = GC.g;
     const float dtf = narrow_f64(clk->dt);
     const float dt_half = 0.5f * dtf;
-    const float4 g = face_geo[m];
-    const float2 ar = face_ar[m];
+    const float4 g = H.g;
+    const float2 ar = H.ar;
     const float nrm[2] = {g.x, g.y};
     const float inv_r = 1.f / ar.y;
-    const float4 a = prim4[i], b = prim4[j];
+    float4 a, b, gi0, gi1, gj0, gj1;
+    float4 ci = make_float4(0.f, 0.f, 0.f, 0.f), cj = ci;     // (dcom_x, dcom_y, w_x, w_y)
+    if (LINEAR) {
+        load_cellrec(cellrec + 4 * (size_t)i, a, gi0, gi1, ci);
+        load_cellrec(cellrec + 4 * (size_t)j, b, gj0, gj1, cj);
+    } else {
+        a = prim4[i];
+        b = prim4[j];
+        if (moving) {
+            const float2 wi = w2[i], wj = w2[j];
+            ci = make_float4(0.f, 0.f, wi.x, wi.y);
+            cj = make_float4(0.f, 0.f, wj.x, wj.y);
+        }
+    }
     const float pi[4] = {a.x, a.y, a.z, a.w}, pj[4] = {b.x, b.y, b.z, b.w};
     float w[2] = {0.f, 0.f};
     if (moving) {   // Mesh.assign_face_velocities mesh.pyx:462-477: (w_i+w_j)/2 + ((w_i-w_j).c / r) n
-        const float2 wi = w2[i], wj = w2[j];
-        const float fac = ((wi.x - wj.x) * g.z + (wi.y - wj.y) * g.w) * inv_r;
-        w[0] = 0.5f * (wi.x + wj.x) + fac * g.x;
-        w[1] = 0.5f * (wi.y + wj.y) + fac * g.y;
+        const float fac = ((ci.z - cj.z) * g.z + (ci.w - cj.w) * g.w) * inv_r;
+        w[0] = 0.5f * (ci.z + cj.z) + fac * g.x;
+        w[1] = 0.5f * (ci.w + cj.w) + fac * g.y;
     }
     float L[4], R[4];
 #pragma unroll
     for (int f = 0; f < 4; f++) { L[f] = pi[f]; R[f] = pj[f]; }
     if (boost) { L[1] -= w[0]; L[2] -= w[1]; R[1] -= w[0]; R[2] -= w[1]; }
     if (LINEAR) {
-        const float4 gi0 = grad8[2 * (size_t)i], gi1 = grad8[2 * (size_t)i + 1];
-        const float4 gj0 = grad8[2 * (size_t)j], gj1 = grad8[2 * (size_t)j + 1];
         const float gi[8] = {gi0.x, gi0.y, gi0.z, gi0.w, gi1.x, gi1.y, gi1.z, gi1.w};
         const float gj[8] = {gj0.x, gj0.y, gj0.z, gj0.w, gj1.x, gj1.y, gj1.z, gj1.w};
-        const float4 ci = cell_geo[i], cj = cell_geo[j];
         const float hr = 0.5f * ar.y;
         const float six = g.z + hr * g.x - ci.x, siy = g.w + hr * g.y - ci.y;   // f - (x_i + dcom_i)
         const float sjx = g.z - hr * g.x - cj.x, sjy = g.w - hr * g.y - cj.y;   // f - (x_j + dcom_j)
@@ -657,18 +755,26 @@ __device__ __forceinline__ void face32_face(int m, const phd_mesh &M, const phd_
 // per SM as its minimum (118-138 registers, no spills; measured 4% faster).
 constexpr int FACE_MAX_BLOCK = 384;
 
-template <int SOLVER, bool LINEAR>
+template <int SOLVER, bool LINEAR, int ITEMS>
 __global__ void __launch_bounds__(FACE_MAX_BLOCK, SOLVER == PHD_EXACT ? 1 : 3) k_face32(phd_mesh M, phd_params P, int moving,
                                                 const float4 *__restrict__ face_geo,
                                                 const float2 *__restrict__ face_ar,
-                                                const float4 *__restrict__ cell_geo,
                                                 const float4 *__restrict__ prim4,
-                                                const float4 *__restrict__ grad8, const float2 *__restrict__ w2,
+                                                const float4 *__restrict__ cellrec, const float2 *__restrict__ w2,
                                                 float4 *__restrict__ flux4, phd_clock *clocks,
                                                 const int32_t *__restrict__ cell_run, const __grid_constant__ GasC GC) {
-    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < M.n_faces; m += gridDim.x * blockDim.x)
-        face32_face<SOLVER, LINEAR>(m, M, P, moving, face_geo, face_ar, cell_geo, prim4, grad8, w2, flux4, clocks,
-                                    cell_run, GC);
+    pdl_launch_dependents();
+    const int tile = blockDim.x * ITEMS;
+    pdl_wait();                                  // cellrec / prim4, w2 and the clock: earlier kernels'
+    for (int base = blockIdx.x * tile; base < M.n_faces; base += gridDim.x * tile) {
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const int m = base + k * blockDim.x + threadIdx.x;
+            if (m < M.n_faces)
+                face32_face<SOLVER, LINEAR>(m, face_head(m, M, face_geo, face_ar), M, P, moving, prim4, cellrec, w2,
+                                            flux4, clocks, cell_run, GC);
+        }
+    }
 }
 
 // ---- segmented update, primitive recovery and CFL -----------------------------------
@@ -680,7 +786,24 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 
 // One cell of the update: segmented sum, FP64 totals, primitives; returns the CFL
 // candidate (INFINITY for ghosts) and the cell's run.
-__device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const phd_params &P,
+// A cell's mesh rows for the update (tag and list bounds).
+struct UpdHead {
+    int real, e0, e1;
+};
+
+__device__ __forceinline__ UpdHead upd_head(int i, const phd_mesh &M) {
+    UpdHead h;
+    h.real = 0;
+    h.e0 = h.e1 = 0;
+    if (i < M.n_cells) {
+        h.real = M.tag[i] == PHD_REAL_TAG;
+        h.e0 = M.nbr_ptr[i];
+        h.e1 = M.nbr_ptr[i + 1];
+    }
+    return h;
+}
+
+__device__ __forceinline__ float update32_cell(int i, const UpdHead &H, const phd_mesh &M, const phd_params &P,
                                                const int32_t *__restrict__ csr_face,
                                                const float4 *__restrict__ flux4,
                                                const float4 *__restrict__ cell_geo,
@@ -689,11 +812,17 @@ __device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const p
                                                const int32_t *__restrict__ cell_run, float gam) {
     const int n = M.n_cells;
     phd_clock *clk = cell_run ? clocks + cell_run[i] : clocks;
-    const bool real = M.tag[i] == PHD_REAL_TAG;
+    // the cell's own list bounds were loaded before its tag was known (a real cell's are
+    // the ones it needs); a ghost reloads its image's
+    const bool real = H.real;
+    int e0 = H.e0, e1 = H.e1;
     const int c = real ? i : M.map[i];
     if (c < 0 || c >= n) { set_status32(clk, PHD_STATUS_BAD_INDEX); return INFINITY; }
+    if (!real) {
+        e0 = M.nbr_ptr[c];
+        e1 = M.nbr_ptr[c + 1];
+    }
     float hs[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
-    const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
     constexpr int CH = 8;          // measured best for this kernel (CH = 1, 2, 4, 8 tried)
     for (int eb = e0; eb < e1; eb += CH) {
         int code[CH];
@@ -757,35 +886,43 @@ __device__ __forceinline__ float update32_cell(int i, const phd_mesh &M, const p
     return cg.w / (boost ? cs : cs + sqrtf(vx * vx + vy * vy));
 }
 
+template <int ITEMS>
 __global__ void __launch_bounds__(512) k_update32(phd_mesh M, phd_params P, const int32_t *__restrict__ csr_face,
                                                   const float4 *__restrict__ flux4, const float4 *__restrict__ cell_geo,
                                                   const double *__restrict__ cons, double *__restrict__ cons_next,
                                                   float4 *__restrict__ prim4, phd_clock *clocks,
                                                   const int32_t *__restrict__ cell_run, int n_runs) {
+    pdl_launch_dependents();
     const int n = M.n_cells;
     const float gam = narrow_f64(P.gamma);
-    const int stride = gridDim.x * blockDim.x;
+    const int tile = blockDim.x * ITEMS;
+    const int stride = gridDim.x * tile;
     const int n_iter = (n + stride - 1) / stride;     // uniform trip count: all lanes reach the shuffles
     float cand_all = INFINITY;
+    pdl_wait();                                       // flux4: the face kernel's; the clocks
     for (int it = 0; it < n_iter; it++) {
-        const int i = blockIdx.x * blockDim.x + threadIdx.x + it * stride;
-        float cand = INFINITY;
-        int run = 0;
-        if (i < n) {
-            cand = update32_cell(i, M, P, csr_face, flux4, cell_geo, cons, cons_next, prim4, clocks, cell_run,
-                                 gam);
-            if (cell_run) run = cell_run[i];
-        }
-        if (!cell_run) {
-            cand_all = fminf(cand_all, cand);
-        } else {
-            // per-run minimum: one atomic per warp when the warp lies in one run
-            const int r0 = __shfl_sync(0xffffffffu, run, 0);
-            if (__all_sync(0xffffffffu, run == r0 || cand == INFINITY)) {
-                const float wm = warp_min_f(cand);
-                if ((threadIdx.x & 31) == 0 && wm < INFINITY) atomic_min_fenced(&clocks[r0].dtmin_bits, dbits((double)wm));
-            } else if (cand < INFINITY) {
-                atomic_min_fenced(&clocks[run].dtmin_bits, dbits((double)cand));
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            const int i = blockIdx.x * tile + it * stride + k * blockDim.x + threadIdx.x;
+            float cand = INFINITY;
+            int run = 0;
+            if (i < n) {
+                cand = update32_cell(i, upd_head(i, M), M, P, csr_face, flux4, cell_geo, cons, cons_next, prim4,
+                                     clocks, cell_run, gam);
+                if (cell_run) run = cell_run[i];
+            }
+            if (!cell_run) {
+                cand_all = fminf(cand_all, cand);
+            } else {
+                // per-run minimum: one atomic per warp when the warp lies in one run
+                const int r0 = __shfl_sync(0xffffffffu, run, 0);
+                if (__all_sync(0xffffffffu, run == r0 || cand == INFINITY)) {
+                    const float wm = warp_min_f(cand);
+                    if ((threadIdx.x & 31) == 0 && wm < INFINITY)
+                        atomic_min_fenced(&clocks[r0].dtmin_bits, dbits((double)wm));
+                } else if (cand < INFINITY) {
+                    atomic_min_fenced(&clocks[run].dtmin_bits, dbits((double)cand));
+                }
             }
         }
     }
@@ -862,12 +999,14 @@ __global__ void __launch_bounds__(512) k_prim32(phd_mesh M, phd_params P, const 
 }
 
 // The tail of a mesh hand-over in one pass per cell: the cell geometry from the faces
-// (k_cells_from_faces32), a ghost's FP64 totals from its image with the momentum
+// (k_cells_from_faces32) with the real cells' gradient records (k_entry_rec32) from the
+// same loads, a ghost's FP64 totals from its image with the momentum
 // flipped across reflective walls (k_ghost_cons), the primitives and the CFL step
 // (k_prim32) -- the same expressions as the three kernels, so the same bits.
 __global__ void __launch_bounds__(512) k_cells_prim32(phd_mesh M, phd_params P, const float4 *__restrict__ face_geo,
                                                       const float2 *__restrict__ face_ar,
                                                       const int32_t *__restrict__ csr_face,
+                                                      float4 *__restrict__ entry_rec,
                                                       float4 *__restrict__ cell_geo, double *__restrict__ cons,
                                                       float4 *__restrict__ prim4, phd_clock *clocks) {
     const int n = M.n_cells;
@@ -878,7 +1017,7 @@ __global__ void __launch_bounds__(512) k_cells_prim32(phd_mesh M, phd_params P, 
     for (int it = 0; it < n_iter; it++) {
         const int i = blockIdx.x * blockDim.x + threadIdx.x + it * stride;
         if (i >= n) continue;
-        const float4 cg = cell_geo_of(M, i, face_geo, face_ar, csr_face);
+        const float4 cg = cell_geo_of(M, i, face_geo, face_ar, csr_face, entry_rec);
         cell_geo[i] = cg;
         const bool real = M.tag[i] == PHD_REAL_TAG;
         const int c = real ? i : M.map[i];
@@ -909,23 +1048,60 @@ int cells_prim_f32(const phd_mesh *mesh, const phd_params *par, const phd_geom32
     if (!mesh || mesh->dim != 2 || mesh->n_cells <= 0 || !par || !out || !out->cell_geo || !cons || !prim4 || !clk) return PHD_ERR_ARG;
     k_cells_prim32<<<(mesh->n_cells + B32 - 1) / B32, B32, 0, stream>>>(
         *mesh, *par, reinterpret_cast<const float4 *>(out->face_geo), reinterpret_cast<const float2 *>(out->face_ar),
-        out->csr_face, reinterpret_cast<float4 *>(out->cell_geo), cons, reinterpret_cast<float4 *>(prim4), clk);
+        out->csr_face, reinterpret_cast<float4 *>(out->entry_rec), reinterpret_cast<float4 *>(out->cell_geo), cons,
+        reinterpret_cast<float4 *>(prim4), clk);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
-template <int SOLVER>
-void launch_face32(bool linear, int grid, int block, cudaStream_t s, const phd_mesh &M, const phd_params &P,
-                   int moving, const phd_geom32 *G, const float4 *prim4, const float4 *grad8, const float2 *w2,
-                   float4 *flux4, phd_clock *clocks, const int32_t *cell_run) {
+// A step kernel launched with programmatic stream serialization: it may be scheduled
+// while the previous kernel of the stream drains (the kernels wait for it with
+// pdl_wait before reading what it writes).  Captured into CUDA graphs as programmatic
+// edges.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t s, Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
+template <int SOLVER, int ITEMS>
+void launch_face32_items(bool linear, int grid, int block, cudaStream_t s, const phd_mesh &M, const phd_params &P,
+                         int moving, const phd_geom32 *G, const float4 *prim4, const float4 *cellrec, const float2 *w2,
+                         float4 *flux4, phd_clock *clocks, const int32_t *cell_run) {
     const float4 *fg = reinterpret_cast<const float4 *>(G->face_geo);
     const float2 *fa = reinterpret_cast<const float2 *>(G->face_ar);
-    const float4 *cg = reinterpret_cast<const float4 *>(G->cell_geo);
+    const GasC gc = gas_consts(P.gamma);
     if (linear)
-        k_face32<SOLVER, true><<<grid, block, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clocks,
-                                                      cell_run, gas_consts(P.gamma));
+        launch_pdl(k_face32<SOLVER, true, ITEMS>, grid, block, s, M, P, moving, fg, fa, prim4, cellrec, w2, flux4,
+                   clocks, cell_run, gc);
     else
-        k_face32<SOLVER, false><<<grid, block, 0, s>>>(M, P, moving, fg, fa, cg, prim4, grad8, w2, flux4, clocks,
-                                                       cell_run, gas_consts(P.gamma));
+        launch_pdl(k_face32<SOLVER, false, ITEMS>, grid, block, s, M, P, moving, fg, fa, prim4, cellrec, w2, flux4,
+                   clocks, cell_run, gc);
+}
+
+// The exact solver's face kernel is bound by the FP64 pipe and holds 120+ registers:
+// it runs one face per thread whatever the requested items.
+template <int SOLVER>
+void launch_face32(bool linear, int items, int grid, int block, cudaStream_t s, const phd_mesh &M,
+                   const phd_params &P, int moving, const phd_geom32 *G, const float4 *prim4, const float4 *cellrec,
+                   const float2 *w2, float4 *flux4, phd_clock *clocks, const int32_t *cell_run) {
+    if (SOLVER == PHD_EXACT || items == 1)
+        launch_face32_items<SOLVER, 1>(linear, grid, block, s, M, P, moving, G, prim4, cellrec, w2, flux4, clocks,
+                                       cell_run);
+    else if (items == 2)
+        launch_face32_items<SOLVER, 2>(linear, grid, block, s, M, P, moving, G, prim4, cellrec, w2, flux4, clocks,
+                                       cell_run);
+    else
+        launch_face32_items<SOLVER, 4>(linear, grid, block, s, M, P, moving, G, prim4, cellrec, w2, flux4, clocks,
+                                       cell_run);
 }
 
 // grid for n items: one thread per item, or at most `cap` blocks looping over the rest
@@ -935,6 +1111,22 @@ inline int grid_for(int n, int block, int cap) {
 }
 
 inline bool block_ok(int b) { return b >= 32 && b <= 512 && (b % 32) == 0; }
+
+// items per thread: 0 (default) or 1 -> 1, 2, 4
+inline bool items_ok(int k) { return k == 0 || k == 1 || k == 2 || k == 4; }
+inline int items_of(int k) { return k <= 1 ? 1 : k; }
+
+template <int LIMITER>
+void launch_grad32(int items, int grid, int block, cudaStream_t s, const phd_mesh &M, const phd_params &P, int moving,
+                   const float4 *er, const int32_t *csr_nbr, const float4 *cg, const float4 *p4, float4 *cr,
+                   float2 *w, phd_clock *clocks) {
+    if (items == 1)
+        launch_pdl(k_grad32<LIMITER, 1>, grid, block, s, M, P, moving, er, csr_nbr, cg, p4, cr, w, clocks);
+    else if (items == 2)
+        launch_pdl(k_grad32<LIMITER, 2>, grid, block, s, M, P, moving, er, csr_nbr, cg, p4, cr, w, clocks);
+    else
+        launch_pdl(k_grad32<LIMITER, 4>, grid, block, s, M, P, moving, er, csr_nbr, cg, p4, cr, w, clocks);
+}
 
 inline int g32(int n) { return n > 0 ? (n + B32 - 1) / B32 : 1; }
 
@@ -947,7 +1139,10 @@ extern "C" {
 int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out, int32_t parts,
                           cudaStream_t stream) {
     phd::NvtxRange nvtx_range("phd_prepare_f32");
-    if (!mesh || mesh->dim != 2 || !out || parts < 0 || parts > (PHD_PREP_ALL | PHD_PREP_CELLS_FROM_FACES))
+    if (!mesh || mesh->dim != 2 || !out || parts < 0 ||
+        parts > (PHD_PREP_ALL | PHD_PREP_CELLS_FROM_FACES | PHD_PREP_RECORDS))
+        return PHD_ERR_ARG;
+    if ((parts & PHD_PREP_RECORDS) && (!out->entry_rec || !out->face_geo || !out->face_ar || !out->csr_face))
         return PHD_ERR_ARG;
     if ((parts & PHD_PREP_CELLS) && (parts & PHD_PREP_CELLS_FROM_FACES)) return PHD_ERR_ARG;
     if ((parts & PHD_PREP_CELLS_FROM_FACES) &&
@@ -968,6 +1163,10 @@ int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_
         k_cells_from_faces32<<<g32(mesh->n_cells), B32, 0, stream>>>(
             *mesh, reinterpret_cast<const float4 *>(out->face_geo), reinterpret_cast<const float2 *>(out->face_ar),
             out->csr_face, reinterpret_cast<float4 *>(out->cell_geo));
+    if (parts & PHD_PREP_RECORDS)              // after the faces and lists (stream order)
+        k_entry_rec32<<<g32(mesh->n_cells), B32, 0, stream>>>(
+            *mesh, reinterpret_cast<const float4 *>(out->face_geo), reinterpret_cast<const float2 *>(out->face_ar),
+            out->csr_face, reinterpret_cast<float4 *>(out->entry_rec));
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
@@ -992,7 +1191,8 @@ int phd_pair_i_from_face_ptr(const phd_mesh *mesh, const int32_t *face_ptr, int3
 }
 
 int phd_prepare_f32(const phd_mesh *mesh, const int32_t *twin, phd_geom32_out *out, cudaStream_t stream) {
-    return phd_prepare_f32_parts(mesh, twin, out, PHD_PREP_ALL, stream);
+    return phd_prepare_f32_parts(mesh, twin, out, PHD_PREP_ALL | (out && out->entry_rec ? PHD_PREP_RECORDS : 0),
+                                 stream);
 }
 
 int phd_prim_f32_batched(const phd_mesh *mesh, const phd_params *par, const double *cons, float *prim4,
@@ -1018,80 +1218,90 @@ int phd_prim_f32_cells(const phd_mesh *mesh, const float *cell_geo, const phd_pa
 }
 
 int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
-                         const phd_launch *launch, float *prim4, const double *cons, double *cons_next, float *grad8,
+                         const phd_launch *launch, float *prim4, const double *cons, double *cons_next, float *cellrec,
                          float *w2, float *flux4, phd_clock *clocks, int32_t n_runs, const int32_t *cell_run,
                          cudaStream_t stream, cudaEvent_t *marks) {
     phd::NvtxRange nvtx_range("phd_step_f32");
     if (!mesh || mesh->dim != 2 || !geo || !par || !prim4 || !cons || !cons_next || !flux4 || !clocks)
         return PHD_ERR_ARG;
     const bool linear = par->reconstruction == PHD_LINEAR;
-    if ((linear || moving) && !grad8) return PHD_ERR_ARG;
+    if ((linear || moving) && (!cellrec || !geo->entry_rec || !geo->csr_nbr)) return PHD_ERR_ARG;
     if (moving && !w2) return PHD_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(cellrec) & 31u) != 0) return PHD_ERR_ARG;    // 256-bit loads
     if (par->solver < PHD_HLL || par->solver > PHD_EXACT) return PHD_ERR_ARG;
     if (n_runs < 1 || (n_runs > 1 && !cell_run)) return PHD_ERR_ARG;
-    phd_launch L = {B32, B32, B32, 0, 0, 0};
+    phd_launch L = {B32, B32, B32, 0, 0, 0, 1, 1, 1};
     if (launch) {
         if (!block_ok(launch->block_grad) || !block_ok(launch->block_face) || !block_ok(launch->block_update) ||
-            launch->block_face > FACE_MAX_BLOCK)
+            launch->block_face > FACE_MAX_BLOCK || !items_ok(launch->items_grad) || !items_ok(launch->items_face) ||
+            !items_ok(launch->items_update))
             return PHD_ERR_ARG;
         L = *launch;
     }
+    const int ig = items_of(L.items_grad), ifc = par->solver == PHD_EXACT ? 1 : items_of(L.items_face),
+              iu = items_of(L.items_update);
     const phd_mesh &M = *mesh;
-    const int gc = grid_for(M.n_cells, L.block_grad, L.grid_cap_grad);
-    const int gf = grid_for(M.n_faces, L.block_face, L.grid_cap_face);
-    const int gu = grid_for(M.n_cells, L.block_update, L.grid_cap_update);
+    const int gc = grid_for((M.n_cells + ig - 1) / ig, L.block_grad, L.grid_cap_grad);
+    const int gf = grid_for((M.n_faces + ifc - 1) / ifc, L.block_face, L.grid_cap_face);
+    const int gu = grid_for((M.n_cells + iu - 1) / iu, L.block_update, L.grid_cap_update);
     float4 *p4 = reinterpret_cast<float4 *>(prim4);
-    float4 *g8 = reinterpret_cast<float4 *>(grad8);
+    float4 *cr = reinterpret_cast<float4 *>(cellrec);
     float2 *w = reinterpret_cast<float2 *>(w2);
     float4 *fx = reinterpret_cast<float4 *>(flux4);
-    const float4 *fg = reinterpret_cast<const float4 *>(geo->face_geo);
-    const float2 *fa = reinterpret_cast<const float2 *>(geo->face_ar);
+    const float4 *er = reinterpret_cast<const float4 *>(geo->entry_rec);
     const float4 *cg = reinterpret_cast<const float4 *>(geo->cell_geo);
     const int32_t *runs = n_runs > 1 ? cell_run : nullptr;
     if (marks) cudaEventRecord(marks[0], stream);
     if (linear || moving) {
         if (par->limiter == PHD_LIMITER_TESS)
-            k_grad32<PHD_LIMITER_TESS><<<gc, L.block_grad, 0, stream>>>(M, *par, moving, fg, fa, geo->csr_face,
-                                                                        geo->csr_nbr, cg, p4, g8, w, clocks);
+            launch_grad32<PHD_LIMITER_TESS>(ig, gc, L.block_grad, stream, M, *par, (int)moving, er, geo->csr_nbr, cg,
+                                            p4, cr, w, clocks);
         else
-            k_grad32<PHD_LIMITER_AREPO><<<gc, L.block_grad, 0, stream>>>(M, *par, moving, fg, fa, geo->csr_face,
-                                                                         geo->csr_nbr, cg, p4, g8, w, clocks);
+            launch_grad32<PHD_LIMITER_AREPO>(ig, gc, L.block_grad, stream, M, *par, (int)moving, er, geo->csr_nbr, cg,
+                                             p4, cr, w, clocks);
     }
     if (marks) cudaEventRecord(marks[1], stream);
     if (M.n_faces) {
         switch (par->solver) {
             case PHD_HLL:
-                launch_face32<PHD_HLL>(linear, gf, L.block_face, stream, M, *par, moving, geo, p4, g8, w, fx, clocks,
+                launch_face32<PHD_HLL>(linear, ifc, gf, L.block_face, stream, M, *par, moving, geo, p4, cr, w, fx, clocks,
                                        runs);
                 break;
             case PHD_HLLC:
-                launch_face32<PHD_HLLC>(linear, gf, L.block_face, stream, M, *par, moving, geo, p4, g8, w, fx, clocks,
+                launch_face32<PHD_HLLC>(linear, ifc, gf, L.block_face, stream, M, *par, moving, geo, p4, cr, w, fx, clocks,
                                         runs);
                 break;
             default:
-                launch_face32<PHD_EXACT>(linear, gf, L.block_face, stream, M, *par, moving, geo, p4, g8, w, fx,
+                launch_face32<PHD_EXACT>(linear, 1, gf, L.block_face, stream, M, *par, moving, geo, p4, cr, w, fx,
                                          clocks, runs);
                 break;
         }
     }
     if (marks) cudaEventRecord(marks[2], stream);
-    k_update32<<<gu, L.block_update, 0, stream>>>(M, *par, geo->csr_face, fx, cg, cons, cons_next, p4, clocks,
-                                                  runs, n_runs);
+    if (iu == 1)
+        launch_pdl(k_update32<1>, gu, L.block_update, stream, M, *par, geo->csr_face, (const float4 *)fx, cg, cons,
+                   cons_next, p4, clocks, runs, (int)n_runs);
+    else if (iu == 2)
+        launch_pdl(k_update32<2>, gu, L.block_update, stream, M, *par, geo->csr_face, (const float4 *)fx, cg, cons,
+                   cons_next, p4, clocks, runs, (int)n_runs);
+    else
+        launch_pdl(k_update32<4>, gu, L.block_update, stream, M, *par, geo->csr_face, (const float4 *)fx, cg, cons,
+                   cons_next, p4, clocks, runs, (int)n_runs);
     if (marks) cudaEventRecord(marks[3], stream);
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
 int phd_step_f32_marked(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
-                        float *prim4, const double *cons, double *cons_next, float *grad8, float *w2,
+                        float *prim4, const double *cons, double *cons_next, float *cellrec, float *w2,
                         float *flux4, phd_clock *clk, cudaStream_t stream, cudaEvent_t *marks) {
-    return phd_step_f32_batched(mesh, geo, par, moving, nullptr, prim4, cons, cons_next, grad8, w2, flux4, clk, 1,
+    return phd_step_f32_batched(mesh, geo, par, moving, nullptr, prim4, cons, cons_next, cellrec, w2, flux4, clk, 1,
                                 nullptr, stream, marks);
 }
 
 int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par, int32_t moving,
-                 float *prim4, const double *cons, double *cons_next, float *grad8, float *w2, float *flux4,
+                 float *prim4, const double *cons, double *cons_next, float *cellrec, float *w2, float *flux4,
                  phd_clock *clk, cudaStream_t stream) {
-    return phd_step_f32_batched(mesh, geo, par, moving, nullptr, prim4, cons, cons_next, grad8, w2, flux4, clk, 1,
+    return phd_step_f32_batched(mesh, geo, par, moving, nullptr, prim4, cons, cons_next, cellrec, w2, flux4, clk, 1,
                                 nullptr, stream, nullptr);
 }
 

@@ -117,13 +117,13 @@ class EnsembleStepper:
         self.csr_face = torch.zeros(max(2 * F, 1), dtype=torch.int32, device=dev)
         self.csr_nbr = torch.zeros(max(2 * F, 1), dtype=torch.int32, device=dev)
         self.cell_geo = torch.zeros((n, 4), dtype=F32, device=dev)
-        out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face, self.csr_nbr,
-                                                       self.cell_geo)))
+        self.entry_rec = torch.zeros((max(2 * F, 1), 4), dtype=F32, device=dev)
+        geo = (self.face_geo, self.face_ar, self.csr_face, self.csr_nbr, self.cell_geo, self.entry_rec)
+        out = L.geom32(geo, out=True)
         L.check(lib.phd_prepare_f32(dm.ref, L.ptr(twin), ctypes.byref(out), s), "prepare")
-        self.geo = L.PhdGeom32(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face, self.csr_nbr,
-                                                         self.cell_geo)))
+        self.geo = L.geom32(geo)
         self.prim4 = torch.zeros((n, 4), dtype=F32, device=dev)
-        self.grad8 = torch.zeros((n, 8), dtype=F32, device=dev)
+        self.cellrec = torch.zeros((n, 16), dtype=F32, device=dev)
         self.w2 = torch.zeros((n, 2), dtype=F32, device=dev)
         self.flux4 = torch.zeros((max(F, 1), 4), dtype=F32, device=dev)
         L.check(lib.phd_prim_f32_batched(dm.ref, ctypes.byref(self.params), L.ptr(self.cons), L.ptr(self.prim4),
@@ -136,7 +136,7 @@ class EnsembleStepper:
         lch = ctypes.byref(self.launch) if self.launch is not None else None
         rc = L.lib().phd_step_f32_batched(self.dmesh.ref, ctypes.byref(self.geo), ctypes.byref(self.params),
                                           int(self.moving), lch, L.ptr(self.prim4), L.ptr(self.cons),
-                                          L.ptr(self.cons_next), L.ptr(self.grad8), L.ptr(self.w2),
+                                          L.ptr(self.cons_next), L.ptr(self.cellrec), L.ptr(self.w2),
                                           L.ptr(self.flux4), L.ptr(self.clocks), self.n_runs, L.ptr(self.cell_run),
                                           s, marks)
         L.check(rc, "phd_step_f32_batched")

@@ -74,19 +74,27 @@ class FluxStepper:
             self.csr_face = torch.zeros(max(2 * F, 1), dtype=torch.int32, device=dev)
             self.csr_nbr = torch.zeros(max(2 * F, 1), dtype=torch.int32, device=dev)
             self.cell_geo = torch.zeros((n, 4), dtype=f32, device=dev)
-            out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
-                                                            self.csr_nbr, self.cell_geo)))
+            self.entry_rec = torch.zeros((max(2 * F, 1), 4), dtype=f32, device=dev)
+            out = L.geom32(self._geo_tensors(), out=True)
             L.check(lib.phd_prepare_f32(dm.ref, L.ptr(self.twin), ctypes.byref(out), s), "phd_prepare_f32")
-            self.geo = L.PhdGeom32(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
-                                                              self.csr_nbr, self.cell_geo)))
+            self.geo = L.geom32(self._geo_tensors())
             self.prim4 = torch.zeros((n, 4), dtype=f32, device=dev)
-            self.grad8 = torch.zeros((n, 8), dtype=f32, device=dev)
+            self.cellrec = torch.zeros((n, 16), dtype=f32, device=dev)
             self.w2 = torch.zeros((n, 2), dtype=f32, device=dev)
             self.flux4 = torch.zeros((max(F, 1), 4), dtype=f32, device=dev)
             L.check(lib.phd_prim_f32(dm.ref, ctypes.byref(self.params), L.ptr(self.cons), L.ptr(self.prim4),
                                      self.clock.ptr, s), "phd_prim_f32")
 
     # ------------------------------------------------------------------------------
+    def _geo_tensors(self):
+        return (self.face_geo, self.face_ar, self.csr_face, self.csr_nbr, self.cell_geo, self.entry_rec)
+
+    @property
+    def grad8(self):
+        """FP32 limited gradients [n][8] (d/dx, d/dy of rho, v_x, v_y, p) of the last step:
+        a view into the cell records the gradient stage writes."""
+        return self.cellrec[:, 4:12]
+
     def initial_time_step(self):
         """dt for the first step from the current primitives (riemann.pyx:120-188)."""
         p = self.params
@@ -150,12 +158,12 @@ class FluxStepper:
             self.csr_face = view("csr_face", (max(2 * n_faces, 1),), i32)
             self.csr_nbr = view("csr_nbr", (max(2 * n_faces, 1),), i32)
             self.cell_geo = view("cell_geo", (n_cells, 4), f32)
+            self.entry_rec = view("entry_rec", (max(2 * n_faces, 1), 4), f32)
             self.prim4 = view("prim4", (n_cells, 4), f32)
-            self.grad8 = view("grad8", (n_cells, 8), f32)
+            self.cellrec = view("cellrec", (n_cells, 16), f32)
             self.w2 = view("w2", (n_cells, 2), f32)
             self.flux4 = view("flux4", (F1, 4), f32)
-            self.geo = L.PhdGeom32(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
-                                                              self.csr_nbr, self.cell_geo)))
+            self.geo = L.geom32(self._geo_tensors())
         self._graph = None
         self._graph_steps = 0
 
@@ -211,8 +219,7 @@ class FluxStepper:
         s, ss = L.stream_handle(main), L.stream_handle(side)
         out = None
         if fp32:
-            out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face,
-                                                            self.csr_nbr, self.cell_geo)))
+            out = L.geom32(self._geo_tensors(), out=True)
         # copies on the main stream in the order the side stream needs them; the side
         # stream builds the neighbour lists, twins, list codes and face geometry meanwhile
         dm.reset_errors(main)
@@ -242,8 +249,8 @@ class FluxStepper:
             ev[2].record(main)
             side.wait_event(ev[2])
             dm.set_normals("none", side)
-            L.check(lib.phd_prepare_f32_parts(dm.ref, None, ctypes.byref(out), L.PREP_FACES | L.PREP_CELLS_FROM_FACES,
-                                              ss), "phd_prepare_f32_parts")
+            L.check(lib.phd_prepare_f32_parts(dm.ref, None, ctypes.byref(out), L.PREP_FACES | L.PREP_CELLS_FROM_FACES |
+                                              L.PREP_RECORDS, ss), "phd_prepare_f32_parts")
         ev[3].record(side)
         if not fp32:
             nbytes += dm.copy_fields(pinned, ("dcom", "vol"), main)
@@ -291,8 +298,7 @@ class FluxStepper:
                             periodic=int(dm.boundary == "periodic"), dedup_periodic=int(self.dedup_periodic),
                             xmin=(ctypes.c_double * 2)(*dm.xmin[:2]),
                             xmax=(ctypes.c_double * 2)(*dm.xmax[:2]))
-        out = L.PhdGeom32Out(*(t.data_ptr() for t in (self.face_geo, self.face_ar, self.csr_face, self.csr_nbr,
-                                                        self.cell_geo)))
+        out = L.geom32(self._geo_tensors(), out=True)
         events = (ctypes.c_void_p * 8)(*(e.cuda_event for e in self._ev))
         sides = (ctypes.c_void_p * 2)(self._side.cuda_stream, self._side2.cuda_stream)
         L.check(lib.phd_load_mesh_f32(dm.ref, ctypes.byref(h), ctypes.byref(self.params), ctypes.byref(out),
@@ -318,7 +324,7 @@ class FluxStepper:
             lch = ctypes.byref(self.launch) if self.launch is not None else None
             rc = L.lib().phd_step_f32_batched(dm.ref, ctypes.byref(self.geo), ctypes.byref(p), int(self.moving), lch,
                                               L.ptr(self.prim4), L.ptr(self.cons), L.ptr(self.cons_next),
-                                              L.ptr(self.grad8), L.ptr(self.w2), L.ptr(self.flux4), self.clock.ptr,
+                                              L.ptr(self.cellrec), L.ptr(self.w2), L.ptr(self.flux4), self.clock.ptr,
                                               1, None, s, marks)
         L.check(rc, "phd_step_" + self.precision)
         self.cons, self.cons_next = self.cons_next, self.cons

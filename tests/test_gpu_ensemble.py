@@ -34,8 +34,9 @@ def test_graph_and_tuned_launch_are_bitwise_equal(runs):
     a = EnsembleStepper(runs)
     a.step(8)
     b = EnsembleStepper(runs)
-    launch, table = tune(b, blocks=(128, 256), cap_waves=(0, 2), reps=1)
-    assert len(table) == 4
+    launch, table = tune(b, blocks=(128, 256), cap_waves=(0, 2), items=(1, 2, 4), reps=1)
+    assert len(table) == 12
+    assert (launch.items_grad, launch.items_face, launch.items_update) != (0, 0, 0)
     b.launch = launch
     b.capture(4)
     b.replay()
@@ -43,6 +44,25 @@ def test_graph_and_tuned_launch_are_bitwise_equal(runs):
     torch.cuda.synchronize()
     for r in range(len(runs)):
         assert np.array_equal(a.run_cons(r), b.run_cons(r))
+
+
+@pytest.mark.parametrize("items", [1, 2, 4])
+def test_every_tuned_shape_is_bitwise_equal(runs, items):
+    """Each candidate of the tuner's space (block, grid cap, items per thread) advances
+    the batch to the same bits as the default launch."""
+    import phd_code_gb300._lib as L
+    ref = EnsembleStepper(runs)
+    ref.step(5)
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    for block in (128, 256, 512):
+        for waves in (0, 2):
+            e = EnsembleStepper(runs)
+            cap = waves * sms
+            e.launch = L.PhdLaunch(block, min(block, 384), block, cap, cap, cap, items, items, items)
+            e.step(5)
+            e.check_status()
+            for r in range(len(runs)):
+                assert np.array_equal(ref.run_cons(r), e.run_cons(r)), (block, waves, items, r)
 
 
 def test_sequential_baseline_matches(runs):

@@ -61,6 +61,8 @@ def test_shear_1024_device_mesh_data_and_compact_hand_over(shear):
     mesh, prim, gamma = shear
     st = FluxStepper(mesh, prim, gamma=gamma, precision="fp32")
     geo = [t.clone() for t in (st.face_geo, st.face_ar, st.csr_face, st.csr_nbr, st.cell_geo)]
+    e_real = int(mesh.nbr_ptr[mesh.n_real])
+    rec = st.entry_rec[:e_real].clone()
     st.load_mesh(st.dmesh.pinned_host_compact(mesh))             # lists, twins, geometry on the device
     torch.cuda.synchronize()
     assert st.dmesh.upload_errors() == 0
@@ -73,6 +75,8 @@ def test_shear_1024_device_mesh_data_and_compact_hand_over(shear):
     assert torch.max(torch.abs(geo[0][:, :2] - st.face_geo[:, :2])).item() <= 4e-7
     for old, new in zip(geo[1:4], (st.face_ar, st.csr_face, st.csr_nbr)):
         assert torch.equal(old, new)
+    # the gradient records follow the normals: equal to FP32 rounding of the geometry
+    assert torch.max(torch.abs(rec - st.entry_rec[:e_real])).item() <= 1e-6 * torch.max(torch.abs(rec)).item()
 
 
 def test_explosion_256_fp32_tracks_fp64():

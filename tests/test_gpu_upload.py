@@ -268,6 +268,8 @@ def test_compact_hand_over_equals_the_full_one(boundary):
         assert b.dmesh.upload_errors() == 0
         for name in ("face_geo", "face_ar", "csr_face", "csr_nbr", "cell_geo", "twin", "prim4"):
             assert torch.equal(getattr(a, name), getattr(b, name)), name
+        e = int(a.dmesh.nbr_ptr[a.dmesh.n_real].item())
+        assert torch.equal(a.entry_rec[:e], b.entry_rec[:e])
         assert torch.equal(a.dmesh.pair_i, b.dmesh.pair_i)
     a.step(3)
     b.step(3)
@@ -435,6 +437,8 @@ def test_compact_hand_over_without_periodic_dedup():
         assert bool((b.twin == -1).all())
         for name in ("face_geo", "face_ar", "csr_face", "csr_nbr", "cell_geo", "twin", "prim4"):
             assert torch.equal(getattr(a, name), getattr(b, name)), name
+        e = int(a.dmesh.nbr_ptr[a.dmesh.n_real].item())
+        assert torch.equal(a.entry_rec[:e], b.entry_rec[:e])
     a.step(2)
     b.step(2)
     assert np.array_equal(a.cons_host(), b.cons_host())
