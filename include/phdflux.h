@@ -447,9 +447,11 @@ int phd_adjoint_step_f64_taped(const phd_mesh *mesh, const phd_adj_index *index,
  * 32 MiB, present on every GPU that loads the library until the process exits), so
  * the mesh must satisfy phd_adjoint_work_doubles(n_cells, n_faces) <=
  * PHD_ADJ_NOALLOC_MAX_DOUBLES -- about 36,000 cells in 2D at three faces per cell --
- * else PHD_ERR_SCRATCH_TOO_SMALL is returned and nothing runs.  The first call on a
- * device looks up the array's device address (once per device, with that device
- * current) and keeps it for later calls.  All calls share the one array:
+ * else PHD_ERR_SCRATCH_TOO_SMALL is returned and nothing runs.  Every call looks up
+ * the array's device address for the device current at the call (so it stays right
+ * after cudaDeviceReset or in another context); the first call on a device also loads
+ * the library's device code there, so make it before any stream capture.  All calls
+ * share the one array:
  * calls that overlap on the GPU (different streams, or two threads) race on it.
  * Nothing is allocated; the entries that must start at zero are cleared on the
  * stream by every call. */

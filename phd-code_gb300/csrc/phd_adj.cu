@@ -12,7 +12,6 @@
 //   k_adj_gather2  per cell: own + partner-entry contributions -> lam_prim
 //   k_adj_final    per real cell: fold ghost rows, reverse the primitive recovery,
 //                  lam = lam' + J^T lam_prim
-#include <mutex>
 
 #include "phd_common.cuh"
 #include "phd_physics.cuh"
@@ -493,28 +492,19 @@ static __device__ __align__(256) double g_adj_scratch[PHD_ADJ_NOALLOC_MAX_DOUBLE
 
 namespace {
 
-// Device address of g_adj_scratch on the current device.  In host code the symbol
-// name is only a host-side stand-in, so the address is asked from the runtime once per
-// device (with that device current) and cached.
+// Device address of g_adj_scratch in the current device's current context.  In host
+// code the symbol name is only a host-side stand-in, so the address is asked from the
+// runtime on every call (cheap once the library's device code is loaded there): a
+// cached address would go stale after cudaDeviceReset, or point into the wrong module
+// when the caller switches contexts.
 double *adj_scratch_on_current_device(int *rc) {
-    static std::mutex lock;
-    static double *addr[256] = {nullptr};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_adj_scratch);
+    if (e != cudaSuccess || !p) {
         *rc = PHD_ERR_LAUNCH;
         return nullptr;
     }
-    std::lock_guard<std::mutex> guard(lock);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_adj_scratch);
-        if (e != cudaSuccess || !p) {
-            *rc = PHD_ERR_LAUNCH;
-            return nullptr;
-        }
-        addr[dev] = static_cast<double *>(p);
-    }
-    return addr[dev];
+    return static_cast<double *>(p);
 }
 
 }  // namespace

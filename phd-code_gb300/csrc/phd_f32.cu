@@ -443,15 +443,15 @@ __global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int mo
 
 // ---- FP32 Riemann solver with the gas constants formed once on the host -------------
 // HLL.get_waves riemann.pyx:375-504 and HLL/HLLC.riemann_solver riemann.pyx:243-373,
-// 521-682 in FP32: the same formulas and branch structure as hll_family<float>, with
-// every quantity that depends only on gamma ((g-1)/(2g), 1/(g-1), (g+1)/2, ...)
-// precomputed, and the divisions and square roots rewritten so that each side needs
-// one reciprocal of its density (shared by its sound speed, its shock speed and the
-// HLLC star flux): the face kernel is bound by its issue rate, and every FP32 division
-// or square root is a multi-function-unit instruction plus fix-ups.  The HLLC left /
-// right star branches are merged into one (selects instead of divergence).
+// 521-682 in FP32: the same formulas as hll_family<float> with every quantity that
+// depends only on gamma ((g-1)/(2g), 1/(g-1), (g+1)/(2g), ...) precomputed, and the
+// HLLC left / right star branches merged into one (selects instead of divergence).
+// (A variant sharing one density reciprocal per side between the sound speed, the
+// shock speeds and the star flux issued fewer multi-function-unit instructions but
+// more instructions in all, and measured no faster: with fast-math a division is
+// already one reciprocal and one multiply.)
 struct GasC {
-    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1, gp1_half, half_gm1;
+    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1;
     ExGas64 X;                 // the exact solver's FP64 Newton constants
 };
 
@@ -466,49 +466,39 @@ inline GasC gas_consts(double gamma) {
     c.inv_z = 1.f / c.z;
     c.two_gp1 = 2.f / (g + 1.f);
     c.gm1_gp1 = (g - 1.f) / (g + 1.f);
-    c.gp1_half = 0.5f * (g + 1.f);
-    c.half_gm1 = 0.5f * (g - 1.f);
     c.X = ex_gas64(gamma);
     return c;
 }
 
-// idl, idr: 1/dl, 1/dr.
-__device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float dr, float ur, float pr, float idl,
-                                            float idr, const GasC &C, float &sl, float &sc, float &sr) {
-    // c^2 = g p / d (riemann.pyx:404-405), floored at c = 1e-10 as the reference does
-    const float cl2 = (C.g * pl) * idl, cr2 = (C.g * pr) * idr;
-    const float cl = fmaxf(sqrtf(cl2), 1.0e-10f);
-    const float cr = fmaxf(sqrtf(cr2), 1.0e-10f);
+__device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float dr, float ur, float pr,
+                                            const GasC &C, float &sl, float &sc, float &sr) {
+    float p_star;
+    const float cl = fmaxf(sqrtf((C.g * pl) / dl), 1.0e-10f);
+    const float cr = fmaxf(sqrtf((C.g * pr) / dr), 1.0e-10f);
     const float d_avg = 0.5f * (dl + dr);
     const float c_avg = 0.5f * (cl + cr);
-    float p_star = fmaxf(0.f, ((0.5f * (pl + pr)) + (((0.5f * (ul - ur)) * d_avg) * c_avg)));
+    p_star = fmaxf(0.f, ((0.5f * (pl + pr)) + (((0.5f * (ul - ur)) * d_avg) * c_avg)));
     const float p_min = fminf(pl, pr);
     const float p_max = fmaxf(pl, pr);
-    // p_max / p_min < 2 without the division (dividing by a negative p_min flips it)
-    const bool ratio2 = (p_min > 0.f) ? (p_max < 2.f * p_min) : (p_min < 0.f && p_max > 2.f * p_min);
-    if (ratio2 && ((p_min < p_star) && (p_star < p_max))) {
+    if (((p_max / p_min) < 2.f) && ((p_min < p_star) && (p_star < p_max))) {
         // PVRS estimate stands
     } else if (p_star <= p_min) {          // two-rarefaction (TRRS)
-        const float icl = 1.f / cl, icr = 1.f / cr;
         const float plr = __powf(pl / pr, C.z);
-        const float u_star = ((((plr * ul) * icl) + (ur * icr)) + ((2.f * (plr - 1.f)) * C.inv_gm1)) /
-                             ((plr * icl) + icr);
-        p_star = (0.5f * pl) * __powf(1.f + (C.half_gm1 * (ul - u_star)) * icl, C.inv_z);
-        p_star = p_star + ((0.5f * pr) * __powf(1.f + (C.half_gm1 * (u_star - ur)) * icr, C.inv_z));
+        const float u_star = ((((plr * ul) / cl) + (ur / cr)) + ((2.f * (plr - 1.f)) * C.inv_gm1)) /
+                             ((plr / cl) + (1.f / cr));
+        p_star = (0.5f * pl) * __powf((1.f + ((C.gm1 * (ul - u_star)) / (2.f * cl))), C.inv_z);
+        p_star = p_star + ((0.5f * pr) * __powf((1.f + ((C.gm1 * (u_star - ur)) / (2.f * cr))), C.inv_z));
     } else {                               // two-shock (TSRS)
-        // sqrt(A / (p + B)) with A = 2/((g+1) d) as one reciprocal square root
-        const float gl = rsqrtf((C.gp1_half * dl) * (p_star + pl * C.gm1_gp1));
-        const float gr = rsqrtf((C.gp1_half * dr) * (p_star + pr * C.gm1_gp1));
+        const float Al = C.two_gp1 / dl;
+        const float Ar = C.two_gp1 / dr;
+        const float gl = sqrtf(Al / (p_star + pl * C.gm1_gp1));
+        const float gr = sqrtf(Ar / (p_star + pr * C.gm1_gp1));
         p_star = (((gl * pl) + (gr * pr)) - (ur - ul)) / (gl + gr);
     }
-    // shock speeds c sqrt(1 + (g+1)/(2g) (p*/p - 1)) = sqrt(c^2 + (g+1)/2 (p* - p) / d);
-    // a floored sound speed (vacuum-like side) keeps the reference's form
-    float ql = cl2 + (C.gp1_half * (p_star - pl)) * idl;
-    float qr = cr2 + (C.gp1_half * (p_star - pr)) * idr;
-    if (__builtin_expect(!(cl2 >= 1.0e-20f), 0)) ql = (cl * cl) * (1.f + (C.gp1_2g * ((p_star / pl) - 1.f)));
-    if (__builtin_expect(!(cr2 >= 1.0e-20f), 0)) qr = (cr * cr) * (1.f + (C.gp1_2g * ((p_star / pr) - 1.f)));
-    sl = (p_star <= pl) ? ul - cl : ul - sqrtf(ql);
-    sr = (p_star <= pr) ? ur + cr : ur + sqrtf(qr);
+    if (p_star <= pl) sl = ul - cl;
+    else sl = ul - (cl * sqrtf((1.f + (C.gp1_2g * ((p_star / pl) - 1.f)))));
+    if (p_star <= pr) sr = ur + cr;
+    else sr = ur + (cr * sqrtf((1.f + (C.gp1_2g * ((p_star / pr) - 1.f)))));
     sc = (((pr - pl) + ((dl * ul) * (sl - ul))) - ((dr * ur) * (sr - ur))) /
          ((dl * (sl - ul)) - (dr * (sr - ur)));
 }
@@ -516,12 +506,11 @@ __device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float 
 __device__ __forceinline__ void hll_family32(bool hllc, const float *L, const float *R, const float *n,
                                              const float *w, const GasC &C, bool boost, float *f) {
     const float _dl = L[0], _pl = L[3], _dr = R[0], _pr = R[3];
-    const float idl = 1.f / _dl, idr = 1.f / _dr;
     const float vl_sq = L[1] * L[1] + L[2] * L[2], vr_sq = R[1] * R[1] + R[2] * R[2];
     const float Vnl = L[1] * n[0] + L[2] * n[1], Vnr = R[1] * n[0] + R[2] * n[1];
     const float wn = boost ? 0.f : (w[0] * n[0] + w[1] * n[1]);
     float sl, sc, sr;
-    get_waves32(_dl, Vnl, _pl, _dr, Vnr, _pr, idl, idr, C, sl, sc, sr);
+    get_waves32(_dl, Vnl, _pl, _dr, Vnr, _pr, C, sl, sc, sr);
     if (wn <= sl) {
         f[0] = _dl * (Vnl - wn);
         f[3] = ((((0.5f * _dl) * vl_sq) + (_pl * C.inv_gm1)) * (Vnl - wn)) + (_pl * Vnl);
@@ -544,17 +533,15 @@ __device__ __forceinline__ void hll_family32(bool hllc, const float *L, const fl
         } else {                           // star region on the side of the contact
             const bool left = wn <= sc;
             const float d = left ? _dl : _dr, p = left ? _pl : _pr, Vn = left ? Vnl : Vnr, s = left ? sl : sr;
-            const float id = left ? idl : idr;
             const float vsq = left ? vl_sq : vr_sq;
             const float *S = left ? L : R;
-            const float a = s - Vn;
-            const float factor_1 = (d * a) / (s - sc);
+            const float factor_1 = (d * (s - Vn)) / (s - sc);
             const float factor_2 = ((factor_1 * (s - wn)) * (sc - Vn)) + p;
             const float frho = (d * (Vn - s)) + (factor_1 * (s - wn));
             const float e = ((0.5f * d) * vsq) + (p * C.inv_gm1);
             f[0] = frho;
-            // e/d and p/(d (s - Vn)) with the side's density reciprocal
-            f[3] = (((e + p) * Vn) - (s * e)) + (((s - wn) * factor_1) * ((e * id) + ((sc - Vn) * (sc + (p * id) / a))));
+            f[3] = (((e + p) * Vn) - (s * e)) +
+                   (((s - wn) * factor_1) * ((e / d) + ((sc - Vn) * (sc + (p / (d * (s - Vn)))))));
             for (int k = 0; k < 2; k++) f[1 + k] = (frho * S[1 + k]) + (factor_2 * n[k]);
         }
     } else {
@@ -665,18 +652,19 @@ __device__ __forceinline__ FaceHead face_head(int m, const phd_mesh &M, const fl
     return h;
 }
 
+// dt_run: the step's dt in FP32 when all faces belong to one run (read once per thread).
 template <int SOLVER, bool LINEAR>
 __device__ __forceinline__ void face32_face(int m, const FaceHead &H, const phd_mesh &M, const phd_params &P,
                                             int moving, const float4 *__restrict__ prim4,
                                             const float4 *__restrict__ cellrec, const float2 *__restrict__ w2,
                                             float4 *__restrict__ flux4, phd_clock *clocks,
-                                            const int32_t *__restrict__ cell_run, const GasC &GC) {
+                                            const int32_t *__restrict__ cell_run, const GasC &GC, float dt_run) {
     const int i = H.i, j = H.j;
     if (i < 0 || i >= M.n_cells || j < 0 || j >= M.n_cells) { set_status32(clocks, PHD_STATUS_BAD_INDEX); return; }
     phd_clock *clk = cell_run ? clocks + cell_run[i] : clocks;
     const bool boost = (SOLVER == PHD_EXACT) ? true : (P.boost != 0);
     const float gamma = GC.g;
-    const float dtf = narrow_f64(clk->dt);
+    const float dtf = cell_run ? narrow_f64(clk->dt) : dt_run;
     const float dt_half = 0.5f * dtf;
     const float4 g = H.g;
     const float2 ar = H.ar;
@@ -766,13 +754,14 @@ __global__ void __launch_bounds__(FACE_MAX_BLOCK, SOLVER == PHD_EXACT ? 1 : 3) k
     pdl_launch_dependents();
     const int tile = blockDim.x * ITEMS;
     pdl_wait();                                  // cellrec / prim4, w2 and the clock: earlier kernels'
+    const float dt_run = cell_run ? 0.f : narrow_f64(clocks->dt);
     for (int base = blockIdx.x * tile; base < M.n_faces; base += gridDim.x * tile) {
 #pragma unroll
         for (int k = 0; k < ITEMS; k++) {
             const int m = base + k * blockDim.x + threadIdx.x;
             if (m < M.n_faces)
                 face32_face<SOLVER, LINEAR>(m, face_head(m, M, face_geo, face_ar), M, P, moving, prim4, cellrec, w2,
-                                            flux4, clocks, cell_run, GC);
+                                            flux4, clocks, cell_run, GC, dt_run);
         }
     }
 }

@@ -1,4 +1,5 @@
 """Shared helpers for the test-suite (fixtures, tolerances, states)."""
+import json
 import os
 
 import numpy as np
@@ -47,6 +48,43 @@ def rel_rows(a, b):
         d = np.max(np.abs(a[r] - b[r]))
         worst = max(worst, d / s if s > 0 else d)
     return worst
+
+
+# Element-wise parity: each element against its own magnitude, down to ELEM_FLOOR times
+# its field's largest magnitude (a field's elements that are exactly zero in the
+# reference, or cancellation results near zero, are measured against that floor).  On
+# the GB300 every parity comparison of the suite holds at 1e-12 element-wise with a
+# floor of 1e-14 (worst element 5.8e-13, worst field normwise 5e-15).
+ELEM_FLOOR = 1e-14
+
+
+def elem_rel(a, b, floor=ELEM_FLOOR):
+    """Worst element-wise relative difference of [field][index] arrays:
+    max |a - b| / max(|b|, floor * max|b_field|); an identically zero field is compared
+    with an absolute floor of 1e-300."""
+    a = np.atleast_2d(np.asarray(a, dtype=np.float64))
+    b = np.atleast_2d(np.asarray(b, dtype=np.float64))
+    worst = 0.0
+    for r in range(b.shape[0]):
+        scale = np.max(np.abs(b[r])) if b[r].size else 0.0
+        den = np.maximum(np.abs(b[r]), max(floor * scale, 1e-300))
+        if b[r].size:
+            worst = max(worst, float(np.max(np.abs(a[r] - b[r]) / den)))
+    return worst
+
+
+def assert_parity(a, b, tol=FP64_TOL, tag=None):
+    """FP64 parity of [field][index] arrays: normwise (per field) and element-wise
+    (elem_rel) both within tol.  With PHD_PARITY_REPORT set, the figures (and the
+    element-wise one at a floor of 1e-14 of the field scale) are appended to that file."""
+    nw, ew = rel_rows(a, b), elem_rel(a, b)
+    path = os.environ.get("PHD_PARITY_REPORT")
+    if path:
+        with open(path, "a") as fh:
+            fh.write(json.dumps({"tag": tag or os.environ.get("PYTEST_CURRENT_TEST", "?"), "normwise": nw,
+                                 "elementwise": ew, "elementwise_floor_1e-14": elem_rel(a, b, 1e-14)}) + "\n")
+    assert nw <= tol, "normwise %.3e > %.1e" % (nw, tol)
+    assert ew <= tol, "element-wise %.3e > %.1e" % (ew, tol)
 
 
 def smooth_state(m, kind="wave"):

@@ -12,7 +12,7 @@ import torch
 import oracle as O
 import phd_code_gb300 as pkg
 from phd_code_gb300.step import FluxStepper
-from _util import FP64_TOL, rel_rows
+from _util import FP64_TOL, assert_parity, rel_rows
 
 pytestmark = pytest.mark.gpu
 
@@ -34,8 +34,8 @@ def test_shear_1024_fp64_step_matches_the_oracle(shear):
     dt = O.time_step(mesh, p, gamma, 0.5, True)
     assert O.OracleStepper(mesh, gamma=gamma, solver="hllc", moving=True).step(dt, p, c) == 0
     nr = mesh.n_real
-    assert rel_rows(st.cons_host()[:, :nr], c[:, :nr]) <= FP64_TOL
-    assert rel_rows(st.prim_host(), p) <= FP64_TOL
+    assert_parity(st.cons_host()[:, :nr], c[:, :nr])
+    assert_parity(st.prim_host(), p)
 
 
 def test_shear_1024_fp32_conserves_tracks_fp64_and_repeats(shear):
@@ -79,14 +79,24 @@ def test_shear_1024_device_mesh_data_and_compact_hand_over(shear):
     assert torch.max(torch.abs(rec - st.entry_rec[:e_real])).item() <= 1e-6 * torch.max(torch.abs(rec)).item()
 
 
-def test_explosion_256_fp32_tracks_fp64():
+@pytest.mark.parametrize("solver", ["hllc", "exact"])
+def test_explosion_256_fp32_tracks_fp64(solver):
+    """The point explosion at its configured size (256x256, E = 1) run to t = 0.05 with
+    each solver: FP32 + FP64 accumulation against the FP64 path -- L1 density error
+    <= 1e-5 and total-energy drift <= 1e-12 for both precisions.  The exact solver keeps
+    its Newton pressure iteration in FP64 inside the FP32 path."""
     mesh, prim, info = pkg.problems.point_explosion(256, seed=0)
-    nr, gamma = mesh.n_real, info["gamma"]
+    nr, gamma, t_end = mesh.n_real, info["gamma"], info["t_end"]
     out = {}
     for precision in ("fp32", "fp64"):
-        st = FluxStepper(mesh, prim, gamma=gamma, cfl=0.5, solver="hllc", moving=True, precision=precision)
+        st = FluxStepper(mesh, prim, gamma=gamma, cfl=0.5, solver=solver, moving=True, precision=precision,
+                         t_end=t_end)
         e0 = st.cons_host()[3, :nr].sum()
-        st.step(40)
+        steps = 0
+        while st.read_clock().t < t_end * (1.0 - 1e-12) and steps < 2000:
+            st.step(25)
+            steps += 25
+        assert st.read_clock().t >= t_end * (1.0 - 1e-12)
         st.check_status()
         cons = st.cons_host()[:, :nr]
         assert abs(cons[3].sum() - e0) <= 1e-12 * abs(e0)

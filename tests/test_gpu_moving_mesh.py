@@ -6,7 +6,7 @@ import pytest
 
 import oracle as O
 import phd_code_gb300 as pkg
-from _util import FP64_TOL, rel_rows
+from _util import FP64_TOL, assert_parity, rel_rows
 
 pytestmark = pytest.mark.gpu
 
@@ -69,8 +69,8 @@ def test_moving_mesh_with_remesh_matches_oracle(boundary):
         c = O.ghost_refresh_cons(nxt, c_new)
         p = O.prim_from_cons(nxt, c, gamma)
     n = meshes[-1].n_real
-    assert rel_rows(gpu_cons[:, :n], c[:, :n]) <= FP64_TOL
-    assert rel_rows(gpu_prim, p) <= FP64_TOL
+    assert_parity(gpu_cons[:, :n], c[:, :n])
+    assert_parity(gpu_prim, p)
 
 
 def test_shock_tube_full_run_to_t_end_matches_oracle():
@@ -117,5 +117,5 @@ def test_shock_tube_full_run_to_t_end_matches_oracle():
         c = O.ghost_refresh_cons(nxt, c_new)
         p = O.prim_from_cons(nxt, c, gamma)
     n = meshes[-1].n_real
-    assert rel_rows(gpu_cons[:, :n], c[:, :n]) <= 1e-10
-    assert rel_rows(gpu_prim, p) <= 1e-10
+    assert_parity(gpu_cons[:, :n], c[:, :n], tol=1e-10)
+    assert_parity(gpu_prim, p, tol=1e-10)

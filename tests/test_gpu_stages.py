@@ -5,7 +5,7 @@ import pytest
 import torch
 
 import phd_code_gb300 as pkg
-from _util import CONFIGS, FP64_TOL, load_golden, rel_rows, split
+from _util import CONFIGS, FP64_TOL, load_golden, assert_parity, rel_rows, split
 
 pytestmark = pytest.mark.gpu
 
@@ -44,19 +44,19 @@ def test_plugin_stages(boundary, cfg):
     dt = it.compute_time_step()
     assert abs(dt - float(d[cfg + "/dt"])) <= FP64_TOL * dt
     mesh.assign_generator_velocities(pc, it.equation_state)
-    assert rel_rows(pc.block("w").cpu().numpy(), d[cfg + "/w"]) <= FP64_TOL
+    assert_parity(pc.block("w").cpu().numpy(), d[cfg + "/w"])
     mesh.assign_face_velocities(pc)
-    assert rel_rows(mesh.faces.block("velocity").cpu().numpy(), d[cfg + "/face_w"]) <= FP64_TOL
+    assert_parity(mesh.faces.block("velocity").cpu().numpy(), d[cfg + "/face_w"])
     it.reconstruction.compute_gradients(pc, mesh, it.domain_manager)
-    assert rel_rows(it.reconstruction.grad.block("primitive").cpu().numpy(), d[cfg + "/grad"]) <= FP64_TOL
+    assert_parity(it.reconstruction.grad.block("primitive").cpu().numpy(), d[cfg + "/grad"])
     it.reconstruction.compute_states(pc, mesh, 1.4, it.domain_manager, 0.5 * dt, it.riemann.boost)
-    assert rel_rows(it.reconstruction.left_states.block("primitive").cpu().numpy(), d[cfg + "/left"]) <= FP64_TOL
-    assert rel_rows(it.reconstruction.right_states.block("primitive").cpu().numpy(), d[cfg + "/right"]) <= FP64_TOL
+    assert_parity(it.reconstruction.left_states.block("primitive").cpu().numpy(), d[cfg + "/left"])
+    assert_parity(it.reconstruction.right_states.block("primitive").cpu().numpy(), d[cfg + "/right"])
     it.riemann.compute_fluxes(pc, mesh, it.reconstruction, it.equation_state)
-    assert rel_rows(it.riemann.fluxes.block("flux").cpu().numpy(), d[cfg + "/flux"]) <= FP64_TOL
+    assert_parity(it.riemann.fluxes.block("flux").cpu().numpy(), d[cfg + "/flux"])
     mesh.update_from_fluxes(pc, it.riemann, dt)
     n = m.n_real
-    assert rel_rows(pc.block("conservative").cpu().numpy()[:, :n], d[cfg + "/cons1"][:, :n]) <= FP64_TOL
+    assert_parity(pc.block("conservative").cpu().numpy()[:, :n], d[cfg + "/cons1"][:, :n])
 
 
 @pytest.mark.parametrize("boundary", ["periodic", "reflective"])
@@ -70,8 +70,8 @@ def test_spatial_then_temporal_equals_compute_states(boundary):
     rec.compute_gradients(pc, mesh, it.domain_manager)
     rec.add_spatial(pc, mesh, 1.4, it.domain_manager, 0.5 * dt, True)
     rec.add_temporal(pc, mesh, 1.4, it.domain_manager, 0.5 * dt, True)
-    assert rel_rows(rec.left_states.block("primitive").cpu().numpy(), d["hllc_arepo_boost/left"]) <= FP64_TOL
-    assert rel_rows(rec.right_states.block("primitive").cpu().numpy(), d["hllc_arepo_boost/right"]) <= FP64_TOL
+    assert_parity(rec.left_states.block("primitive").cpu().numpy(), d["hllc_arepo_boost/left"])
+    assert_parity(rec.right_states.block("primitive").cpu().numpy(), d["hllc_arepo_boost/right"])
 
 
 @pytest.mark.parametrize("boundary", ["periodic", "reflective"])
@@ -81,9 +81,9 @@ def test_constant_reconstruction(boundary):
     pc, mesh = it.particles, it.mesh
     dt = it.compute_time_step()
     it.reconstruction.compute_states(pc, mesh, 1.4, it.domain_manager, 0.5 * dt, True)
-    assert rel_rows(it.reconstruction.left_states.block("primitive").cpu().numpy(), d["pwc_hllc/left"]) <= FP64_TOL
+    assert_parity(it.reconstruction.left_states.block("primitive").cpu().numpy(), d["pwc_hllc/left"])
     it.riemann.compute_fluxes(pc, mesh, it.reconstruction, it.equation_state)
-    assert rel_rows(it.riemann.fluxes.block("flux").cpu().numpy(), d["pwc_hllc/flux"]) <= FP64_TOL
+    assert_parity(it.riemann.fluxes.block("flux").cpu().numpy(), d["pwc_hllc/flux"])
 
 
 @pytest.mark.parametrize("boundary", ["periodic", "reflective"])
@@ -95,9 +95,9 @@ def test_integrator_three_steps(boundary, solver):
     for _ in range(3):
         dts.append(it.compute_time_step())
         it.evolve_timestep()
-    assert rel_rows(np.array(dts), d["run3_%s/dts" % solver]) <= FP64_TOL
-    assert rel_rows(it.particles.block("primitive").cpu().numpy(), d["run3_%s/prim" % solver]) <= FP64_TOL
-    assert rel_rows(it.particles.block("conservative").cpu().numpy(), d["run3_%s/cons" % solver]) <= FP64_TOL
+    assert_parity(np.array(dts), d["run3_%s/dts" % solver])
+    assert_parity(it.particles.block("primitive").cpu().numpy(), d["run3_%s/prim" % solver])
+    assert_parity(it.particles.block("conservative").cpu().numpy(), d["run3_%s/cons" % solver])
 
 
 def test_known_answer_riemann():

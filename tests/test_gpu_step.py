@@ -6,7 +6,7 @@ import torch
 
 import oracle as O
 import phd_code_gb300 as pkg
-from _util import FP64_TOL, lattice_mesh, rel_rows, smooth_state
+from _util import FP64_TOL, lattice_mesh, assert_parity, rel_rows, smooth_state
 
 pytestmark = pytest.mark.gpu
 
@@ -37,9 +37,9 @@ def test_fused_step_matches_oracle(boundary, n_side, solver, moving):
         got.append(st.read_clock().dt)
         st.step(1)
     st.check_status()
-    assert rel_rows(np.array(got), dts) <= FP64_TOL
-    assert rel_rows(st.prim_host(), p_ref) <= FP64_TOL
-    assert rel_rows(st.cons_host(), c_ref) <= FP64_TOL
+    assert_parity(np.array(got), dts)
+    assert_parity(st.prim_host(), p_ref)
+    assert_parity(st.cons_host(), c_ref)
 
 
 @pytest.mark.parametrize("limiter", ["arepo", "tess"])
@@ -50,7 +50,7 @@ def test_fused_step_options(limiter, boost):
     p_ref, c_ref, _ = run_oracle(m, prim, "hllc", 3, limiter=0 if limiter == "arepo" else 1, boost=boost)
     st = pkg.FluxStepper(m, prim, solver="hllc", limiter=limiter, boost=boost)
     st.step(3)
-    assert rel_rows(st.prim_host(), p_ref) <= FP64_TOL
+    assert_parity(st.prim_host(), p_ref)
 
 
 def test_constant_reconstruction_step():
@@ -59,7 +59,7 @@ def test_constant_reconstruction_step():
     p_ref, _, _ = run_oracle(m, prim, "hllc", 3, reconstruction="constant")
     st = pkg.FluxStepper(m, prim, solver="hllc", reconstruction="constant")
     st.step(3)
-    assert rel_rows(st.prim_host(), p_ref) <= FP64_TOL
+    assert_parity(st.prim_host(), p_ref)
 
 
 def test_sod_reflective_many_steps():
@@ -69,7 +69,7 @@ def test_sod_reflective_many_steps():
     st = pkg.FluxStepper(m, prim, solver="hllc")
     st.step(20)
     st.check_status()
-    assert rel_rows(st.prim_host(), p_ref) <= FP64_TOL
+    assert_parity(st.prim_host(), p_ref)
 
 
 def test_graph_replay_equals_eager_and_is_deterministic():

@@ -21,7 +21,7 @@ from phd_code_gb300.device import DeviceMesh
 from phd_code_gb300.meshgen import HostMesh
 from phd_code_gb300.step import FluxStepper
 from phd_code_gb300.twins import periodic_twins
-from _util import FP64_TOL, lattice_mesh, rel_rows, smooth_state
+from _util import FP64_TOL, lattice_mesh, assert_parity, rel_rows, smooth_state
 
 pytestmark = pytest.mark.gpu
 
@@ -122,8 +122,8 @@ def test_load_mesh_fp64_continues_like_the_oracle(boundary):
     assert st.dmesh.upload_errors() == 0
     c, p = _oracle_replay(meshes, prim, 1.4)
     nr = m.n_real
-    assert rel_rows(st.cons_host()[:, :nr], c[:, :nr]) <= FP64_TOL
-    assert rel_rows(st.prim_host(), p) <= FP64_TOL
+    assert_parity(st.cons_host()[:, :nr], c[:, :nr])
+    assert_parity(st.prim_host(), p)
 
 
 def test_load_mesh_fp32_conserves_and_tracks_fp64():
@@ -206,8 +206,8 @@ def test_load_mesh_with_changing_counts_fp64_follows_the_oracle(boundary):
     assert st.dmesh.upload_errors() == 0
     c, p = _oracle_replay(meshes, prim, 1.4)
     nr = meshes[0].n_real
-    assert rel_rows(st.cons_host()[:, :nr], c[:, :nr]) <= FP64_TOL
-    assert rel_rows(st.prim_host(), p) <= FP64_TOL
+    assert_parity(st.cons_host()[:, :nr], c[:, :nr])
+    assert_parity(st.prim_host(), p)
 
 
 def test_load_mesh_with_changing_counts_fp32_conserves_and_replays():

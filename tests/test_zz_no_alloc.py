@@ -82,3 +82,21 @@ def test_noalloc_adjoint_refuses_meshes_beyond_its_array():
     rc = lib.phd_adjoint_step_f64_noalloc(ctypes.byref(big), None, None, 1e-3, None, None, None, None, None, None,
                                           L.stream_handle())
     assert rc == L.PHD_ERR_SCRATCH_TOO_SMALL
+
+
+def test_noalloc_adjoint_size_limit_is_exact():
+    """A mesh whose work space is exactly the array's size is accepted (the call then
+    fails only its argument check, here a missing index table); one face more is
+    refused before anything runs."""
+    lib = L.lib()
+    m = L.PhdMesh()
+    m.dim, m.n_cells, m.n_real, m.n_faces = 2, 49712, 49712, 100002    # 32 F + 20 n == the array
+    assert lib.phd_adjoint_work_doubles(m.n_cells, m.n_faces) == L.ADJ_NOALLOC_MAX_DOUBLES
+    rc = lib.phd_adjoint_step_f64_noalloc(ctypes.byref(m), None, None, 1e-3, None, None, None, None, None, None,
+                                          L.stream_handle())
+    assert rc == L.PHD_ERR_ARG
+    m.n_faces += 1
+    assert lib.phd_adjoint_work_doubles(m.n_cells, m.n_faces) == L.ADJ_NOALLOC_MAX_DOUBLES + 32
+    rc = lib.phd_adjoint_step_f64_noalloc(ctypes.byref(m), None, None, 1e-3, None, None, None, None, None, None,
+                                          L.stream_handle())
+    assert rc == L.PHD_ERR_SCRATCH_TOO_SMALL
