@@ -544,8 +544,16 @@ def adjoint_cost(dev, n_side=128, n_steps=200, checkpoint=20, n_dirs=16, h=1e-6,
     fd_rows = []
     with torch.no_grad():
         L0 = float(loss_of(p0.detach()))
+        # the same differences through the branch-frozen forward (every limiter
+        # selection, GIZMO clamp, positivity revert, wave-speed estimate and Riemann
+        # region of the run from p0 replayed): the derivative on the branch the run takes
+        L0f = float(((run.final_density_frozen(p0.detach(), record=True) - target) ** 2).sum())
+
+        def frozen(pp):
+            return float(((run.final_density_frozen(pp) - target) ** 2).sum())
         for _ in range(n_dirs):
             d = torch.as_tensor(drng.standard_normal((4, nr))).to(dev)
+            d = d / torch.linalg.norm(d)               # unit direction: the step is h
             gd = float((g * d).sum())
             row = {"gd": gd}
             for tag, hh in (("h", h), ("h_small", h_small)):
@@ -553,12 +561,33 @@ def adjoint_cost(dev, n_side=128, n_steps=200, checkpoint=20, n_dirs=16, h=1e-6,
                 fd = (Lp - Lm) / (2 * hh)
                 row[tag] = {"rel_err": abs(fd - gd) / max(abs(gd), 1e-300),
                             "one_sided_spread": abs((Lp - L0) - (L0 - Lm)) / hh / max(abs(gd), 1e-300)}
+            for tag, hh in (("frozen_h", h), ("frozen_h10", 10 * h), ("frozen_h100", 100 * h)):
+                Lp, Lm = frozen(p0.detach() + hh * d), frozen(p0.detach() - hh * d)
+                fd = (Lp - Lm) / (2 * hh)
+                row[tag] = {"rel_err": abs(fd - gd) / max(abs(gd), 1e-300), "fd": fd}
             fd_rows.append(row)
     return {"config": "gaussian bump %dx%d periodic, HLLC, FP64, CFL 0.4, %d steps, checkpoint every %d; start = "
                       "background + %g noise" % (n_side, n_side, n_steps, checkpoint, noise),
             "forward_ms": fwd, "backward_ms": bwd, "ratio": bwd / fwd,
             "forward_step_ms": fwd / n_steps, "adjoint_step_ms": adj_step, "step_ratio": adj_step * n_steps / fwd,
             "fd_check": {"directions": n_dirs, "h": h, "h_small": h_small,
+                         "max_rel_err_frozen_h": max((r["frozen_h"]["rel_err"] for r in fd_rows), default=None),
+                         "median_rel_err_frozen_h": float(np.median([r["frozen_h"]["rel_err"] for r in fd_rows]))
+                         if fd_rows else None,
+                         "frozen_loss_vs_forward_loss": abs(L0f - L0) / max(abs(L0), 1e-300),
+                         "normwise_rel_err_frozen_h": float(np.sqrt(sum((r["frozen_h"]["fd"] - r["gd"]) ** 2
+                                                                        for r in fd_rows) /
+                                                                    max(sum(r["gd"] ** 2 for r in fd_rows), 1e-300)))
+                         if fd_rows else None,
+                         "max_abs_err_frozen_h": max((abs(r["frozen_h"]["fd"] - r["gd"]) for r in fd_rows),
+                                                     default=None),
+                         "max_abs_directional_derivative": max((abs(r["gd"]) for r in fd_rows), default=None),
+                         "max_rel_err_frozen_10h": max((r["frozen_h10"]["rel_err"] for r in fd_rows), default=None),
+                         "max_rel_err_frozen_100h": max((r["frozen_h100"]["rel_err"] for r in fd_rows), default=None),
+                         "directions_are": "unit vectors (seeded normal draws divided by their norm)",
+                         "frozen": "central differences through phd_step_f64_frozen replaying the decisions "
+                                   "(limiter selections, GIZMO clamps, positivity reverts, wave-speed estimate, "
+                                   "Riemann region) recorded on the run from p0",
                          "max_rel_err_h": max((r["h"]["rel_err"] for r in fd_rows), default=None),
                          "max_rel_err_h_small": max((r["h_small"]["rel_err"] for r in fd_rows), default=None),
                          "median_rel_err_h_small": float(np.median([r["h_small"]["rel_err"] for r in fd_rows]))

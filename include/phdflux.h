@@ -195,6 +195,27 @@ int phd_step_f64_taped(const phd_mesh *mesh, const phd_params *par, int32_t movi
                        double *flux, double *tape_f64, int32_t *tape_i32, phd_clock *clk,
                        cudaStream_t stream);
 
+/* The FP64 step of a static mesh (phd_step_f64 with moving = 0) with its branch
+ * decisions recorded (mode PHD_FROZEN_RECORD) or replayed (PHD_FROZEN_REPLAY): for
+ * checking the adjoint against central finite differences on the branch a run takes.
+ * No reference counterpart (the reference has no adjoint).  RECORD computes the
+ * ordinary step and writes the limiter's selections (tape_f64 / tape_i32, the rows of
+ * phd_gradients_f64_taped) and 64 decision bits per face into face_bits [F]: the GIZMO
+ * clamps, minima and sign tests, the spatial and temporal positivity reverts, the
+ * sound-speed floors, the pressure estimate's branch, the shock / rarefaction tests and
+ * the Riemann region.  REPLAY does the same arithmetic with every decision read back
+ * (tape_f64 unused), so near the recorded state the step is the smooth map the adjoint
+ * differentiates.  dt is the step's (host) time step, held fixed; prim is overwritten
+ * with the next primitives, cons_next receives the next totals (all cells), flux the
+ * face fluxes.  HLL / HLLC with the AREPO limiter or constant reconstruction (else
+ * PHD_ERR_UNSUPPORTED). */
+#define PHD_FROZEN_RECORD 0
+#define PHD_FROZEN_REPLAY 1
+int phd_step_f64_frozen(const phd_mesh *mesh, const phd_params *par, int32_t mode, double dt, double *prim,
+                        const double *cons, double *cons_next, double *grad, const double *face_w, double *flux,
+                        double *tape_f64, int32_t *tape_i32, uint64_t *face_bits, phd_clock *clk,
+                        cudaStream_t stream);
+
 /* ---- fused FP32 step (FP32 reconstruction / Riemann, FP64 conserved totals) --------
  * Mesh-relative FP32 geometry, formed once per mesh by phd_prepare_f32 (the
  * cancelling differences in FP64, each rounded once to FP32):

@@ -22,6 +22,7 @@ PREP_FACES, PREP_CELLS, PREP_LISTS, PREP_ALL, PREP_CELLS_FROM_FACES, PREP_RECORD
 CONSTANT, LINEAR = 0, 1
 LIMITER_AREPO, LIMITER_TESS = 0, 1
 STAGE_SPATIAL, STAGE_TEMPORAL = 1, 2
+FROZEN_RECORD, FROZEN_REPLAY = 0, 1
 
 STATUS_MESSAGES = {
     STATUS_NEG_MASS: "Mass less than zero in flux update",
@@ -138,6 +139,7 @@ SIGNATURES = {
     "phd_load_mesh_f32": ([_PM, C.POINTER(PhdHandover32), C.POINTER(PhdParams), C.POINTER(PhdGeom32Out), _vp, _vp,
                            _vp, _vp, _vp, _vp], C.c_int),
     "phd_periodic_twins": ([_PM, _i32, _f64, _f64, _vp, _vp], C.c_int),
+    "phd_step_f64_frozen": ([_PM, _PP, _i32, _f64, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], C.c_int),
 }
 
 

@@ -227,6 +227,52 @@ class FluxRunRecord:
         L.raise_status(st)
         return UT
 
+    # --- branch-frozen forward (finite differences on the branch the run takes) ----
+    def forward_frozen(self, U0, record):
+        """U_T from U0 through phd_step_f64_frozen.  With ``record`` the run from U0 is
+        the ordinary forward, and every step's limiter selections and face decisions are
+        written to this run's tapes; without it they are read back, so U0 -> U_T is the
+        smooth map of the recorded run's branches, whose derivative the adjoint
+        computes -- central differences through it check the adjoint even where the
+        limited scheme itself has kinks within the difference step."""
+        lib = L.lib()
+        if record or getattr(self, "_frozen", None) is None:
+            if not record:
+                raise RuntimeError("forward_frozen: record a run before replaying it")
+            self._frozen = []
+            for rec in self.steps:
+                dm = rec.dmesh
+                self._frozen.append((torch.empty((L.GRAD_TAPE_F64_ROWS, dm.n_cells), dtype=F64, device=self.device),
+                                     torch.empty((L.GRAD_TAPE_I32_ROWS, dm.n_cells), dtype=torch.int32,
+                                                 device=self.device),
+                                     torch.zeros(max(dm.n_faces, 1), dtype=torch.int64, device=self.device)))
+        self.clock.set(dt=self.steps[0].dt)
+        mode = L.FROZEN_RECORD if record else L.FROZEN_REPLAY
+        prev = None
+        for k, rec in enumerate(self.steps):
+            dm = rec.dmesh
+            b = self._buffers(dm)
+            if prev is None:
+                self._load_real(dm, U0, b.cons, b.prim)
+            elif prev is not b:
+                self._load_real(dm, prev.cons[:, :dm.n_real], b.cons, b.prim)
+            tf, ti, fb = self._frozen[k]
+            L.check(lib.phd_step_f64_frozen(dm.ref, ctypes.byref(self.params), mode, rec.dt, L.ptr(b.prim),
+                                            L.ptr(b.cons), L.ptr(b.nxt), L.ptr(b.grad), L.ptr(rec.face_w),
+                                            L.ptr(b.flux), L.ptr(tf), L.ptr(ti), L.ptr(fb), self.clock.ptr,
+                                            L.stream_handle()), "phd_step_f64_frozen")
+            b.cons, b.nxt = b.nxt, b.cons
+            prev = b
+        self.clock.check_status()
+        return prev.cons[:, :self.steps[-1].dmesh.n_real].clone()
+
+    def final_density_frozen(self, prim0, record=False):
+        """Final densities [n_real] from the real cells' initial primitives through the
+        branch-frozen forward (see forward_frozen)."""
+        vol0 = self.steps[0].dmesh.vol[:self.n_real]
+        U0 = cons_from_prim_t(prim0, vol0, self.params.gamma)
+        return self.forward_frozen(U0.contiguous(), record)[0] / self.final_vol
+
     def _replay_segment(self, a, b):
         """Recompute the all-cell states (totals, primitives, gradients and the
         gradients' limiter tape) entering steps a..b-1 from the checkpoint at a."""

@@ -9,7 +9,9 @@ shared library exporting the C ABI of ``include/phdflux.h``:
   division and square root (``--use_fast_math`` touches FP32 only);
 * ``phd_util.cu`` mesh-preparation kernels;
 * ``phd_adj.cu``  hand-written adjoint of the FP64 step, ``--fmad=false`` so its
-  recomputed forward branches are those of the forward kernels.
+  recomputed forward branches are those of the forward kernels;
+* ``phd_frozen.cu`` the FP64 step with its branch decisions recorded / replayed (the
+  finite-difference check of the adjoint), ``--fmad=false`` like the forward.
 
 The host tessellation ``phd_tess2d.cpp`` (C ABI of ``include/phdtess.h``) is a plain
 C++ library, ``libphdtess.so``, built with the host compiler and
@@ -36,6 +38,7 @@ UNITS = {
     "phd_f32.cu": ["--use_fast_math"],
     "phd_util.cu": [],
     "phd_adj.cu": ["--fmad=false"],
+    "phd_frozen.cu": ["--fmad=false"],
 }
 
 
