@@ -601,7 +601,7 @@ def run_e2e(args, st, mesh, prim, dev):
     """The same step through the public API with host buffers: every step the host
     hands over its tessellation from pinned memory with FluxStepper.load_mesh -- for
     FP32 the compact hand-over (per-cell face ranges, pair-j, FP32 area and centroid
-    offset: 16 B per face, plus the ghost map and ghost codes; the real cells' positions
+    offset along the face: 12 B per face, plus the ghost map and ghost codes; the real cells' positions
     are the device's own, as after its generator move), for FP64 the full one (pair-i/j,
     FP64 area and centroid, x, dcom, vol, map) -- which forms the neighbour lists, ghost
     positions, flip bits, periodic twins and FP32 geometry on the device, re-creates the

@@ -300,19 +300,23 @@ int phd_ghost_positions(const phd_mesh *mesh, const int8_t *ghost_code, double x
                         double xmax1, int32_t *bad, cudaStream_t stream);
 
 /* Compact FP32 hand-over of a re-mesh (the per-step upload of the face list,
- * mesh.pyx:255-323, in 16 B per face instead of 32): the host sends pair-j, the area
- * and the centroid offset com - (x_i + x_j)/2 (formed in FP64) rounded once to FP32,
- * and pair-i as per-real-cell face ranges.
+ * mesh.pyx:255-323, in 12 B per face instead of 32): the host sends pair-j, the area
+ * and the centroid offset along the face rounded once to FP32, and pair-i as
+ * per-real-cell face ranges.  The offset: with (dx, dy) = x_j - x_i, r = sqrt(dx dx +
+ * dy dy) and c = com - (x_i + x_j)/2, all in FP64 with each operation rounded
+ * separately (no fused multiply-add), s = (c_x (-dy) + c_y dx) / r, 0 where r = 0 (c
+ * lies along the face: a Voronoi face is on the perpendicular bisector of x_i x_j).
  *
  * phd_pair_i_from_face_ptr: pair_i[m] = c for m in [face_ptr[c], face_ptr[c+1]);
  * face_ptr (n_real + 1 entries) must start at 0, end at n_faces and not decrease --
  * each real cell whose range breaks that adds 1 to *bad (device) and writes nothing.
  * phd_prepare_f32_faces_compact: out->face_geo / face_ar as PHD_PREP_FACES forms them,
- * from area32 [F] and crel32 [F][2] instead of mesh->area / com (needs pair ids and
- * x); the values equal PHD_PREP_FACES's bit for bit. */
+ * from area32 [F] and ct32 [F] (the offsets s) instead of mesh->area / com (needs pair
+ * ids and x); the values equal PHD_PREP_FACES's bit for bit (both form the FP32 offset
+ * as s times the FP32 face tangent). */
 int phd_pair_i_from_face_ptr(const phd_mesh *mesh, const int32_t *face_ptr, int32_t *pair_i, int32_t *bad,
                              cudaStream_t stream);
-int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, const float *crel32,
+int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, const float *ct32,
                                   phd_geom32_out *out, cudaStream_t stream);
 
 /* One hand-over of a re-mesh to an FP32 stepper in one call: the host tessellation of
@@ -340,7 +344,7 @@ typedef struct phd_handover32 {
     const int32_t *face_ptr;      /* [n_real + 1] faces of each real cell */
     const int32_t *pair_j;        /* [n_faces] */
     const float *area32;          /* [n_faces] face areas, FP32 */
-    const float *crel32;          /* [n_faces][2] centroid - (x_i + x_j)/2, FP32 */
+    const float *ct32;            /* [n_faces] centroid offset along the face, FP32 (see above) */
     const int32_t *ghost_map;     /* [n_cells - n_real] images of the ghosts; NULL: mesh->map holds them */
     const int8_t *ghost_code;     /* [n_cells - n_real] phd_ghost_positions codes (with x == NULL) */
     const double *x;              /* [2][n_cells] every position; NULL: real rows from x_real, ghost
@@ -351,7 +355,7 @@ typedef struct phd_handover32 {
     const int8_t *type;           /* [n_cells] particle types (the flip bits' Exterior test) */
     int32_t *d_face_ptr;          /* [n_real + 1] staging */
     float *d_area32;              /* [n_faces] staging */
-    float *d_crel32;              /* [n_faces][2] staging */
+    float *d_ct32;                /* [n_faces] staging */
     int8_t *d_ghost_code;         /* [n_cells - n_real] staging (with x == NULL) */
     int32_t *twin;                /* [n_faces] periodic twin table */
     int32_t *csr_work;            /* phd_csr_work_ints(n_cells) */

@@ -96,8 +96,8 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
 /* The last phd_mesh2d_build result as the flux path's compact FP32 hand-over
  * (phd_pair_i_from_face_ptr / phd_prepare_f32_faces_compact of phdflux.h): per-real-cell
  * face ranges face_ptr[n_real + 1], pair_j[n_faces], the area and the centroid offset
- * com - (x_i + x_j)/2 (formed in FP64) rounded to FP32 -- area32[n_faces],
- * crel32[n_faces][2] -- and the cells' positions x[2][n_cells] (x row then y row), image
+ * along the face (formed in FP64 as phdflux.h's compact hand-over states) rounded to
+ * FP32 -- area32[n_faces], ct32[n_faces] -- and the cells' positions x[2][n_cells] (x row then y row), image
  * map, tags (Real 0 / Ghost 1) and types (Undefined 4 for real cells, Exterior 2 for
  * ghosts), written into caller buffers (e.g. pinned host memory reused across steps).
  * x may be NULL (the device already holds the real cells' positions, e.g. from its own
@@ -106,7 +106,7 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
  * (phd_ghost_positions of phdflux.h): 1 + 3 (sx + 1) + (sy + 1) for a periodic copy
  * shifted by (sx, sy) box lengths, 16 + 2 k + h for a mirror image across axis k at its
  * low (h = 0) or high (h = 1) wall. */
-int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *crel32,
+int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *ct32,
                             double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code);
 
 /* hilbert_key_2d (phd/hilbert/hilbert.pyx:9-23) for n integer coordinate pairs. */

@@ -78,8 +78,8 @@ class PhdGeom32Out(C.Structure):
 
 class PhdHandover32(C.Structure):
     """phd_handover32: one compact re-mesh hand-over to an FP32 stepper (phd_load_mesh_f32)."""
-    _fields_ = [(nm, C.c_void_p) for nm in ("face_ptr", "pair_j", "area32", "crel32", "ghost_map", "ghost_code", "x",
-                                            "x_real", "type", "d_face_ptr", "d_area32", "d_crel32", "d_ghost_code",
+    _fields_ = [(nm, C.c_void_p) for nm in ("face_ptr", "pair_j", "area32", "ct32", "ghost_map", "ghost_code", "x",
+                                            "x_real", "type", "d_face_ptr", "d_area32", "d_ct32", "d_ghost_code",
                                             "twin", "csr_work", "bad")] + \
         [("periodic", C.c_int32), ("dedup_periodic", C.c_int32), ("xmin", C.c_double * 2), ("xmax", C.c_double * 2)]
 

@@ -53,36 +53,57 @@ __device__ __forceinline__ void face_normal32(float fx, float fy, float &r, floa
     ny = __fmul_rn(fy, inv);
 }
 
+// The face centroid's offset from the generator midpoint, c = com - (x_i + x_j)/2,
+// lies along the face (a Voronoi face is on the perpendicular bisector of x_i x_j), so
+// one number carries it: s = c . t, t = (-n_y, n_x), formed in FP64 with every
+// rounding spelled out --
+//   dx = x_j - x_i, r = sqrt(dx.dx), s = (c_x (-dy) + c_y dx) / r --
+// exactly as the host forms it for the compact hand-over, and rounded once to FP32.
+// The FP32 offset is then s t with t from the FP32 normal of the rounded separation,
+// in both hand-overs, so their FP32 geometry is the same bit for bit.
+__device__ __forceinline__ double face_offset_f64(double xi, double yi, double xj, double yj, double comx,
+                                                  double comy) {
+    const double dx = __dsub_rn(xj, xi), dy = __dsub_rn(yj, yi);
+    const double cx = __dsub_rn(comx, __dmul_rn(0.5, __dadd_rn(xi, xj)));
+    const double cy = __dsub_rn(comy, __dmul_rn(0.5, __dadd_rn(yi, yj)));
+    const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+    return r > 0.0 ? __ddiv_rn(__dadd_rn(__dmul_rn(cx, -dy), __dmul_rn(cy, dx)), r) : 0.0;
+}
+
+__device__ __forceinline__ float2 face_offset32(float s, float nx, float ny) {
+    return make_float2(__fmul_rn(s, -ny), __fmul_rn(s, nx));
+}
+
 __global__ void k_prepare_faces32(phd_mesh M, float4 *__restrict__ face_geo, float2 *__restrict__ face_ar) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M.n_faces) return;
     const int n = M.n_cells, F = M.n_faces;
     const int i = M.pair_i[m], j = M.pair_j[m];
-    double dx = 0, dy = 0, cx = 0, cy = 0;
+    double dx = 0, dy = 0, sc = 0;
     if (i >= 0 && i < n && j >= 0 && j < n) {
         const double xi = M.x[i], yi = M.x[(size_t)n + i], xj = M.x[j], yj = M.x[(size_t)n + j];
         dx = xj - xi;
         dy = yj - yi;
-        cx = M.com[m] - 0.5 * (xi + xj);
-        cy = M.com[(size_t)F + m] - 0.5 * (yi + yj);
+        sc = face_offset_f64(xi, yi, xj, yj, M.com[m], M.com[(size_t)F + m]);
     }
     const float fx = narrow_f64(dx), fy = narrow_f64(dy);
     float r, nx, ny;                // n = (x_j - x_i)/|x_j - x_i| (tess.cpp:367-369)
     face_normal32(fx, fy, r, nx, ny);
+    const float2 c = face_offset32(narrow_f64(sc), nx, ny);
     if (M.normal) {
         nx = narrow_f64(M.normal[m]);
         ny = narrow_f64(M.normal[(size_t)F + m]);
     }
-    face_geo[m] = make_float4(nx, ny, narrow_f64(cx), narrow_f64(cy));
+    face_geo[m] = make_float4(nx, ny, c.x, c.y);
     face_ar[m] = make_float2(narrow_f64(M.area[m]), r);
 }
 
 // The same face geometry from the compact FP32 hand-over: the host rounds the area and
-// the centroid offset com - (x_i + x_j)/2 (formed in FP64 as above) once to FP32, so
-// the face record crosses the link in 16 bytes (pair-j, area, offset) instead of 32;
+// the centroid offset along the face (face_offset_f64) once to FP32, so the face
+// record crosses the link in 12 bytes (pair-j, area, offset) instead of 32;
 // separations and normals still come from the FP64 positions.
 __global__ void k_prepare_faces32_compact(phd_mesh M, const float *__restrict__ area32,
-                                          const float2 *__restrict__ crel32, float4 *__restrict__ face_geo,
+                                          const float *__restrict__ ct32, float4 *__restrict__ face_geo,
                                           float2 *__restrict__ face_ar) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M.n_faces) return;
@@ -96,7 +117,7 @@ __global__ void k_prepare_faces32_compact(phd_mesh M, const float *__restrict__ 
     const float fx = narrow_f64(dx), fy = narrow_f64(dy);
     float r, nx, ny;
     face_normal32(fx, fy, r, nx, ny);
-    const float2 c = crel32[m];
+    const float2 c = face_offset32(ct32[m], nx, ny);
     face_geo[m] = make_float4(nx, ny, c.x, c.y);
     face_ar[m] = make_float2(area32[m], r);
 }
@@ -1159,14 +1180,14 @@ int phd_prepare_f32_parts(const phd_mesh *mesh, const int32_t *twin, phd_geom32_
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
 
-int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, const float *crel32,
+int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, const float *ct32,
                                   phd_geom32_out *out, cudaStream_t stream) {
     phd::NvtxRange nvtx_range("phd_prepare_f32_faces_compact");
     if (!mesh || mesh->dim != 2 || !out || !out->face_geo || !out->face_ar) return PHD_ERR_ARG;
-    if (mesh->n_faces && (!area32 || !crel32 || !mesh->pair_i || !mesh->pair_j || !mesh->x)) return PHD_ERR_ARG;
+    if (mesh->n_faces && (!area32 || !ct32 || !mesh->pair_i || !mesh->pair_j || !mesh->x)) return PHD_ERR_ARG;
     if (mesh->n_faces)
         k_prepare_faces32_compact<<<g32(mesh->n_faces), B32, 0, stream>>>(
-            *mesh, area32, reinterpret_cast<const float2 *>(crel32), reinterpret_cast<float4 *>(out->face_geo),
+            *mesh, area32, ct32, reinterpret_cast<float4 *>(out->face_geo),
             reinterpret_cast<float2 *>(out->face_ar));
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }

@@ -1063,9 +1063,9 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
     return 0;
 }
 
-int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *crel32,
+int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *ct32,
                             double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
-    if (!t || t->G.n_cells == 0 || !face_ptr || !pair_j || !area32 || !crel32 || !map || !tag || !type)
+    if (!t || t->G.n_cells == 0 || !face_ptr || !pair_j || !area32 || !ct32 || !map || !tag || !type)
         return -2;
     const Geometry &G = t->G;
     const int nr = G.n_real, n = G.n_cells, F = G.n_faces;
@@ -1081,8 +1081,12 @@ int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pai
         while (c < i) face_ptr[++c] = f;
         pair_j[f] = j;
         area32[f] = round32(G.area[f]);
-        crel32[2 * size_t(f)] = round32(G.comx[f] - 0.5 * (G.x[i] + G.x[j]));
-        crel32[2 * size_t(f) + 1] = round32(G.comy[f] - 0.5 * (G.y[i] + G.y[j]));
+        // the centroid offset along the face (phdflux.h, compact hand-over): built with
+        // -ffp-contract=off, so every operation rounds as the device's does
+        const double dx = G.x[j] - G.x[i], dy = G.y[j] - G.y[i];
+        const double cx = G.comx[f] - 0.5 * (G.x[i] + G.x[j]), cy = G.comy[f] - 0.5 * (G.y[i] + G.y[j]);
+        const double r = std::sqrt(dx * dx + dy * dy);
+        ct32[f] = round32(r > 0.0 ? (cx * (-dy) + cy * dx) / r : 0.0);
     }
     while (c < nr) face_ptr[++c] = F;
     if (x) {

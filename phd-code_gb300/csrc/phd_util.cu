@@ -531,7 +531,7 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
         return PHD_ERR_ARG;
     if (!mesh->pair_i || !mesh->pair_j || !mesh->map || !mesh->x || !mesh->flip || !mesh->nbr_ptr || !mesh->nbr_idx)
         return PHD_ERR_ARG;
-    if (!h->face_ptr || !h->pair_j || !h->area32 || !h->crel32 || !h->d_face_ptr || !h->d_area32 || !h->d_crel32 ||
+    if (!h->face_ptr || !h->pair_j || !h->area32 || !h->ct32 || !h->d_face_ptr || !h->d_area32 || !h->d_ct32 ||
         !h->type || !h->twin || !h->csr_work || !h->bad || !(h->xmax[0] > h->xmin[0]) || !(h->xmax[1] > h->xmin[1]))
         return PHD_ERR_ARG;
     const int n = mesh->n_cells, nr = mesh->n_real, F = mesh->n_faces, ng = n - nr;
@@ -568,11 +568,10 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     // second half is in flight
     const int F0 = F / 2;
     PHD_TRY_CUDA(cudaMemcpyAsync(h->d_area32, h->area32, (size_t)F0 * sizeof(float), H2D, stream));
-    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_crel32, h->crel32, (size_t)F0 * 2 * sizeof(float), H2D, stream));
+    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_ct32, h->ct32, (size_t)F0 * sizeof(float), H2D, stream));
     PHD_TRY_CUDA(cudaEventRecord(events[7], stream));
     PHD_TRY_CUDA(cudaMemcpyAsync(h->d_area32 + F0, h->area32 + F0, (size_t)(F - F0) * sizeof(float), H2D, stream));
-    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_crel32 + 2 * (size_t)F0, h->crel32 + 2 * (size_t)F0,
-                                 (size_t)(F - F0) * 2 * sizeof(float), H2D, stream));
+    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_ct32 + F0, h->ct32 + F0, (size_t)(F - F0) * sizeof(float), H2D, stream));
     PHD_TRY_CUDA(cudaEventRecord(events[2], stream));
 
     // lists stream, while the face records are in flight: pair-i with the list counts,
@@ -630,7 +629,7 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
         po.face_ar += 2 * (size_t)m0;
         PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[half ? 2 : 7], 0));
         if (cnt > 0)
-            PHD_TRY(phd_prepare_f32_faces_compact(&part, h->d_area32 + m0, h->d_crel32 + 2 * (size_t)m0, &po, geom));
+            PHD_TRY(phd_prepare_f32_faces_compact(&part, h->d_area32 + m0, h->d_ct32 + m0, &po, geom));
     }
     PHD_TRY_CUDA(cudaEventRecord(events[4], geom));
 

@@ -165,11 +165,12 @@ class DeviceMesh:
         return code.astype(np.int8)
 
     def pinned_host_compact(self, host, resident=False):
-        """The compact hand-over of a re-mesh for the FP32 path, 16 B per face instead of
+        """The compact hand-over of a re-mesh for the FP32 path, 12 B per face instead of
         32: per-real-cell face ranges ``face_ptr`` instead of pair-i (faces are emitted
         per real cell in ascending order, tess.cpp:363), pair-j, and the area and the
-        centroid offset com - (x_i + x_j)/2 -- formed in FP64 as the device would --
-        rounded once to FP32 (round to nearest even; magnitudes below 2^-126 to signed
+        centroid offset along the face, s = (c . (-dy, dx)) / r with c = com - (x_i +
+        x_j)/2, (dx, dy) = x_j - x_i, r = |x_j - x_i| -- formed in FP64 with the device's
+        operations, each rounded separately -- rounded once to FP32 (round to nearest even; magnitudes below 2^-126 to signed
         zero, as the device's own rounding does), plus the cells' positions and maps.
         The FP32 face geometry formed from it equals the full hand-over's bit for bit.
         ``resident``: the device already holds the real cells' positions (its own
@@ -181,7 +182,12 @@ class DeviceMesh:
             raise ValueError("faces must be emitted per real cell in ascending cell order")
         face_ptr = np.searchsorted(pi, np.arange(nr + 1)).astype(np.int32)
         x = np.asarray(host.x, dtype=np.float64)
-        c64 = np.asarray(host.com, dtype=np.float64) - 0.5 * (x[:, pi] + x[:, pj])
+        com = np.asarray(host.com, dtype=np.float64)
+        dx, dy = x[0, pj] - x[0, pi], x[1, pj] - x[1, pi]
+        cx, cy = com[0] - 0.5 * (x[0, pi] + x[0, pj]), com[1] - 0.5 * (x[1, pi] + x[1, pj])
+        r = np.sqrt(dx * dx + dy * dy)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            s64 = np.where(r > 0.0, (cx * (-dy) + cy * dx) / r, 0.0)
 
         def round32(a):
             out = a.astype(np.float32)
@@ -189,7 +195,7 @@ class DeviceMesh:
 
         arrays = {"face_ptr": face_ptr, "pair_j": np.ascontiguousarray(pj, dtype=np.int32),
                   "area32": round32(np.asarray(host.area, dtype=np.float64)),
-                  "crel32": np.ascontiguousarray(round32(c64).T),
+                  "ct32": round32(s64),
                   "map": np.ascontiguousarray(host.map, dtype=np.int32),
                   "tag": np.ascontiguousarray(host.tag, dtype=np.int8),
                   "type": np.ascontiguousarray(host.type, dtype=np.int8)}
@@ -210,9 +216,9 @@ class DeviceMesh:
                   "x": (self.dim, self.n_cells), "dcom": (self.dim, self.n_cells), "vol": (self.n_cells,),
                   "pair_i": (self.n_faces,), "pair_j": (self.n_faces,), "area": (self.n_faces,),
                   "com": (self.dim, self.n_faces), "face_ptr": (self.n_real + 1,), "area32": (self.n_faces,),
-                  "crel32": (self.n_faces, self.dim), "ghost_code": (self.n_cells - self.n_real,)}
+                  "ct32": (self.n_faces,), "ghost_code": (self.n_cells - self.n_real,)}
         if "face_ptr" in pinned:
-            names = ("face_ptr", "pair_j", "area32", "crel32", "map", "tag", "type") + \
+            names = ("face_ptr", "pair_j", "area32", "ct32", "map", "tag", "type") + \
                 (("x",) if "x" in pinned else ("ghost_code",))
         else:
             names = [nm for nm, _ in self.UPLOAD]

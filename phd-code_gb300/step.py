@@ -184,7 +184,7 @@ class FluxStepper:
         codes and face geometry are formed on a second stream while the rest of the mesh
         is still being copied.  ``pinned`` is either the full hand-over
         (``DeviceMesh.pinned_host``) or, for FP32 steppers, the compact one
-        (``DeviceMesh.pinned_host_compact`` / ``tess.CompactMesher``: 16 B per face, pair-i
+        (``DeviceMesh.pinned_host_compact`` / ``tess.CompactMesher``: 12 B per face, pair-i
         from per-cell face ranges); a compact hand-over without positions keeps the real
         cells' positions on the device -- the last generator move's (``move_generators``)
         or the current ones -- and forms the ghosts' from their codes
@@ -281,18 +281,18 @@ class FluxStepper:
             dm.reset_errors(main)
         stage = {"face_ptr": self._view("face_ptr_in", (nr + 1,), torch.int32),
                  "area32": self._view("area32_in", (nf,), torch.float32),
-                 "crel32": self._view("crel32_in", (nf, dm.dim), torch.float32)}
+                 "ct32": self._view("ct32_in", (nf,), torch.float32)}
         if xr is not None:
             stage["ghost_code"] = self._view("ghost_code_in", (ng,), torch.int8)
         dm.set_normals("none")
         hp = lambda k: pinned[k].data_ptr() if k in pinned else None
-        h = L.PhdHandover32(face_ptr=hp("face_ptr"), pair_j=hp("pair_j"), area32=hp("area32"), crel32=hp("crel32"),
+        h = L.PhdHandover32(face_ptr=hp("face_ptr"), pair_j=hp("pair_j"), area32=hp("area32"), ct32=hp("ct32"),
                             ghost_map=None if resized else pinned["map"][nr:].data_ptr(),
                             ghost_code=hp("ghost_code") if xr is not None else None,
                             x=None if xr is not None else hp("x"),
                             x_real=xr.data_ptr() if xr is not None else None, type=dm.type.data_ptr(),
                             d_face_ptr=stage["face_ptr"].data_ptr(), d_area32=stage["area32"].data_ptr(),
-                            d_crel32=stage["crel32"].data_ptr(),
+                            d_ct32=stage["ct32"].data_ptr(),
                             d_ghost_code=stage["ghost_code"].data_ptr() if xr is not None else None,
                             twin=self.twin.data_ptr(), csr_work=dm._csr_work.data_ptr(), bad=dm._bad.data_ptr(),
                             periodic=int(dm.boundary == "periodic"), dedup_periodic=int(self.dedup_periodic),
@@ -306,8 +306,10 @@ class FluxStepper:
                                       sides, events), "phd_load_mesh_f32")
         if xr is None:
             self._x_real_valid = False
-        nbytes += 4 * (nr + 1) + 4 * nf + 12 * nf + (0 if resized else 4 * ng)
-        nbytes += ng if xr is not None else 8 * dm.dim * dm.n_cells
+        # what phd_load_mesh_f32 copied, counted from the arrays themselves
+        nb = lambda k: pinned[k].numel() * pinned[k].element_size()
+        nbytes += nb("face_ptr") + nb("pair_j") + nb("area32") + nb("ct32") + (0 if resized else 4 * ng)
+        nbytes += nb("ghost_code") if xr is not None else nb("x")
         return nbytes
 
     def _launch_step(self, marks=None):

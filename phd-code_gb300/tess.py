@@ -211,7 +211,7 @@ class CompactMesher:
         out = {"face_ptr": self._pinned("face_ptr", (n + 1,), torch.int32),
                "pair_j": self._pinned("pair_j", (F,), torch.int32),
                "area32": self._pinned("area32", (F,), torch.float32),
-               "crel32": self._pinned("crel32", (F, 2), torch.float32),
+               "ct32": self._pinned("ct32", (F,), torch.float32),
                "map": self._pinned("map", (nc,), torch.int32),
                "tag": self._pinned("tag", (nc,), torch.int8), "type": self._pinned("type", (nc,), torch.int8)}
         if self.resident:
@@ -222,7 +222,7 @@ class CompactMesher:
         def ptr(k):
             return C.c_void_p(out[k].data_ptr()) if k in out else None
 
-        _check(L.phd_mesh2d_copy_compact(self._h, *(ptr(k) for k in ("face_ptr", "pair_j", "area32", "crel32", "x",
+        _check(L.phd_mesh2d_copy_compact(self._h, *(ptr(k) for k in ("face_ptr", "pair_j", "area32", "ct32", "x",
                                                                       "map", "tag", "type", "ghost_code"))),
                "copy_compact")
         return out

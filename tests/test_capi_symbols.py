@@ -101,7 +101,7 @@ def test_argument_errors_are_rejected_on_the_host(lib):
     assert f.phd_move_generators(ctypes.byref(m), one, one, one, 1, 0.0, 0.0, 1.0, 1.0, one, None) == L.PHD_ERR_ARG
     # one-call compact hand-over: incomplete hand-over, a mesh that still carries FP64
     # normals, an empty box, ghosts without their codes
-    h = L.PhdHandover32(face_ptr=1, pair_j=1, area32=1, crel32=1, type=1, d_face_ptr=1, d_area32=1, d_crel32=1,
+    h = L.PhdHandover32(face_ptr=1, pair_j=1, area32=1, ct32=1, type=1, d_face_ptr=1, d_area32=1, d_ct32=1,
                         twin=1, csr_work=1, bad=1, periodic=1, dedup_periodic=1,
                         xmin=(ctypes.c_double * 2)(0.0, 0.0), xmax=(ctypes.c_double * 2)(1.0, 1.0))
     ev = (ctypes.c_void_p * 8)(1, 1, 1, 1, 1, 1, 1, 1)
