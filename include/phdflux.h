@@ -231,7 +231,11 @@ int phd_step_f64_frozen(const phd_mesh *mesh, const phd_params *par, int32_t mod
  *                   pair-j): (w_x, w_y, t_x, t_y), w = (area/r) c + sigma (area/2) n the
  *                   gradient weight, t = c + sigma (r/2) n the face centroid minus the
  *                   generator (r = |x_j - x_i|); the gradient kernel reads its geometry in
- *                   list order through it (PHD_PREP_RECORDS)
+ *                   list order through it (PHD_PREP_RECORDS).  Optional: NULL makes the
+ *                   gradient kernel form each entry's record from its face's records
+ *                   (csr_face, face_geo, face_ar) with the same roundings, so the same
+ *                   bits -- cheaper for a mesh stepped once, dearer per step when many
+ *                   steps share one mesh
  * twin (optional, [F]): for periodic faces the reference computes twice (once from each
  * side, mesh.pyx:529-544), twin[f] = the kept copy's id for the dropped copy f, else -1;
  * both cells then exchange the same FP32 flux and the totals are conserved exactly. */
@@ -306,6 +310,9 @@ int phd_ghost_positions(const phd_mesh *mesh, const int8_t *ghost_code, double x
  * dy dy) and c = com - (x_i + x_j)/2, all in FP64 with each operation rounded
  * separately (no fused multiply-add), s = (c_x (-dy) + c_y dx) / r, 0 where r = 0 (c
  * lies along the face: a Voronoi face is on the perpendicular bisector of x_i x_j).
+ * pair-j may come packed in 2 B per face: pair_dj[f] = pair_j[f] - pair_i[f] where that
+ * lies in [1, 65535], else 0, with the faces marked 0 listed in pair_x as (face id,
+ * pair-j) pairs in ascending face id (PHD_PAIR16_ESCAPE) -- 10 B per face in all.
  *
  * phd_pair_i_from_face_ptr: pair_i[m] = c for m in [face_ptr[c], face_ptr[c+1]);
  * face_ptr (n_real + 1 entries) must start at 0, end at n_faces and not decrease --
@@ -326,23 +333,27 @@ int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, con
  * mesh->x (phd_ghost_positions) or all of mesh->x from the host, the periodic twins,
  * the FP32 list codes, face geometry and cell geometry (phd_prepare_f32_parts,
  * phd_prepare_f32_faces_compact), the flip bits (phd_flip_mask), the ghost totals
- * (phd_ghost_cons_f64) and the primitives with the next dt (phd_prim_f32_cells).
+ * (phd_ghost_cons_f64) and the primitives with the next dt (phd_prim_f32_cells), and,
+ * when out->entry_rec is not NULL, the gradient records from the same face loads.
  *
  * The copies run on `stream` with the large ones (area, centroid offset) issued right
  * after the small ones the lists need; the derivations run on side[0] (pair-i,
  * positions, neighbour lists, list codes, then the cell geometry) and side[1] (flip
  * bits, periodic twins from the face ranges, and the face geometry as soon as the face
- * records have landed, in two halves) while the copies are in flight, and are joined
+ * records have landed, in two parts) while the copies are in flight, and are joined
  * back into `stream` at the end.  events: 8 CUDA events (created by the caller, reused
  * across calls).  The mesh's own arrays (pair_i, pair_j, map
  * ghost rows, x, nbr_ptr/nbr_idx, flip) are written through the const view; mesh->normal
  * must be NULL (the FP32 geometry forms its own normals).  The counts are the mesh's:
  * a tessellation with other counts needs the arrays re-sized first.  Faces or ghosts
  * whose indices are out of range add to *bad (device; read it after the call). */
+#ifndef PHD_PAIR16_ESCAPE
+#define PHD_PAIR16_ESCAPE 0       /* also in phdtess.h */
+#endif
 typedef struct phd_handover32 {
     /* host arrays (pinned, for the copies to overlap the derivations) */
     const int32_t *face_ptr;      /* [n_real + 1] faces of each real cell */
-    const int32_t *pair_j;        /* [n_faces] */
+    const int32_t *pair_j;        /* [n_faces]; NULL: pair_dj and pair_x carry pair-j */
     const float *area32;          /* [n_faces] face areas, FP32 */
     const float *ct32;            /* [n_faces] centroid offset along the face, FP32 (see above) */
     const int32_t *ghost_map;     /* [n_cells - n_real] images of the ghosts; NULL: mesh->map holds them */
@@ -363,6 +374,12 @@ typedef struct phd_handover32 {
     int32_t periodic;             /* 1: periodic box, 0: reflective walls */
     int32_t dedup_periodic;       /* 1: periodic twin faces counted once (phd_periodic_twins) */
     double xmin[2], xmax[2];      /* the box */
+    /* packed pair-j (with pair_j == NULL; see above) */
+    const uint16_t *pair_dj;      /* [n_faces] host: pair-j minus pair-i, or PHD_PAIR16_ESCAPE */
+    const int32_t *pair_x;        /* [2 n_pair_x] host: (face id, pair-j) of the escaped faces */
+    int32_t n_pair_x;
+    uint16_t *d_pair_dj;          /* [n_faces] staging */
+    int32_t *d_pair_x;            /* [2 n_pair_x] staging */
 } phd_handover32;
 
 int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_params *par, phd_geom32_out *out,
@@ -393,8 +410,8 @@ int phd_prim_f32_batched(const phd_mesh *mesh, const phd_params *par, const doub
  * cellrec [n][16] (FP32, 32-byte aligned) the record the gradient stage writes for the
  * face stage: the cell's primitives, its limited gradient (d/dx, d/dy of rho, v_x,
  * v_y, p, the reference's grad[f*dim+k] order), dcom and generator velocity.  With
- * linear reconstruction or a moving mesh geo->entry_rec, geo->csr_nbr and cellrec are
- * required. */
+ * linear reconstruction or a moving mesh geo->csr_nbr and cellrec are required, and
+ * geo->entry_rec or else geo->face_geo, face_ar and csr_face. */
 int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *par,
                  int32_t moving, float *prim4, const double *cons, double *cons_next, float *cellrec,
                  float *w2, float *flux4, phd_clock *clk, cudaStream_t stream);

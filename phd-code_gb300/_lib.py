@@ -81,7 +81,9 @@ class PhdHandover32(C.Structure):
     _fields_ = [(nm, C.c_void_p) for nm in ("face_ptr", "pair_j", "area32", "ct32", "ghost_map", "ghost_code", "x",
                                             "x_real", "type", "d_face_ptr", "d_area32", "d_ct32", "d_ghost_code",
                                             "twin", "csr_work", "bad")] + \
-        [("periodic", C.c_int32), ("dedup_periodic", C.c_int32), ("xmin", C.c_double * 2), ("xmax", C.c_double * 2)]
+        [("periodic", C.c_int32), ("dedup_periodic", C.c_int32), ("xmin", C.c_double * 2), ("xmax", C.c_double * 2),
+         ("pair_dj", C.c_void_p), ("pair_x", C.c_void_p), ("n_pair_x", C.c_int32), ("d_pair_dj", C.c_void_p),
+         ("d_pair_x", C.c_void_p)]
 
 
 CLOCK_BYTES = C.sizeof(PhdClock)
@@ -182,9 +184,9 @@ def raise_status(status):
 
 def geom32(tensors, out=False):
     """PhdGeom32 (or PhdGeom32Out) over the FP32 geometry tensors (face_geo, face_ar,
-    csr_face, csr_nbr, cell_geo, entry_rec)."""
+    csr_face, csr_nbr, cell_geo, entry_rec); None gives a NULL pointer."""
     cls = PhdGeom32Out if out else PhdGeom32
-    return cls(*(t.data_ptr() for t in tensors))
+    return cls(*(None if t is None else t.data_ptr() for t in tensors))
 
 
 def ptr(t):

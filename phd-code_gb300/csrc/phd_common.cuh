@@ -246,4 +246,46 @@ __device__ __forceinline__ void finish_cfl(phd_clock *clk, double cfl, bool adva
 int cells_prim_f32(const phd_mesh *mesh, const phd_params *par, const phd_geom32_out *out, double *cons,
                    float *prim4, phd_clock *clk, cudaStream_t stream);
 
+// FP32 list codes of cell c's list entries [e0, e1) (face ids in idx, ascending): the
+// face id where c is pair-i, ~face id where it is pair-j, and the other cell.  Where a
+// twin table is given (periodic faces the reference computes twice, once from each
+// side), the entry of a dropped twin points at the kept face from the other side.
+// Invalid face ids give (0, c); an out-of-range other cell gives c.  Each chunk's
+// gathers are issued together.
+__device__ __forceinline__ void emit_list_codes(int c, int e0, int e1, int n, int F, const int32_t *idx,
+                                                const int32_t *__restrict__ pair_i,
+                                                const int32_t *__restrict__ pair_j,
+                                                const int32_t *__restrict__ twin, int32_t *__restrict__ csr_face,
+                                                int32_t *__restrict__ csr_nbr) {
+    constexpr int CH = 4;
+    for (int eb = e0; eb < e1; eb += CH) {
+        int fid[CH], a[CH], b[CH], t[CH];
+#pragma unroll
+        for (int k = 0; k < CH; k++) fid[k] = idx[(eb + k < e1) ? eb + k : e0];
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            const bool ok = fid[k] >= 0 && fid[k] < F;
+            a[k] = ok ? pair_i[fid[k]] : -1;
+            b[k] = ok ? pair_j[fid[k]] : -1;
+            t[k] = (ok && twin) ? twin[fid[k]] : -1;
+        }
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            const int e = eb + k;
+            if (e >= e1) break;
+            if (fid[k] < 0 || fid[k] >= F) { csr_face[e] = 0; csr_nbr[e] = c; continue; }
+            const bool as_i = (a[k] == c);
+            int other = as_i ? b[k] : a[k];
+            int code = as_i ? fid[k] : ~fid[k];
+            if (as_i && t[k] >= 0 && t[k] < F) {   // this face is dropped: use the twin from the j side
+                code = ~t[k];
+                other = pair_i[t[k]];
+            }
+            if (other < 0 || other >= n) other = c;
+            csr_face[e] = code;
+            csr_nbr[e] = other;
+        }
+    }
+}
+
 }  // namespace phd

@@ -167,6 +167,12 @@ __device__ __forceinline__ float4 entry_record(float4 g, float2 ar, bool minus) 
                        __fmaf_rn(hr, g.x, g.z), __fmaf_rn(hr, g.y, g.w));
 }
 
+// The (t_x, t_y) half of entry_record alone, with the same roundings.
+__device__ __forceinline__ float2 entry_t(float4 g, float2 ar, bool minus) {
+    const float hr = (minus ? -0.5f : 0.5f) * ar.y;
+    return make_float2(__fmaf_rn(hr, g.x, g.z), __fmaf_rn(hr, g.y, g.w));
+}
+
 // entry_rec, when given, receives the gradient records of a real cell's list entries
 // (a ghost's gradient is its image's, formed from the image's entries).
 __device__ __forceinline__ float4 cell_geo_of(const phd_mesh &M, int i, const float4 *__restrict__ face_geo,
@@ -224,37 +230,8 @@ __global__ void k_prepare_csr32(phd_mesh M, const int32_t *__restrict__ twin, in
                                 int32_t *__restrict__ csr_nbr) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= M.n_cells) return;
-    const int n = M.n_cells, F = M.n_faces;
-    const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
-    constexpr int CH = 4;          // a chunk's independent gathers are issued together
-    for (int eb = e0; eb < e1; eb += CH) {
-        int fid[CH], a[CH], b[CH], t[CH];
-#pragma unroll
-        for (int k = 0; k < CH; k++) fid[k] = M.nbr_idx[(eb + k < e1) ? eb + k : e0];
-#pragma unroll
-        for (int k = 0; k < CH; k++) {
-            const bool ok = fid[k] >= 0 && fid[k] < F;
-            a[k] = ok ? M.pair_i[fid[k]] : -1;
-            b[k] = ok ? M.pair_j[fid[k]] : -1;
-            t[k] = (ok && twin) ? twin[fid[k]] : -1;
-        }
-#pragma unroll
-        for (int k = 0; k < CH; k++) {
-            const int e = eb + k;
-            if (e >= e1) break;
-            if (fid[k] < 0 || fid[k] >= F) { csr_face[e] = 0; csr_nbr[e] = c; continue; }
-            const bool as_i = (a[k] == c);
-            int other = as_i ? b[k] : a[k];
-            int code = as_i ? fid[k] : ~fid[k];
-            if (as_i && t[k] >= 0 && t[k] < F) {   // this face is dropped: use the twin from the j side
-                code = ~t[k];
-                other = M.pair_i[t[k]];
-            }
-            if (other < 0 || other >= n) other = c;
-            csr_face[e] = code;
-            csr_nbr[e] = other;
-        }
-    }
+    emit_list_codes(c, M.nbr_ptr[c], M.nbr_ptr[c + 1], M.n_cells, M.n_faces, M.nbr_idx, M.pair_i, M.pair_j, twin,
+                    csr_face, csr_nbr);
 }
 
 // ---- gradients + generator velocity ----------------------------------------------
@@ -295,9 +272,32 @@ __device__ __forceinline__ GradHead grad_head(int i, const phd_mesh &M, const fl
     return h;
 }
 
-template <int LIMITER>
+// Where the list entries' gradient records come from: REC, the precomputed entry_rec in
+// list order; otherwise each entry's record is formed here from its face's records
+// (csr_face -> face_geo, face_ar) with entry_record's roundings, the same bits (a mesh
+// stepped once does not pay for writing and reading 32 B of records per face).
+struct EntrySrc {
+    const float4 *__restrict__ entry_rec;
+    const int32_t *__restrict__ csr_face;
+    const float4 *__restrict__ face_geo;
+    const float2 *__restrict__ face_ar;
+    int n_faces;
+};
+
+// An entry's record with at least its (t_x, t_y) half (.z, .w) filled in.
+template <bool REC>
+__device__ __forceinline__ float4 entry_t_of(const EntrySrc &S, int e) {
+    if (REC) return S.entry_rec[e];
+    const int code = S.csr_face[e];
+    const int fid = code < 0 ? ~code : code;
+    if (fid < 0 || fid >= S.n_faces) return make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 t = entry_t(S.face_geo[fid], S.face_ar[fid], code < 0);
+    return make_float4(0.f, 0.f, t.x, t.y);
+}
+
+template <int LIMITER, bool REC>
 __device__ __forceinline__ void grad32_cell(int i, const GradHead &H, const phd_mesh &M, const phd_params &P,
-                                            int moving, const float4 *__restrict__ entry_rec,
+                                            int moving, const EntrySrc &S,
                                             const int32_t *__restrict__ csr_nbr,
                                             const float4 *__restrict__ cell_geo,
                                             const float4 *__restrict__ prim4, float4 *__restrict__ cellrec,
@@ -323,15 +323,42 @@ __device__ __forceinline__ void grad32_cell(int i, const GradHead &H, const phd_
     for (int f = 0; f < 4; f++) { dmx[f] = dmn[f] = 0.f; df[f][0] = df[f][1] = 0.f; }
     // entries in chunks of CH: all of a chunk's loads are issued before any arithmetic,
     // so their latencies overlap (lanes past the end reload entry e0)
-    constexpr int CH = 4;
+    // (two entries per chunk when the records are formed here: 4 took 84 registers and
+    // ran 96 us against 76 at 1M cells)
+    constexpr int CH = REC ? 4 : 2;
     for (int eb = e0; eb < e1; eb += CH) {
         int nb[CH];
         float4 rw[CH];
+        if (REC) {
 #pragma unroll
-        for (int k = 0; k < CH; k++) {
-            const int e = (eb + k < e1) ? eb + k : e0;
-            nb[k] = csr_nbr[e];
-            rw[k] = entry_rec[e];
+            for (int k = 0; k < CH; k++) {
+                const int e = (eb + k < e1) ? eb + k : e0;
+                nb[k] = csr_nbr[e];
+                rw[k] = S.entry_rec[e];
+            }
+        } else {
+            int code[CH];
+#pragma unroll
+            for (int k = 0; k < CH; k++) {
+                const int e = (eb + k < e1) ? eb + k : e0;
+                nb[k] = csr_nbr[e];
+                code[k] = S.csr_face[e];
+            }
+            float4 g[CH];
+            float2 ar[CH];
+#pragma unroll
+            for (int k = 0; k < CH; k++) {
+                const int fid = code[k] < 0 ? ~code[k] : code[k];
+                const int f = (fid >= 0 && fid < S.n_faces) ? fid : 0;
+                g[k] = S.face_geo[f];
+                ar[k] = S.face_ar[f];
+            }
+#pragma unroll
+            for (int k = 0; k < CH; k++) {
+                const int fid = code[k] < 0 ? ~code[k] : code[k];
+                rw[k] = (fid >= 0 && fid < S.n_faces) ? entry_record(g[k], ar[k], code[k] < 0)
+                                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
         }
         float4 pj[CH];
 #pragma unroll
@@ -369,7 +396,7 @@ __device__ __forceinline__ void grad32_cell(int i, const GradHead &H, const phd_
         for (int eb = e0; eb < e1; eb += CH) {
             float4 rt[CH];
 #pragma unroll
-            for (int k = 0; k < CH; k++) rt[k] = entry_rec[(eb + k < e1) ? eb + k : e0];
+            for (int k = 0; k < CH; k++) rt[k] = entry_t_of<REC>(S, (eb + k < e1) ? eb + k : e0);
 #pragma unroll
             for (int k = 0; k < CH; k++) {
                 if (eb + k >= e1) break;
@@ -389,7 +416,7 @@ __device__ __forceinline__ void grad32_cell(int i, const GradHead &H, const phd_
         }
     } else {
         for (int e = e0; e < e1; e++) {
-            const float4 rt = entry_rec[e];
+            const float4 rt = entry_t_of<REC>(S, e);
             const float sx = rt.z - gc.x, sy = rt.w - gc.y;
             const float4 pj = prim4[csr_nbr[e]];
             const float Pj[4] = {pj.x, pj.y, pj.z, pj.w};
@@ -441,9 +468,8 @@ __device__ __forceinline__ void grad32_cell(int i, const GradHead &H, const phd_
 
 // ITEMS cells per thread: a block covers blockDim * ITEMS consecutive cells, thread t
 // taking cells t, t + blockDim, ... of each tile (the autotuner picks 1, 2 or 4).
-template <int LIMITER, int ITEMS>
-__global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int moving,
-                                                const float4 *__restrict__ entry_rec,
+template <int LIMITER, int ITEMS, bool REC>
+__global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int moving, EntrySrc S,
                                                 const int32_t *__restrict__ csr_nbr,
                                                 const float4 *__restrict__ cell_geo,
                                                 const float4 *__restrict__ prim4, float4 *__restrict__ cellrec,
@@ -456,8 +482,8 @@ __global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int mo
         for (int k = 0; k < ITEMS; k++) {
             const int i = base + k * blockDim.x + threadIdx.x;
             if (i < M.n_cells)
-                grad32_cell<LIMITER>(i, grad_head(i, M, cell_geo), M, P, moving, entry_rec, csr_nbr, cell_geo, prim4,
-                                     cellrec, w2, clk);
+                grad32_cell<LIMITER, REC>(i, grad_head(i, M, cell_geo), M, P, moving, S, csr_nbr, cell_geo, prim4,
+                                          cellrec, w2, clk);
         }
     }
 }
@@ -1127,15 +1153,29 @@ inline bool items_ok(int k) { return k == 0 || k == 1 || k == 2 || k == 4; }
 inline int items_of(int k) { return k <= 1 ? 1 : k; }
 
 template <int LIMITER>
-void launch_grad32(int items, int grid, int block, cudaStream_t s, const phd_mesh &M, const phd_params &P, int moving,
-                   const float4 *er, const int32_t *csr_nbr, const float4 *cg, const float4 *p4, float4 *cr,
-                   float2 *w, phd_clock *clocks) {
+void launch_grad32_rec(int items, int grid, int block, cudaStream_t s, const phd_mesh &M, const phd_params &P,
+                       int moving, const EntrySrc &S, const int32_t *csr_nbr, const float4 *cg, const float4 *p4,
+                       float4 *cr, float2 *w, phd_clock *clocks) {
     if (items == 1)
-        launch_pdl(k_grad32<LIMITER, 1>, grid, block, s, M, P, moving, er, csr_nbr, cg, p4, cr, w, clocks);
+        launch_pdl(k_grad32<LIMITER, 1, true>, grid, block, s, M, P, moving, S, csr_nbr, cg, p4, cr, w, clocks);
     else if (items == 2)
-        launch_pdl(k_grad32<LIMITER, 2>, grid, block, s, M, P, moving, er, csr_nbr, cg, p4, cr, w, clocks);
+        launch_pdl(k_grad32<LIMITER, 2, true>, grid, block, s, M, P, moving, S, csr_nbr, cg, p4, cr, w, clocks);
     else
-        launch_pdl(k_grad32<LIMITER, 4>, grid, block, s, M, P, moving, er, csr_nbr, cg, p4, cr, w, clocks);
+        launch_pdl(k_grad32<LIMITER, 4, true>, grid, block, s, M, P, moving, S, csr_nbr, cg, p4, cr, w, clocks);
+}
+
+// without entry records (S.entry_rec null): one item per thread, the records formed
+// from the faces (the launch a freshly handed-over mesh's first step takes)
+template <int LIMITER>
+void launch_grad32(int items, int grid, int block, cudaStream_t s, const phd_mesh &M, const phd_params &P, int moving,
+                   const EntrySrc &S, const int32_t *csr_nbr, const float4 *cg, const float4 *p4, float4 *cr,
+                   float2 *w, phd_clock *clocks) {
+    if (S.entry_rec)
+        launch_grad32_rec<LIMITER>(items, grid, block, s, M, P, moving, S, csr_nbr, cg, p4, cr, w, clocks);
+    else if (items == 1)
+        launch_pdl(k_grad32<LIMITER, 1, false>, grid, block, s, M, P, moving, S, csr_nbr, cg, p4, cr, w, clocks);
+    else
+        launch_pdl(k_grad32<LIMITER, 2, false>, grid, block, s, M, P, moving, S, csr_nbr, cg, p4, cr, w, clocks);
 }
 
 inline int g32(int n) { return n > 0 ? (n + B32 - 1) / B32 : 1; }
@@ -1235,7 +1275,9 @@ int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_
     if (!mesh || mesh->dim != 2 || !geo || !par || !prim4 || !cons || !cons_next || !flux4 || !clocks)
         return PHD_ERR_ARG;
     const bool linear = par->reconstruction == PHD_LINEAR;
-    if ((linear || moving) && (!cellrec || !geo->entry_rec || !geo->csr_nbr)) return PHD_ERR_ARG;
+    if ((linear || moving) && (!cellrec || !geo->csr_nbr)) return PHD_ERR_ARG;
+    if ((linear || moving) && !geo->entry_rec && (!geo->face_geo || !geo->face_ar || !geo->csr_face))
+        return PHD_ERR_ARG;
     if (moving && !w2) return PHD_ERR_ARG;
     if ((reinterpret_cast<uintptr_t>(cellrec) & 31u) != 0) return PHD_ERR_ARG;    // 256-bit loads
     if (par->solver < PHD_HLL || par->solver > PHD_EXACT) return PHD_ERR_ARG;
@@ -1258,7 +1300,9 @@ int phd_step_f32_batched(const phd_mesh *mesh, const phd_geom32 *geo, const phd_
     float4 *cr = reinterpret_cast<float4 *>(cellrec);
     float2 *w = reinterpret_cast<float2 *>(w2);
     float4 *fx = reinterpret_cast<float4 *>(flux4);
-    const float4 *er = reinterpret_cast<const float4 *>(geo->entry_rec);
+    const EntrySrc er = {reinterpret_cast<const float4 *>(geo->entry_rec), geo->csr_face,
+                         reinterpret_cast<const float4 *>(geo->face_geo), reinterpret_cast<const float2 *>(geo->face_ar),
+                         M.n_faces};
     const float4 *cg = reinterpret_cast<const float4 *>(geo->cell_geo);
     const int32_t *runs = n_runs > 1 ? cell_run : nullptr;
     if (marks) cudaEventRecord(marks[0], stream);

@@ -1063,10 +1063,10 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
     return 0;
 }
 
-int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *ct32,
-                            double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
-    if (!t || t->G.n_cells == 0 || !face_ptr || !pair_j || !area32 || !ct32 || !map || !tag || !type)
-        return -2;
+// pair_j, or (pair_j == NULL) pair_dj + pair_x[2 x_cap] with *n_pair_x escapes
+static int copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, uint16_t *pair_dj, int32_t *pair_x,
+                        int32_t x_cap, int32_t *n_pair_x, float *area32, float *ct32, double *x, int32_t *map,
+                        int8_t *tag, int8_t *type, int8_t *ghost_code) {
     const Geometry &G = t->G;
     const int nr = G.n_real, n = G.n_cells, F = G.n_faces;
     // FP64 -> FP32, round to nearest even; magnitudes below 2^-126 to signed zero (the
@@ -1079,7 +1079,21 @@ int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pai
     for (int f = 0; f < F; f++) {
         const int i = G.pair_i[f], j = G.pair_j[f];
         while (c < i) face_ptr[++c] = f;
-        pair_j[f] = j;
+        if (pair_j) {
+            pair_j[f] = j;
+        } else {
+            const int64_t d = int64_t(j) - int64_t(i);
+            if (d >= 1 && d <= 65535) {
+                pair_dj[f] = uint16_t(d);
+            } else {
+                pair_dj[f] = PHD_PAIR16_ESCAPE;
+                if (*n_pair_x < x_cap) {
+                    pair_x[2 * *n_pair_x] = f;
+                    pair_x[2 * *n_pair_x + 1] = j;
+                }
+                ++*n_pair_x;
+            }
+        }
         area32[f] = round32(G.area[f]);
         // the centroid offset along the face (phdflux.h, compact hand-over): built with
         // -ffp-contract=off, so every operation rounds as the device's does
@@ -1099,7 +1113,26 @@ int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pai
         tag[k] = k < nr ? 0 : 1;                        // Real / Ghost (particle_tags.py:1-6)
         type[k] = k < nr ? 4 : 2;                       // Undefined / Exterior
     }
-    return 0;
+    return (n_pair_x && *n_pair_x > x_cap) ? -3 : 0;
+}
+
+int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *ct32,
+                            double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
+    if (!t || t->G.n_cells == 0 || !face_ptr || !pair_j || !area32 || !ct32 || !map || !tag || !type)
+        return -2;
+    return copy_compact(t, face_ptr, pair_j, nullptr, nullptr, 0, nullptr, area32, ct32, x, map, tag, type,
+                        ghost_code);
+}
+
+int phd_mesh2d_copy_compact16(const phd_tess2d *t, int32_t *face_ptr, uint16_t *pair_dj, int32_t *pair_x,
+                              int32_t x_cap, int32_t *n_pair_x, float *area32, float *ct32, double *x,
+                              int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
+    if (!t || t->G.n_cells == 0 || !face_ptr || !pair_dj || !n_pair_x || x_cap < 0 || (x_cap > 0 && !pair_x) ||
+        !area32 || !ct32 || !map || !tag || !type)
+        return -2;
+    *n_pair_x = 0;
+    return copy_compact(t, face_ptr, nullptr, pair_dj, pair_x, x_cap, n_pair_x, area32, ct32, x, map, tag, type,
+                        ghost_code);
 }
 
 void phd_hilbert_keys_2d_host(const int32_t *xh, const int32_t *yh, int64_t n, int order, int64_t *keys) {

@@ -204,10 +204,8 @@ __device__ __forceinline__ void sort_list_regs(int32_t *__restrict__ idx, int e0
         if (k < d) idx[e0 + k] = v[k];
 }
 
-__global__ void k_csr_sort(int n, const int32_t *__restrict__ ptr, int32_t *__restrict__ idx) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    const int e0 = ptr[c], e1 = ptr[c + 1], d = e1 - e0;
+__device__ __forceinline__ void sort_list(int32_t *__restrict__ idx, int e0, int e1) {
+    const int d = e1 - e0;
     if (d <= 1) return;
     if (d <= 8) { sort_list_regs<8>(idx, e0, d); return; }
     if (d <= 16) { sort_list_regs<16>(idx, e0, d); return; }
@@ -219,6 +217,61 @@ __global__ void k_csr_sort(int n, const int32_t *__restrict__ ptr, int32_t *__re
             k--;
         }
         idx[k + 1] = v;
+    }
+}
+
+__global__ void k_csr_sort(int n, const int32_t *__restrict__ ptr, int32_t *__restrict__ idx) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    sort_list(idx, ptr[c], ptr[c + 1]);
+}
+
+// k_csr_sort followed, by the same thread, by the FP32 list codes of the sorted list, for
+// a hand-over whose faces come in per-real-cell ranges: an entry is pair-i side exactly
+// when its face lies in the cell's own range (pair-i was written from the ranges), so
+// one gather per entry gives the other cell -- pair-j of an own face, pair-i of another
+// -- and only own faces to a ghost look up the twin table (the table built from the
+// ranges holds twins of such faces only).  The codes equal emit_list_codes' (the
+// PHD_PREP_LISTS kernel) on any hand-over whose ranges tile the face list.
+__global__ void k_csr_sort_codes_ranges(phd_mesh M, const int32_t *__restrict__ face_ptr,
+                                        const int32_t *__restrict__ twin, int32_t *idx,
+                                        int32_t *__restrict__ csr_face, int32_t *__restrict__ csr_nbr) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= M.n_cells) return;
+    const int n = M.n_cells, nr = M.n_real, F = M.n_faces;
+    const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
+    const int f0 = c < nr ? face_ptr[c] : 0, f1 = c < nr ? face_ptr[c + 1] : 0;
+    sort_list(idx, e0, e1);
+    constexpr int CH = 4;
+    for (int eb = e0; eb < e1; eb += CH) {
+        int fid[CH], o[CH];
+#pragma unroll
+        for (int k = 0; k < CH; k++) fid[k] = idx[(eb + k < e1) ? eb + k : e0];
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            const bool ok = fid[k] >= 0 && fid[k] < F;
+            const bool own = fid[k] >= f0 && fid[k] < f1;
+            o[k] = ok ? (own ? M.pair_j[fid[k]] : M.pair_i[fid[k]]) : -1;
+        }
+#pragma unroll
+        for (int k = 0; k < CH; k++) {
+            const int e = eb + k;
+            if (e >= e1) break;
+            if (fid[k] < 0 || fid[k] >= F) { csr_face[e] = 0; csr_nbr[e] = c; continue; }
+            const bool own = fid[k] >= f0 && fid[k] < f1;
+            int other = o[k];
+            int code = own ? fid[k] : ~fid[k];
+            if (own && other >= nr && twin) {
+                const int t = twin[fid[k]];
+                if (t >= 0 && t < F) {          // this face is dropped: use the twin from the j side
+                    code = ~t;
+                    other = M.pair_i[t];
+                }
+            }
+            if (other < 0 || other >= n) other = c;
+            csr_face[e] = code;
+            csr_nbr[e] = other;
+        }
     }
 }
 
@@ -382,8 +435,25 @@ __device__ __forceinline__ bool range_ok(int c, int n_real, int F, int a, int b)
     return !(a < 0 || b < a || b > F || (c == 0 && a != 0) || (c == n_real - 1 && b != F));
 }
 
+// pair-j of an escaped face from the (face id, pair-j) list px[K] (ascending face ids);
+// -1 when the face is not listed.
+__device__ __forceinline__ int pair_j_escaped(int m, const int32_t *__restrict__ px, int K) {
+    int lo = 0, hi = K;
+    while (lo < hi) {                    // at most log2(K) + 1 rounds
+        const int mid = (lo + hi) >> 1;
+        if (px[2 * mid] < m)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    return (lo < K && px[2 * lo] == m) ? px[2 * lo + 1] : -1;
+}
+
+// dj (optional): pair-j packed as the difference to the owner (PHD_PAIR16_ESCAPE and the
+// list px[K] for the rest), decoded here into pair_j.
 __global__ void k_csr_count_ranges(int n_real, int n, int F, const int32_t *__restrict__ face_ptr,
-                                   const int32_t *__restrict__ pair_j, int32_t *__restrict__ pair_i,
+                                   int32_t *__restrict__ pair_j, const uint16_t *__restrict__ dj,
+                                   const int32_t *__restrict__ px, int K, int32_t *__restrict__ pair_i,
                                    int32_t *__restrict__ cnt, int32_t *__restrict__ bad) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n_real) return;
@@ -392,7 +462,14 @@ __global__ void k_csr_count_ranges(int n_real, int n, int F, const int32_t *__re
     int own = 0;
     for (int m = a; m < b; m++) {
         pair_i[m] = c;
-        const int j = pair_j[m];
+        int j;
+        if (dj) {
+            const int d = dj[m];
+            j = d != PHD_PAIR16_ESCAPE ? c + d : pair_j_escaped(m, px, K);
+            pair_j[m] = j;
+        } else {
+            j = pair_j[m];
+        }
         if (j >= 0 && j < n && j != c) {
             atomicAdd(&cnt[j], 1);
             own++;
@@ -531,10 +608,15 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
         return PHD_ERR_ARG;
     if (!mesh->pair_i || !mesh->pair_j || !mesh->map || !mesh->x || !mesh->flip || !mesh->nbr_ptr || !mesh->nbr_idx)
         return PHD_ERR_ARG;
-    if (!h->face_ptr || !h->pair_j || !h->area32 || !h->ct32 || !h->d_face_ptr || !h->d_area32 || !h->d_ct32 ||
+    if (!h->face_ptr || !h->area32 || !h->ct32 || !h->d_face_ptr || !h->d_area32 || !h->d_ct32 ||
         !h->type || !h->twin || !h->csr_work || !h->bad || !(h->xmax[0] > h->xmin[0]) || !(h->xmax[1] > h->xmin[1]))
         return PHD_ERR_ARG;
     const int n = mesh->n_cells, nr = mesh->n_real, F = mesh->n_faces, ng = n - nr;
+    if (!out->csr_face || !out->csr_nbr) return PHD_ERR_ARG;
+    const bool packed = h->pair_j == nullptr;      // pair-j as 16-bit differences + escapes
+    if (packed && (!h->pair_dj || !h->d_pair_dj || h->n_pair_x < 0 || h->n_pair_x > F ||
+                   (h->n_pair_x > 0 && (!h->pair_x || !h->d_pair_x))))
+        return PHD_ERR_ARG;
     if (!h->x && ng > 0 && (!h->ghost_code || !h->d_ghost_code)) return PHD_ERR_ARG;
     int32_t *pair_i = const_cast<int32_t *>(mesh->pair_i);
     int32_t *pair_j = const_cast<int32_t *>(mesh->pair_j);
@@ -554,7 +636,14 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     // face records; each group's event releases the work that needs it
     PHD_TRY_CUDA(cudaMemsetAsync(h->bad, 0, sizeof(int32_t), stream));
     PHD_TRY_CUDA(cudaMemcpyAsync(h->d_face_ptr, h->face_ptr, (size_t)(nr + 1) * sizeof(int32_t), H2D, stream));
-    PHD_TRY_CUDA(cudaMemcpyAsync(pair_j, h->pair_j, (size_t)F * sizeof(int32_t), H2D, stream));
+    if (!packed) {
+        PHD_TRY_CUDA(cudaMemcpyAsync(pair_j, h->pair_j, (size_t)F * sizeof(int32_t), H2D, stream));
+    } else {
+        PHD_TRY_CUDA(cudaMemcpyAsync(h->d_pair_dj, h->pair_dj, (size_t)F * sizeof(uint16_t), H2D, stream));
+        if (h->n_pair_x > 0)
+            PHD_TRY_CUDA(cudaMemcpyAsync(h->d_pair_x, h->pair_x, (size_t)2 * h->n_pair_x * sizeof(int32_t), H2D,
+                                         stream));
+    }
     PHD_TRY_CUDA(cudaEventRecord(events[0], stream));
     if (h->ghost_map && ng > 0)
         PHD_TRY_CUDA(cudaMemcpyAsync(const_cast<int32_t *>(mesh->map) + nr, h->ghost_map, (size_t)ng * sizeof(int32_t),
@@ -564,9 +653,10 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     else if (ng > 0)
         PHD_TRY_CUDA(cudaMemcpyAsync(h->d_ghost_code, h->ghost_code, (size_t)ng, H2D, stream));
     PHD_TRY_CUDA(cudaEventRecord(events[1], stream));
-    // the face records in two halves: the first half's geometry is formed while the
-    // second half is in flight
-    const int F0 = F / 2;
+    // the face records in two parts, three quarters and the rest: the first part's
+    // geometry is formed while the rest is in flight, so only a quarter of it is left
+    // once the copies end
+    const int F0 = (int)(((int64_t)F * 3) / 4);
     PHD_TRY_CUDA(cudaMemcpyAsync(h->d_area32, h->area32, (size_t)F0 * sizeof(float), H2D, stream));
     PHD_TRY_CUDA(cudaMemcpyAsync(h->d_ct32, h->ct32, (size_t)F0 * sizeof(float), H2D, stream));
     PHD_TRY_CUDA(cudaEventRecord(events[7], stream));
@@ -583,7 +673,9 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[0], 0));
     PHD_TRY_CUDA(cudaMemsetAsync(h->csr_work, 0, sizeof(int32_t) * phd_csr_work_ints(n), lists));
     if (nr > 0)
-        phd::k_csr_count_ranges<<<gr, phd::UBLOCK, 0, lists>>>(nr, n, F, h->d_face_ptr, pair_j, pair_i, cnt, h->bad);
+        phd::k_csr_count_ranges<<<gr, phd::UBLOCK, 0, lists>>>(nr, n, F, h->d_face_ptr, pair_j,
+                                                               packed ? h->d_pair_dj : nullptr, h->d_pair_x,
+                                                               packed ? h->n_pair_x : 0, pair_i, cnt, h->bad);
     PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[1], 0));
     if (!h->x && n > 0) {
         const bool copy_real = h->x_real != nullptr;
@@ -600,8 +692,6 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     if (nr > 0 && F > 0) {
         phd::k_csr_scatter_ranges<<<gr, phd::UBLOCK, 0, lists>>>(nr, n, F, h->d_face_ptr, pair_j, nbr_ptr, cursor,
                                                                  const_cast<int32_t *>(mesh->nbr_idx));
-        phd::k_csr_sort<<<(n + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, lists>>>(
-            n, nbr_ptr, const_cast<int32_t *>(mesh->nbr_idx));
     }
     PHD_TRY_CUDA(cudaPeekAtLastError());
 
@@ -633,9 +723,13 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     }
     PHD_TRY_CUDA(cudaEventRecord(events[4], geom));
 
-    // lists stream: the FP32 list codes once the twins are there
+    // lists stream, once the twins are there: each list sorted and its FP32 codes formed
+    // in one pass (k_csr_sort + PHD_PREP_LISTS)
     PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[6], 0));
-    PHD_TRY(phd_prepare_f32_parts(mesh, h->twin, out, PHD_PREP_LISTS, lists));
+    if (n > 0)
+        phd::k_csr_sort_codes_ranges<<<(n + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, lists>>>(
+            *mesh, h->d_face_ptr, h->twin, const_cast<int32_t *>(mesh->nbr_idx), out->csr_face, out->csr_nbr);
+    PHD_TRY_CUDA(cudaPeekAtLastError());
     PHD_TRY_CUDA(cudaEventRecord(events[5], lists));
 
     // stream, once the lists and the faces are in: cell geometry, ghost totals from

@@ -164,7 +164,7 @@ class DeviceMesh:
             code = 16 + 2 * k + high.astype(np.int64)
         return code.astype(np.int8)
 
-    def pinned_host_compact(self, host, resident=False):
+    def pinned_host_compact(self, host, resident=False, pair16=True):
         """The compact hand-over of a re-mesh for the FP32 path, 12 B per face instead of
         32: per-real-cell face ranges ``face_ptr`` instead of pair-i (faces are emitted
         per real cell in ascending order, tess.cpp:363), pair-j, and the area and the
@@ -174,7 +174,10 @@ class DeviceMesh:
         zero, as the device's own rounding does), plus the cells' positions and maps.
         The FP32 face geometry formed from it equals the full hand-over's bit for bit.
         ``resident``: the device already holds the real cells' positions (its own
-        generator move); ghost codes replace the positions (``phd_ghost_positions``)."""
+        generator move); ghost codes replace the positions (``phd_ghost_positions``).
+        ``pair16``: pair-j as the 16-bit difference to the owner cell (``pair_dj``, 0 =
+        escape) plus the escaped faces' (face id, pair-j) pairs (``pair_x``): 10 B per
+        face."""
         self._check_remesh(host)
         nr = self.n_real
         pi, pj = np.asarray(host.pair_i), np.asarray(host.pair_j)
@@ -193,12 +196,20 @@ class DeviceMesh:
             out = a.astype(np.float32)
             return np.where(np.abs(a) < 2.0 ** -126, np.copysign(np.float32(0.0), out), out).astype(np.float32)
 
-        arrays = {"face_ptr": face_ptr, "pair_j": np.ascontiguousarray(pj, dtype=np.int32),
-                  "area32": round32(np.asarray(host.area, dtype=np.float64)),
+        arrays = {"face_ptr": face_ptr, "area32": round32(np.asarray(host.area, dtype=np.float64)),
                   "ct32": round32(s64),
                   "map": np.ascontiguousarray(host.map, dtype=np.int32),
                   "tag": np.ascontiguousarray(host.tag, dtype=np.int8),
                   "type": np.ascontiguousarray(host.type, dtype=np.int8)}
+        if pair16:
+            d = pj.astype(np.int64) - pi.astype(np.int64)
+            ok = (d >= 1) & (d <= 65535)
+            esc = np.flatnonzero(~ok)
+            # the 16-bit patterns as int16 (the device reads them as uint16)
+            arrays["pair_dj"] = np.where(ok, d, 0).astype(np.uint16).view(np.int16)
+            arrays["pair_x"] = np.stack([esc, pj[esc]], axis=1).astype(np.int32).reshape(-1)
+        else:
+            arrays["pair_j"] = np.ascontiguousarray(pj, dtype=np.int32)
         if resident:            # the device holds the real positions; ghosts from their codes
             arrays["ghost_code"] = self.ghost_codes(host)
         else:
@@ -208,7 +219,7 @@ class DeviceMesh:
     @staticmethod
     def pinned_sizes(pinned):
         """(n_cells, n_faces) of a pinned hand-over (full or compact)."""
-        return int(pinned["map"].shape[0]), int(pinned["pair_j"].shape[0])
+        return int(pinned["map"].shape[0]), int((pinned["pair_j"] if "pair_j" in pinned else pinned["pair_dj"]).shape[0])
 
     def check_upload(self, pinned):
         """Raise unless the pinned arrays have this mesh's cell and face counts."""
@@ -216,10 +227,14 @@ class DeviceMesh:
                   "x": (self.dim, self.n_cells), "dcom": (self.dim, self.n_cells), "vol": (self.n_cells,),
                   "pair_i": (self.n_faces,), "pair_j": (self.n_faces,), "area": (self.n_faces,),
                   "com": (self.dim, self.n_faces), "face_ptr": (self.n_real + 1,), "area32": (self.n_faces,),
-                  "ct32": (self.n_faces,), "ghost_code": (self.n_cells - self.n_real,)}
+                  "ct32": (self.n_faces,), "ghost_code": (self.n_cells - self.n_real,), "pair_dj": (self.n_faces,)}
         if "face_ptr" in pinned:
-            names = ("face_ptr", "pair_j", "area32", "ct32", "map", "tag", "type") + \
-                (("x",) if "x" in pinned else ("ghost_code",))
+            names = ("face_ptr", "pair_j" if "pair_j" in pinned else "pair_dj", "area32", "ct32", "map", "tag",
+                     "type") + (("x",) if "x" in pinned else ("ghost_code",))
+            if "pair_dj" in pinned:
+                px = pinned["pair_x"]
+                if px.dim() != 1 or px.numel() % 2 or px.numel() > 2 * self.n_faces:
+                    raise ValueError("upload: pair_x must hold (face id, pair-j) pairs of at most n_faces faces")
         else:
             names = [nm for nm, _ in self.UPLOAD]
         for nm in names:

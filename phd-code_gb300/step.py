@@ -24,8 +24,15 @@ class FluxStepper:
     def __init__(self, mesh, prim, gamma=1.4, cfl=0.5, solver="hllc", reconstruction="linear",
                  limiter="arepo", gizmo=True, boost=True, moving=True, regularize=True, eta=0.25,
                  precision="fp64", t_end=0.0, face_velocity=None, device="cuda", stream=None,
-                 dedup_periodic=True):
+                 dedup_periodic=True, handover_records=False):
+        """handover_records (FP32): whether load_mesh also writes the per-entry gradient
+        records (entry_rec).  Without them the first steps on a handed-over mesh form
+        each entry's record from its face in the gradient kernel (the same bits); that
+        is cheaper for a mesh stepped once, as in the moving-mesh loop, while
+        build_entry_records() (called by capture()) pays off over many steps."""
         self.device = torch.device(device)
+        self.handover_records = bool(handover_records)
+        self.records = False        # entry_rec holds the current mesh's records
         self.dmesh = mesh if isinstance(mesh, DeviceMesh) else DeviceMesh(mesh, device=self.device)
         dm = self.dmesh
         self.params = make_params(gamma=gamma, cfl=cfl, eta=eta, reconstruction=reconstruction,
@@ -77,7 +84,8 @@ class FluxStepper:
             self.entry_rec = torch.zeros((max(2 * F, 1), 4), dtype=f32, device=dev)
             out = L.geom32(self._geo_tensors(), out=True)
             L.check(lib.phd_prepare_f32(dm.ref, L.ptr(self.twin), ctypes.byref(out), s), "phd_prepare_f32")
-            self.geo = L.geom32(self._geo_tensors())
+            self.records = True
+            self._set_geo()
             self.prim4 = torch.zeros((n, 4), dtype=f32, device=dev)
             self.cellrec = torch.zeros((n, 16), dtype=f32, device=dev)
             self.w2 = torch.zeros((n, 2), dtype=f32, device=dev)
@@ -86,8 +94,26 @@ class FluxStepper:
                                      self.clock.ptr, s), "phd_prim_f32")
 
     # ------------------------------------------------------------------------------
-    def _geo_tensors(self):
-        return (self.face_geo, self.face_ar, self.csr_face, self.csr_nbr, self.cell_geo, self.entry_rec)
+    def _geo_tensors(self, records=True):
+        return (self.face_geo, self.face_ar, self.csr_face, self.csr_nbr, self.cell_geo,
+                self.entry_rec if records else None)
+
+    def _set_geo(self):
+        """The step's geometry: with entry_rec only while it holds the current mesh's."""
+        self.geo = L.geom32(self._geo_tensors(self.records))
+
+    def build_entry_records(self):
+        """(FP32) Write the per-entry gradient records of the current mesh, so the steps
+        that follow read them instead of forming them from the faces (the same bits,
+        about 8 us less per step at 1M cells; the build costs about as much as 7 steps
+        save).  A no-op when they are current."""
+        if self.precision != "fp32" or self.records:
+            return
+        out = L.geom32(self._geo_tensors(), out=True)
+        L.check(L.lib().phd_prepare_f32_parts(self.dmesh.ref, None, ctypes.byref(out), L.PREP_RECORDS,
+                                              L.stream_handle(self.stream)), "phd_prepare_f32_parts")
+        self.records = True
+        self._set_geo()
 
     @property
     def grad8(self):
@@ -163,7 +189,8 @@ class FluxStepper:
             self.cellrec = view("cellrec", (n_cells, 16), f32)
             self.w2 = view("w2", (n_cells, 2), f32)
             self.flux4 = view("flux4", (F1, 4), f32)
-            self.geo = L.geom32(self._geo_tensors())
+            self.records = False
+            self._set_geo()
         self._graph = None
         self._graph_steps = 0
 
@@ -219,7 +246,7 @@ class FluxStepper:
         s, ss = L.stream_handle(main), L.stream_handle(side)
         out = None
         if fp32:
-            out = L.geom32(self._geo_tensors(), out=True)
+            out = L.geom32(self._geo_tensors(self.handover_records), out=True)
         # copies on the main stream in the order the side stream needs them; the side
         # stream builds the neighbour lists, twins, list codes and face geometry meanwhile
         dm.reset_errors(main)
@@ -250,7 +277,8 @@ class FluxStepper:
             side.wait_event(ev[2])
             dm.set_normals("none", side)
             L.check(lib.phd_prepare_f32_parts(dm.ref, None, ctypes.byref(out), L.PREP_FACES | L.PREP_CELLS_FROM_FACES |
-                                              L.PREP_RECORDS, ss), "phd_prepare_f32_parts")
+                                              (L.PREP_RECORDS if self.handover_records else 0), ss),
+                    "phd_prepare_f32_parts")
         ev[3].record(side)
         if not fp32:
             nbytes += dm.copy_fields(pinned, ("dcom", "vol"), main)
@@ -265,6 +293,9 @@ class FluxStepper:
             L.check(lib.phd_prim_from_cons_f64(dm.dim, dm.n_cells, p.gamma, L.ptr(dm.vol), L.ptr(self.cons),
                                                L.ptr(self.prim), s), "phd_prim_from_cons_f64")
             self.initial_time_step()
+        if fp32:
+            self.records = self.handover_records
+            self._set_geo()
         return nbytes
 
     def _load_mesh_compact(self, pinned, resized, xr, main):
@@ -284,6 +315,11 @@ class FluxStepper:
                  "ct32": self._view("ct32_in", (nf,), torch.float32)}
         if xr is not None:
             stage["ghost_code"] = self._view("ghost_code_in", (ng,), torch.int8)
+        packed = "pair_dj" in pinned
+        n_x = pinned["pair_x"].numel() // 2 if packed else 0
+        if packed:
+            stage["pair_dj"] = self._view("pair_dj_in", (nf,), torch.int16)
+            stage["pair_x"] = self._view("pair_x_in", (max(2 * n_x, 2),), torch.int32)
         dm.set_normals("none")
         hp = lambda k: pinned[k].data_ptr() if k in pinned else None
         h = L.PhdHandover32(face_ptr=hp("face_ptr"), pair_j=hp("pair_j"), area32=hp("area32"), ct32=hp("ct32"),
@@ -297,8 +333,11 @@ class FluxStepper:
                             twin=self.twin.data_ptr(), csr_work=dm._csr_work.data_ptr(), bad=dm._bad.data_ptr(),
                             periodic=int(dm.boundary == "periodic"), dedup_periodic=int(self.dedup_periodic),
                             xmin=(ctypes.c_double * 2)(*dm.xmin[:2]),
-                            xmax=(ctypes.c_double * 2)(*dm.xmax[:2]))
-        out = L.geom32(self._geo_tensors(), out=True)
+                            xmax=(ctypes.c_double * 2)(*dm.xmax[:2]),
+                            pair_dj=hp("pair_dj"), pair_x=hp("pair_x") if n_x else None, n_pair_x=n_x,
+                            d_pair_dj=stage["pair_dj"].data_ptr() if packed else None,
+                            d_pair_x=stage["pair_x"].data_ptr() if packed else None)
+        out = L.geom32(self._geo_tensors(self.handover_records), out=True)
         events = (ctypes.c_void_p * 8)(*(e.cuda_event for e in self._ev))
         sides = (ctypes.c_void_p * 2)(self._side.cuda_stream, self._side2.cuda_stream)
         L.check(lib.phd_load_mesh_f32(dm.ref, ctypes.byref(h), ctypes.byref(self.params), ctypes.byref(out),
@@ -306,9 +345,12 @@ class FluxStepper:
                                       sides, events), "phd_load_mesh_f32")
         if xr is None:
             self._x_real_valid = False
+        self.records = self.handover_records
+        self._set_geo()
         # what phd_load_mesh_f32 copied, counted from the arrays themselves
         nb = lambda k: pinned[k].numel() * pinned[k].element_size()
-        nbytes += nb("face_ptr") + nb("pair_j") + nb("area32") + nb("ct32") + (0 if resized else 4 * ng)
+        pair_bytes = nb("pair_dj") + nb("pair_x") if packed else nb("pair_j")
+        nbytes += nb("face_ptr") + pair_bytes + nb("area32") + nb("ct32") + (0 if resized else 4 * ng)
         nbytes += nb("ghost_code") if xr is not None else nb("x")
         return nbytes
 
@@ -397,6 +439,7 @@ class FluxStepper:
         same buffer) into a CUDA graph; replay() then launches them as one unit."""
         if n_steps % 2:
             raise ValueError("capture an even number of steps")
+        self.build_entry_records()                 # a graph replays many steps on one mesh
         torch.cuda.synchronize(self.device)
         g = torch.cuda.CUDAGraph()
         cap_stream = torch.cuda.Stream(self.device)

@@ -33,6 +33,7 @@ _SIGNATURES = {
     "phd_mesh2d_sizes": ([_vp, _vp, _vp, _vp], C.c_int),
     "phd_mesh2d_copy": ([_vp] * 16, C.c_int),
     "phd_mesh2d_copy_compact": ([_vp] * 10, C.c_int),
+    "phd_mesh2d_copy_compact16": ([_vp] * 4 + [C.c_int32] + [_vp] * 8, C.c_int),
     "phd_hilbert_keys_2d_host": ([_vp, _vp, C.c_int64, C.c_int, _vp], None),
 }
 
@@ -167,14 +168,17 @@ class CompactMesher:
     overwrites them: let the copies of the previous hand-over finish (any
     synchronisation of the stepper's stream) before calling again."""
 
-    def __init__(self, boundary, xmin=(0.0, 0.0), xmax=(1.0, 1.0), n_strips=0, resident=False):
+    def __init__(self, boundary, xmin=(0.0, 0.0), xmax=(1.0, 1.0), n_strips=0, resident=False, pair16=True):
         """``resident``: the device already holds the real cells' positions (from its own
         generator move, ``FluxStepper.move_generators``): hand over ghost codes instead of
-        positions (``phd_ghost_positions``)."""
+        positions (``phd_ghost_positions``).  ``pair16``: pair-j packed as 16-bit
+        differences to the owner cell plus a list of the faces that do not fit
+        (``pair_dj``, ``pair_x``; 10 B per face instead of 12)."""
         if boundary not in ("periodic", "reflective"):
             raise ValueError("boundary must be 'periodic' or 'reflective'")
         self.boundary, self.xmin, self.xmax, self.n_strips = boundary, tuple(xmin), tuple(xmax), int(n_strips)
         self.resident = bool(resident)
+        self.pair16 = bool(pair16)
         self._h = lib().phd_tess2d_create()
         if not self._h:
             raise MemoryError("phd_tess2d_create")
@@ -209,7 +213,6 @@ class CompactMesher:
         L.phd_mesh2d_sizes(self._h, C.byref(nc), C.byref(nf), C.byref(pad_used))
         nc, F = nc.value, nf.value
         out = {"face_ptr": self._pinned("face_ptr", (n + 1,), torch.int32),
-               "pair_j": self._pinned("pair_j", (F,), torch.int32),
                "area32": self._pinned("area32", (F,), torch.float32),
                "ct32": self._pinned("ct32", (F,), torch.float32),
                "map": self._pinned("map", (nc,), torch.int32),
@@ -222,9 +225,25 @@ class CompactMesher:
         def ptr(k):
             return C.c_void_p(out[k].data_ptr()) if k in out else None
 
-        _check(L.phd_mesh2d_copy_compact(self._h, *(ptr(k) for k in ("face_ptr", "pair_j", "area32", "ct32", "x",
-                                                                      "map", "tag", "type", "ghost_code"))),
-               "copy_compact")
+        rest = ("area32", "ct32", "x", "map", "tag", "type", "ghost_code")
+        if not self.pair16:
+            out["pair_j"] = self._pinned("pair_j", (F,), torch.int32)
+            _check(L.phd_mesh2d_copy_compact(self._h, *(ptr(k) for k in ("face_ptr", "pair_j") + rest)),
+                   "copy_compact")
+            return out
+        # 16-bit bit patterns held as int16 (the device reads them as uint16)
+        out["pair_dj"] = self._pinned("pair_dj", (F,), torch.int16)
+        cap = self._buf["pair_x"].numel() // 2 if "pair_x" in self._buf else max(256, F // 64)
+        k = C.c_int32()
+        for _ in range(2):
+            px = self._pinned("pair_x", (2 * cap,), torch.int32)
+            rc = L.phd_mesh2d_copy_compact16(self._h, ptr("face_ptr"), ptr("pair_dj"), C.c_void_p(px.data_ptr()),
+                                             cap, C.byref(k), *(ptr(nm) for nm in rest))
+            if rc != -3:
+                break
+            cap = k.value
+        _check(rc, "copy_compact16")
+        out["pair_x"] = px[:2 * k.value]
         return out
 
 

@@ -59,7 +59,7 @@ def test_shear_1024_fp32_conserves_tracks_fp64_and_repeats(shear):
 
 def test_shear_1024_device_mesh_data_and_compact_hand_over(shear):
     mesh, prim, gamma = shear
-    st = FluxStepper(mesh, prim, gamma=gamma, precision="fp32")
+    st = FluxStepper(mesh, prim, gamma=gamma, precision="fp32", handover_records=True)
     geo = [t.clone() for t in (st.face_geo, st.face_ar, st.csr_face, st.csr_nbr, st.cell_geo)]
     e_real = int(mesh.nbr_ptr[mesh.n_real])
     rec = st.entry_rec[:e_real].clone()

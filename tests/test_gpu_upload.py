@@ -256,8 +256,9 @@ def test_compact_hand_over_equals_the_full_one(boundary):
     the steps that follow are identical; it moves about half the bytes."""
     meshes = _moved_meshes(20, boundary, 3, 4)
     prim = smooth_state(meshes[0])
-    a = FluxStepper(meshes[0], prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32")
-    b = FluxStepper(meshes[0], prim, gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32")
+    kw = dict(gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32", handover_records=True)
+    a = FluxStepper(meshes[0], prim, **kw)
+    b = FluxStepper(meshes[0], prim, **kw)
     for k in range(1, len(meshes)):
         a.step(1)
         b.step(1)
@@ -424,7 +425,8 @@ def test_compact_hand_over_without_periodic_dedup():
     the full hand-over with de-duplication off."""
     meshes = _moved_meshes(20, "periodic", 5, 3)
     prim = smooth_state(meshes[0])
-    kw = dict(gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32", dedup_periodic=False)
+    kw = dict(gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32", dedup_periodic=False,
+              handover_records=True)
     a = FluxStepper(meshes[0], prim, **kw)
     b = FluxStepper(meshes[0], prim, **kw)
     for k in range(1, len(meshes)):
@@ -442,3 +444,79 @@ def test_compact_hand_over_without_periodic_dedup():
     a.step(2)
     b.step(2)
     assert np.array_equal(a.cons_host(), b.cons_host())
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+@pytest.mark.parametrize("limiter", ["arepo", "tess"])
+def test_steps_without_entry_records_equal_steps_with_them(boundary, limiter):
+    """A hand-over without the per-entry gradient records: the gradient kernel forms
+    each entry's record from its face with the same roundings, so cell records,
+    velocities and conserved totals equal those of a stepper whose hand-over wrote the
+    records, bit for bit, through the device generator move and compact re-meshes; the
+    records built afterwards equal the hand-over's, and a captured graph uses them."""
+    meshes = _moved_meshes(20, boundary, 13, 2)
+    prim = smooth_state(meshes[0])
+    kw = dict(gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32", limiter=limiter)
+    a = FluxStepper(meshes[0], prim, handover_records=True, **kw)
+    b = FluxStepper(meshes[0], prim, **kw)
+    mesher = pkg.tess.CompactMesher(boundary, resident=True)
+    for _ in range(3):
+        a.step(1)
+        b.step(1)
+        xa = a.move_generators()
+        xb = b.move_generators()
+        a.check_status()
+        b.check_status()
+        x_host = xa.cpu().numpy()
+        assert np.array_equal(x_host, xb.cpu().numpy())
+        a.load_mesh(mesher(x_host))
+        b.load_mesh(mesher(x_host))
+        assert a.records and not b.records and b.geo.entry_rec is None
+        a.step(1)
+        b.step(1)
+        torch.cuda.synchronize()
+        assert torch.equal(a.cellrec, b.cellrec)
+        assert torch.equal(a.w2, b.w2)
+        assert np.array_equal(a.cons_host(), b.cons_host())
+    e = int(a.dmesh.nbr_ptr[a.dmesh.n_real].item())
+    b.capture(2)                                  # builds the records first
+    assert b.records and b.geo.entry_rec is not None
+    torch.cuda.synchronize()
+    assert torch.equal(a.entry_rec[:e], b.entry_rec[:e])
+    a.step(2)
+    b.replay()
+    torch.cuda.synchronize()
+    assert np.array_equal(a.cons_host(), b.cons_host())
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+def test_packed_pair_j_hand_over_equals_the_int32_one(boundary):
+    """pair-j handed over as 16-bit differences to the owner cell plus the escaped faces
+    (pair_dj, pair_x) decodes on the device to the int32 hand-over's pair-j: every derived
+    array and the steps that follow are the same, bit for bit.  67,600 real cells, so
+    faces to far ghosts escape; the C++ mesher's packed hand-over equals numpy's."""
+    meshes = _moved_meshes(260, boundary, 23, 2)
+    prim = smooth_state(meshes[0])
+    kw = dict(gamma=1.4, cfl=0.5, solver="hllc", moving=True, precision="fp32")
+    a = FluxStepper(meshes[0], prim, **kw)
+    b = FluxStepper(meshes[0], prim, **kw)
+    pa = a.dmesh.pinned_host_compact(meshes[1], pair16=False)
+    pb = b.dmesh.pinned_host_compact(meshes[1])
+    assert pb["pair_x"].numel() > 0
+    na = a.load_mesh(pa)
+    nb = b.load_mesh(pb)
+    assert nb < na
+    torch.cuda.synchronize()
+    assert a.dmesh.upload_errors() == 0 and b.dmesh.upload_errors() == 0
+    for name in ("pair_i", "pair_j", "nbr_ptr", "nbr_idx", "x", "flip"):
+        assert torch.equal(getattr(a.dmesh, name), getattr(b.dmesh, name)), name
+    for name in ("face_geo", "face_ar", "csr_face", "csr_nbr", "cell_geo", "twin", "prim4"):
+        assert torch.equal(getattr(a, name), getattr(b, name)), name
+    a.step(2)
+    b.step(2)
+    a.check_status()
+    assert np.array_equal(a.cons_host(), b.cons_host())
+    c = pkg.tess.CompactMesher(boundary)(meshes[1].x[:, :meshes[1].n_real])
+    assert sorted(c) == sorted(pb)
+    for k in pb:
+        assert torch.equal(c[k], pb[k]), k

@@ -190,3 +190,60 @@ def test_insertion_order_does_not_change_the_mesh():
     assert a["pair_i"].size == b["pair_i"].size
     assert pairs(a, np.arange(nr)) == pairs(b, perm)
     np.testing.assert_allclose(b["vol"][:nr], a["vol"][perm], rtol=1e-13)
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "reflective"])
+def test_compact_pair_j_packing_round_trips(boundary):
+    """phd_mesh2d_copy_compact16: pair-j as the 16-bit difference to the owner cell with
+    the faces that do not fit listed as (face id, pair-j) in ascending face id -- decoded,
+    the int32 pair-j of phd_mesh2d_copy_compact; every other array is the same; a list
+    buffer that is too small gives -3 and the number needed."""
+    import ctypes as C
+    L = tess.lib()
+    x = meshgen.jittered_lattice(260, jitter=0.4, seed=3)         # 67,600 real cells: escapes
+    h = L.phd_tess2d_create()
+    try:
+        pad = 3.0 / 260
+        assert L.phd_mesh2d_build_strips(h, x[0].ctypes.data_as(C.c_void_p), x[1].ctypes.data_as(C.c_void_p),
+                                         x.shape[1], {"periodic": 0, "reflective": 1}[boundary], 0.0, 0.0, 1.0,
+                                         1.0, pad, 0) >= 0
+        nc, nf, pu = C.c_int32(), C.c_int32(), C.c_double()
+        L.phd_mesh2d_sizes(h, C.byref(nc), C.byref(nf), C.byref(pu))
+        n, F, nr = nc.value, nf.value, x.shape[1]
+
+        def bufs():
+            return {"face_ptr": np.zeros(nr + 1, np.int32), "area32": np.zeros(F, np.float32),
+                    "ct32": np.zeros(F, np.float32), "x": np.zeros((2, n)), "map": np.zeros(n, np.int32),
+                    "tag": np.zeros(n, np.int8), "type": np.zeros(n, np.int8),
+                    "ghost_code": np.zeros(max(n - nr, 1), np.int8)}
+
+        p = lambda a: a.ctypes.data_as(C.c_void_p)
+        rest = ("area32", "ct32", "x", "map", "tag", "type", "ghost_code")
+        a = bufs()
+        pair_j = np.zeros(F, np.int32)
+        assert L.phd_mesh2d_copy_compact(h, p(a["face_ptr"]), p(pair_j), *(p(a[k]) for k in rest)) == 0
+        b = bufs()
+        dj = np.zeros(F, np.uint16)
+        k = C.c_int32()
+        small = np.zeros(2 * 4, np.int32)
+        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(small), 4, C.byref(k),
+                                           *(p(b[nm]) for nm in rest)) == -3
+        K = k.value
+        assert K > 4
+        px = np.zeros(2 * K, np.int32)
+        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(px), K, C.byref(k),
+                                           *(p(b[nm]) for nm in rest)) == 0
+        assert k.value == K
+    finally:
+        L.phd_tess2d_destroy(h)
+    for nm in a:
+        np.testing.assert_array_equal(a[nm], b[nm], err_msg=nm)
+    owner = np.repeat(np.arange(nr), np.diff(a["face_ptr"]))
+    fid, pj = px[0::2], px[1::2]
+    assert np.all(np.diff(fid) > 0)
+    assert np.array_equal(np.flatnonzero(dj == 0), fid)
+    decoded = owner + dj.astype(np.int64)
+    decoded[fid] = pj
+    np.testing.assert_array_equal(decoded, pair_j)
+    d = pair_j.astype(np.int64) - owner
+    assert np.array_equal((d >= 1) & (d <= 65535), dj != 0)
