@@ -311,8 +311,9 @@ int phd_ghost_positions(const phd_mesh *mesh, const int8_t *ghost_code, double x
  * separately (no fused multiply-add), s = (c_x (-dy) + c_y dx) / r, 0 where r = 0 (c
  * lies along the face: a Voronoi face is on the perpendicular bisector of x_i x_j).
  * pair-j may come packed in 2 B per face: pair_dj[f] = pair_j[f] - pair_i[f] where that
- * lies in [1, 65535], else 0, with the faces marked 0 listed in pair_x as (face id,
- * pair-j) pairs in ascending face id (PHD_PAIR16_ESCAPE) -- 10 B per face in all.
+ * lies in [1, 65534], else 0 (PHD_PAIR16_ESCAPE), with the faces marked 0 listed in
+ * pair_x as (face id, pair-j) pairs in ascending face id -- 10 B per face in all (65535
+ * is not used: the device marks the listed faces with it while decoding).
  *
  * phd_pair_i_from_face_ptr: pair_i[m] = c for m in [face_ptr[c], face_ptr[c+1]);
  * face_ptr (n_real + 1 entries) must start at 0, end at n_faces and not decrease --
@@ -375,11 +376,16 @@ typedef struct phd_handover32 {
     int32_t dedup_periodic;       /* 1: periodic twin faces counted once (phd_periodic_twins) */
     double xmin[2], xmax[2];      /* the box */
     /* packed pair-j (with pair_j == NULL; see above) */
-    const uint16_t *pair_dj;      /* [n_faces] host: pair-j minus pair-i, or PHD_PAIR16_ESCAPE */
+    const uint16_t *pair_dj;      /* [n_faces] host: pair-j minus pair-i in [1, 65534], or PHD_PAIR16_ESCAPE */
     const int32_t *pair_x;        /* [2 n_pair_x] host: (face id, pair-j) of the escaped faces */
     int32_t n_pair_x;
-    uint16_t *d_pair_dj;          /* [n_faces] staging */
+    uint16_t *d_pair_dj;          /* [n_faces] staging (the call marks the listed faces in it) */
     int32_t *d_pair_x;            /* [2 n_pair_x] staging */
+    /* optional: each cell's neighbour-list length (its faces; every length <= 255), so
+     * the lists are laid out without counting them on the device.  Lengths that do not
+     * match the faces add to *bad; the lists then stay inside their storage. */
+    const uint8_t *list_len;      /* [n_cells] host, or NULL */
+    uint8_t *d_list_len;          /* [n_cells] staging */
 } phd_handover32;
 
 int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_params *par, phd_geom32_out *out,

@@ -1083,7 +1083,7 @@ static int copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j,
             pair_j[f] = j;
         } else {
             const int64_t d = int64_t(j) - int64_t(i);
-            if (d >= 1 && d <= 65535) {
+            if (d >= 1 && d <= 65534) {
                 pair_dj[f] = uint16_t(d);
             } else {
                 pair_dj[f] = PHD_PAIR16_ESCAPE;
@@ -1113,7 +1113,7 @@ static int copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j,
         tag[k] = k < nr ? 0 : 1;                        // Real / Ghost (particle_tags.py:1-6)
         type[k] = k < nr ? 4 : 2;                       // Undefined / Exterior
     }
-    return (n_pair_x && *n_pair_x > x_cap) ? -3 : 0;
+    return (n_pair_x && *n_pair_x > x_cap) ? -5 : 0;
 }
 
 int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *ct32,
@@ -1125,14 +1125,28 @@ int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pai
 }
 
 int phd_mesh2d_copy_compact16(const phd_tess2d *t, int32_t *face_ptr, uint16_t *pair_dj, int32_t *pair_x,
-                              int32_t x_cap, int32_t *n_pair_x, float *area32, float *ct32, double *x,
-                              int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
+                              int32_t x_cap, int32_t *n_pair_x, uint8_t *list_len, float *area32, float *ct32,
+                              double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
     if (!t || t->G.n_cells == 0 || !face_ptr || !pair_dj || !n_pair_x || x_cap < 0 || (x_cap > 0 && !pair_x) ||
         !area32 || !ct32 || !map || !tag || !type)
         return -2;
     *n_pair_x = 0;
-    return copy_compact(t, face_ptr, nullptr, pair_dj, pair_x, x_cap, n_pair_x, area32, ct32, x, map, tag, type,
-                        ghost_code);
+    const int rc = copy_compact(t, face_ptr, nullptr, pair_dj, pair_x, x_cap, n_pair_x, area32, ct32, x, map, tag,
+                                type, ghost_code);
+    if (rc < 0 || !list_len) return rc;
+    // each face adds one entry to the lists of both its cells (tess.cpp:378-379)
+    const Geometry &G = t->G;
+    std::vector<int32_t> len(G.n_cells, 0);
+    for (int f = 0; f < G.n_faces; f++) {
+        len[G.pair_i[f]]++;
+        len[G.pair_j[f]]++;
+    }
+    bool fits = true;
+    for (int c = 0; c < G.n_cells; c++) {
+        fits = fits && len[c] <= 255;
+        list_len[c] = uint8_t(len[c] <= 255 ? len[c] : 255);
+    }
+    return fits ? 0 : -6;
 }
 
 void phd_hilbert_keys_2d_host(const int32_t *xh, const int32_t *yh, int64_t n, int order, int64_t *keys) {

@@ -128,12 +128,13 @@ __device__ __forceinline__ void tile_scan(const int32_t v[SCAN_ITEMS], int32_t e
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(int n, const int32_t *__restrict__ cnt,
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_tiles(int n, const T *__restrict__ cnt,
                                                              int32_t *__restrict__ tile_sum) {
     const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int32_t v[SCAN_ITEMS], ex[SCAN_ITEMS], total;
 #pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = (base + k < n) ? cnt[base + k] : 0;
+    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = (base + k < n) ? int32_t(cnt[base + k]) : 0;
     tile_scan(v, ex, total);
     if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
 }
@@ -154,19 +155,22 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_tile_sums(int n_tiles, in
     }
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_offsets(int n, const int32_t *__restrict__ cnt,
+// cap: offsets are clamped to it (list lengths from the host are not trusted to add
+// up to the entries' storage; with them clamped every list stays inside it)
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_offsets(int n, const T *__restrict__ cnt,
                                                                const int32_t *__restrict__ tile_sum,
-                                                               int32_t *__restrict__ ptr) {
+                                                               int32_t *__restrict__ ptr, int cap) {
     const int base = blockIdx.x * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
     int32_t v[SCAN_ITEMS], ex[SCAN_ITEMS], total;
 #pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = (base + k < n) ? cnt[base + k] : 0;
+    for (int k = 0; k < SCAN_ITEMS; k++) v[k] = (base + k < n) ? int32_t(cnt[base + k]) : 0;
     tile_scan(v, ex, total);
     const int32_t off = tile_sum[blockIdx.x];
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; k++) {
-        if (base + k < n) ptr[base + k] = off + ex[k];
-        if (base + k == n - 1) ptr[n] = off + ex[k] + v[k];
+        if (base + k < n) ptr[base + k] = min(off + ex[k], cap);
+        if (base + k == n - 1) ptr[n] = min(off + ex[k] + v[k], cap);
     }
 }
 
@@ -226,27 +230,23 @@ __global__ void k_csr_sort(int n, const int32_t *__restrict__ ptr, int32_t *__re
     sort_list(idx, ptr[c], ptr[c + 1]);
 }
 
-// k_csr_sort followed, by the same thread, by the FP32 list codes of the sorted list, for
-// a hand-over whose faces come in per-real-cell ranges: an entry is pair-i side exactly
-// when its face lies in the cell's own range (pair-i was written from the ranges), so
-// one gather per entry gives the other cell -- pair-j of an own face, pair-i of another
-// -- and only own faces to a ghost look up the twin table (the table built from the
-// ranges holds twins of such faces only).  The codes equal emit_list_codes' (the
-// PHD_PREP_LISTS kernel) on any hand-over whose ranges tile the face list.
-__global__ void k_csr_sort_codes_ranges(phd_mesh M, const int32_t *__restrict__ face_ptr,
-                                        const int32_t *__restrict__ twin, int32_t *idx,
-                                        int32_t *__restrict__ csr_face, int32_t *__restrict__ csr_nbr) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= M.n_cells) return;
+// The FP32 list codes of cell c's sorted list entries [e0, e1) of src (face ids), for a
+// hand-over whose faces come in per-real-cell ranges ([f0, f1) the cell's own, empty
+// for a ghost), written at the same positions of code / nbr: an entry is pair-i side
+// exactly when its face lies in the cell's own range (pair-i was written from the
+// ranges), so one gather per entry gives the other cell -- pair-j of an own face, pair-i
+// of another -- and only own faces to a ghost look up the twin table (the table built
+// from the ranges holds twins of such faces only).  The codes equal emit_list_codes'
+// (the PHD_PREP_LISTS kernel) on any hand-over whose ranges tile the face list.
+__device__ __forceinline__ void range_list_codes(const phd_mesh &M, int c, int f0, int f1,
+                                                 const int32_t *__restrict__ twin, const int32_t *src, int e0,
+                                                 int e1, int32_t *code_out, int32_t *nbr_out) {
     const int n = M.n_cells, nr = M.n_real, F = M.n_faces;
-    const int e0 = M.nbr_ptr[c], e1 = M.nbr_ptr[c + 1];
-    const int f0 = c < nr ? face_ptr[c] : 0, f1 = c < nr ? face_ptr[c + 1] : 0;
-    sort_list(idx, e0, e1);
     constexpr int CH = 4;
     for (int eb = e0; eb < e1; eb += CH) {
         int fid[CH], o[CH];
 #pragma unroll
-        for (int k = 0; k < CH; k++) fid[k] = idx[(eb + k < e1) ? eb + k : e0];
+        for (int k = 0; k < CH; k++) fid[k] = src[(eb + k < e1) ? eb + k : e0];
 #pragma unroll
         for (int k = 0; k < CH; k++) {
             const bool ok = fid[k] >= 0 && fid[k] < F;
@@ -257,7 +257,7 @@ __global__ void k_csr_sort_codes_ranges(phd_mesh M, const int32_t *__restrict__ 
         for (int k = 0; k < CH; k++) {
             const int e = eb + k;
             if (e >= e1) break;
-            if (fid[k] < 0 || fid[k] >= F) { csr_face[e] = 0; csr_nbr[e] = c; continue; }
+            if (fid[k] < 0 || fid[k] >= F) { code_out[e] = 0; nbr_out[e] = c; continue; }
             const bool own = fid[k] >= f0 && fid[k] < f1;
             int other = o[k];
             int code = own ? fid[k] : ~fid[k];
@@ -269,9 +269,60 @@ __global__ void k_csr_sort_codes_ranges(phd_mesh M, const int32_t *__restrict__ 
                 }
             }
             if (other < 0 || other >= n) other = c;
-            csr_face[e] = code;
-            csr_nbr[e] = other;
+            code_out[e] = code;
+            nbr_out[e] = other;
         }
+    }
+}
+
+// k_csr_sort followed by the FP32 list codes (range_list_codes), one pass.  Each warp
+// takes 32 consecutive cells, whose lists are one contiguous span of entries: the span
+// is loaded into shared memory with coalesced loads, each thread sorts and codes its
+// own cell's list there, and the sorted ids and codes go back with coalesced stores.
+// A span longer than SC_CAP entries (cells with unusually many faces) is done by each
+// thread in global memory instead.
+constexpr int SC_WARPS = UBLOCK / 32, SC_CAP = 320;
+
+// cursor (with list lengths from the host): each list's pair-j entries as scattered,
+// checked against its length less its own range (a mismatch adds to *bad).
+__global__ void __launch_bounds__(UBLOCK) k_csr_sort_codes_ranges(phd_mesh M, const int32_t *__restrict__ face_ptr,
+                                                                  const int32_t *__restrict__ twin, int32_t *idx,
+                                                                  int32_t *__restrict__ csr_face,
+                                                                  int32_t *__restrict__ csr_nbr,
+                                                                  const int32_t *__restrict__ cursor,
+                                                                  int32_t *__restrict__ bad) {
+    __shared__ int32_t s_idx[SC_WARPS][SC_CAP], s_code[SC_WARPS][SC_CAP], s_nbr[SC_WARPS][SC_CAP];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n = M.n_cells, nr = M.n_real;
+    const int c0 = blockIdx.x * blockDim.x + w * 32;
+    if (c0 >= n) return;                                      // the whole warp
+    const int c = c0 + lane;
+    const bool live = c < n;
+    const int e0 = live ? M.nbr_ptr[c] : 0, e1 = live ? M.nbr_ptr[c + 1] : 0;
+    const int f0 = (live && c < nr) ? face_ptr[c] : 0, f1 = (live && c < nr) ? face_ptr[c + 1] : 0;
+    if (cursor && live && cursor[c] != (e1 - e0) - (f1 - f0)) atomicAdd(bad, 1);
+    const int last = min(31, n - 1 - c0);
+    const int E0 = __shfl_sync(0xffffffffu, e0, 0), E1 = __shfl_sync(0xffffffffu, e1, last);
+    const bool fits = !live || (e0 >= E0 && e0 <= e1 && e1 <= E1);
+    if (!__all_sync(0xffffffffu, fits) || E1 - E0 > SC_CAP) {
+        if (live) {
+            sort_list(idx, e0, e1);
+            range_list_codes(M, c, f0, f1, twin, idx, e0, e1, csr_face, csr_nbr);
+        }
+        return;
+    }
+    const int span = E1 - E0;
+    for (int k = lane; k < span; k += 32) s_idx[w][k] = idx[E0 + k];
+    __syncwarp();
+    if (live) {
+        sort_list(&s_idx[w][0], e0 - E0, e1 - E0);
+        range_list_codes(M, c, f0, f1, twin, &s_idx[w][0], e0 - E0, e1 - E0, &s_code[w][0], &s_nbr[w][0]);
+    }
+    __syncwarp();
+    for (int k = lane; k < span; k += 32) {
+        idx[E0 + k] = s_idx[w][k];
+        csr_face[E0 + k] = s_code[w][k];
+        csr_nbr[E0 + k] = s_nbr[w][k];
     }
 }
 
@@ -435,65 +486,108 @@ __device__ __forceinline__ bool range_ok(int c, int n_real, int F, int a, int b)
     return !(a < 0 || b < a || b > F || (c == 0 && a != 0) || (c == n_real - 1 && b != F));
 }
 
-// pair-j of an escaped face from the (face id, pair-j) list px[K] (ascending face ids);
-// -1 when the face is not listed.
-__device__ __forceinline__ int pair_j_escaped(int m, const int32_t *__restrict__ px, int K) {
-    int lo = 0, hi = K;
-    while (lo < hi) {                    // at most log2(K) + 1 rounds
-        const int mid = (lo + hi) >> 1;
-        if (px[2 * mid] < m)
-            lo = mid + 1;
-        else
-            hi = mid;
+// The escaped faces of a packed pair-j hand-over: pair_j[fid] from the (face id, pair-j)
+// list px[K], and the face's packed entry (the device staging copy) turned from
+// PHD_PAIR16_ESCAPE into PAIR16_LISTED, so k_faces_from_ranges can tell a listed face
+// from one marked escaped but missing from the list (an error).  A listed face that is
+// not marked escaped, or out of range, adds to *bad.
+constexpr uint16_t PAIR16_LISTED = 0xffff;
+
+__global__ void k_pair_escapes(int K, int F, const int32_t *__restrict__ px, uint16_t *__restrict__ dj,
+                               int32_t *__restrict__ pair_j, int32_t *__restrict__ bad) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= K) return;
+    const int fid = px[2 * k];
+    if (fid < 0 || fid >= F || (dj[fid] != PHD_PAIR16_ESCAPE && dj[fid] != PAIR16_LISTED)) {
+        atomicAdd(bad, 1);
+        return;
     }
-    return (lo < K && px[2 * lo] == m) ? px[2 * lo + 1] : -1;
+    pair_j[fid] = px[2 * k + 1];
+    dj[fid] = PAIR16_LISTED;
 }
 
-// dj (optional): pair-j packed as the difference to the owner (PHD_PAIR16_ESCAPE and the
-// list px[K] for the rest), decoded here into pair_j.
-__global__ void k_csr_count_ranges(int n_real, int n, int F, const int32_t *__restrict__ face_ptr,
-                                   int32_t *__restrict__ pair_j, const uint16_t *__restrict__ dj,
-                                   const int32_t *__restrict__ px, int K, int32_t *__restrict__ pair_i,
-                                   int32_t *__restrict__ cnt, int32_t *__restrict__ bad) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_real) return;
-    const int a = face_ptr[c], b = face_ptr[c + 1];
-    if (!range_ok(c, n_real, F, a, b)) { atomicAdd(bad, 1); return; }
-    int own = 0;
-    for (int m = a; m < b; m++) {
+// pair-i (and pair-j, when packed) of every face from the per-real-cell face ranges,
+// one thread per face: a block takes UBLOCK consecutive real cells, stages their range
+// bounds in shared memory, and each thread finds its face's owner there by bisection,
+// so every face array is read and written coalesced.  dj (optional): pair-j packed as
+// the difference to the owner (PAIR16_LISTED: k_pair_escapes has written it;
+// PHD_PAIR16_ESCAPE: escaped but not listed, an error).  COUNT: the list lengths counted
+// with atomics into cnt; otherwise they came from the host.  A block holding a broken
+// range (face_ptr not starting at 0, decreasing, or not ending at n_faces) adds 1 to
+// *bad per broken cell and writes nothing; faces with out-of-range or equal cells add 1.
+template <bool COUNT>
+__global__ void __launch_bounds__(UBLOCK) k_faces_from_ranges(int n_real, int n, int F,
+                                                              const int32_t *__restrict__ face_ptr,
+                                                              int32_t *__restrict__ pair_j, const uint16_t *dj,
+                                                              int32_t *__restrict__ pair_i,
+                                                              int32_t *__restrict__ cnt, int32_t *__restrict__ bad) {
+    __shared__ int32_t s_fp[UBLOCK + 1];
+    __shared__ int s_broken;
+    const int c0 = blockIdx.x * UBLOCK;
+    const int nc = min(UBLOCK, n_real - c0);
+    if (nc <= 0) return;
+    if (threadIdx.x == 0) s_broken = 0;
+    for (int k = threadIdx.x; k <= nc; k += blockDim.x) s_fp[k] = face_ptr[c0 + k];
+    __syncthreads();
+    if (threadIdx.x < nc && !range_ok(c0 + threadIdx.x, n_real, F, s_fp[threadIdx.x], s_fp[threadIdx.x + 1])) {
+        atomicAdd(bad, 1);
+        s_broken = 1;
+    }
+    __syncthreads();
+    if (s_broken) return;
+    const int m1 = s_fp[nc];
+    for (int m = s_fp[0] + threadIdx.x; m < m1; m += blockDim.x) {
+        int lo = 0, hi = nc;                       // s_fp[lo] <= m < s_fp[hi]
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (s_fp[mid] <= m)
+                lo = mid;
+            else
+                hi = mid;
+        }
+        const int c = c0 + lo;
         pair_i[m] = c;
         int j;
-        if (dj) {
-            const int d = dj[m];
-            j = d != PHD_PAIR16_ESCAPE ? c + d : pair_j_escaped(m, px, K);
-            pair_j[m] = j;
-        } else {
+        const int d = dj ? dj[m] : PAIR16_LISTED;
+        if (d == PAIR16_LISTED) {
             j = pair_j[m];
+        } else {
+            j = d != PHD_PAIR16_ESCAPE ? c + d : -1;
+            pair_j[m] = j;
         }
         if (j >= 0 && j < n && j != c) {
-            atomicAdd(&cnt[j], 1);
-            own++;
+            if (COUNT) {
+                atomicAdd(&cnt[j], 1);
+                atomicAdd(&cnt[c], 1);
+            }
         } else {
             atomicAdd(bad, 1);
         }
     }
-    if (own) atomicAdd(&cnt[c], own);
 }
 
-__global__ void k_csr_scatter_ranges(int n_real, int n, int F, const int32_t *__restrict__ face_ptr,
-                                     const int32_t *__restrict__ pair_j, const int32_t *__restrict__ ptr,
-                                     int32_t *__restrict__ cursor, int32_t *__restrict__ idx) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n_real) return;
-    const int a = face_ptr[c], b = face_ptr[c + 1];
-    if (!range_ok(c, n_real, F, a, b)) return;
-    int end = ptr[c + 1];
-    for (int m = b - 1; m >= a; m--) {
-        const int j = pair_j[m];
-        if (j >= 0 && j < n && j != c) {
-            idx[--end] = m;
-            idx[ptr[j] + atomicAdd(&cursor[j], 1)] = m;
-        }
+// The faces into the neighbour lists, one thread per face: the owner's entry at the
+// tail of its list in face order (its own range, so the list ends with it sorted), the
+// other cell's through its cursor.  Faces with bad cells (counted by
+// k_faces_from_ranges) are skipped.  Every write lands inside idx[0, cap): with list
+// lengths from the host, a face set that does not match them adds to *bad here (a
+// write outside) or in the sort (a list not filled exactly), and never writes out of
+// bounds.
+__global__ void k_csr_scatter_faces(int n_real, int n, int F, const int32_t *__restrict__ face_ptr,
+                                    const int32_t *__restrict__ pair_i, const int32_t *__restrict__ pair_j,
+                                    const int32_t *__restrict__ ptr, int32_t *__restrict__ cursor,
+                                    int32_t *__restrict__ idx, int cap, int32_t *__restrict__ bad) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= F) return;
+    const int i = pair_i[m], j = pair_j[m];
+    if (i < 0 || i >= n_real || j < 0 || j >= n || j == i) return;
+    const int own = ptr[i + 1] - (face_ptr[i + 1] - m);
+    const int q = ptr[j] + atomicAdd(&cursor[j], 1);
+    if (own >= 0 && own < cap && q >= 0 && q < cap) {
+        idx[own] = m;
+        idx[q] = m;
+    } else {
+        atomicAdd(bad, 1);
     }
 }
 
@@ -547,7 +641,7 @@ int phd_build_csr(const phd_mesh *mesh, int32_t *nbr_ptr, int32_t *nbr_idx, int3
     if (F) phd::k_csr_count<<<gf, phd::UBLOCK, 0, stream>>>(n, F, mesh->pair_i, mesh->pair_j, cnt, bad);
     phd::k_scan_tiles<<<n_tiles, phd::SCAN_THREADS, 0, stream>>>(n, cnt, tile_sum);
     phd::k_scan_tile_sums<<<1, phd::SCAN_THREADS, 0, stream>>>(n_tiles, tile_sum);
-    phd::k_scan_offsets<<<n_tiles, phd::SCAN_THREADS, 0, stream>>>(n, cnt, tile_sum, nbr_ptr);
+    phd::k_scan_offsets<<<n_tiles, phd::SCAN_THREADS, 0, stream>>>(n, cnt, tile_sum, nbr_ptr, INT32_MAX);
     if (F) {
         phd::k_csr_scatter<<<gf, phd::UBLOCK, 0, stream>>>(n, F, mesh->pair_i, mesh->pair_j, nbr_ptr, cursor,
                                                             nbr_idx);
@@ -618,6 +712,8 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
                    (h->n_pair_x > 0 && (!h->pair_x || !h->d_pair_x))))
         return PHD_ERR_ARG;
     if (!h->x && ng > 0 && (!h->ghost_code || !h->d_ghost_code)) return PHD_ERR_ARG;
+    const bool host_len = h->list_len != nullptr;  // list lengths from the host: no atomic count
+    if (host_len && !h->d_list_len) return PHD_ERR_ARG;
     int32_t *pair_i = const_cast<int32_t *>(mesh->pair_i);
     int32_t *pair_j = const_cast<int32_t *>(mesh->pair_j);
     double *x = const_cast<double *>(mesh->x);
@@ -635,6 +731,7 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     // stream: the face ranges and pair-j, then the per-ghost arrays, then the large FP32
     // face records; each group's event releases the work that needs it
     PHD_TRY_CUDA(cudaMemsetAsync(h->bad, 0, sizeof(int32_t), stream));
+    if (host_len) PHD_TRY_CUDA(cudaMemcpyAsync(h->d_list_len, h->list_len, (size_t)n, H2D, stream));
     PHD_TRY_CUDA(cudaMemcpyAsync(h->d_face_ptr, h->face_ptr, (size_t)(nr + 1) * sizeof(int32_t), H2D, stream));
     if (!packed) {
         PHD_TRY_CUDA(cudaMemcpyAsync(pair_j, h->pair_j, (size_t)F * sizeof(int32_t), H2D, stream));
@@ -671,35 +768,56 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     const int n_tiles = (n + phd::SCAN_TILE - 1) / phd::SCAN_TILE;
     const int gr = nr > 0 ? (nr + phd::UBLOCK - 1) / phd::UBLOCK : 1;
     PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[0], 0));
-    PHD_TRY_CUDA(cudaMemsetAsync(h->csr_work, 0, sizeof(int32_t) * phd_csr_work_ints(n), lists));
-    if (nr > 0)
-        phd::k_csr_count_ranges<<<gr, phd::UBLOCK, 0, lists>>>(nr, n, F, h->d_face_ptr, pair_j,
-                                                               packed ? h->d_pair_dj : nullptr, h->d_pair_x,
-                                                               packed ? h->n_pair_x : 0, pair_i, cnt, h->bad);
-    PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[1], 0));
-    if (!h->x && n > 0) {
-        const bool copy_real = h->x_real != nullptr;
-        const int first = copy_real ? 0 : nr;
-        if (n > first)
-            phd::k_positions<<<(n - first + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, lists>>>(
-                nr, n, copy_real, mesh->map, h->d_ghost_code, h->xmin[0], h->xmin[1], h->xmax[0], h->xmax[1],
-                copy_real ? h->x_real : x, copy_real ? (size_t)nr : (size_t)n, x, h->bad);
+    if (host_len)                                      // the cursors only
+        PHD_TRY_CUDA(cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (size_t)n, lists));
+    else
+        PHD_TRY_CUDA(cudaMemsetAsync(h->csr_work, 0, sizeof(int32_t) * phd_csr_work_ints(n), lists));
+    if (packed && h->n_pair_x > 0)        // the escaped faces first
+        phd::k_pair_escapes<<<(h->n_pair_x + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, lists>>>(
+            h->n_pair_x, F, h->d_pair_x, h->d_pair_dj, pair_j, h->bad);
+    if (nr > 0) {
+        const uint16_t *dj = packed ? h->d_pair_dj : nullptr;
+        if (host_len)
+            phd::k_faces_from_ranges<false><<<gr, phd::UBLOCK, 0, lists>>>(nr, n, F, h->d_face_ptr, pair_j, dj,
+                                                                           pair_i, cnt, h->bad);
+        else
+            phd::k_faces_from_ranges<true><<<gr, phd::UBLOCK, 0, lists>>>(nr, n, F, h->d_face_ptr, pair_j, dj,
+                                                                          pair_i, cnt, h->bad);
     }
     PHD_TRY_CUDA(cudaEventRecord(events[3], lists));
-    phd::k_scan_tiles<<<n_tiles, phd::SCAN_THREADS, 0, lists>>>(n, cnt, tile_sum);
-    phd::k_scan_tile_sums<<<1, phd::SCAN_THREADS, 0, lists>>>(n_tiles, tile_sum);
-    phd::k_scan_offsets<<<n_tiles, phd::SCAN_THREADS, 0, lists>>>(n, cnt, tile_sum, const_cast<int32_t *>(nbr_ptr));
+    if (host_len) {
+        phd::k_scan_tiles<<<n_tiles, phd::SCAN_THREADS, 0, lists>>>(n, h->d_list_len, tile_sum);
+        phd::k_scan_tile_sums<<<1, phd::SCAN_THREADS, 0, lists>>>(n_tiles, tile_sum);
+        phd::k_scan_offsets<<<n_tiles, phd::SCAN_THREADS, 0, lists>>>(n, h->d_list_len, tile_sum,
+                                                                      const_cast<int32_t *>(nbr_ptr), 2 * F);
+    } else {
+        phd::k_scan_tiles<<<n_tiles, phd::SCAN_THREADS, 0, lists>>>(n, cnt, tile_sum);
+        phd::k_scan_tile_sums<<<1, phd::SCAN_THREADS, 0, lists>>>(n_tiles, tile_sum);
+        phd::k_scan_offsets<<<n_tiles, phd::SCAN_THREADS, 0, lists>>>(n, cnt, tile_sum,
+                                                                      const_cast<int32_t *>(nbr_ptr), INT32_MAX);
+    }
     if (nr > 0 && F > 0) {
-        phd::k_csr_scatter_ranges<<<gr, phd::UBLOCK, 0, lists>>>(nr, n, F, h->d_face_ptr, pair_j, nbr_ptr, cursor,
-                                                                 const_cast<int32_t *>(mesh->nbr_idx));
+        phd::k_csr_scatter_faces<<<(F + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, lists>>>(
+            nr, n, F, h->d_face_ptr, pair_i, pair_j, nbr_ptr, cursor, const_cast<int32_t *>(mesh->nbr_idx), 2 * F,
+            h->bad);
     }
     PHD_TRY_CUDA(cudaPeekAtLastError());
 
     // geometry stream, beside the lists: the flip bits and periodic twins once the
     // positions are there, the FP32 face geometry once the face records are too
     const double lo[3] = {h->xmin[0], h->xmin[1], 0.}, hi[3] = {h->xmax[0], h->xmax[1], 0.};
-    PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[3], 0));
+    // every position first (the ghosts' from their codes), beside the list counts
+    PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[1], 0));
+    if (!h->x && n > 0) {
+        const bool copy_real = h->x_real != nullptr;
+        const int first = copy_real ? 0 : nr;
+        if (n > first)
+            phd::k_positions<<<(n - first + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, geom>>>(
+                nr, n, copy_real, mesh->map, h->d_ghost_code, h->xmin[0], h->xmin[1], h->xmax[0], h->xmax[1],
+                copy_real ? h->x_real : x, copy_real ? (size_t)nr : (size_t)n, x, h->bad);
+    }
     PHD_TRY(phd_flip_mask(2, n, h->type, x, lo, hi, !h->periodic, const_cast<int8_t *>(mesh->flip), geom));
+    PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[3], 0));      // pair-i and pair-j
     if (F > 0) {
         if (h->periodic && h->dedup_periodic)
             phd::k_periodic_twins_ranges<<<(F + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, geom>>>(
@@ -728,7 +846,8 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     PHD_TRY_CUDA(cudaStreamWaitEvent(lists, events[6], 0));
     if (n > 0)
         phd::k_csr_sort_codes_ranges<<<(n + phd::UBLOCK - 1) / phd::UBLOCK, phd::UBLOCK, 0, lists>>>(
-            *mesh, h->d_face_ptr, h->twin, const_cast<int32_t *>(mesh->nbr_idx), out->csr_face, out->csr_nbr);
+            *mesh, h->d_face_ptr, h->twin, const_cast<int32_t *>(mesh->nbr_idx), out->csr_face, out->csr_nbr,
+            host_len ? cursor : nullptr, h->bad);
     PHD_TRY_CUDA(cudaPeekAtLastError());
     PHD_TRY_CUDA(cudaEventRecord(events[5], lists));
 

@@ -177,7 +177,8 @@ class DeviceMesh:
         generator move); ghost codes replace the positions (``phd_ghost_positions``).
         ``pair16``: pair-j as the 16-bit difference to the owner cell (``pair_dj``, 0 =
         escape) plus the escaped faces' (face id, pair-j) pairs (``pair_x``): 10 B per
-        face."""
+        face; and each cell's list length (``list_len``, one byte) so the device lays out
+        the neighbour lists without counting them."""
         self._check_remesh(host)
         nr = self.n_real
         pi, pj = np.asarray(host.pair_i), np.asarray(host.pair_j)
@@ -203,11 +204,14 @@ class DeviceMesh:
                   "type": np.ascontiguousarray(host.type, dtype=np.int8)}
         if pair16:
             d = pj.astype(np.int64) - pi.astype(np.int64)
-            ok = (d >= 1) & (d <= 65535)
+            ok = (d >= 1) & (d <= 65534)
             esc = np.flatnonzero(~ok)
             # the 16-bit patterns as int16 (the device reads them as uint16)
             arrays["pair_dj"] = np.where(ok, d, 0).astype(np.uint16).view(np.int16)
             arrays["pair_x"] = np.stack([esc, pj[esc]], axis=1).astype(np.int32).reshape(-1)
+            ln = np.bincount(np.concatenate([pi, pj]).astype(np.int64), minlength=len(host.map))
+            if ln.max(initial=0) <= 255:            # else the device counts them
+                arrays["list_len"] = ln.astype(np.uint8)
         else:
             arrays["pair_j"] = np.ascontiguousarray(pj, dtype=np.int32)
         if resident:            # the device holds the real positions; ghosts from their codes
@@ -231,6 +235,8 @@ class DeviceMesh:
         if "face_ptr" in pinned:
             names = ("face_ptr", "pair_j" if "pair_j" in pinned else "pair_dj", "area32", "ct32", "map", "tag",
                      "type") + (("x",) if "x" in pinned else ("ghost_code",))
+            if "list_len" in pinned and tuple(pinned["list_len"].shape) != (self.n_cells,):
+                raise ValueError("upload: list_len must hold one length per cell")
             if "pair_dj" in pinned:
                 px = pinned["pair_x"]
                 if px.dim() != 1 or px.numel() % 2 or px.numel() > 2 * self.n_faces:

@@ -320,6 +320,8 @@ class FluxStepper:
         if packed:
             stage["pair_dj"] = self._view("pair_dj_in", (nf,), torch.int16)
             stage["pair_x"] = self._view("pair_x_in", (max(2 * n_x, 2),), torch.int32)
+        if "list_len" in pinned:
+            stage["list_len"] = self._view("list_len_in", (dm.n_cells,), torch.uint8)
         dm.set_normals("none")
         hp = lambda k: pinned[k].data_ptr() if k in pinned else None
         h = L.PhdHandover32(face_ptr=hp("face_ptr"), pair_j=hp("pair_j"), area32=hp("area32"), ct32=hp("ct32"),
@@ -336,7 +338,9 @@ class FluxStepper:
                             xmax=(ctypes.c_double * 2)(*dm.xmax[:2]),
                             pair_dj=hp("pair_dj"), pair_x=hp("pair_x") if n_x else None, n_pair_x=n_x,
                             d_pair_dj=stage["pair_dj"].data_ptr() if packed else None,
-                            d_pair_x=stage["pair_x"].data_ptr() if packed else None)
+                            d_pair_x=stage["pair_x"].data_ptr() if packed else None,
+                            list_len=hp("list_len"),
+                            d_list_len=stage["list_len"].data_ptr() if "list_len" in stage else None)
         out = L.geom32(self._geo_tensors(self.handover_records), out=True)
         events = (ctypes.c_void_p * 8)(*(e.cuda_event for e in self._ev))
         sides = (ctypes.c_void_p * 2)(self._side.cuda_stream, self._side2.cuda_stream)
@@ -350,6 +354,7 @@ class FluxStepper:
         # what phd_load_mesh_f32 copied, counted from the arrays themselves
         nb = lambda k: pinned[k].numel() * pinned[k].element_size()
         pair_bytes = nb("pair_dj") + nb("pair_x") if packed else nb("pair_j")
+        pair_bytes += nb("list_len") if "list_len" in pinned else 0
         nbytes += nb("face_ptr") + pair_bytes + nb("area32") + nb("ct32") + (0 if resized else 4 * ng)
         nbytes += nb("ghost_code") if xr is not None else nb("x")
         return nbytes

@@ -33,7 +33,7 @@ _SIGNATURES = {
     "phd_mesh2d_sizes": ([_vp, _vp, _vp, _vp], C.c_int),
     "phd_mesh2d_copy": ([_vp] * 16, C.c_int),
     "phd_mesh2d_copy_compact": ([_vp] * 10, C.c_int),
-    "phd_mesh2d_copy_compact16": ([_vp] * 4 + [C.c_int32] + [_vp] * 8, C.c_int),
+    "phd_mesh2d_copy_compact16": ([_vp] * 4 + [C.c_int32] + [_vp] * 9, C.c_int),
     "phd_hilbert_keys_2d_host": ([_vp, _vp, C.c_int64, C.c_int, _vp], None),
 }
 
@@ -233,15 +233,19 @@ class CompactMesher:
             return out
         # 16-bit bit patterns held as int16 (the device reads them as uint16)
         out["pair_dj"] = self._pinned("pair_dj", (F,), torch.int16)
+        out["list_len"] = self._pinned("list_len", (nc,), torch.uint8)
         cap = self._buf["pair_x"].numel() // 2 if "pair_x" in self._buf else max(256, F // 64)
         k = C.c_int32()
         for _ in range(2):
             px = self._pinned("pair_x", (2 * cap,), torch.int32)
             rc = L.phd_mesh2d_copy_compact16(self._h, ptr("face_ptr"), ptr("pair_dj"), C.c_void_p(px.data_ptr()),
-                                             cap, C.byref(k), *(ptr(nm) for nm in rest))
-            if rc != -3:
+                                             cap, C.byref(k), ptr("list_len"), *(ptr(nm) for nm in rest))
+            if rc != -5:                                # -5: the escape list needs room for k
                 break
             cap = k.value
+        if rc == -6:                                    # a list longer than 255: counted on the device
+            del out["list_len"]
+            rc = 0
         _check(rc, "copy_compact16")
         out["pair_x"] = px[:2 * k.value]
         return out

@@ -520,3 +520,26 @@ def test_packed_pair_j_hand_over_equals_the_int32_one(boundary):
     assert sorted(c) == sorted(pb)
     for k in pb:
         assert torch.equal(c[k], pb[k]), k
+
+
+@pytest.mark.parametrize("delta", [1, -1])
+def test_wrong_list_lengths_are_upload_errors(delta):
+    """List lengths handed over with the packed pair-j that do not match the faces (one
+    cell's length off by one, so the lists either overrun their storage by one entry or
+    leave one unfilled) are counted as upload errors; the lists stay inside their storage
+    and a correct hand-over afterwards is clean again."""
+    meshes = _moved_meshes(16, "periodic", 29, 2)
+    prim = smooth_state(meshes[0])
+    st = FluxStepper(meshes[0], prim, gamma=1.4, precision="fp32")
+    bad = st.dmesh.pinned_host_compact(meshes[1])
+    assert "list_len" in bad
+    bad["list_len"][7] += delta
+    st.load_mesh(bad)
+    torch.cuda.synchronize()
+    assert st.dmesh.upload_errors() >= 1
+    e = st.dmesh.nbr_ptr.cpu().numpy()
+    assert np.all(np.diff(e) >= 0) and e[-1] <= 2 * meshes[1].n_faces
+    st.load_mesh(st.dmesh.pinned_host_compact(meshes[1]))
+    torch.cuda.synchronize()
+    assert st.dmesh.upload_errors() == 0
+    assert np.array_equal(st.dmesh.nbr_idx.cpu().numpy(), meshes[1].nbr_idx)

@@ -197,7 +197,8 @@ def test_compact_pair_j_packing_round_trips(boundary):
     """phd_mesh2d_copy_compact16: pair-j as the 16-bit difference to the owner cell with
     the faces that do not fit listed as (face id, pair-j) in ascending face id -- decoded,
     the int32 pair-j of phd_mesh2d_copy_compact; every other array is the same; a list
-    buffer that is too small gives -3 and the number needed."""
+    buffer that is too small gives -5 and the number needed; the list lengths are each
+    cell's face count."""
     import ctypes as C
     L = tess.lib()
     x = meshgen.jittered_lattice(260, jitter=0.4, seed=3)         # 67,600 real cells: escapes
@@ -226,12 +227,13 @@ def test_compact_pair_j_packing_round_trips(boundary):
         dj = np.zeros(F, np.uint16)
         k = C.c_int32()
         small = np.zeros(2 * 4, np.int32)
-        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(small), 4, C.byref(k),
-                                           *(p(b[nm]) for nm in rest)) == -3
+        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(small), 4, C.byref(k), None,
+                                           *(p(b[nm]) for nm in rest)) == -5
         K = k.value
         assert K > 4
         px = np.zeros(2 * K, np.int32)
-        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(px), K, C.byref(k),
+        ln = np.zeros(n, np.uint8)
+        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(px), K, C.byref(k), p(ln),
                                            *(p(b[nm]) for nm in rest)) == 0
         assert k.value == K
     finally:
@@ -246,4 +248,6 @@ def test_compact_pair_j_packing_round_trips(boundary):
     decoded[fid] = pj
     np.testing.assert_array_equal(decoded, pair_j)
     d = pair_j.astype(np.int64) - owner
-    assert np.array_equal((d >= 1) & (d <= 65535), dj != 0)
+    assert np.array_equal((d >= 1) & (d <= 65534), dj != 0)
+    np.testing.assert_array_equal(ln, np.bincount(np.concatenate([owner, pair_j]), minlength=n))
+    assert not np.any(dj == 65535)
