@@ -338,7 +338,9 @@ int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, con
  * when out->entry_rec is not NULL, the gradient records from the same face loads.
  *
  * The copies run on `stream` with the large ones (area, centroid offset) issued right
- * after the small ones the lists need; the derivations run on side[0] (pair-i,
+ * after the small ones the lists need (arrays laid out back to back both on the host and
+ * in their staging -- pair_x, face_ptr, pair_dj, list_len, ghost_code, in that order --
+ * go over as one copy); the derivations run on side[0] (pair-i,
  * positions, neighbour lists, list codes, then the cell geometry) and side[1] (flip
  * bits, periodic twins from the face ranges, and the face geometry as soon as the face
  * records have landed, in two parts) while the copies are in flight, and are joined
@@ -355,7 +357,7 @@ typedef struct phd_handover32 {
     /* host arrays (pinned, for the copies to overlap the derivations) */
     const int32_t *face_ptr;      /* [n_real + 1] faces of each real cell */
     const int32_t *pair_j;        /* [n_faces]; NULL: pair_dj and pair_x carry pair-j */
-    const float *area32;          /* [n_faces] face areas, FP32 */
+    const float *area32;          /* [n_faces] face areas, FP32 (NULL with face32) */
     const float *ct32;            /* [n_faces] centroid offset along the face, FP32 (see above) */
     const int32_t *ghost_map;     /* [n_cells - n_real] images of the ghosts; NULL: mesh->map holds them */
     const int8_t *ghost_code;     /* [n_cells - n_real] phd_ghost_positions codes (with x == NULL) */
@@ -386,6 +388,10 @@ typedef struct phd_handover32 {
      * match the faces add to *bad; the lists then stay inside their storage. */
     const uint8_t *list_len;      /* [n_cells] host, or NULL */
     uint8_t *d_list_len;          /* [n_cells] staging */
+    /* optional: area and offset interleaved, one (area, offset) pair per face, in place of
+     * area32 and ct32 (which are then NULL) */
+    const float *face32;          /* [n_faces][2] host */
+    float *d_face32;              /* [n_faces][2] staging */
 } phd_handover32;
 
 int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_params *par, phd_geom32_out *out,

@@ -109,7 +109,8 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
 int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, float *area32, float *ct32,
                             double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code);
 
-/* phd_mesh2d_copy_compact with pair-j packed (phdflux.h, phd_handover32.pair_dj):
+/* phd_mesh2d_copy_compact with pair-j packed (phdflux.h, phd_handover32.pair_dj) and
+ * the area and offset interleaved, one (area, offset) pair per face in face32[n_faces][2]:
  * pair_dj[f] = pair_j - pair_i where that lies in [1, 65534], else PHD_PAIR16_ESCAPE,
  * and the escaped faces as (face id, pair-j) pairs in ascending face id in
  * pair_x[2 x_cap]; *n_pair_x receives their number.  Returns -5 (everything but
@@ -120,8 +121,8 @@ int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pai
 #define PHD_PAIR16_ESCAPE 0       /* also in phdflux.h */
 #endif
 int phd_mesh2d_copy_compact16(const phd_tess2d *t, int32_t *face_ptr, uint16_t *pair_dj, int32_t *pair_x,
-                              int32_t x_cap, int32_t *n_pair_x, uint8_t *list_len, float *area32, float *ct32,
-                              double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code);
+                              int32_t x_cap, int32_t *n_pair_x, uint8_t *list_len, float *face32, double *x,
+                              int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code);
 
 /* hilbert_key_2d (phd/hilbert/hilbert.pyx:9-23) for n integer coordinate pairs. */
 void phd_hilbert_keys_2d_host(const int32_t *xh, const int32_t *yh, int64_t n, int order, int64_t *keys);

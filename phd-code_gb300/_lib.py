@@ -83,7 +83,8 @@ class PhdHandover32(C.Structure):
                                             "twin", "csr_work", "bad")] + \
         [("periodic", C.c_int32), ("dedup_periodic", C.c_int32), ("xmin", C.c_double * 2), ("xmax", C.c_double * 2),
          ("pair_dj", C.c_void_p), ("pair_x", C.c_void_p), ("n_pair_x", C.c_int32), ("d_pair_dj", C.c_void_p),
-         ("d_pair_x", C.c_void_p), ("list_len", C.c_void_p), ("d_list_len", C.c_void_p)]
+         ("d_pair_x", C.c_void_p), ("list_len", C.c_void_p), ("d_list_len", C.c_void_p), ("face32", C.c_void_p),
+         ("d_face32", C.c_void_p)]
 
 
 CLOCK_BYTES = C.sizeof(PhdClock)

@@ -240,6 +240,9 @@ __device__ __forceinline__ void finish_cfl(phd_clock *clk, double cfl, bool adva
     finish_cfl_multi(clk, 1, cfl, advance);
 }
 
+// The compact FP32 face geometry from one interleaved (area, offset) array [F][2]
+// (defined with the FP32 kernels).
+int prepare_faces32_interleaved(const phd_mesh *mesh, const float *face32, phd_geom32_out *out, cudaStream_t stream);
 // The tail of an FP32 mesh hand-over in one kernel (defined with the FP32 kernels):
 // cell geometry from the prepared faces and lists, ghost totals from their images,
 // primitives and the next dt.

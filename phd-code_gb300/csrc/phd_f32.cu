@@ -102,8 +102,9 @@ __global__ void k_prepare_faces32(phd_mesh M, float4 *__restrict__ face_geo, flo
 // the centroid offset along the face (face_offset_f64) once to FP32, so the face
 // record crosses the link in 12 bytes (pair-j, area, offset) instead of 32;
 // separations and normals still come from the FP64 positions.
+// stride: 1 for separate area / offset arrays, 2 for one interleaved (area, offset) array
 __global__ void k_prepare_faces32_compact(phd_mesh M, const float *__restrict__ area32,
-                                          const float *__restrict__ ct32, float4 *__restrict__ face_geo,
+                                          const float *__restrict__ ct32, int stride, float4 *__restrict__ face_geo,
                                           float2 *__restrict__ face_ar) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M.n_faces) return;
@@ -117,9 +118,9 @@ __global__ void k_prepare_faces32_compact(phd_mesh M, const float *__restrict__ 
     const float fx = narrow_f64(dx), fy = narrow_f64(dy);
     float r, nx, ny;
     face_normal32(fx, fy, r, nx, ny);
-    const float2 c = face_offset32(ct32[m], nx, ny);
+    const float2 c = face_offset32(ct32[(size_t)m * stride], nx, ny);
     face_geo[m] = make_float4(nx, ny, c.x, c.y);
-    face_ar[m] = make_float2(area32[m], r);
+    face_ar[m] = make_float2(area32[(size_t)m * stride], r);
 }
 
 // pair-i of every face from the per-real-cell face ranges (faces are emitted per real
@@ -1180,6 +1181,15 @@ void launch_grad32(int items, int grid, int block, cudaStream_t s, const phd_mes
 
 inline int g32(int n) { return n > 0 ? (n + B32 - 1) / B32 : 1; }
 
+// The compact face geometry from one interleaved (area, offset) array face32 [F][2].
+int prepare_faces32_interleaved(const phd_mesh *mesh, const float *face32, phd_geom32_out *out, cudaStream_t stream) {
+    if (mesh->n_faces)
+        k_prepare_faces32_compact<<<g32(mesh->n_faces), B32, 0, stream>>>(
+            *mesh, face32, face32 + 1, 2, reinterpret_cast<float4 *>(out->face_geo),
+            reinterpret_cast<float2 *>(out->face_ar));
+    return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
+}
+
 }  // namespace phd
 
 using namespace phd;
@@ -1227,10 +1237,11 @@ int phd_prepare_f32_faces_compact(const phd_mesh *mesh, const float *area32, con
     if (mesh->n_faces && (!area32 || !ct32 || !mesh->pair_i || !mesh->pair_j || !mesh->x)) return PHD_ERR_ARG;
     if (mesh->n_faces)
         k_prepare_faces32_compact<<<g32(mesh->n_faces), B32, 0, stream>>>(
-            *mesh, area32, ct32, reinterpret_cast<float4 *>(out->face_geo),
+            *mesh, area32, ct32, 1, reinterpret_cast<float4 *>(out->face_geo),
             reinterpret_cast<float2 *>(out->face_ar));
     return cudaPeekAtLastError() == cudaSuccess ? PHD_OK : PHD_ERR_LAUNCH;
 }
+
 
 int phd_pair_i_from_face_ptr(const phd_mesh *mesh, const int32_t *face_ptr, int32_t *pair_i, int32_t *bad,
                              cudaStream_t stream) {

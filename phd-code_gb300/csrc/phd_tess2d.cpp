@@ -1065,8 +1065,8 @@ int phd_mesh2d_copy(const phd_tess2d *t, double *x, double *y, int32_t *map, dou
 
 // pair_j, or (pair_j == NULL) pair_dj + pair_x[2 x_cap] with *n_pair_x escapes
 static int copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j, uint16_t *pair_dj, int32_t *pair_x,
-                        int32_t x_cap, int32_t *n_pair_x, float *area32, float *ct32, double *x, int32_t *map,
-                        int8_t *tag, int8_t *type, int8_t *ghost_code) {
+                        int32_t x_cap, int32_t *n_pair_x, float *area32, float *ct32, int stride, double *x,
+                        int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
     const Geometry &G = t->G;
     const int nr = G.n_real, n = G.n_cells, F = G.n_faces;
     // FP64 -> FP32, round to nearest even; magnitudes below 2^-126 to signed zero (the
@@ -1094,13 +1094,13 @@ static int copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pair_j,
                 ++*n_pair_x;
             }
         }
-        area32[f] = round32(G.area[f]);
+        area32[(size_t)f * stride] = round32(G.area[f]);
         // the centroid offset along the face (phdflux.h, compact hand-over): built with
         // -ffp-contract=off, so every operation rounds as the device's does
         const double dx = G.x[j] - G.x[i], dy = G.y[j] - G.y[i];
         const double cx = G.comx[f] - 0.5 * (G.x[i] + G.x[j]), cy = G.comy[f] - 0.5 * (G.y[i] + G.y[j]);
         const double r = std::sqrt(dx * dx + dy * dy);
-        ct32[f] = round32(r > 0.0 ? (cx * (-dy) + cy * dx) / r : 0.0);
+        ct32[(size_t)f * stride] = round32(r > 0.0 ? (cx * (-dy) + cy * dx) / r : 0.0);
     }
     while (c < nr) face_ptr[++c] = F;
     if (x) {
@@ -1120,19 +1120,19 @@ int phd_mesh2d_copy_compact(const phd_tess2d *t, int32_t *face_ptr, int32_t *pai
                             double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
     if (!t || t->G.n_cells == 0 || !face_ptr || !pair_j || !area32 || !ct32 || !map || !tag || !type)
         return -2;
-    return copy_compact(t, face_ptr, pair_j, nullptr, nullptr, 0, nullptr, area32, ct32, x, map, tag, type,
+    return copy_compact(t, face_ptr, pair_j, nullptr, nullptr, 0, nullptr, area32, ct32, 1, x, map, tag, type,
                         ghost_code);
 }
 
 int phd_mesh2d_copy_compact16(const phd_tess2d *t, int32_t *face_ptr, uint16_t *pair_dj, int32_t *pair_x,
-                              int32_t x_cap, int32_t *n_pair_x, uint8_t *list_len, float *area32, float *ct32,
-                              double *x, int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
+                              int32_t x_cap, int32_t *n_pair_x, uint8_t *list_len, float *face32, double *x,
+                              int32_t *map, int8_t *tag, int8_t *type, int8_t *ghost_code) {
     if (!t || t->G.n_cells == 0 || !face_ptr || !pair_dj || !n_pair_x || x_cap < 0 || (x_cap > 0 && !pair_x) ||
-        !area32 || !ct32 || !map || !tag || !type)
+        !face32 || !map || !tag || !type)
         return -2;
     *n_pair_x = 0;
-    const int rc = copy_compact(t, face_ptr, nullptr, pair_dj, pair_x, x_cap, n_pair_x, area32, ct32, x, map, tag,
-                                type, ghost_code);
+    const int rc = copy_compact(t, face_ptr, nullptr, pair_dj, pair_x, x_cap, n_pair_x, face32, face32 + 1, 2, x, map,
+                                tag, type, ghost_code);
     if (rc < 0 || !list_len) return rc;
     // each face adds one entry to the lists of both its cells (tess.cpp:378-379)
     const Geometry &G = t->G;

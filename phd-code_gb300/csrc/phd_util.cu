@@ -486,6 +486,41 @@ __device__ __forceinline__ bool range_ok(int c, int n_real, int F, int a, int b)
     return !(a < 0 || b < a || b > F || (c == 0 && a != 0) || (c == n_real - 1 && b != F));
 }
 
+// Host-to-device copies issued in order, each merged into the one before when both its
+// source and its destination continue that copy's exactly.
+struct CopyRun {
+    static constexpr int N = 8;
+    void *dst[N];
+    const void *src[N];
+    size_t bytes[N];
+    int k = 0;
+    cudaError_t err = cudaSuccess;
+    void add(void *d, const void *s, size_t b) {
+        if (b == 0) return;
+        if (k > 0 && static_cast<const char *>(src[k - 1]) + bytes[k - 1] == s &&
+            static_cast<char *>(dst[k - 1]) + bytes[k - 1] == d) {
+            bytes[k - 1] += b;
+            return;
+        }
+        if (k == N) {
+            err = cudaErrorInvalidValue;
+            return;
+        }
+        dst[k] = d;
+        src[k] = s;
+        bytes[k] = b;
+        k++;
+    }
+    cudaError_t issue(cudaStream_t stream) {
+        cudaError_t e = err;
+        for (int q = 0; q < k && e == cudaSuccess; q++)
+            e = cudaMemcpyAsync(dst[q], src[q], bytes[q], cudaMemcpyHostToDevice, stream);
+        k = 0;
+        err = cudaSuccess;
+        return e;
+    }
+};
+
 // The escaped faces of a packed pair-j hand-over: pair_j[fid] from the (face id, pair-j)
 // list px[K], and the face's packed entry (the device staging copy) turned from
 // PHD_PAIR16_ESCAPE into PAIR16_LISTED, so k_faces_from_ranges can tell a listed face
@@ -702,7 +737,9 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
         return PHD_ERR_ARG;
     if (!mesh->pair_i || !mesh->pair_j || !mesh->map || !mesh->x || !mesh->flip || !mesh->nbr_ptr || !mesh->nbr_idx)
         return PHD_ERR_ARG;
-    if (!h->face_ptr || !h->area32 || !h->ct32 || !h->d_face_ptr || !h->d_area32 || !h->d_ct32 ||
+    const bool interleaved = h->face32 != nullptr;    // one (area, offset) array
+    if (!h->face_ptr || !h->d_face_ptr || (interleaved ? !h->d_face32 : (!h->area32 || !h->ct32 || !h->d_area32 ||
+                                                                          !h->d_ct32)) ||
         !h->type || !h->twin || !h->csr_work || !h->bad || !(h->xmax[0] > h->xmin[0]) || !(h->xmax[1] > h->xmin[1]))
         return PHD_ERR_ARG;
     const int n = mesh->n_cells, nr = mesh->n_real, F = mesh->n_faces, ng = n - nr;
@@ -728,37 +765,46 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     do {                                                                   \
         if ((call) != cudaSuccess) return PHD_ERR_LAUNCH;                  \
     } while (0)
-    // stream: the face ranges and pair-j, then the per-ghost arrays, then the large FP32
-    // face records; each group's event releases the work that needs it
+    // stream: the face ranges, pair-j, the list lengths and ghost codes, then the ghost
+    // map (and positions), then the large FP32 face records; each group's event releases
+    // the work that needs it.  Arrays adjacent both on the host and in the staging are
+    // copied as one (each copy costs a few microseconds on top of its bytes).
     PHD_TRY_CUDA(cudaMemsetAsync(h->bad, 0, sizeof(int32_t), stream));
-    if (host_len) PHD_TRY_CUDA(cudaMemcpyAsync(h->d_list_len, h->list_len, (size_t)n, H2D, stream));
-    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_face_ptr, h->face_ptr, (size_t)(nr + 1) * sizeof(int32_t), H2D, stream));
-    if (!packed) {
-        PHD_TRY_CUDA(cudaMemcpyAsync(pair_j, h->pair_j, (size_t)F * sizeof(int32_t), H2D, stream));
-    } else {
-        PHD_TRY_CUDA(cudaMemcpyAsync(h->d_pair_dj, h->pair_dj, (size_t)F * sizeof(uint16_t), H2D, stream));
-        if (h->n_pair_x > 0)
-            PHD_TRY_CUDA(cudaMemcpyAsync(h->d_pair_x, h->pair_x, (size_t)2 * h->n_pair_x * sizeof(int32_t), H2D,
-                                         stream));
-    }
+    phd::CopyRun run;
+    if (packed && h->n_pair_x > 0) run.add(h->d_pair_x, h->pair_x, (size_t)2 * h->n_pair_x * sizeof(int32_t));
+    run.add(h->d_face_ptr, h->face_ptr, (size_t)(nr + 1) * sizeof(int32_t));
+    if (!packed)
+        run.add(pair_j, h->pair_j, (size_t)F * sizeof(int32_t));
+    else
+        run.add(h->d_pair_dj, h->pair_dj, (size_t)F * sizeof(uint16_t));
+    if (host_len) run.add(h->d_list_len, h->list_len, (size_t)n);
+    if (!h->x && ng > 0) run.add(h->d_ghost_code, h->ghost_code, (size_t)ng);
+    PHD_TRY_CUDA(run.issue(stream));
     PHD_TRY_CUDA(cudaEventRecord(events[0], stream));
     if (h->ghost_map && ng > 0)
-        PHD_TRY_CUDA(cudaMemcpyAsync(const_cast<int32_t *>(mesh->map) + nr, h->ghost_map, (size_t)ng * sizeof(int32_t),
-                                     H2D, stream));
-    if (h->x)
-        PHD_TRY_CUDA(cudaMemcpyAsync(x, h->x, (size_t)2 * n * sizeof(double), H2D, stream));
-    else if (ng > 0)
-        PHD_TRY_CUDA(cudaMemcpyAsync(h->d_ghost_code, h->ghost_code, (size_t)ng, H2D, stream));
+        run.add(const_cast<int32_t *>(mesh->map) + nr, h->ghost_map, (size_t)ng * sizeof(int32_t));
+    if (h->x) run.add(x, h->x, (size_t)2 * n * sizeof(double));
+    PHD_TRY_CUDA(run.issue(stream));
     PHD_TRY_CUDA(cudaEventRecord(events[1], stream));
     // the face records in two parts, three quarters and the rest: the first part's
     // geometry is formed while the rest is in flight, so only a quarter of it is left
     // once the copies end
     const int F0 = (int)(((int64_t)F * 3) / 4);
-    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_area32, h->area32, (size_t)F0 * sizeof(float), H2D, stream));
-    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_ct32, h->ct32, (size_t)F0 * sizeof(float), H2D, stream));
+    if (interleaved) {
+        run.add(h->d_face32, h->face32, (size_t)2 * F0 * sizeof(float));
+    } else {
+        run.add(h->d_area32, h->area32, (size_t)F0 * sizeof(float));
+        run.add(h->d_ct32, h->ct32, (size_t)F0 * sizeof(float));
+    }
+    PHD_TRY_CUDA(run.issue(stream));
     PHD_TRY_CUDA(cudaEventRecord(events[7], stream));
-    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_area32 + F0, h->area32 + F0, (size_t)(F - F0) * sizeof(float), H2D, stream));
-    PHD_TRY_CUDA(cudaMemcpyAsync(h->d_ct32 + F0, h->ct32 + F0, (size_t)(F - F0) * sizeof(float), H2D, stream));
+    if (interleaved) {
+        run.add(h->d_face32 + 2 * (size_t)F0, h->face32 + 2 * (size_t)F0, (size_t)2 * (F - F0) * sizeof(float));
+    } else {
+        run.add(h->d_area32 + F0, h->area32 + F0, (size_t)(F - F0) * sizeof(float));
+        run.add(h->d_ct32 + F0, h->ct32 + F0, (size_t)(F - F0) * sizeof(float));
+    }
+    PHD_TRY_CUDA(run.issue(stream));
     PHD_TRY_CUDA(cudaEventRecord(events[2], stream));
 
     // lists stream, while the face records are in flight: pair-i with the list counts,
@@ -836,7 +882,9 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
         po.face_geo += 4 * (size_t)m0;
         po.face_ar += 2 * (size_t)m0;
         PHD_TRY_CUDA(cudaStreamWaitEvent(geom, events[half ? 2 : 7], 0));
-        if (cnt > 0)
+        if (cnt > 0 && interleaved)
+            PHD_TRY(phd::prepare_faces32_interleaved(&part, h->d_face32 + 2 * (size_t)m0, &po, geom));
+        else if (cnt > 0)
             PHD_TRY(phd_prepare_f32_faces_compact(&part, h->d_area32 + m0, h->d_ct32 + m0, &po, geom));
     }
     PHD_TRY_CUDA(cudaEventRecord(events[4], geom));

@@ -32,6 +32,34 @@ def _dev(device):
     return d
 
 
+# The small arrays of a packed compact hand-over back to back in one block, in the order
+# phd_load_mesh_f32 copies them (each array's offset a multiple of its element size: the
+# element sizes do not increase along the block), so the host block and a staging block
+# of the same layout go over as one copy.
+COMPACT_BLOCK = (("pair_x", torch.int32), ("face_ptr", torch.int32), ("pair_dj", torch.int16),
+                 ("list_len", torch.uint8), ("ghost_code", torch.int8))
+
+
+def compact_block_layout(sizes):
+    """{name: (byte offset, count, dtype)} and the block's bytes for the arrays named in
+    ``sizes`` (element counts) in COMPACT_BLOCK order."""
+    layout, off = {}, 0
+    for nm, dt in COMPACT_BLOCK:
+        if nm in sizes:
+            layout[nm] = (off, int(sizes[nm]), dt)
+            off += int(sizes[nm]) * torch.empty((), dtype=dt).element_size()
+    return layout, off
+
+
+def block_views(block, layout):
+    """Typed views of a uint8 block at the layout's offsets."""
+    out = {}
+    for nm, (off, cnt, dt) in layout.items():
+        es = torch.empty((), dtype=dt).element_size()
+        out[nm] = block[off:off + cnt * es].view(dt)
+    return out
+
+
 class DeviceMesh:
     """One tessellation in HBM (cells real-then-ghost, faces, CSR neighbour lists)."""
 
@@ -177,8 +205,10 @@ class DeviceMesh:
         generator move); ghost codes replace the positions (``phd_ghost_positions``).
         ``pair16``: pair-j as the 16-bit difference to the owner cell (``pair_dj``, 0 =
         escape) plus the escaped faces' (face id, pair-j) pairs (``pair_x``): 10 B per
-        face; and each cell's list length (``list_len``, one byte) so the device lays out
-        the neighbour lists without counting them."""
+        face; each cell's list length (``list_len``, one byte) so the device lays out
+        the neighbour lists without counting them; the area and offset interleaved
+        (``face32`` [F][2]); and the small arrays back to back in one pinned block
+        (``compact_block``), so the hand-over copies them as one."""
         self._check_remesh(host)
         nr = self.n_real
         pi, pj = np.asarray(host.pair_i), np.asarray(host.pair_j)
@@ -197,28 +227,41 @@ class DeviceMesh:
             out = a.astype(np.float32)
             return np.where(np.abs(a) < 2.0 ** -126, np.copysign(np.float32(0.0), out), out).astype(np.float32)
 
-        arrays = {"face_ptr": face_ptr, "area32": round32(np.asarray(host.area, dtype=np.float64)),
-                  "ct32": round32(s64),
-                  "map": np.ascontiguousarray(host.map, dtype=np.int32),
+        area32, ct32 = round32(np.asarray(host.area, dtype=np.float64)), round32(s64)
+        arrays = {"map": np.ascontiguousarray(host.map, dtype=np.int32),
                   "tag": np.ascontiguousarray(host.tag, dtype=np.int8),
                   "type": np.ascontiguousarray(host.type, dtype=np.int8)}
-        if pair16:
-            d = pj.astype(np.int64) - pi.astype(np.int64)
-            ok = (d >= 1) & (d <= 65534)
-            esc = np.flatnonzero(~ok)
-            # the 16-bit patterns as int16 (the device reads them as uint16)
-            arrays["pair_dj"] = np.where(ok, d, 0).astype(np.uint16).view(np.int16)
-            arrays["pair_x"] = np.stack([esc, pj[esc]], axis=1).astype(np.int32).reshape(-1)
-            ln = np.bincount(np.concatenate([pi, pj]).astype(np.int64), minlength=len(host.map))
-            if ln.max(initial=0) <= 255:            # else the device counts them
-                arrays["list_len"] = ln.astype(np.uint8)
-        else:
-            arrays["pair_j"] = np.ascontiguousarray(pj, dtype=np.int32)
         if resident:            # the device holds the real positions; ghosts from their codes
-            arrays["ghost_code"] = self.ghost_codes(host)
+            ghost_code = self.ghost_codes(host)
         else:
             arrays["x"] = np.ascontiguousarray(x)
-        return {k: torch.from_numpy(v).pin_memory() for k, v in arrays.items()}
+        if not pair16:
+            arrays.update(face_ptr=face_ptr, pair_j=np.ascontiguousarray(pj, dtype=np.int32), area32=area32,
+                          ct32=ct32)
+            if resident:
+                arrays["ghost_code"] = ghost_code
+            return {k: torch.from_numpy(v).pin_memory() for k, v in arrays.items()}
+        d = pj.astype(np.int64) - pi.astype(np.int64)
+        ok = (d >= 1) & (d <= 65534)
+        esc = np.flatnonzero(~ok)
+        small = {"face_ptr": face_ptr, "pair_x": np.stack([esc, pj[esc]], axis=1).astype(np.int32).reshape(-1),
+                 # the 16-bit patterns as int16 (the device reads them as uint16)
+                 "pair_dj": np.where(ok, d, 0).astype(np.uint16).view(np.int16)}
+        ln = np.bincount(np.concatenate([pi, pj]).astype(np.int64), minlength=len(host.map))
+        if ln.max(initial=0) <= 255:                # else the device counts them
+            small["list_len"] = ln.astype(np.uint8)
+        if resident:
+            small["ghost_code"] = ghost_code
+        out = {k: torch.from_numpy(v).pin_memory() for k, v in arrays.items()}
+        sizes = {k: v.size for k, v in small.items()}
+        layout, nbytes = compact_block_layout(sizes)
+        block = torch.empty(max(nbytes, 16), dtype=torch.uint8, pin_memory=True)
+        out.update(block_views(block, layout))
+        for k, v in small.items():
+            out[k].copy_(torch.from_numpy(v))
+        out["compact_block"] = block
+        out["face32"] = torch.from_numpy(np.stack([area32, ct32], axis=1)).pin_memory()
+        return out
 
     @staticmethod
     def pinned_sizes(pinned):
@@ -231,10 +274,12 @@ class DeviceMesh:
                   "x": (self.dim, self.n_cells), "dcom": (self.dim, self.n_cells), "vol": (self.n_cells,),
                   "pair_i": (self.n_faces,), "pair_j": (self.n_faces,), "area": (self.n_faces,),
                   "com": (self.dim, self.n_faces), "face_ptr": (self.n_real + 1,), "area32": (self.n_faces,),
-                  "ct32": (self.n_faces,), "ghost_code": (self.n_cells - self.n_real,), "pair_dj": (self.n_faces,)}
+                  "ct32": (self.n_faces,), "ghost_code": (self.n_cells - self.n_real,), "pair_dj": (self.n_faces,),
+                  "face32": (self.n_faces, 2)}
         if "face_ptr" in pinned:
-            names = ("face_ptr", "pair_j" if "pair_j" in pinned else "pair_dj", "area32", "ct32", "map", "tag",
-                     "type") + (("x",) if "x" in pinned else ("ghost_code",))
+            names = ("face_ptr", "pair_j" if "pair_j" in pinned else "pair_dj", "map", "tag", "type") + \
+                (("face32",) if "face32" in pinned else ("area32", "ct32")) + \
+                (("x",) if "x" in pinned else ("ghost_code",))
             if "list_len" in pinned and tuple(pinned["list_len"].shape) != (self.n_cells,):
                 raise ValueError("upload: list_len must hold one length per cell")
             if "pair_dj" in pinned:

@@ -310,18 +310,31 @@ class FluxStepper:
             nbytes += dm.copy_fields(pinned, ("tag", "type", "map"), main)
         if not hasattr(dm, "_bad"):
             dm.reset_errors(main)
-        stage = {"face_ptr": self._view("face_ptr_in", (nr + 1,), torch.int32),
-                 "area32": self._view("area32_in", (nf,), torch.float32),
-                 "ct32": self._view("ct32_in", (nf,), torch.float32)}
-        if xr is not None:
-            stage["ghost_code"] = self._view("ghost_code_in", (ng,), torch.int8)
         packed = "pair_dj" in pinned
         n_x = pinned["pair_x"].numel() // 2 if packed else 0
-        if packed:
-            stage["pair_dj"] = self._view("pair_dj_in", (nf,), torch.int16)
-            stage["pair_x"] = self._view("pair_x_in", (max(2 * n_x, 2),), torch.int32)
-        if "list_len" in pinned:
-            stage["list_len"] = self._view("list_len_in", (dm.n_cells,), torch.uint8)
+        small = [k for k in ("pair_x", "face_ptr", "pair_dj", "list_len", "ghost_code")
+                 if k in pinned and pinned[k].numel() > 0]
+        if xr is None and "ghost_code" in small:
+            small.remove("ghost_code")
+        stage = {}
+        if "compact_block" in pinned:
+            # a staging block laid out like the host block: adjacent arrays go over as one copy
+            hb = pinned["compact_block"]
+            db = self._view("compact_block_in", (hb.numel(),), torch.uint8)
+            for k in small:
+                off = pinned[k].data_ptr() - hb.data_ptr()
+                if not 0 <= off <= hb.numel() - pinned[k].numel() * pinned[k].element_size():
+                    raise ValueError("upload: %s lies outside compact_block" % k)
+                stage[k] = db.data_ptr() + off
+        else:
+            for k in small:
+                t = pinned[k]
+                stage[k] = self._view(k + "_in", (max(t.numel(), 1),), t.dtype).data_ptr()
+        if "face32" in pinned:
+            stage["face32"] = self._view("face32_in", (nf, 2), torch.float32).data_ptr()
+        else:
+            stage["area32"] = self._view("area32_in", (nf,), torch.float32).data_ptr()
+            stage["ct32"] = self._view("ct32_in", (nf,), torch.float32).data_ptr()
         dm.set_normals("none")
         hp = lambda k: pinned[k].data_ptr() if k in pinned else None
         h = L.PhdHandover32(face_ptr=hp("face_ptr"), pair_j=hp("pair_j"), area32=hp("area32"), ct32=hp("ct32"),
@@ -329,18 +342,16 @@ class FluxStepper:
                             ghost_code=hp("ghost_code") if xr is not None else None,
                             x=None if xr is not None else hp("x"),
                             x_real=xr.data_ptr() if xr is not None else None, type=dm.type.data_ptr(),
-                            d_face_ptr=stage["face_ptr"].data_ptr(), d_area32=stage["area32"].data_ptr(),
-                            d_ct32=stage["ct32"].data_ptr(),
-                            d_ghost_code=stage["ghost_code"].data_ptr() if xr is not None else None,
+                            d_face_ptr=stage["face_ptr"], d_area32=stage.get("area32"), d_ct32=stage.get("ct32"),
+                            d_ghost_code=stage.get("ghost_code"),
                             twin=self.twin.data_ptr(), csr_work=dm._csr_work.data_ptr(), bad=dm._bad.data_ptr(),
                             periodic=int(dm.boundary == "periodic"), dedup_periodic=int(self.dedup_periodic),
                             xmin=(ctypes.c_double * 2)(*dm.xmin[:2]),
                             xmax=(ctypes.c_double * 2)(*dm.xmax[:2]),
                             pair_dj=hp("pair_dj"), pair_x=hp("pair_x") if n_x else None, n_pair_x=n_x,
-                            d_pair_dj=stage["pair_dj"].data_ptr() if packed else None,
-                            d_pair_x=stage["pair_x"].data_ptr() if packed else None,
-                            list_len=hp("list_len"),
-                            d_list_len=stage["list_len"].data_ptr() if "list_len" in stage else None)
+                            d_pair_dj=stage.get("pair_dj"), d_pair_x=stage.get("pair_x"),
+                            list_len=hp("list_len"), d_list_len=stage.get("list_len"),
+                            face32=hp("face32"), d_face32=stage.get("face32"))
         out = L.geom32(self._geo_tensors(self.handover_records), out=True)
         events = (ctypes.c_void_p * 8)(*(e.cuda_event for e in self._ev))
         sides = (ctypes.c_void_p * 2)(self._side.cuda_stream, self._side2.cuda_stream)
@@ -355,7 +366,8 @@ class FluxStepper:
         nb = lambda k: pinned[k].numel() * pinned[k].element_size()
         pair_bytes = nb("pair_dj") + nb("pair_x") if packed else nb("pair_j")
         pair_bytes += nb("list_len") if "list_len" in pinned else 0
-        nbytes += nb("face_ptr") + pair_bytes + nb("area32") + nb("ct32") + (0 if resized else 4 * ng)
+        face_bytes = nb("face32") if "face32" in pinned else nb("area32") + nb("ct32")
+        nbytes += nb("face_ptr") + pair_bytes + face_bytes + (0 if resized else 4 * ng)
         nbytes += nb("ghost_code") if xr is not None else nb("x")
         return nbytes
 

@@ -33,7 +33,7 @@ _SIGNATURES = {
     "phd_mesh2d_sizes": ([_vp, _vp, _vp, _vp], C.c_int),
     "phd_mesh2d_copy": ([_vp] * 16, C.c_int),
     "phd_mesh2d_copy_compact": ([_vp] * 10, C.c_int),
-    "phd_mesh2d_copy_compact16": ([_vp] * 4 + [C.c_int32] + [_vp] * 9, C.c_int),
+    "phd_mesh2d_copy_compact16": ([_vp] * 4 + [C.c_int32] + [_vp] * 8, C.c_int),
     "phd_hilbert_keys_2d_host": ([_vp, _vp, C.c_int64, C.c_int, _vp], None),
 }
 
@@ -212,42 +212,56 @@ class CompactMesher:
         nc, nf, pad_used = C.c_int32(), C.c_int32(), C.c_double()
         L.phd_mesh2d_sizes(self._h, C.byref(nc), C.byref(nf), C.byref(pad_used))
         nc, F = nc.value, nf.value
-        out = {"face_ptr": self._pinned("face_ptr", (n + 1,), torch.int32),
-               "area32": self._pinned("area32", (F,), torch.float32),
-               "ct32": self._pinned("ct32", (F,), torch.float32),
-               "map": self._pinned("map", (nc,), torch.int32),
+        out = {"map": self._pinned("map", (nc,), torch.int32),
                "tag": self._pinned("tag", (nc,), torch.int8), "type": self._pinned("type", (nc,), torch.int8)}
-        if self.resident:
-            out["ghost_code"] = self._pinned("ghost_code", (nc - n,), torch.int8)
-        else:
+        if not self.resident:
             out["x"] = self._pinned("x", (2, nc), torch.float64)
 
         def ptr(k):
             return C.c_void_p(out[k].data_ptr()) if k in out else None
 
-        rest = ("area32", "ct32", "x", "map", "tag", "type", "ghost_code")
         if not self.pair16:
-            out["pair_j"] = self._pinned("pair_j", (F,), torch.int32)
-            _check(L.phd_mesh2d_copy_compact(self._h, *(ptr(k) for k in ("face_ptr", "pair_j") + rest)),
+            out.update(face_ptr=self._pinned("face_ptr", (n + 1,), torch.int32),
+                       pair_j=self._pinned("pair_j", (F,), torch.int32),
+                       area32=self._pinned("area32", (F,), torch.float32),
+                       ct32=self._pinned("ct32", (F,), torch.float32))
+            if self.resident:
+                out["ghost_code"] = self._pinned("ghost_code", (nc - n,), torch.int8)
+            _check(L.phd_mesh2d_copy_compact(self._h, *(ptr(k) for k in ("face_ptr", "pair_j", "area32", "ct32", "x",
+                                                                          "map", "tag", "type", "ghost_code"))),
                    "copy_compact")
             return out
-        # 16-bit bit patterns held as int16 (the device reads them as uint16)
-        out["pair_dj"] = self._pinned("pair_dj", (F,), torch.int16)
-        out["list_len"] = self._pinned("list_len", (nc,), torch.uint8)
-        cap = self._buf["pair_x"].numel() // 2 if "pair_x" in self._buf else max(256, F // 64)
+        # the small arrays back to back in one pinned block (one copy to the device): the
+        # escape list first, in a region of room for `cap` entries, moved to the region's
+        # end once its length is known, so that it joins the arrays behind it
+        from .device import block_views, compact_block_layout
+        out["face32"] = self._pinned("face32", (F, 2), torch.float32)
+        cap = getattr(self, "_cap", max(256, F // 64))
         k = C.c_int32()
         for _ in range(2):
-            px = self._pinned("pair_x", (2 * cap,), torch.int32)
-            rc = L.phd_mesh2d_copy_compact16(self._h, ptr("face_ptr"), ptr("pair_dj"), C.c_void_p(px.data_ptr()),
-                                             cap, C.byref(k), ptr("list_len"), *(ptr(nm) for nm in rest))
+            sizes = {"pair_x": 2 * cap, "face_ptr": n + 1, "pair_dj": F, "list_len": nc}
+            if self.resident:
+                sizes["ghost_code"] = nc - n
+            layout, nbytes = compact_block_layout(sizes)
+            block = self._pinned("compact_block", (nbytes,), torch.uint8)
+            out.update(block_views(block, layout))
+            # 16-bit bit patterns held as int16 (the device reads them as uint16)
+            rc = L.phd_mesh2d_copy_compact16(self._h, ptr("face_ptr"), ptr("pair_dj"), ptr("pair_x"), cap,
+                                             C.byref(k), ptr("list_len"), ptr("face32"), ptr("x"), ptr("map"),
+                                             ptr("tag"), ptr("type"), ptr("ghost_code"))
             if rc != -5:                                # -5: the escape list needs room for k
                 break
-            cap = k.value
+            cap = self._cap = k.value + k.value // 8 + 16
         if rc == -6:                                    # a list longer than 255: counted on the device
-            del out["list_len"]
             rc = 0
+            out.pop("list_len")
         _check(rc, "copy_compact16")
-        out["pair_x"] = px[:2 * k.value]
+        K = k.value
+        start = 8 * (cap - K)                           # byte offset of the moved escape list
+        moved = block[start:8 * cap].view(torch.int32)
+        moved.copy_(out["pair_x"][:2 * K].clone())
+        out["pair_x"] = moved
+        out["compact_block"] = block[start:]
         return out
 
 

@@ -196,9 +196,9 @@ def test_insertion_order_does_not_change_the_mesh():
 def test_compact_pair_j_packing_round_trips(boundary):
     """phd_mesh2d_copy_compact16: pair-j as the 16-bit difference to the owner cell with
     the faces that do not fit listed as (face id, pair-j) in ascending face id -- decoded,
-    the int32 pair-j of phd_mesh2d_copy_compact; every other array is the same; a list
-    buffer that is too small gives -5 and the number needed; the list lengths are each
-    cell's face count."""
+    the int32 pair-j of phd_mesh2d_copy_compact; every other array is the same (area and
+    offset interleaved in face32); a list buffer that is too small gives -5 and the number
+    needed; the list lengths are each cell's face count."""
     import ctypes as C
     L = tess.lib()
     x = meshgen.jittered_lattice(260, jitter=0.4, seed=3)         # 67,600 real cells: escapes
@@ -219,25 +219,28 @@ def test_compact_pair_j_packing_round_trips(boundary):
                     "ghost_code": np.zeros(max(n - nr, 1), np.int8)}
 
         p = lambda a: a.ctypes.data_as(C.c_void_p)
-        rest = ("area32", "ct32", "x", "map", "tag", "type", "ghost_code")
+        rest = ("x", "map", "tag", "type", "ghost_code")
         a = bufs()
         pair_j = np.zeros(F, np.int32)
-        assert L.phd_mesh2d_copy_compact(h, p(a["face_ptr"]), p(pair_j), *(p(a[k]) for k in rest)) == 0
+        assert L.phd_mesh2d_copy_compact(h, p(a["face_ptr"]), p(pair_j), p(a["area32"]), p(a["ct32"]),
+                                         *(p(a[k]) for k in rest)) == 0
         b = bufs()
         dj = np.zeros(F, np.uint16)
+        face32 = np.zeros((F, 2), np.float32)
         k = C.c_int32()
         small = np.zeros(2 * 4, np.int32)
-        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(small), 4, C.byref(k), None,
+        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(small), 4, C.byref(k), None, p(face32),
                                            *(p(b[nm]) for nm in rest)) == -5
         K = k.value
         assert K > 4
         px = np.zeros(2 * K, np.int32)
         ln = np.zeros(n, np.uint8)
-        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(px), K, C.byref(k), p(ln),
+        assert L.phd_mesh2d_copy_compact16(h, p(b["face_ptr"]), p(dj), p(px), K, C.byref(k), p(ln), p(face32),
                                            *(p(b[nm]) for nm in rest)) == 0
         assert k.value == K
     finally:
         L.phd_tess2d_destroy(h)
+    b["area32"], b["ct32"] = face32[:, 0].copy(), face32[:, 1].copy()
     for nm in a:
         np.testing.assert_array_equal(a[nm], b[nm], err_msg=nm)
     owner = np.repeat(np.arange(nr), np.diff(a["face_ptr"]))
