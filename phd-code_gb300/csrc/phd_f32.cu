@@ -26,6 +26,7 @@
 //                         (dcom_x, dcom_y, w_x, w_y); written by the gradient kernel
 //   w2        float2 [n]  generator velocity (the host re-mesh reads it)
 //   flux4     float4 [F]  dt*A*F: the face's conserved increment (mass, mom_x, mom_y, energy)
+#include <cmath>
 #include <utility>
 #include "phd_common.cuh"
 #include "phd_physics.cuh"
@@ -499,7 +500,7 @@ __global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int mo
 // more instructions in all, and measured no faster: with fast-math a division is
 // already one reciprocal and one multiply.)
 struct GasC {
-    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1;
+    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1, half_gm1, sq_two_gp1;
     ExGas64 X;                 // the exact solver's FP64 Newton constants
 };
 
@@ -514,6 +515,8 @@ inline GasC gas_consts(double gamma) {
     c.inv_z = 1.f / c.z;
     c.two_gp1 = 2.f / (g + 1.f);
     c.gm1_gp1 = (g - 1.f) / (g + 1.f);
+    c.half_gm1 = 0.5f * (g - 1.f);
+    c.sq_two_gp1 = std::sqrt(c.two_gp1);
     c.X = ex_gas64(gamma);
     return c;
 }
@@ -531,16 +534,17 @@ __device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float 
     if (((p_max / p_min) < 2.f) && ((p_min < p_star) && (p_star < p_max))) {
         // PVRS estimate stands
     } else if (p_star <= p_min) {          // two-rarefaction (TRRS)
+        // The reference forms u* from both rarefaction relations and averages the two
+        // side pressures they give at u*; both equal the root p*, whose closed form is
+        // p*^z = (c_l + c_r - (g-1)/2 (u_r - u_l)) / (c_l / p_l^z + c_r / p_r^z) (Toro,
+        // eq. 9.42), here with p_l^z / p_r^z = (p_l/p_r)^z: two powers, one division.
         const float plr = __powf(pl / pr, C.z);
-        const float u_star = ((((plr * ul) / cl) + (ur / cr)) + ((2.f * (plr - 1.f)) * C.inv_gm1)) /
-                             ((plr / cl) + (1.f / cr));
-        p_star = (0.5f * pl) * __powf((1.f + ((C.gm1 * (ul - u_star)) / (2.f * cl))), C.inv_z);
-        p_star = p_star + ((0.5f * pr) * __powf((1.f + ((C.gm1 * (u_star - ur)) / (2.f * cr))), C.inv_z));
+        const float num = (cl + cr) - C.half_gm1 * (ur - ul);
+        p_star = pr * __powf((plr * num) / (cl + plr * cr), C.inv_z);
     } else {                               // two-shock (TSRS)
-        const float Al = C.two_gp1 / dl;
-        const float Ar = C.two_gp1 / dr;
-        const float gl = sqrtf(Al / (p_star + pl * C.gm1_gp1));
-        const float gr = sqrtf(Ar / (p_star + pr * C.gm1_gp1));
+        // g_K = sqrt(A_K / (p + B_K)), A_K = 2 / ((g+1) d_K): sqrt(2/(g+1)) / sqrt(d_K (p + B_K))
+        const float gl = C.sq_two_gp1 * rsqrtf(dl * (p_star + pl * C.gm1_gp1));
+        const float gr = C.sq_two_gp1 * rsqrtf(dr * (p_star + pr * C.gm1_gp1));
         p_star = (((gl * pl) + (gr * pr)) - (ur - ul)) / (gl + gr);
     }
     if (p_star <= pl) sl = ul - cl;
@@ -632,35 +636,34 @@ __device__ __forceinline__ void temporal32(float *L, float *R, const float *pi, 
     }
 }
 
-// FP32 GIZMO pair limit (gizmo_pair of phd_physics.cuh) with the separation quotients
-// formed once per face and the sign-changing bound phi / (1 + delta/|phi|) written as
-// phi |phi| / (|phi| + delta): one division on that (rare) branch.
-__device__ __forceinline__ void gizmo_pair32(float sl, float sr, float ci, float cj, float qi, float qj,
-                                             float &xl, float &xr) {
-    const float ad = fabsf(sl - sr);
-    const float delta1 = 0.5f * ad, delta2 = 0.25f * ad;
-    const float phi_min = fminf(sl, sr), phi_max = fmaxf(sl, sr);
-    const float phibar_l = sl + qi * (sr - sl);
-    const float phibar_r = sr + qj * (sl - sr);
-    float phi_plus = phi_max + delta1, phi_minus = phi_min - delta1;
-    if (__builtin_expect(phi_plus * phi_max < 0.f, 0)) {
-        const float a = fabsf(phi_max);
-        phi_plus = (phi_max * a) / (a + delta1);
+// FP32 GIZMO pair limit for one field (reconstruction.pyx:877-915, gizmo_pair of
+// phd_physics.cuh) without the reference's case split on the cells' order.  The
+// boosted states s_l, s_r are the cells' primitives less one common face velocity, and
+// a common shift rounds monotonically, so d = s_r - s_l has the sign of p_j - p_i (or is
+// zero).  Then the two ordered cases are one rule per side: the extrapolated state is
+// clamped to the interval between an outer bound on its own side, s_l - d/2 (phi_minus
+// when p_i < p_j, phi_plus when p_i > p_j; pulled towards zero as phi / (1 + delta1/|phi|)
+// = phi |phi| / (|phi| + delta1) where it would change sign), and an inner bound
+// s_l + (q_i + 1/4) d (phibar_l + delta2, resp. phibar_l - delta2); the right side
+// mirrors it with s_r + d/2 and s_r - (q_j + 1/4) d.  Equal cells give d = 0 and the
+// interval {s_l}: the reference's third case.  In both ordered cases the outer bound
+// lies on the far side of s_l from the inner one, so the interval is never empty and
+// the reference's max(lo, min(hi, x)) and min(hi, max(lo, x)) are the same clamp.
+// qi4, qj4: the face's separation quotients plus 1/4.
+__device__ __forceinline__ void gizmo_pair32(float sl, float sr, float qi4, float qj4, float &xl, float &xr) {
+    const float d = sr - sl;
+    float ol = fmaf(-0.5f, d, sl), orr = fmaf(0.5f, d, sr);
+    const float il = fmaf(qi4, d, sl), ir = fmaf(-qj4, d, sr);
+    if (__builtin_expect(ol * sl < 0.f, 0)) {
+        const float a = fabsf(sl);
+        ol = (sl * a) / (a + 0.5f * fabsf(d));
     }
-    if (__builtin_expect(phi_minus * phi_min < 0.f, 0)) {
-        const float a = fabsf(phi_min);
-        phi_minus = (phi_min * a) / (a + delta1);
+    if (__builtin_expect(orr * sr < 0.f, 0)) {
+        const float a = fabsf(sr);
+        orr = (sr * a) / (a + 0.5f * fabsf(d));
     }
-    if (ci < cj) {
-        xl = fmaxf(phi_minus, fminf(phibar_l + delta2, xl));
-        xr = fminf(phi_plus, fmaxf(phibar_r - delta2, xr));
-    } else if (ci > cj) {
-        xl = fminf(phi_plus, fmaxf(phibar_l - delta2, xl));
-        xr = fmaxf(phi_minus, fminf(phibar_r + delta2, xr));
-    } else {
-        xl = sl;
-        xr = sr;
-    }
+    xl = fminf(fmaxf(xl, fminf(ol, il)), fmaxf(ol, il));
+    xr = fminf(fmaxf(xr, fminf(orr, ir)), fmaxf(orr, ir));
 }
 
 // 64 bytes of a cell record in two 256-bit loads through the read-only path (the
@@ -759,9 +762,9 @@ __device__ __forceinline__ void face32_face(int m, const FaceHead &H, const phd_
         }
         if (P.gizmo) {
             const float smi = sqrtf(six * six + siy * siy), smj = sqrtf(sjx * sjx + sjy * sjy);
-            const float qi = smi * inv_r, qj = smj * inv_r;
+            const float qi4 = fmaf(smi, inv_r, 0.25f), qj4 = fmaf(smj, inv_r, 0.25f);
 #pragma unroll
-            for (int f = 0; f < 4; f++) gizmo_pair32(sl[f], sr[f], pi[f], pj[f], qi, qj, L[f], R[f]);
+            for (int f = 0; f < 4; f++) gizmo_pair32(sl[f], sr[f], qi4, qj4, L[f], R[f]);
             if (L[0] < 0.f || L[3] < 0.f) {
 #pragma unroll
                 for (int f = 0; f < 4; f++) L[f] = sl[f];
