@@ -429,7 +429,7 @@ int phd_step_f32(const phd_mesh *mesh, const phd_geom32 *geo, const phd_params *
                  float *w2, float *flux4, phd_clock *clk, cudaStream_t stream);
 
 /* Launch shape of the three step kernels (chosen by an autotuner): threads per block
- * (multiple of 32, <= 512; the face kernel <= 384), a cap on blocks per grid (0: enough
+ * (multiple of 32, <= 512; the face kernel <= 256), a cap on blocks per grid (0: enough
  * blocks for every item; > 0: that many blocks, each looping over items -- a persistent
  * launch) and items per thread (0 or 1, 2, 4: a block covers block * items consecutive
  * cells or faces, thread t taking items t, t + block, ...; a warp then handles 32 *

@@ -17,7 +17,7 @@ import torch
 from . import _lib as L
 
 BLOCKS = (128, 256, 384, 512)
-FACE_MAX_BLOCK = 384           # k_face32's launch bound (56 registers per thread)
+FACE_MAX_BLOCK = 256           # k_face32's launch bound (48 registers per thread)
 CAP_WAVES = (0, 2, 4, 8)       # 0: one thread per item; k: k blocks per SM
 ITEMS = (1, 2, 4)              # cells / faces per thread
 

@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int mo
 // more instructions in all, and measured no faster: with fast-math a division is
 // already one reciprocal and one multiply.)
 struct GasC {
-    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1, half_gm1, sq_two_gp1;
+    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1, half_gm1, sq_two_gp1, one_m_gp1_2g;
     ExGas64 X;                 // the exact solver's FP64 Newton constants
 };
 
@@ -517,12 +517,15 @@ inline GasC gas_consts(double gamma) {
     c.gm1_gp1 = (g - 1.f) / (g + 1.f);
     c.half_gm1 = 0.5f * (g - 1.f);
     c.sq_two_gp1 = std::sqrt(c.two_gp1);
+    c.one_m_gp1_2g = 1.f - c.gp1_2g;
     c.X = ex_gas64(gamma);
     return c;
 }
 
+// ml = d_l (s_l - u_l) and mr = d_r (s_r - u_r) go back with the wave speeds: the
+// contact speed is formed from them, and the HLLC star flux reuses them.
 __device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float dr, float ur, float pr,
-                                            const GasC &C, float &sl, float &sc, float &sr) {
+                                            const GasC &C, float &sl, float &sc, float &sr, float &ml, float &mr) {
     float p_star;
     const float cl = fmaxf(sqrtf((C.g * pl) / dl), 1.0e-10f);
     const float cr = fmaxf(sqrtf((C.g * pr) / dr), 1.0e-10f);
@@ -547,28 +550,34 @@ __device__ __forceinline__ void get_waves32(float dl, float ul, float pl, float 
         const float gr = C.sq_two_gp1 * rsqrtf(dr * (p_star + pr * C.gm1_gp1));
         p_star = (((gl * pl) + (gr * pr)) - (ur - ul)) / (gl + gr);
     }
-    if (p_star <= pl) sl = ul - cl;
-    else sl = ul - (cl * sqrtf((1.f + (C.gp1_2g * ((p_star / pl) - 1.f)))));
-    if (p_star <= pr) sr = ur + cr;
-    else sr = ur + (cr * sqrtf((1.f + (C.gp1_2g * ((p_star / pr) - 1.f)))));
-    sc = (((pr - pl) + ((dl * ul) * (sl - ul))) - ((dr * ur) * (sr - ur))) /
-         ((dl * (sl - ul)) - (dr * (sr - ur)));
+    // shock factor sqrt(1 + (g+1)/(2g) (p*/p_K - 1)) where p* > p_K, else 1 (rarefaction),
+    // chosen by a select: both sides' lanes run one code path
+    const float xl = sqrtf(fmaf(C.gp1_2g, p_star / pl, C.one_m_gp1_2g));
+    const float xr = sqrtf(fmaf(C.gp1_2g, p_star / pr, C.one_m_gp1_2g));
+    sl = ul - cl * (p_star <= pl ? 1.f : xl);
+    sr = ur + cr * (p_star <= pr ? 1.f : xr);
+    ml = dl * (sl - ul);
+    mr = dr * (sr - ur);
+    sc = (((pr - pl) + ul * ml) - ur * mr) / (ml - mr);
 }
 
-__device__ __forceinline__ void hll_family32(bool hllc, const float *L, const float *R, const float *n,
-                                             const float *w, const GasC &C, bool boost, float *f) {
+// HLL / HLLC flux in FP32.  BOOST: the states are in the face's frame (w.n = 0 there)
+// and the flux is de-boosted; else the face moves at w through the lab-frame states.
+template <bool HLLC, bool BOOST>
+__device__ __forceinline__ void hll_family32(const float *L, const float *R, const float *n, const float *w,
+                                             const GasC &C, float *f) {
     const float _dl = L[0], _pl = L[3], _dr = R[0], _pr = R[3];
     const float vl_sq = L[1] * L[1] + L[2] * L[2], vr_sq = R[1] * R[1] + R[2] * R[2];
     const float Vnl = L[1] * n[0] + L[2] * n[1], Vnr = R[1] * n[0] + R[2] * n[1];
-    const float wn = boost ? 0.f : (w[0] * n[0] + w[1] * n[1]);
-    float sl, sc, sr;
-    get_waves32(_dl, Vnl, _pl, _dr, Vnr, _pr, C, sl, sc, sr);
+    const float wn = BOOST ? 0.f : (w[0] * n[0] + w[1] * n[1]);
+    float sl, sc, sr, ml, mr;
+    get_waves32(_dl, Vnl, _pl, _dr, Vnr, _pr, C, sl, sc, sr, ml, mr);
     if (wn <= sl) {
         f[0] = _dl * (Vnl - wn);
         f[3] = ((((0.5f * _dl) * vl_sq) + (_pl * C.inv_gm1)) * (Vnl - wn)) + (_pl * Vnl);
         for (int k = 0; k < 2; k++) f[1 + k] = ((_dl * L[1 + k]) * (Vnl - wn)) + (_pl * n[k]);
     } else if ((sl < wn) && (wn <= sr)) {
-        if (!hllc) {
+        if (!HLLC) {
             const float fac1 = sr - wn, fac2 = sl - wn, inv3 = 1.f / (sr - sl);
             f[0] = (((((_dl * Vnl) * fac1) - ((_dr * Vnr) * fac2)) - ((sl * _dl) * fac1)) + ((sr * _dr) * fac2)) *
                    inv3;
@@ -583,17 +592,20 @@ __device__ __forceinline__ void hll_family32(bool hllc, const float *L, const fl
             f[3] = ((((((el + _pl) * Vnl) * fac1) - (((er + _pr) * Vnr) * fac2)) - ((sl * el) * fac1)) +
                     ((sr * er) * fac2)) * inv3;
         } else {                           // star region on the side of the contact
+            // with m = d (s - Vn) from the wave speeds: factor_1 = m / (s - sc),
+            // p / (d (s - Vn)) = p / m
             const bool left = wn <= sc;
             const float d = left ? _dl : _dr, p = left ? _pl : _pr, Vn = left ? Vnl : Vnr, s = left ? sl : sr;
+            const float m = left ? ml : mr;
             const float vsq = left ? vl_sq : vr_sq;
             const float *S = left ? L : R;
-            const float factor_1 = (d * (s - Vn)) / (s - sc);
-            const float factor_2 = ((factor_1 * (s - wn)) * (sc - Vn)) + p;
-            const float frho = (d * (Vn - s)) + (factor_1 * (s - wn));
+            const float sw = s - wn;
+            const float factor_1 = m / (s - sc);
+            const float factor_2 = ((factor_1 * sw) * (sc - Vn)) + p;
+            const float frho = (factor_1 * sw) - m;
             const float e = ((0.5f * d) * vsq) + (p * C.inv_gm1);
             f[0] = frho;
-            f[3] = (((e + p) * Vn) - (s * e)) +
-                   (((s - wn) * factor_1) * ((e / d) + ((sc - Vn) * (sc + (p / (d * (s - Vn)))))));
+            f[3] = (((e + p) * Vn) - (s * e)) + ((sw * factor_1) * ((e / d) + ((sc - Vn) * (sc + (p / m)))));
             for (int k = 0; k < 2; k++) f[1 + k] = (frho * S[1 + k]) + (factor_2 * n[k]);
         }
     } else {
@@ -601,38 +613,31 @@ __device__ __forceinline__ void hll_family32(bool hllc, const float *L, const fl
         f[3] = ((((0.5f * _dr) * vr_sq) + (_pr * C.inv_gm1)) * (Vnr - wn)) + (_pr * Vnr);
         for (int k = 0; k < 2; k++) f[1 + k] = ((_dr * R[1 + k]) * (Vnr - wn)) + (_pr * n[k]);
     }
-    if (boost) deboost<float, 2>(w, f);
+    if (BOOST) deboost<float, 2>(w, f);
 }
 
 // ---- fused face kernel ------------------------------------------------------------
 
-// FP32 MUSCL-Hancock half step (temporal of phd_physics.cuh, 2D) with each side's
-// 1/rho formed once and the divergence / advection terms written out per side.
-__device__ __forceinline__ void temporal32(float *L, float *R, const float *pi, const float *pj, const float *gi,
-                                           const float *gj, const float *w, float gamma, float dt, bool boost) {
-    float sl[4], sr[4];
-#pragma unroll
-    for (int f = 0; f < 4; f++) { sl[f] = L[f]; sr[f] = R[f]; }
-    const float vi[2] = {boost ? pi[1] - w[0] : pi[1], boost ? pi[2] - w[1] : pi[2]};
-    const float vj[2] = {boost ? pj[1] - w[0] : pj[1], boost ? pj[2] - w[1] : pj[2]};
-    const float ri = dt / pi[0], rj = dt / pj[0];
-    // grad rows: rho (0, 1), vx (2, 3), vy (4, 5), p (6, 7)
-    const float divi = gi[2] + gi[5], divj = gj[2] + gj[5];
-    L[0] -= dt * (pi[0] * divi + vi[0] * gi[0] + vi[1] * gi[1]);
-    R[0] -= dt * (pj[0] * divj + vj[0] * gj[0] + vj[1] * gj[1]);
-    L[1] -= ri * gi[6] + dt * (vi[0] * gi[2] + vi[1] * gi[3]);
-    R[1] -= rj * gj[6] + dt * (vj[0] * gj[2] + vj[1] * gj[3]);
-    L[2] -= ri * gi[7] + dt * (vi[0] * gi[4] + vi[1] * gi[5]);
-    R[2] -= rj * gj[7] + dt * (vj[0] * gj[4] + vj[1] * gj[5]);
-    L[3] -= dt * (gamma * pi[3] * divi + vi[0] * gi[6] + vi[1] * gi[7]);
-    R[3] -= dt * (gamma * pj[3] * divj + vj[0] * gj[6] + vj[1] * gj[7]);
-    if (L[0] < 0.f || L[3] < 0.f) {
-#pragma unroll
-        for (int f = 0; f < 4; f++) L[f] = sl[f];
-    }
-    if (R[0] < 0.f || R[3] < 0.f) {
-#pragma unroll
-        for (int f = 0; f < 4; f++) R[f] = sr[f];
+// FP32 MUSCL-Hancock half step for one side (add_temporal reconstruction.pyx:923-1072,
+// temporal of phd_physics.cuh, 2D): X is the side's limited spatial state, p its cell's
+// primitives, g the cell's gradient rows (rho 0 1, v_x 2 3, v_y 4 5, p 6 7), (v0, v1)
+// the cell's velocity in the frame the states are in, h the half step.  Each field is
+// one chain of fused multiply-adds; the state reverts to X where density or pressure
+// would turn negative.
+__device__ __forceinline__ void half_step32(float *X, const float *p, const float *g, float v0, float v1,
+                                            float gamma, float h) {
+    const float a0 = h * v0, a1 = h * v1;
+    const float hr = h / p[0];
+    const float hdiv = h * (g[2] + g[5]);
+    const float x0 = fmaf(-p[0], hdiv, fmaf(-a1, g[1], fmaf(-a0, g[0], X[0])));
+    const float x1 = fmaf(-hr, g[6], fmaf(-a1, g[3], fmaf(-a0, g[2], X[1])));
+    const float x2 = fmaf(-hr, g[7], fmaf(-a1, g[5], fmaf(-a0, g[4], X[2])));
+    const float x3 = fmaf(-(gamma * p[3]), hdiv, fmaf(-a1, g[7], fmaf(-a0, g[6], X[3])));
+    if (!(x0 < 0.f || x3 < 0.f)) {
+        X[0] = x0;
+        X[1] = x1;
+        X[2] = x2;
+        X[3] = x3;
     }
 }
 
@@ -704,7 +709,9 @@ __device__ __forceinline__ FaceHead face_head(int m, const phd_mesh &M, const fl
 }
 
 // dt_run: the step's dt in FP32 when all faces belong to one run (read once per thread).
-template <int SOLVER, bool LINEAR>
+// BOOST: the reconstruction and the Riemann solver work in the face's frame (always for
+// the exact solver, which the reference runs boosted).
+template <int SOLVER, bool LINEAR, bool BOOST>
 __device__ __forceinline__ void face32_face(int m, const FaceHead &H, const phd_mesh &M, const phd_params &P,
                                             int moving, const float4 *__restrict__ prim4,
                                             const float4 *__restrict__ cellrec, const float2 *__restrict__ w2,
@@ -713,7 +720,6 @@ __device__ __forceinline__ void face32_face(int m, const FaceHead &H, const phd_
     const int i = H.i, j = H.j;
     if (i < 0 || i >= M.n_cells || j < 0 || j >= M.n_cells) { set_status32(clocks, PHD_STATUS_BAD_INDEX); return; }
     phd_clock *clk = cell_run ? clocks + cell_run[i] : clocks;
-    const bool boost = (SOLVER == PHD_EXACT) ? true : (P.boost != 0);
     const float gamma = GC.g;
     const float dtf = cell_run ? narrow_f64(clk->dt) : dt_run;
     const float dt_half = 0.5f * dtf;
@@ -745,14 +751,14 @@ __device__ __forceinline__ void face32_face(int m, const FaceHead &H, const phd_
     float L[4], R[4];
 #pragma unroll
     for (int f = 0; f < 4; f++) { L[f] = pi[f]; R[f] = pj[f]; }
-    if (boost) { L[1] -= w[0]; L[2] -= w[1]; R[1] -= w[0]; R[2] -= w[1]; }
+    if (BOOST) { L[1] -= w[0]; L[2] -= w[1]; R[1] -= w[0]; R[2] -= w[1]; }
     if (LINEAR) {
         const float gi[8] = {gi0.x, gi0.y, gi0.z, gi0.w, gi1.x, gi1.y, gi1.z, gi1.w};
         const float gj[8] = {gj0.x, gj0.y, gj0.z, gj0.w, gj1.x, gj1.y, gj1.z, gj1.w};
         const float hr = 0.5f * ar.y;
         const float six = g.z + hr * g.x - ci.x, siy = g.w + hr * g.y - ci.y;   // f - (x_i + dcom_i)
         const float sjx = g.z - hr * g.x - cj.x, sjy = g.w - hr * g.y - cj.y;   // f - (x_j + dcom_j)
-        float sl[4], sr[4];
+        float sl[4], sr[4];     // the states at the cells (in the face's frame when boosted)
 #pragma unroll
         for (int f = 0; f < 4; f++) {
             sl[f] = L[f];
@@ -774,12 +780,14 @@ __device__ __forceinline__ void face32_face(int m, const FaceHead &H, const phd_
                 for (int f = 0; f < 4; f++) R[f] = sr[f];
             }
         }
-        temporal32(L, R, pi, pj, gi, gj, w, gamma, dt_half, boost);
+        // the half step takes each cell's velocity in the states' frame: sl[1..2]
+        half_step32(L, pi, gi, sl[1], sl[2], gamma, dt_half);
+        half_step32(R, pj, gj, sr[1], sr[2], gamma, dt_half);
     }
     float f[4];
     bool failed = false;
     if (SOLVER == PHD_EXACT) exact_flux<float, 2>(L, R, nrm, w, gamma, P.exact_max_iter, f, &failed, &GC.X);
-    else hll_family32(SOLVER == PHD_HLLC, L, R, nrm, w, GC, boost, f);
+    else hll_family32<SOLVER == PHD_HLLC, BOOST>(L, R, nrm, w, GC, f);
     if (failed) set_status32(clk, PHD_STATUS_RIEMANN_NONCONVERGED);
     // the face's conserved increment dt*A*F (mesh.pyx:519-544), formed once here so both
     // cells of the face apply exactly the same value
@@ -787,15 +795,16 @@ __device__ __forceinline__ void face32_face(int m, const FaceHead &H, const phd_
     flux4[m] = make_float4(s * f[0], s * f[1], s * f[2], s * f[3]);
 }
 
-// At most 384 threads per block and at least 3 blocks per SM: 56 registers per thread,
-// which lets more warps hide the face kernel's gather latency (measured faster than the
-// 61-register build at 512 threads).  The exact solver's kernel is bound by the FP64
-// pipe instead, and at 56 registers its FP64 Newton iteration spills; it takes one block
-// per SM as its minimum (118-138 registers, no spills; measured 4% faster).
-constexpr int FACE_MAX_BLOCK = 384;
+// At most 256 threads per block and at least 5 blocks per SM: 48 registers per thread
+// (no spills), 40 resident warps per SM to hide the face kernel's record -> gather
+// latency (measured 4% faster than 56 registers at 384 x 3; at 40 registers it spills).
+// The exact solver's kernel is bound by the FP64 pipe instead, and at these caps its
+// FP64 Newton iteration spills; it takes one block per SM as its minimum (118-138
+// registers, no spills; measured 4% faster).
+constexpr int FACE_MAX_BLOCK = 256;
 
-template <int SOLVER, bool LINEAR, int ITEMS>
-__global__ void __launch_bounds__(FACE_MAX_BLOCK, SOLVER == PHD_EXACT ? 1 : 3) k_face32(phd_mesh M, phd_params P, int moving,
+template <int SOLVER, bool LINEAR, int ITEMS, bool BOOST>
+__global__ void __launch_bounds__(FACE_MAX_BLOCK, SOLVER == PHD_EXACT ? 1 : 5) k_face32(phd_mesh M, phd_params P, int moving,
                                                 const float4 *__restrict__ face_geo,
                                                 const float2 *__restrict__ face_ar,
                                                 const float4 *__restrict__ prim4,
@@ -811,8 +820,8 @@ __global__ void __launch_bounds__(FACE_MAX_BLOCK, SOLVER == PHD_EXACT ? 1 : 3) k
         for (int k = 0; k < ITEMS; k++) {
             const int m = base + k * blockDim.x + threadIdx.x;
             if (m < M.n_faces)
-                face32_face<SOLVER, LINEAR>(m, face_head(m, M, face_geo, face_ar), M, P, moving, prim4, cellrec, w2,
-                                            flux4, clocks, cell_run, GC, dt_run);
+                face32_face<SOLVER, LINEAR, BOOST>(m, face_head(m, M, face_geo, face_ar), M, P, moving, prim4,
+                                                   cellrec, w2, flux4, clocks, cell_run, GC, dt_run);
         }
     }
 }
@@ -1119,12 +1128,22 @@ void launch_face32_items(bool linear, int grid, int block, cudaStream_t s, const
     const float4 *fg = reinterpret_cast<const float4 *>(G->face_geo);
     const float2 *fa = reinterpret_cast<const float2 *>(G->face_ar);
     const GasC gc = gas_consts(P.gamma);
-    if (linear)
-        launch_pdl(k_face32<SOLVER, true, ITEMS>, grid, block, s, M, P, moving, fg, fa, prim4, cellrec, w2, flux4,
-                   clocks, cell_run, gc);
-    else
-        launch_pdl(k_face32<SOLVER, false, ITEMS>, grid, block, s, M, P, moving, fg, fa, prim4, cellrec, w2, flux4,
-                   clocks, cell_run, gc);
+    constexpr bool EX = SOLVER == PHD_EXACT;      // the exact solver always works boosted
+    if (EX || P.boost) {
+        if (linear)
+            launch_pdl(k_face32<SOLVER, true, ITEMS, true>, grid, block, s, M, P, moving, fg, fa, prim4, cellrec, w2,
+                       flux4, clocks, cell_run, gc);
+        else
+            launch_pdl(k_face32<SOLVER, false, ITEMS, true>, grid, block, s, M, P, moving, fg, fa, prim4, cellrec, w2,
+                       flux4, clocks, cell_run, gc);
+    } else if constexpr (!EX) {
+        if (linear)
+            launch_pdl(k_face32<SOLVER, true, ITEMS, false>, grid, block, s, M, P, moving, fg, fa, prim4, cellrec,
+                       w2, flux4, clocks, cell_run, gc);
+        else
+            launch_pdl(k_face32<SOLVER, false, ITEMS, false>, grid, block, s, M, P, moving, fg, fa, prim4, cellrec,
+                       w2, flux4, clocks, cell_run, gc);
+    }
 }
 
 // The exact solver's face kernel is bound by the FP64 pipe and holds 120+ registers:

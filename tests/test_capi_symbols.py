@@ -84,7 +84,7 @@ def test_argument_errors_are_rejected_on_the_host(lib):
     par = L.PhdParams()
     geo = L.PhdGeom32()
     for lch in (L.PhdLaunch(48, 128, 128, 0, 0, 0),       # not a multiple of 32
-                L.PhdLaunch(128, 512, 128, 0, 0, 0),      # face kernel above its 384-thread bound
+                L.PhdLaunch(128, 512, 128, 0, 0, 0),      # face kernel above its 256-thread bound
                 L.PhdLaunch(128, 128, 128, 0, 0, 0, 3, 1, 1)):   # items per thread other than 1, 2, 4
         rc = f.phd_step_f32_batched(ctypes.byref(m), ctypes.byref(geo), ctypes.byref(par), 0, ctypes.byref(lch),
                                     one, one, one, one, one, one, one, 1, None, None, None)

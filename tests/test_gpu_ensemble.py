@@ -58,7 +58,7 @@ def test_every_tuned_shape_is_bitwise_equal(runs, items):
         for waves in (0, 2):
             e = EnsembleStepper(runs)
             cap = waves * sms
-            e.launch = L.PhdLaunch(block, min(block, 384), block, cap, cap, cap, items, items, items)
+            e.launch = L.PhdLaunch(block, min(block, 256), block, cap, cap, cap, items, items, items)
             e.step(5)
             e.check_status()
             for r in range(len(runs)):
