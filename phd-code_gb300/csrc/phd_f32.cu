@@ -500,7 +500,7 @@ __global__ void __launch_bounds__(512) k_grad32(phd_mesh M, phd_params P, int mo
 // more instructions in all, and measured no faster: with fast-math a division is
 // already one reciprocal and one multiply.)
 struct GasC {
-    float g, gm1, inv_gm1, gp1_2g, z, inv_z, two_gp1, gm1_gp1, half_gm1, sq_two_gp1, one_m_gp1_2g;
+    float g, inv_gm1, gp1_2g, one_m_gp1_2g, z, inv_z, gm1_gp1, half_gm1, sq_two_gp1;
     ExGas64 X;                 // the exact solver's FP64 Newton constants
 };
 
@@ -508,16 +508,14 @@ inline GasC gas_consts(double gamma) {
     const float g = (float)gamma;
     GasC c;
     c.g = g;
-    c.gm1 = g - 1.f;
     c.inv_gm1 = 1.f / (g - 1.f);
     c.gp1_2g = (g + 1.f) / (2.f * g);
+    c.one_m_gp1_2g = 1.f - c.gp1_2g;
     c.z = (g - 1.f) / (2.f * g);
     c.inv_z = 1.f / c.z;
-    c.two_gp1 = 2.f / (g + 1.f);
     c.gm1_gp1 = (g - 1.f) / (g + 1.f);
     c.half_gm1 = 0.5f * (g - 1.f);
-    c.sq_two_gp1 = std::sqrt(c.two_gp1);
-    c.one_m_gp1_2g = 1.f - c.gp1_2g;
+    c.sq_two_gp1 = std::sqrt(2.f / (g + 1.f));
     c.X = ex_gas64(gamma);
     return c;
 }
