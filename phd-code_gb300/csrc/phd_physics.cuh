@@ -209,14 +209,28 @@ PHD_HD __forceinline__ double ex_get_pstar(double dl, double ul, double pl, doub
 //    |e| <= 2^-12: tail below 1e-19);
 //  * one reciprocal of the iterate per Newton step serves both sides, the shock-branch
 //    guess takes one division and one square root per side, and the convergence test
-//    2|dp|/(p_new + p_old) <= TOL is evaluated as 2|dp| <= TOL |p_new + p_old|.
+//    2|dp|/(p_new + p_old) <= TOL is evaluated as 2|dp| <= TOL |p_new + p_old|;
+//  * on the device every FP64 reciprocal and reciprocal square root of the iteration
+//    is the hardware approximation (rcp.approx.ftz.f64, rsqrt.approx.ftz.f64) refined
+//    by two Newton-Raphson steps (ex_rcp, ex_rsqrt): full FP64 precision for the
+//    positive normal arguments the iteration takes, in a few fused multiply-adds
+//    instead of the correctly rounded division and square root sequences.
 // Results agree with ex_get_pstar to FP64 rounding of the guess (the converged p*
 // within 1e-12 relative; iteration counts can differ by one only where the relative
 // change sits within rounding of TOL).
+// The FP32 path (exact_flux<float>) also starts the iteration from the guess formed in
+// FP32 from its FP32 states (ex_p_guess32: the guess is an estimate, not part of the
+// iteration; the FP64 guess stands in where the FP32 one is not positive and finite),
+// and forms the side functions at p*, which only u* needs, from the last Newton step's
+// values and slopes, f_K(p*) = f_K(p_old) + f_K'(p_old) (p* - p_old): converged to
+// 2|dp| <= 1e-6 (p_old + p*), the dropped term (f_K'' dp^2 / 2) is below 1e-12 of
+// f_K, far below the FP32 rounding of the sampled state.
 struct ExGas64 {
     double two_gm1, two_gp1, gm1_gp1, gm1_2, gp1_2, z, inv_z;
     int n_inv_z;              // 1/z when it is an integer in [1, 64], else 0
     double c[9];              // C(z, k), k = 0..8
+    double sq_two_gp1;        // sqrt(2/(g+1))
+    float zf, inv_zf, two_gm1f, gm1_2f, gm1_gp1f, sq_two_gp1f;   // the same in FP32 (ex_p_guess32)
 };
 
 inline ExGas64 ex_gas64(double gamma) {
@@ -231,9 +245,49 @@ inline ExGas64 ex_gas64(double gamma) {
     const double r = X.inv_z + 0.5;
     const int n = (r >= 1. && r < 65.) ? int(r) : 0;
     X.n_inv_z = (n > 0 && fabs(X.inv_z - double(n)) <= 1e-12 * X.inv_z) ? n : 0;
+    X.sq_two_gp1 = sqrt(X.two_gp1);
+    X.zf = (float)X.z;
+    X.inv_zf = (float)X.inv_z;
+    X.two_gm1f = (float)X.two_gm1;
+    X.gm1_2f = (float)X.gm1_2;
+    X.gm1_gp1f = (float)X.gm1_gp1;
+    X.sq_two_gp1f = (float)X.sq_two_gp1;
     X.c[0] = 1.;
     for (int k = 1; k < 9; k++) X.c[k] = X.c[k - 1] * (X.z - double(k - 1)) / double(k);
     return X;
+}
+
+// 1/x and 1/sqrt(x) for positive normal x: on the device the hardware approximations
+// refined by two Newton-Raphson steps, y <- y (2 - x y) and y <- y (3 - x y^2) / 2 (each
+// squares the relative error, so the approximations' error reaches FP64 rounding),
+// written as a small correction added to y, y + y e with e = 1 - x y, resp.
+// e = 1/2 - (x/2) y^2, formed by fused multiply-adds so that the last rounding falls on
+// the correction; on the host (the check program) IEEE division and square root.
+PHD_HD __forceinline__ double ex_rcp(double x) {
+#ifdef __CUDA_ARCH__
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    double e = fma(-x, y, 1.0);
+    y = fma(y, e, y);
+    e = fma(-x, y, 1.0);
+    return fma(y, e, y);
+#else
+    return 1.0 / x;
+#endif
+}
+
+PHD_HD __forceinline__ double ex_rsqrt(double x) {
+#ifdef __CUDA_ARCH__
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double h = 0.5 * x;
+    double e = fma(-h * y, y, 0.5);
+    y = fma(y, e, y);
+    e = fma(-h * y, y, 0.5);
+    return fma(y, e, y);
+#else
+    return 1.0 / sqrt(x);
+#endif
 }
 
 constexpr double EX_NEAR_ONE = 0.015625;
@@ -278,18 +332,41 @@ PHD_HD __forceinline__ double ex_p_guess_lean(double dl, double ul, double pl, d
     const double p_min = (pr < pl) ? pr : pl;
     if ((p_max <= 2. * p_min) && (p_min <= ppv && ppv <= p_max)) return ppv;
     if (ppv <= p_min) {
-        const double inv_cl = 1. / cl, inv_cr = 1. / cr;
-        const double p_lr = ex_pow_z(X, pl / pr);
-        const double u_star = (((p_lr * ul) * inv_cl + ur * inv_cr) + X.two_gm1 * (p_lr - 1.)) /
-                              (p_lr * inv_cl + inv_cr);
+        const double inv_cl = ex_rcp(cl), inv_cr = ex_rcp(cr);
+        const double p_lr = ex_pow_z(X, pl * ex_rcp(pr));
+        const double u_star = (((p_lr * ul) * inv_cl + ur * inv_cr) + X.two_gm1 * (p_lr - 1.)) *
+                              ex_rcp(p_lr * inv_cl + inv_cr);
         const double p_tl = ex_pow_inv_z(X, 1. + (X.gm1_2 * (ul - u_star)) * inv_cl);
         const double p_tr = ex_pow_inv_z(X, 1. + (X.gm1_2 * (u_star - ur)) * inv_cr);
         return .5 * ((pl * p_tl) + (pr * p_tr));
     }
-    const double gl = sqrt(X.two_gp1 / (dl * (X.gm1_gp1 * pl + ppv)));
-    const double gr = sqrt(X.two_gp1 / (dr * (X.gm1_gp1 * pr + ppv)));
+    const double gl = X.sq_two_gp1 * ex_rsqrt(dl * (X.gm1_gp1 * pl + ppv));
+    const double gr = X.sq_two_gp1 * ex_rsqrt(dr * (X.gm1_gp1 * pr + ppv));
+    return (((gl * pl) + (gr * pr)) - (ur - ul)) * ex_rcp(gr + gl);
+}
+
+#ifdef __CUDACC__
+// ex_p_guess_lean in FP32 from the FP32 path's states (fast-math powers and
+// reciprocal square roots): PVRS, else the two-rarefaction or two-shock estimate.
+__device__ __forceinline__ float ex_p_guess32(float dl, float ul, float pl, float cl, float dr, float ur, float pr,
+                                              float cr, const ExGas64 &X) {
+    const float ppv = (.5f * (pl + pr)) - (((.125f * (ur - ul)) * (dl + dr)) * (cl + cr));
+    const float p_max = fmaxf(pl, pr), p_min = fminf(pl, pr);
+    if ((p_max <= 2.f * p_min) && (p_min <= ppv && ppv <= p_max)) return ppv;
+    if (ppv <= p_min) {
+        const float inv_cl = 1.f / cl, inv_cr = 1.f / cr;
+        const float p_lr = __powf(pl / pr, X.zf);
+        const float u_star = (((p_lr * ul) * inv_cl + ur * inv_cr) + X.two_gm1f * (p_lr - 1.f)) /
+                             (p_lr * inv_cl + inv_cr);
+        const float p_tl = __powf(1.f + (X.gm1_2f * (ul - u_star)) * inv_cl, X.inv_zf);
+        const float p_tr = __powf(1.f + (X.gm1_2f * (u_star - ur)) * inv_cr, X.inv_zf);
+        return .5f * ((pl * p_tl) + (pr * p_tr));
+    }
+    const float gl = X.sq_two_gp1f * rsqrtf(dl * (X.gm1_gp1f * pl + ppv));
+    const float gr = X.sq_two_gp1f * rsqrtf(dr * (X.gm1_gp1f * pr + ppv));
     return (((gl * pl) + (gr * pr)) - (ur - ul)) / (gr + gl);
 }
+#endif
 
 struct ExSide {
     double d, p, c, Bk;
@@ -301,7 +378,7 @@ struct ExSide {
 PHD_HD __forceinline__ double ex_side_power(ExSide &S, const ExGas64 &X, double p_old) {
     const double r = fma(p_old, S.inv_ref, -1.);
     if (fabs(r) <= EX_NEAR_ONE) return S.qz_ref * ex_pow_near_one(X, r);
-    return ex_pow_z(X, p_old / S.p);
+    return ex_pow_z(X, p_old * ex_rcp(S.p));
 }
 
 // f_K(p_old) and f_K'(p_old) of ex_p_func / ex_p_func_deriv; inv_pold = 1 / p_old
@@ -311,11 +388,11 @@ PHD_HD __forceinline__ void ex_side_eval(ExSide &S, const ExGas64 &X, double p_o
         const double qz = ex_side_power(S, X, p_old);
         S.inv_ref = inv_pold;
         S.qz_ref = qz;
-        if (S.inv_cd == 0.) S.inv_cd = 1. / (S.c * S.d);
+        if (S.inv_cd == 0.) S.inv_cd = ex_rcp(S.c * S.d);
         f = (S.c * X.two_gm1) * (qz - 1.);
         df = (qz * (S.p * inv_pold)) * S.inv_cd;
     } else {
-        const double s = sqrt(X.two_gp1 / (S.d * (p_old + S.Bk)));
+        const double s = X.sq_two_gp1 * ex_rsqrt(S.d * (p_old + S.Bk));
         const double u = ((s * s) * S.d) * X.gp1_2;         // 1/(p_old + B_K)
         S.ps_ref = p_old;
         S.s_ref = s;
@@ -330,27 +407,37 @@ PHD_HD __forceinline__ double ex_side_f(ExSide &S, const ExGas64 &X, double p) {
     if (p <= S.p) return (S.c * X.two_gm1) * (ex_side_power(S, X, p) - 1.);
     const double e = (p - S.ps_ref) * S.u_ref;
     if (S.s_ref != 0. && fabs(e) <= 0.000244140625) return (p - S.p) * (S.s_ref * ex_rsqrt_near_one(e));
-    return (p - S.p) * sqrt(X.two_gp1 / (S.d * (p + S.Bk)));
+    return (p - S.p) * (X.sq_two_gp1 * ex_rsqrt(S.d * (p + S.Bk)));
 }
 
 // p* of ex_get_pstar, and the two side functions at p* (for u*).
 PHD_HD __forceinline__ double ex_get_pstar_lean(double dl, double ul, double pl, double cl, double dr,
                                                 double ur, double pr, double cr, const ExGas64 &X, int max_iter,
-                                                bool *failed, double &fl_star, double &fr_star) {
+                                                bool *failed, double &fl_star, double &fr_star,
+                                                float guess32 = -1.f) {
+    // guess32 > 0: the FP32 path's guess, and the side functions at p* linearised
     const double TOL = 1.0e-6;
     ExSide Ls{dl, pl, cl, pl * X.gm1_gp1, 0., 0., 0., 0., 0., 0.};
     ExSide Rs{dr, pr, cr, pr * X.gm1_gp1, 0., 0., 0., 0., 0., 0.};
-    double p_old = ex_p_guess_lean(dl, ul, pl, cl, dr, ur, pr, cr, X), p_new = p_old;
+    const bool f32 = guess32 > 0.f && guess32 < INFINITY;
+    double p_old = f32 ? double(guess32) : ex_p_guess_lean(dl, ul, pl, cl, dr, ur, pr, cr, X);
+    double p_new = p_old;
     for (int it = 0; it < max_iter; it++) {
         double fl, fr, dfl, dfr;
-        const double inv_pold = (p_old <= pl || p_old <= pr) ? 1. / p_old : 0.;
+        const double inv_pold = (p_old <= pl || p_old <= pr) ? ex_rcp(p_old) : 0.;
         ex_side_eval(Ls, X, p_old, inv_pold, fl, dfl);
         ex_side_eval(Rs, X, p_old, inv_pold, fr, dfr);
-        p_new = p_old - ((((fl + fr) + ur) - ul) / (dfl + dfr));
+        p_new = p_old - ((((fl + fr) + ur) - ul) * ex_rcp(dfl + dfr));
         const double sum = p_new + p_old;
         if (2. * fabs(p_new - p_old) <= TOL * fabs(sum) && sum != 0.) {
-            fl_star = ex_side_f(Ls, X, p_new);
-            fr_star = ex_side_f(Rs, X, p_new);
+            if (f32) {
+                const double dp = p_new - p_old;
+                fl_star = fma(dfl, dp, fl);
+                fr_star = fma(dfr, dp, fr);
+            } else {
+                fl_star = ex_side_f(Ls, X, p_new);
+                fr_star = ex_side_f(Rs, X, p_new);
+            }
             return p_new;
         }
         if (p_new < 0.) p_new = TOL;
@@ -391,9 +478,15 @@ PHD_HD __forceinline__ void exact_flux(const T *L, const T *R, const T *n, const
         u_star = T(0.5 * (((double(vnl) + double(vnr)) + fr_d) - fl_d));
     } else {                                  // FP32 path: FP64 Newton, powers reused across steps
         double fl_d, fr_d;
+#ifdef __CUDA_ARCH__
+        const float g32 = ex_p_guess32(float(_dl), float(vnl), float(_pl), float(cl), float(_dr), float(vnr),
+                                       float(_pr), float(cr), *X);
+#else
+        const float g32 = -1.f;
+#endif
         const double p_star_d = ex_get_pstar_lean(double(_dl), double(vnl), double(_pl), double(cl),
                                                   double(_dr), double(vnr), double(_pr), double(cr), *X, max_iter,
-                                                  failed, fl_d, fr_d);
+                                                  failed, fl_d, fr_d, g32);
         p_star = T(p_star_d);
         u_star = T(0.5 * (((double(vnl) + double(vnr)) + fr_d) - fl_d));
     }
