@@ -754,7 +754,6 @@ int phd_load_mesh_f32(const phd_mesh *mesh, const phd_handover32 *h, const phd_p
     int32_t *pair_i = const_cast<int32_t *>(mesh->pair_i);
     int32_t *pair_j = const_cast<int32_t *>(mesh->pair_j);
     double *x = const_cast<double *>(mesh->x);
-    const cudaMemcpyKind H2D = cudaMemcpyHostToDevice;
     const cudaStream_t lists = side[0], geom = side[1];
     int rc = PHD_OK;
 #define PHD_TRY(call)                                                      \
